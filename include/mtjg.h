@@ -1,0 +1,203 @@
+/*
+ * mtjg.h -- C ABI of the GB300 preconditioned Krylov library.
+ *
+ * Drop-in for the sparse iterative path of MTJ (no.uib.cipr.matrix.sparse):
+ * CompRowMatrix's products, the CG / BiCGstab / GMRES(m) solvers, the
+ * Jacobi / ILU(0) / ICC preconditioners and DefaultIterationMonitor.  Each
+ * declaration names the reference method it replaces (file:line inside the
+ * reference project; S/ = src/main/java/no/uib/cipr/matrix/sparse/,
+ * M/ = src/main/java/no/uib/cipr/matrix/).
+ *
+ * Conventions
+ *  - Every function returns an int status: MTJG_OK (0) or a code below.
+ *    Nothing throws.  mtjg_last_error() gives the message of the calling
+ *    thread's last failure.  The codes map one to one onto the exceptions
+ *    the reference throws (see INTEGRATION.md for the Java mapping).
+ *  - CSR is MTJ's: 0-based int32 row pointers and column indices, column
+ *    indices ascending inside each row, float64 values.
+ *  - Host pointers are borrowed for the duration of the call only.  "_dev"
+ *    variants take device pointers that stay valid until the call returns.
+ *  - Handles are not thread-safe (as the Java objects are not): one thread
+ *    per context, or an external lock.  All work of a context runs in order
+ *    on that context's CUDA stream.
+ */
+#ifndef MTJG_H
+#define MTJG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define MTJG_API __attribute__((visibility("default")))
+#else
+#define MTJG_API
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+enum {
+    MTJG_OK = 0,
+    /* IterativeSolverNotConvergedException(Reason.*), S/IterativeSolverNotConvergedException.java:29-91,
+     * reasons M/NotConvergedException.java:33-49 */
+    MTJG_NOT_CONVERGED_ITERATIONS = 1,
+    MTJG_NOT_CONVERGED_DIVERGENCE = 2,
+    MTJG_NOT_CONVERGED_BREAKDOWN = 3,
+    /* IllegalArgumentException (sizes, S/AbstractIterativeSolver.java:70-77) */
+    MTJG_ERR_ILLEGAL_ARGUMENT = 10,
+    /* IndexOutOfBoundsException (M/AbstractMatrix.java:170-177) */
+    MTJG_ERR_INDEX_OUT_OF_BOUNDS = 11,
+    /* RuntimeException("Zero pivot encountered on row ..."), S/ILU.java:105-107, S/ICC.java:112-114 */
+    MTJG_ERR_ZERO_PIVOT = 20,
+    /* "Zero diagonal entry encountered on row ..." S/ICC.java:128-131,
+     * "Zero diagonal on row ..." S/DiagonalPreconditioner.java:71-72 */
+    MTJG_ERR_ZERO_DIAGONAL = 21,
+    /* "Missing diagonal entry on row ..." S/ILU.java:134-136, S/ICC.java:148-150 */
+    MTJG_ERR_MISSING_DIAGONAL = 22,
+    /* MatrixSingularException from GMRES's triangular solve, M/AbstractTriangDenseMatrix.java:251-252 */
+    MTJG_ERR_SINGULAR = 23,
+    MTJG_ERR_UNSUPPORTED = 30,
+    MTJG_ERR_CUDA = 40,
+    MTJG_ERR_OUT_OF_MEMORY = 41,
+    /* a bounded wait on the device gave up; the context stays usable */
+    MTJG_ERR_DEVICE_TIMEOUT = 42
+};
+
+/* Vector.Norm, M/Vector.java:159-182 */
+enum { MTJG_NORM_ONE = 0, MTJG_NORM_TWO = 1, MTJG_NORM_TWO_ROBUST = 2, MTJG_NORM_INFINITY = 3 };
+
+/* Preconditioner kinds: identity (S/AbstractIterativeSolver.java:82-96),
+ * DiagonalPreconditioner, ILU, ICC */
+enum { MTJG_PC_IDENTITY = 0, MTJG_PC_JACOBI = 1, MTJG_PC_ILU = 2, MTJG_PC_ICC = 3 };
+
+/* IterativeSolver implementations: S/CG.java, S/BiCGstab.java, S/GMRES.java */
+enum { MTJG_CG = 0, MTJG_BICGSTAB = 1, MTJG_GMRES = 2 };
+
+/* Arithmetic of the products and vector updates.  FAST uses fused
+ * multiply-add.  STRICT rounds every product and sum separately, as Java
+ * does, which makes CSR products bit-identical to CompRowMatrix.mult; only
+ * the order of the dot-product and norm reductions then differs from MTJ. */
+enum { MTJG_NUMERICS_FAST = 0, MTJG_NUMERICS_STRICT = 1 };
+
+/* DefaultIterationMonitor(maxIter, rtol, atol, dtol), S/DefaultIterationMonitor.java:72-90,
+ * with the norm of AbstractIterationMonitor.setNormType (S/AbstractIterationMonitor.java:110-112).
+ * history_cap > 0 records the residual and the iteration number passed to
+ * IterationReporter.monitor at every convergence test (S/AbstractIterationMonitor.java:81-93). */
+typedef struct mtjg_monitor {
+    int max_iter;      /* default 100000 */
+    double rtol;       /* default 1e-5   */
+    double atol;       /* default 1e-50  */
+    double dtol;       /* default 1e+5   */
+    int norm;          /* default MTJG_NORM_TWO */
+    int history_cap;   /* 0: no history */
+} mtjg_monitor;
+
+/* Outcome of a solve: IterationMonitor.iterations()/residual() at exit and
+ * the exception reason, if any.  detail: 1 = breakdown on "rho",
+ * 2 = breakdown on "omega" (S/BiCGstab.java:77-83). */
+typedef struct mtjg_result {
+    int status;
+    int iterations;
+    double residual;
+    int detail;
+    int history_len;   /* convergence tests made (may exceed history_cap) */
+} mtjg_result;
+
+typedef struct mtjg_ctx mtjg_ctx;
+typedef struct mtjg_csr mtjg_csr;
+typedef struct mtjg_precond mtjg_precond;
+typedef struct mtjg_solver mtjg_solver;
+
+/* ---- library and context --------------------------------------------- */
+MTJG_API const char *mtjg_last_error(void);
+MTJG_API const char *mtjg_version(void);
+/* Default DefaultIterationMonitor settings (S/DefaultIterationMonitor.java:85-90). */
+MTJG_API void mtjg_monitor_defaults(mtjg_monitor *mon);
+
+/* A context owns one CUDA device and one stream. */
+MTJG_API int mtjg_ctx_create(int device, mtjg_ctx **out);
+MTJG_API int mtjg_ctx_destroy(mtjg_ctx *ctx);
+MTJG_API int mtjg_ctx_set_numerics(mtjg_ctx *ctx, int numerics);
+MTJG_API int mtjg_ctx_synchronize(mtjg_ctx *ctx);
+/* Number of this library's kernel launches on the context so far. */
+MTJG_API int64_t mtjg_ctx_launch_count(mtjg_ctx *ctx);
+/* CUDA events on the context's stream, for timing: record into slot 0..15,
+ * elapsed milliseconds between two recorded slots (synchronizes on b). */
+MTJG_API int mtjg_ctx_event_record(mtjg_ctx *ctx, int slot);
+MTJG_API int mtjg_ctx_event_elapsed(mtjg_ctx *ctx, int a, int b, float *ms);
+/* Device scratch: n doubles, for callers that keep vectors on the GPU. */
+MTJG_API int mtjg_dev_alloc(mtjg_ctx *ctx, int64_t bytes, void **dptr);
+MTJG_API int mtjg_dev_free(mtjg_ctx *ctx, void *dptr);
+MTJG_API int mtjg_memcpy_h2d(mtjg_ctx *ctx, void *dst, const void *src, int64_t bytes);
+MTJG_API int mtjg_memcpy_d2h(mtjg_ctx *ctx, void *dst, const void *src, int64_t bytes);
+
+/* ---- CompRowMatrix ----------------------------------------------------- */
+/* CompRowMatrix(numRows, numColumns, nz) + data, S/CompRowMatrix.java:178-208:
+ * copies the CSR to the device.  Rejects unsorted or out-of-range column
+ * indices (S/CompRowMatrix.java:200-203) with MTJG_ERR_ILLEGAL_ARGUMENT. */
+MTJG_API int mtjg_csr_upload(mtjg_ctx *ctx, int num_rows, int num_cols,
+                             const int *rowptr, const int *colind, const double *val,
+                             mtjg_csr **out);
+/* New values, same pattern (CompRowMatrix.set on the data array). */
+MTJG_API int mtjg_csr_update_values(mtjg_csr *A, const double *val);
+MTJG_API int mtjg_csr_destroy(mtjg_csr *A);
+MTJG_API int mtjg_csr_dims(const mtjg_csr *A, int *num_rows, int *num_cols, int64_t *nnz);
+
+/* CompRowMatrix.mult(Vector x, Vector y): y = A x, S/CompRowMatrix.java:295-314 */
+MTJG_API int mtjg_csr_mult(mtjg_csr *A, const double *x, double *y);
+/* CompRowMatrix.multAdd(alpha, x, y): y += alpha A x, S/CompRowMatrix.java:330-347 */
+MTJG_API int mtjg_csr_mult_add(mtjg_csr *A, double alpha, const double *x, double *y);
+/* CompRowMatrix.transMult(x, y): y = A' x, S/CompRowMatrix.java:350-366 */
+MTJG_API int mtjg_csr_trans_mult(mtjg_csr *A, const double *x, double *y);
+/* CompRowMatrix.transMultAdd(alpha, x, y): y = alpha A' x + y, S/CompRowMatrix.java:369-388 */
+MTJG_API int mtjg_csr_trans_mult_add(mtjg_csr *A, double alpha, const double *x, double *y);
+/* Device-pointer forms of mult / multAdd / transMult (no host copies). */
+MTJG_API int mtjg_csr_mult_dev(mtjg_csr *A, const double *dx, double *dy);
+MTJG_API int mtjg_csr_mult_add_dev(mtjg_csr *A, double alpha, const double *dx, double *dy);
+MTJG_API int mtjg_csr_trans_mult_dev(mtjg_csr *A, const double *dx, double *dy);
+
+/* ---- Preconditioner ---------------------------------------------------- */
+/* new DiagonalPreconditioner(n) / new ILU(CompRowMatrix) / new ICC(CompRowMatrix),
+ * S/DiagonalPreconditioner.java:43-45, S/ILU.java:54-62, S/ICC.java:57-65 */
+MTJG_API int mtjg_precond_create(mtjg_ctx *ctx, int kind, int n, mtjg_precond **out);
+/* Preconditioner.setMatrix(A), S/Preconditioner.java:56-63: Jacobi extracts
+ * the inverse diagonal, ILU and ICC copy A and factor it.  On a setup error
+ * *err_row receives the number MTJ's message prints. */
+MTJG_API int mtjg_precond_set_matrix(mtjg_precond *M, mtjg_csr *A, int *err_row);
+/* Preconditioner.apply(b, x) / transApply(b, x), S/Preconditioner.java:30-54 */
+MTJG_API int mtjg_precond_apply(mtjg_precond *M, const double *b, double *x);
+MTJG_API int mtjg_precond_trans_apply(mtjg_precond *M, const double *b, double *x);
+MTJG_API int mtjg_precond_apply_dev(mtjg_precond *M, const double *db, double *dx);
+/* The factored values (ILU/ICC: the in-place CSR data array of MTJ's copy,
+ * Jacobi: the inverse diagonal), copied to host; returns the count in *len. */
+MTJG_API int mtjg_precond_values(mtjg_precond *M, double *out, int64_t cap, int64_t *len);
+MTJG_API int mtjg_precond_destroy(mtjg_precond *M);
+
+/* ---- IterativeSolver ---------------------------------------------------- */
+/* new CG(template) / new BiCGstab(template) / new GMRES(template, restart):
+ * scratch vectors of size n live on the device with the solver
+ * (S/CG.java:51-56, S/BiCGstab.java:53-63, S/GMRES.java:99-125).
+ * restart <= 0 for GMRES is MTJG_ERR_ILLEGAL_ARGUMENT (S/GMRES.java:114-116). */
+MTJG_API int mtjg_solver_create(mtjg_ctx *ctx, int kind, int n, int restart,
+                                mtjg_solver **out);
+/* setPreconditioner(M) (NULL = identity), S/AbstractIterativeSolver.java:50-52 */
+MTJG_API int mtjg_solver_set_precond(mtjg_solver *S, mtjg_precond *M);
+/* setIterationMonitor(new DefaultIterationMonitor(...)), S/AbstractIterativeSolver.java:62-64 */
+MTJG_API int mtjg_solver_set_monitor(mtjg_solver *S, const mtjg_monitor *mon);
+/* IterativeSolver.solve(A, b, x), S/IterativeSolver.java:30-44: x is the
+ * initial guess and receives the solution (also on a not-converged status,
+ * where it holds the iterate MTJ would leave). */
+MTJG_API int mtjg_solver_solve(mtjg_solver *S, mtjg_csr *A, const double *b, double *x,
+                               mtjg_result *res);
+MTJG_API int mtjg_solver_solve_dev(mtjg_solver *S, mtjg_csr *A, const double *db,
+                                   double *dx, mtjg_result *res);
+/* Residual history of the last solve: the (residual, iteration) pairs passed
+ * to IterationReporter.monitor, oldest first (up to history_cap). */
+MTJG_API int mtjg_solver_history(mtjg_solver *S, double *resid, int *iters, int cap, int *len);
+MTJG_API int mtjg_solver_destroy(mtjg_solver *S);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,165 @@
+// internal.h -- shared declarations of the GB300 Krylov library (host side).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/mtjg.h"
+
+namespace mtjg {
+
+// ----------------------------------------------------------------- errors
+void set_error(const std::string &msg);
+int fail(int code, const std::string &msg);
+int cuda_fail(cudaError_t e, const char *what);
+
+}  // namespace mtjg
+struct mtjg_ctx;
+namespace mtjg {
+// Objects made with a context keep it alive: the context is freed when its
+// handle has been destroyed and the last object made with it is gone.
+void ctx_retain(mtjg_ctx *ctx);
+void ctx_release(mtjg_ctx *ctx);
+
+#define MTJG_CUDA(call)                                       \
+    do {                                                      \
+        cudaError_t e_ = (call);                              \
+        if (e_ != cudaSuccess) return ::mtjg::cuda_fail(e_, #call); \
+    } while (0)
+
+// ------------------------------------------------------------ tiling
+// Rows are cut into tiles of at most kTileRows/vec rows and kTileNnz entries
+// (one long row may exceed kTileNnz; it forms a tile of its own).  Every
+// kernel walks the same tiles, so per-tile partial sums, and therefore every
+// reduction, do not depend on the grid size or on the other systems of a
+// batch.
+constexpr int kBlock = 256;
+constexpr int kTileRows = 256;
+constexpr int kTileNnz = 2816;
+constexpr int kParts = 4;             // partial-sum slots per tile
+
+// device status of a system (SysState::status)
+enum : int {
+    ST_RUNNING = 0,
+    ST_DONE = 100  // converged
+    // otherwise an MTJG_* code
+};
+
+// Per-system scalars of a solve, in device memory.
+struct SysState {
+    int status;
+    int iter;
+    int detail;
+    int hist_len;
+    int inner;      // GMRES: inner index i of the running cycle
+    int inner_done; // GMRES: inner loop left (converged or exception)
+    int gate;       // ST_RUNNING while inner-step kernels must run (GMRES), else 1
+    int pad1;
+    double initR;
+    double residual;
+    double rho, rho_1, rho_2;
+    double alpha, beta, omega;
+    double normr;   // GMRES: ||r||2 of the running cycle
+    double scratch[3];
+};
+
+struct MonCfgDev {
+    int max_iter;
+    int norm;
+    int hist_cap;
+    int pad;
+    double rtol, atol, dtol;
+};
+
+// Reduction context: per-tile partial sums, per-system arrival counters and
+// tile ranges (tiles of system s are [sys_tile[s], sys_tile[s+1])).
+struct RedCtx {
+    double *part;          // [num_tiles * kParts]
+    unsigned *cnt;         // [num_sys]
+    const int *sys_tile;   // [num_sys + 1]
+    int *num_running;      // number of systems with status RUNNING
+};
+
+struct TileSet {
+    int num_tiles = 0;
+    int num_sys = 1;
+    int vec = 1;
+    int *tile_row = nullptr;   // device [num_tiles + 1]
+    int *tile_sys = nullptr;   // device [num_tiles] (nullptr: all system 0)
+    int *sys_tile = nullptr;   // device [num_sys + 1]
+    unsigned char *tile_long = nullptr;  // device [num_tiles]: 1 = single long row
+    std::vector<int> h_tile_row;
+};
+
+// A row-ordered triangular operator solved level by level.
+struct LevelSchedule {
+    int n = 0;
+    int num_levels = 0;
+    int *perm = nullptr;               // device: rows ordered by level
+    std::vector<int> level_ptr;        // host: [num_levels + 1]
+};
+
+}  // namespace mtjg
+
+// --------------------------------------------------------------- handles
+struct mtjg_ctx {
+    std::atomic<int> refs{1};       // the handle itself + every object made with it
+    bool closed = false;            // mtjg_ctx_destroy was called
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t events[16] = {};
+    int numerics = MTJG_NUMERICS_FAST;
+    int num_sms = 0;
+    int64_t launches = 0;
+    int *d_flag = nullptr;          // device error flag (bounded waits)
+    int *h_pinned = nullptr;        // pinned host words for status polling
+};
+
+struct mtjg_csr {
+    mtjg_ctx *ctx = nullptr;
+    int n = 0, m = 0;
+    int64_t nnz = 0;
+    int *rowptr = nullptr;     // device [n+1]
+    int *colind = nullptr;     // device [nnz + 4] (padded for 16-byte bulk copies)
+    double *val = nullptr;     // device [nnz + 2]
+    std::vector<int> h_rowptr; // host copy (tiling, validation)
+    mtjg::TileSet tiles;
+    // transpose (built on first transMult): CSR of A'
+    int *t_rowptr = nullptr, *t_colind = nullptr;
+    double *t_val = nullptr;
+    mtjg::TileSet t_tiles;
+    // reduction scratch sized for this matrix's tiles
+    double *part = nullptr;
+    unsigned *cnt = nullptr;
+    int *num_running = nullptr;
+    // staging vectors for host-pointer calls
+    double *d_x = nullptr, *d_y = nullptr;
+};
+
+struct mtjg_precond {
+    mtjg_ctx *ctx = nullptr;
+    int kind = MTJG_PC_IDENTITY;
+    int n = 0;
+    bool ready = false;
+    int64_t version = 0;               // changes whenever setMatrix reallocates
+    double *invdiag = nullptr;         // Jacobi
+    // ILU / ICC factor: private CSR copy with A's pattern
+    int64_t nnz = 0;
+    int *rowptr = nullptr, *colind = nullptr, *diag = nullptr;
+    double *data = nullptr;
+    // ICC: transpose of the strict upper part (gather form of R'\b)
+    int *rt_rowptr = nullptr, *rt_colind = nullptr;
+    double *rt_val = nullptr;
+    double *diagv = nullptr;            // R_ii
+    mtjg::LevelSchedule lo;             // ILU: L solve; ICC: R' solve
+    mtjg::LevelSchedule up;             // U / R solve (rows descending)
+    double *y = nullptr;                // temporary of apply
+    double *d_b = nullptr, *d_x = nullptr;  // host-call staging
+    void *trans = nullptr;              // ILU transApply operators, built on first use
+};
+
+struct mtjg_solver;

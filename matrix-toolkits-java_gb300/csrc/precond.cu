@@ -1,0 +1,672 @@
+// precond.cu -- Jacobi, ILU(0) and ICC preconditioners (S/DiagonalPreconditioner.java,
+// S/ILU.java, S/ICC.java) with level-scheduled triangular solves.
+//
+// Levels of a triangular operator are found on the device by k_levels: warps
+// take rows in dependency order from a ticket counter and each row waits
+// (bounded) for the levels of the rows it reads, so one launch finds all
+// levels in O(nnz).  The rows are then grouped by level on the host (a
+// counting sort, stable in row index) and every level is one launch of a
+// row-per-thread kernel that sums in MTJ's entry order.
+#include <algorithm>
+#include <cstring>
+
+#include "spmv.cuh"
+
+namespace mtjg {
+
+int icc_factor_host(int n, const int *rowptr, const int *colind, const int *diag, double *data, int *err_row);
+
+constexpr long long kSpinLimit = 1LL << 24;
+
+// ------------------------------------------------------------- kernels
+__global__ void k_find_diag(int n, const int *rp, const int *ci, int *diag, int *err_min)
+{
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        int lo = rp[k], hi = rp[k + 1] - 1, pos = -1;
+        while (lo <= hi) {
+            int mid = (lo + hi) >> 1;
+            int v = ci[mid];
+            if (v < k) lo = mid + 1;
+            else if (v > k) hi = mid - 1;
+            else { pos = mid; break; }
+        }
+        diag[k] = pos;
+        if (pos < 0) atomicMin(err_min, k + 1);
+    }
+}
+
+// DiagonalPreconditioner.setMatrix, S/DiagonalPreconditioner.java:64-76:
+// invdiag = 1 / A.get(i,i) (binary search, CompRowMatrix.get S/CompRowMatrix.java:407-417).
+__global__ void k_jacobi_set(int n, const int *rp, const int *ci, const double *val, double *invdiag, int *err_min)
+{
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        int lo = rp[k], hi = rp[k + 1] - 1;
+        double d = 0.0;
+        while (lo <= hi) {
+            int mid = (lo + hi) >> 1;
+            int v = ci[mid];
+            if (v < k) lo = mid + 1;
+            else if (v > k) hi = mid - 1;
+            else { d = val[mid]; break; }
+        }
+        if (d == 0) atomicMin(err_min, k + 1);
+        invdiag[k] = 1 / d;
+    }
+}
+
+// DiagonalPreconditioner.apply, S/DiagonalPreconditioner.java:54-55
+__global__ void k_jacobi_apply(int n, const double *invdiag, const double *b, double *x, const int *status)
+{
+    if (status && *status != ST_RUNNING) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] = b[i] * invdiag[i];
+}
+
+__global__ void k_copy(int n, const double *b, double *x, const int *status)
+{
+    if (status && *status != ST_RUNNING) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] = b[i];
+}
+
+__device__ __forceinline__ int wait_level(const int *level, int d, bool &bad)
+{
+    const volatile int *L = level;
+    int v = L[d];
+    long long polls = 0;
+    while (v < 0) {
+        if (++polls > kSpinLimit) {
+            bad = true;
+            return 0;
+        }
+        __nanosleep(32);
+        v = L[d];
+    }
+    return v;
+}
+
+// Dependency levels.  Row i reads rows ci[k] for k in its range:
+//   range 0: [rp[i], rp[i+1]), range 1: [rp[i], diag[i]), range 2: (diag[i], rp[i+1]).
+// desc: rows are taken from n-1 down (dependencies have larger indices).
+// quirk (ILU factor only): row i also reads row i-1 when quirk[i-1] is set.
+__global__ void k_levels(int n, int desc, int range, const int *rp, const int *ci, const int *diag,
+                         const unsigned char *quirk, int *level, unsigned *ticket, int *err)
+{
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        unsigned base = 0;
+        if (lane == 0) base = atomicAdd(ticket, 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= (unsigned)n) return;
+        const unsigned t = base + lane;
+        if (t < (unsigned)n) {
+            const int i = desc ? n - 1 - (int)t : (int)t;
+            int b, e;
+            if (range == 0) { b = rp[i]; e = rp[i + 1]; }
+            else if (range == 1) { b = rp[i]; e = diag[i]; }
+            else { b = diag[i] + 1; e = rp[i + 1]; }
+            bool bad = false;
+            int lvl = 0;
+            for (int k = b; k < e; ++k) lvl = max(lvl, wait_level(level, ci[k], bad) + 1);
+            if (quirk && i > 0 && quirk[i - 1]) lvl = max(lvl, wait_level(level, i - 1, bad) + 1);
+            if (bad) atomicExch(err, 1);
+            __threadfence();
+            ((volatile int *)level)[i] = lvl;
+        }
+    }
+}
+
+// Marks rows k whose ILU elimination (S/ILU.java:113-120) ends a scan at
+// l == rowptr[k+1] on a matching column, i.e. updates the first entry of row
+// k+1.  Row k+1 must then be factored after row k.
+__global__ void k_ilu_quirk(int n, const int *rp, const int *ci, const int *diag, unsigned char *quirk)
+{
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        unsigned char q = 0;
+        if (k >= 1 && k + 1 < n) {
+            for (int i = rp[k]; i < diag[k]; ++i) {
+                const int index = ci[i];
+                for (int j = diag[index] + 1, l = rp[k] + 1; j < rp[index + 1]; ++j) {
+                    while (l < rp[k + 1] && ci[l] < ci[j]) l++;
+                    if (l == rp[k + 1] && ci[l] == ci[j]) q = 1;
+                }
+            }
+        }
+        quirk[k] = q;
+    }
+}
+
+// ILU.factor for the rows of one level (S/ILU.java:98-121), rounding each
+// product and difference separately as Java does, so the factor is
+// bit-identical to MTJ's.  err_min collects MTJ's message number (entry i+1)
+// of the first zero pivot.
+__global__ void k_ilu_level(const int *perm, int beg, int cnt, const int *rp, const int *ci, const int *diag,
+                            double *data, int *err_min)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= cnt) return;
+    const int k = perm[beg + t];
+    if (k == 0) return;
+    for (int i = rp[k]; i < diag[k]; ++i) {
+        const int index = ci[i];
+        const double LUii = data[diag[index]];
+        if (LUii == 0) {
+            atomicMin(err_min, i + 1);
+            return;
+        }
+        const double LUki = data[i] / LUii;
+        data[i] = LUki;
+        for (int j = diag[index] + 1, l = rp[k] + 1; j < rp[index + 1]; ++j) {
+            while (l < rp[k + 1] && ci[l] < ci[j]) l++;
+            if (ci[l] == ci[j]) data[l] = __dsub_rn(data[l], __dmul_rn(LUki, data[j]));
+        }
+    }
+}
+
+// Triangular solve of one level, one row per thread.
+//  MODE 0: UnitLowerCompRowMatrix.solve   x_i = b_i - sum_{k<diag} v_k x_ck  (S/UnitLowerCompRowMatrix.java:56-64)
+//  MODE 1: UpperCompRowMatrix.solve       x_i = (b_i - sum_{k>diag} v_k x_ck) / v_diag (S/UpperCompRowMatrix.java:56-64)
+//  MODE 2: UpperCompRowMatrix.transSolve in gather form on the transpose of
+//          the strict upper part: x_c = b_c, minus R_ic x_i for ascending
+//          source rows i, then divided by R_cc (S/UpperCompRowMatrix.java:78-87)
+//  MODE 3: UnitLowerCompRowMatrix.transSolve in gather form on the
+//          transpose of the strict lower part, source rows descending
+//          (S/UnitLowerCompRowMatrix.java:78-83)
+template <bool S, int MODE>
+__global__ void __launch_bounds__(kBlock) k_trsv(const int *__restrict__ perm, int beg, int cnt,
+                                                 const int *__restrict__ rp, const int *__restrict__ ci,
+                                                 const double *__restrict__ v, const int *__restrict__ diag,
+                                                 const double *__restrict__ diagv, const double *b, double *x,
+                                                 const int *status)
+{
+    if (status && *status != ST_RUNNING) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= cnt) return;
+    const int i = perm[beg + t];
+    if constexpr (MODE == 0) {
+        double sum = 0.0;
+        const int e = diag[i];
+        for (int k = rp[i]; k < e; ++k) sum = fmac<S>(v[k], x[ci[k]], sum);
+        x[i] = b[i] - sum;
+    } else if constexpr (MODE == 1) {
+        double sum = 0.0;
+        const int d = diag[i], e = rp[i + 1];
+        for (int k = d + 1; k < e; ++k) sum = fmac<S>(v[k], x[ci[k]], sum);
+        x[i] = (b[i] - sum) / v[d];
+    } else if constexpr (MODE == 2) {
+        double xc = b[i];
+        const int e = rp[i + 1];
+        for (int k = rp[i]; k < e; ++k) xc = fmac<S>(-v[k], x[ci[k]], xc);
+        x[i] = xc / diagv[i];
+    } else {
+        double xc = b[i];
+        for (int k = rp[i + 1] - 1; k >= rp[i]; --k) xc = fmac<S>(-v[k], x[ci[k]], xc);
+        x[i] = xc;
+    }
+}
+
+__global__ void k_gather_diag(int n, const int *diag, const double *data, double *diagv)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) diagv[i] = data[diag[i]];
+}
+
+// ------------------------------------------------------------- host side
+static int grid_for(mtjg_ctx *ctx, int n)
+{
+    return std::max(1, std::min((n + kBlock - 1) / kBlock, ctx->num_sms * 8));
+}
+
+static void free_sched(LevelSchedule &s)
+{
+    cudaFree(s.perm);
+    s.perm = nullptr;
+    s.level_ptr.clear();
+    s.num_levels = 0;
+}
+
+// Finds the levels on the device, then groups rows by level.
+static int build_levels(mtjg_ctx *ctx, int n, int desc, int range, const int *rp, const int *ci, const int *diag,
+                        const unsigned char *quirk, LevelSchedule &out)
+{
+    free_sched(out);
+    out.n = n;
+    if (n == 0) {
+        out.level_ptr = {0};
+        return MTJG_OK;
+    }
+    int *level = nullptr;
+    unsigned *ticket = nullptr;
+    MTJG_CUDA(cudaMalloc(&level, sizeof(int) * (size_t)n));
+    MTJG_CUDA(cudaMalloc(&ticket, sizeof(unsigned)));
+    MTJG_CUDA(cudaMemsetAsync(level, 0xff, sizeof(int) * (size_t)n, ctx->stream));
+    MTJG_CUDA(cudaMemsetAsync(ticket, 0, sizeof(unsigned), ctx->stream));
+    MTJG_CUDA(cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream));
+    k_levels<<<ctx->num_sms * 4, kBlock, 0, ctx->stream>>>(n, desc, range, rp, ci, diag, quirk, level, ticket,
+                                                            ctx->d_flag);
+    ctx->launches++;
+    MTJG_CUDA(cudaGetLastError());
+    std::vector<int> h(n);
+    MTJG_CUDA(cudaMemcpyAsync(h.data(), level, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
+    int flag = 0;
+    MTJG_CUDA(cudaMemcpyAsync(&flag, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    MTJG_CUDA(cudaStreamSynchronize(ctx->stream));
+    cudaFree(level);
+    cudaFree(ticket);
+    if (flag) {
+        cudaMemset(ctx->d_flag, 0, sizeof(int));
+        return fail(MTJG_ERR_DEVICE_TIMEOUT, "level analysis: a bounded wait gave up");
+    }
+    int nl = 0;
+    for (int i = 0; i < n; ++i) nl = std::max(nl, h[i] + 1);
+    out.num_levels = nl;
+    out.level_ptr.assign(nl + 1, 0);
+    for (int i = 0; i < n; ++i) out.level_ptr[h[i] + 1]++;
+    for (int l = 0; l < nl; ++l) out.level_ptr[l + 1] += out.level_ptr[l];
+    std::vector<int> pos(out.level_ptr.begin(), out.level_ptr.end() - 1), perm(n);
+    for (int i = 0; i < n; ++i) perm[pos[h[i]]++] = i;
+    MTJG_CUDA(cudaMalloc(&out.perm, sizeof(int) * (size_t)n));
+    MTJG_CUDA(cudaMemcpy(out.perm, perm.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice));
+    return MTJG_OK;
+}
+
+template <int MODE>
+static cudaError_t run_levels_t(mtjg_ctx *ctx, bool strict, const LevelSchedule &s, const int *rp, const int *ci,
+                                const double *v, const int *diag, const double *diagv, const double *b, double *x,
+                                const int *status)
+{
+    for (int l = 0; l < s.num_levels; ++l) {
+        const int beg = s.level_ptr[l], cnt = s.level_ptr[l + 1] - beg;
+        const int grid = (cnt + kBlock - 1) / kBlock;
+        if (strict)
+            k_trsv<true, MODE><<<grid, kBlock, 0, ctx->stream>>>(s.perm, beg, cnt, rp, ci, v, diag, diagv, b, x,
+                                                                  status);
+        else
+            k_trsv<false, MODE><<<grid, kBlock, 0, ctx->stream>>>(s.perm, beg, cnt, rp, ci, v, diag, diagv, b, x,
+                                                                   status);
+        ctx->launches++;
+    }
+    return cudaGetLastError();
+}
+
+static cudaError_t run_levels(mtjg_ctx *ctx, int mode, const LevelSchedule &s, const int *rp, const int *ci,
+                              const double *v, const int *diag, const double *diagv, const double *b, double *x,
+                              const int *status)
+{
+    const bool strict = ctx->numerics == MTJG_NUMERICS_STRICT;
+    switch (mode) {
+    case 0: return run_levels_t<0>(ctx, strict, s, rp, ci, v, diag, diagv, b, x, status);
+    case 1: return run_levels_t<1>(ctx, strict, s, rp, ci, v, diag, diagv, b, x, status);
+    case 2: return run_levels_t<2>(ctx, strict, s, rp, ci, v, diag, diagv, b, x, status);
+    default: return run_levels_t<3>(ctx, strict, s, rp, ci, v, diag, diagv, b, x, status);
+    }
+}
+
+static int read_err_min(mtjg_ctx *ctx, int *err_min_dev, int *out)
+{
+    MTJG_CUDA(cudaMemcpyAsync(out, err_min_dev, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    MTJG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return MTJG_OK;
+}
+
+// Applies M to device vectors: x = M \ b.  `status` (nullable) makes every
+// kernel a no-op unless the solve it belongs to is running.
+int precond_apply_dev(mtjg_precond *M, const double *b, double *x, const int *status)
+{
+    mtjg_ctx *ctx = M->ctx;
+    const int n = M->n;
+    if (n == 0) return MTJG_OK;
+    cudaError_t e = cudaSuccess;
+    switch (M->kind) {
+    case MTJG_PC_IDENTITY:
+        if (x != b) {
+            k_copy<<<grid_for(ctx, n), kBlock, 0, ctx->stream>>>(n, b, x, status);
+            ctx->launches++;
+        }
+        e = cudaGetLastError();
+        break;
+    case MTJG_PC_JACOBI:
+        k_jacobi_apply<<<grid_for(ctx, n), kBlock, 0, ctx->stream>>>(n, M->invdiag, b, x, status);
+        ctx->launches++;
+        e = cudaGetLastError();
+        break;
+    case MTJG_PC_ILU:
+        e = run_levels(ctx, 0, M->lo, M->rowptr, M->colind, M->data, M->diag, nullptr, b, M->y, status);
+        if (e == cudaSuccess)
+            e = run_levels(ctx, 1, M->up, M->rowptr, M->colind, M->data, M->diag, nullptr, M->y, x, status);
+        break;
+    default:  // ICC: R' y = b, then R x = y (S/ICC.java:67-73)
+        e = run_levels(ctx, 2, M->lo, M->rt_rowptr, M->rt_colind, M->rt_val, nullptr, M->diagv, b, M->y, status);
+        if (e == cudaSuccess)
+            e = run_levels(ctx, 1, M->up, M->rowptr, M->colind, M->data, M->diag, nullptr, M->y, x, status);
+        break;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "preconditioner apply");
+    return MTJG_OK;
+}
+
+// ILU.transApply (S/ILU.java:72-78): U'y = b, then L'x = y.  Built on first use.
+struct IluTrans {
+    int *ut_rp = nullptr, *ut_ci = nullptr;
+    double *ut_v = nullptr;
+    int *lt_rp = nullptr, *lt_ci = nullptr;
+    double *lt_v = nullptr;
+    LevelSchedule ut, lt;
+};
+
+}  // namespace mtjg
+
+using namespace mtjg;
+
+static void precond_release(mtjg_precond *M)
+{
+    cudaFree(M->invdiag);
+    cudaFree(M->rowptr);
+    cudaFree(M->colind);
+    cudaFree(M->diag);
+    cudaFree(M->data);
+    cudaFree(M->rt_rowptr);
+    cudaFree(M->rt_colind);
+    cudaFree(M->rt_val);
+    cudaFree(M->diagv);
+    free_sched(M->lo);
+    free_sched(M->up);
+    M->invdiag = M->data = M->rt_val = M->diagv = nullptr;
+    M->rowptr = M->colind = M->diag = M->rt_rowptr = M->rt_colind = nullptr;
+    if (M->trans) {
+        IluTrans *t = static_cast<IluTrans *>(M->trans);
+        cudaFree(t->ut_rp);
+        cudaFree(t->ut_ci);
+        cudaFree(t->ut_v);
+        cudaFree(t->lt_rp);
+        cudaFree(t->lt_ci);
+        cudaFree(t->lt_v);
+        free_sched(t->ut);
+        free_sched(t->lt);
+        delete t;
+        M->trans = nullptr;
+    }
+    M->ready = false;
+}
+
+extern "C" int mtjg_precond_create(mtjg_ctx *ctx, int kind, int n, mtjg_precond **out)
+{
+    if (!ctx || !out) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL argument");
+    *out = nullptr;
+    if (kind < MTJG_PC_IDENTITY || kind > MTJG_PC_ICC) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "unknown preconditioner");
+    if (n < 0) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "negative size");
+    MTJG_CUDA(cudaSetDevice(ctx->device));
+    mtjg_precond *M = new mtjg_precond();
+    M->ctx = ctx;
+    ctx_retain(ctx);
+    M->kind = kind;
+    M->n = n;
+    const size_t nb = sizeof(double) * (size_t)std::max(1, n);
+    if (cudaMalloc(&M->y, nb) != cudaSuccess || cudaMalloc(&M->d_b, nb) != cudaSuccess ||
+        cudaMalloc(&M->d_x, nb) != cudaSuccess) {
+        mtjg_precond_destroy(M);
+        return fail(MTJG_ERR_OUT_OF_MEMORY, "cudaMalloc failed for the preconditioner");
+    }
+    if (kind == MTJG_PC_IDENTITY) M->ready = true;
+    *out = M;
+    return MTJG_OK;
+}
+
+extern "C" int mtjg_precond_destroy(mtjg_precond *M)
+{
+    if (!M) return MTJG_OK;
+    cudaSetDevice(M->ctx->device);
+    cudaStreamSynchronize(M->ctx->stream);
+    precond_release(M);
+    cudaFree(M->y);
+    cudaFree(M->d_b);
+    cudaFree(M->d_x);
+    mtjg_ctx *ctx = M->ctx;
+    delete M;
+    ctx_release(ctx);
+    return MTJG_OK;
+}
+
+static int copy_pattern(mtjg_precond *M, mtjg_csr *A)
+{
+    const int n = A->n;
+    M->nnz = A->nnz;
+    MTJG_CUDA(cudaMalloc(&M->rowptr, sizeof(int) * (size_t)(n + 1)));
+    MTJG_CUDA(cudaMalloc(&M->colind, sizeof(int) * (size_t)(A->nnz + 4)));
+    MTJG_CUDA(cudaMalloc(&M->data, sizeof(double) * (size_t)(A->nnz + 2)));
+    MTJG_CUDA(cudaMalloc(&M->diag, sizeof(int) * (size_t)std::max(1, n)));
+    MTJG_CUDA(cudaMemcpyAsync(M->rowptr, A->rowptr, sizeof(int) * (size_t)(n + 1), cudaMemcpyDeviceToDevice,
+                              M->ctx->stream));
+    MTJG_CUDA(cudaMemcpyAsync(M->colind, A->colind, sizeof(int) * (size_t)(A->nnz + 4), cudaMemcpyDeviceToDevice,
+                              M->ctx->stream));
+    MTJG_CUDA(cudaMemcpyAsync(M->data, A->val, sizeof(double) * (size_t)(A->nnz + 2), cudaMemcpyDeviceToDevice,
+                              M->ctx->stream));
+    return MTJG_OK;
+}
+
+static int find_diagonal(mtjg_precond *M, int *err_row)
+{
+    mtjg_ctx *ctx = M->ctx;
+    int *err = ctx->d_flag + 1;
+    const int big = 0x7fffffff;
+    MTJG_CUDA(cudaMemcpyAsync(err, &big, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    if (M->n) {
+        k_find_diag<<<grid_for(ctx, M->n), kBlock, 0, ctx->stream>>>(M->n, M->rowptr, M->colind, M->diag, err);
+        ctx->launches++;
+    }
+    int e = big;
+    int st = read_err_min(ctx, err, &e);
+    if (st != MTJG_OK) return st;
+    if (e != big) {
+        *err_row = e;
+        return fail(MTJG_ERR_MISSING_DIAGONAL, "Missing diagonal entry on row " + std::to_string(e));
+    }
+    return MTJG_OK;
+}
+
+static int ilu_setup(mtjg_precond *M, int *err_row)
+{
+    mtjg_ctx *ctx = M->ctx;
+    const int n = M->n;
+    int st = find_diagonal(M, err_row);
+    if (st != MTJG_OK) return st;
+    unsigned char *quirk = nullptr;
+    MTJG_CUDA(cudaMalloc(&quirk, (size_t)std::max(1, n)));
+    if (n) {
+        k_ilu_quirk<<<grid_for(ctx, n), kBlock, 0, ctx->stream>>>(n, M->rowptr, M->colind, M->diag, quirk);
+        ctx->launches++;
+    }
+    LevelSchedule fac;
+    st = build_levels(ctx, n, 0, 1, M->rowptr, M->colind, M->diag, quirk, fac);
+    cudaFree(quirk);
+    if (st != MTJG_OK) return st;
+    int *err = ctx->d_flag + 1;
+    const int big = 0x7fffffff;
+    MTJG_CUDA(cudaMemcpyAsync(err, &big, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    for (int l = 0; l < fac.num_levels; ++l) {
+        const int beg = fac.level_ptr[l], cnt = fac.level_ptr[l + 1] - beg;
+        k_ilu_level<<<(cnt + kBlock - 1) / kBlock, kBlock, 0, ctx->stream>>>(fac.perm, beg, cnt, M->rowptr,
+                                                                            M->colind, M->diag, M->data, err);
+        ctx->launches++;
+    }
+    MTJG_CUDA(cudaGetLastError());
+    int e = big;
+    st = read_err_min(ctx, err, &e);
+    free_sched(fac);
+    if (st != MTJG_OK) return st;
+    if (e != big) {
+        *err_row = e;
+        return fail(MTJG_ERR_ZERO_PIVOT, "Zero pivot encountered on row " + std::to_string(e) + " during ILU process");
+    }
+    // solve schedules: L (rows ascending, lower range), U (descending, upper range)
+    st = build_levels(ctx, n, 0, 1, M->rowptr, M->colind, M->diag, nullptr, M->lo);
+    if (st != MTJG_OK) return st;
+    return build_levels(ctx, n, 1, 2, M->rowptr, M->colind, M->diag, nullptr, M->up);
+}
+
+static int icc_setup(mtjg_precond *M, mtjg_csr *A, int *err_row)
+{
+    mtjg_ctx *ctx = M->ctx;
+    const int n = M->n;
+    int st = find_diagonal(M, err_row);
+    if (st != MTJG_OK) return st;
+    // ICC.factor (S/ICC.java:85-139) runs on the host over the row reaches,
+    // then the factor returns to the device.
+    std::vector<int> ci((size_t)A->nnz), diag((size_t)n);
+    std::vector<double> data((size_t)A->nnz);
+    if (A->nnz) {
+        MTJG_CUDA(cudaMemcpy(ci.data(), A->colind, sizeof(int) * (size_t)A->nnz, cudaMemcpyDeviceToHost));
+        MTJG_CUDA(cudaMemcpy(data.data(), A->val, sizeof(double) * (size_t)A->nnz, cudaMemcpyDeviceToHost));
+    }
+    if (n) MTJG_CUDA(cudaMemcpy(diag.data(), M->diag, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost));
+    st = icc_factor_host(n, A->h_rowptr.data(), ci.data(), diag.data(), data.data(), err_row);
+    if (st != MTJG_OK) return st;
+    if (A->nnz)
+        MTJG_CUDA(cudaMemcpy(M->data, data.data(), sizeof(double) * (size_t)A->nnz, cudaMemcpyHostToDevice));
+    int64_t tn = 0;
+    st = csr_transpose(ctx, n, n, M->rowptr, M->colind, M->data, 1, &M->rt_rowptr, &M->rt_colind, &M->rt_val, &tn);
+    if (st != MTJG_OK) return st;
+    MTJG_CUDA(cudaMalloc(&M->diagv, sizeof(double) * (size_t)std::max(1, n)));
+    if (n) {
+        k_gather_diag<<<grid_for(ctx, n), kBlock, 0, ctx->stream>>>(n, M->diag, M->data, M->diagv);
+        ctx->launches++;
+    }
+    st = build_levels(ctx, n, 0, 0, M->rt_rowptr, M->rt_colind, nullptr, nullptr, M->lo);
+    if (st != MTJG_OK) return st;
+    return build_levels(ctx, n, 1, 2, M->rowptr, M->colind, M->diag, nullptr, M->up);
+}
+
+extern "C" int mtjg_precond_set_matrix(mtjg_precond *M, mtjg_csr *A, int *err_row)
+{
+    int dummy = 0;
+    if (!err_row) err_row = &dummy;
+    *err_row = 0;
+    if (!M || !A) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL argument");
+    if (A->ctx != M->ctx) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "matrix and preconditioner use different contexts");
+    if (M->kind == MTJG_PC_IDENTITY) return MTJG_OK;
+    if (A->n != M->n)
+        return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "Matrix size differs from preconditioner size");
+    if ((M->kind == MTJG_PC_ILU || M->kind == MTJG_PC_ICC) && A->n != A->m)
+        return fail(MTJG_ERR_ILLEGAL_ARGUMENT, M->kind == MTJG_PC_ILU ? "ILU only applies to square matrices"
+                                                                       : "ICC only applies to square matrices");
+    mtjg_ctx *ctx = M->ctx;
+    MTJG_CUDA(cudaSetDevice(ctx->device));
+    MTJG_CUDA(cudaStreamSynchronize(ctx->stream));
+    precond_release(M);
+    static int64_t s_version = 0;
+    M->version = ++s_version;
+    const int n = M->n;
+    if (M->kind == MTJG_PC_JACOBI) {
+        MTJG_CUDA(cudaMalloc(&M->invdiag, sizeof(double) * (size_t)std::max(1, n)));
+        int *err = ctx->d_flag + 1;
+        const int big = 0x7fffffff;
+        MTJG_CUDA(cudaMemcpyAsync(err, &big, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+        if (n) {
+            k_jacobi_set<<<grid_for(ctx, n), kBlock, 0, ctx->stream>>>(n, A->rowptr, A->colind, A->val, M->invdiag,
+                                                                       err);
+            ctx->launches++;
+        }
+        int e = big;
+        int st = read_err_min(ctx, err, &e);
+        if (st != MTJG_OK) return st;
+        if (e != big) {
+            *err_row = e;
+            return fail(MTJG_ERR_ZERO_DIAGONAL, "Zero diagonal on row " + std::to_string(e));
+        }
+        M->ready = true;
+        return MTJG_OK;
+    }
+    int st = copy_pattern(M, A);
+    if (st != MTJG_OK) return st;
+    st = M->kind == MTJG_PC_ILU ? ilu_setup(M, err_row) : icc_setup(M, A, err_row);
+    if (st != MTJG_OK) return st;
+    MTJG_CUDA(cudaStreamSynchronize(ctx->stream));
+    M->ready = true;
+    return MTJG_OK;
+}
+
+static int ilu_trans_setup(mtjg_precond *M)
+{
+    if (M->trans) return MTJG_OK;
+    mtjg_ctx *ctx = M->ctx;
+    IluTrans *t = new IluTrans();
+    M->trans = t;
+    int64_t tn = 0;
+    int st = csr_transpose(ctx, M->n, M->n, M->rowptr, M->colind, M->data, 1, &t->ut_rp, &t->ut_ci, &t->ut_v, &tn);
+    if (st != MTJG_OK) return st;
+    st = csr_transpose(ctx, M->n, M->n, M->rowptr, M->colind, M->data, 2, &t->lt_rp, &t->lt_ci, &t->lt_v, &tn);
+    if (st != MTJG_OK) return st;
+    if (!M->diagv) {
+        MTJG_CUDA(cudaMalloc(&M->diagv, sizeof(double) * (size_t)std::max(1, M->n)));
+        if (M->n) {
+            k_gather_diag<<<grid_for(ctx, M->n), kBlock, 0, ctx->stream>>>(M->n, M->diag, M->data, M->diagv);
+            ctx->launches++;
+        }
+    }
+    st = build_levels(ctx, M->n, 0, 0, t->ut_rp, t->ut_ci, nullptr, nullptr, t->ut);
+    if (st != MTJG_OK) return st;
+    return build_levels(ctx, M->n, 1, 0, t->lt_rp, t->lt_ci, nullptr, nullptr, t->lt);
+}
+
+static int precond_trans_apply_dev(mtjg_precond *M, const double *b, double *x)
+{
+    if (M->kind != MTJG_PC_ILU) return precond_apply_dev(M, b, x, nullptr);
+    int st = ilu_trans_setup(M);
+    if (st != MTJG_OK) return st;
+    IluTrans *t = static_cast<IluTrans *>(M->trans);
+    cudaError_t e = run_levels(M->ctx, 2, t->ut, t->ut_rp, t->ut_ci, t->ut_v, nullptr, M->diagv, b, M->y, nullptr);
+    if (e == cudaSuccess) e = run_levels(M->ctx, 3, t->lt, t->lt_rp, t->lt_ci, t->lt_v, nullptr, nullptr, M->y, x, nullptr);
+    if (e != cudaSuccess) return cuda_fail(e, "ILU transApply");
+    return MTJG_OK;
+}
+
+static int precond_host_call(mtjg_precond *M, const double *b, double *x, bool trans)
+{
+    if (!M || (!b && M->n) || (!x && M->n)) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL argument");
+    if (!M->ready) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "setMatrix has not been called");
+    mtjg_ctx *ctx = M->ctx;
+    MTJG_CUDA(cudaSetDevice(ctx->device));
+    const size_t nb = sizeof(double) * (size_t)M->n;
+    if (M->n == 0) return MTJG_OK;
+    MTJG_CUDA(cudaMemcpyAsync(M->d_b, b, nb, cudaMemcpyHostToDevice, ctx->stream));
+    int st = trans ? precond_trans_apply_dev(M, M->d_b, M->d_x) : precond_apply_dev(M, M->d_b, M->d_x, nullptr);
+    if (st != MTJG_OK) return st;
+    MTJG_CUDA(cudaMemcpyAsync(x, M->d_x, nb, cudaMemcpyDeviceToHost, ctx->stream));
+    MTJG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return MTJG_OK;
+}
+
+extern "C" int mtjg_precond_apply(mtjg_precond *M, const double *b, double *x)
+{
+    return precond_host_call(M, b, x, false);
+}
+
+extern "C" int mtjg_precond_trans_apply(mtjg_precond *M, const double *b, double *x)
+{
+    return precond_host_call(M, b, x, true);
+}
+
+extern "C" int mtjg_precond_apply_dev(mtjg_precond *M, const double *db, double *dx)
+{
+    if (!M || !db || !dx) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL argument");
+    if (!M->ready) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "setMatrix has not been called");
+    MTJG_CUDA(cudaSetDevice(M->ctx->device));
+    return precond_apply_dev(M, db, dx, nullptr);
+}
+
+extern "C" int mtjg_precond_values(mtjg_precond *M, double *out, int64_t cap, int64_t *len)
+{
+    if (!M) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL preconditioner");
+    MTJG_CUDA(cudaSetDevice(M->ctx->device));
+    MTJG_CUDA(cudaStreamSynchronize(M->ctx->stream));
+    int64_t total = 0;
+    const double *src = nullptr;
+    if (M->kind == MTJG_PC_JACOBI) {
+        total = M->invdiag ? M->n : 0;
+        src = M->invdiag;
+    } else if (M->kind == MTJG_PC_ILU || M->kind == MTJG_PC_ICC) {
+        total = M->data ? M->nnz : 0;
+        src = M->data;
+    }
+    if (len) *len = total;
+    const int64_t m = std::min(total, cap);
+    if (m > 0 && out) MTJG_CUDA(cudaMemcpy(out, src, sizeof(double) * (size_t)m, cudaMemcpyDeviceToHost));
+    return MTJG_OK;
+}

@@ -1,0 +1,1087 @@
+// solver.cu -- CG, BiCGstab and GMRES(m) (S/CG.java, S/BiCGstab.java,
+// S/GMRES.java) as fused device phases.
+//
+// Every phase is one kernel over the matrix's row tiles: a CSR product with
+// a fused epilogue or a row kernel, whose per-tile partial sums are reduced
+// in tile order by the last tile to finish; that tile also runs the phase's
+// scalar step (alpha, beta, omega, Givens rotations, the iteration monitor)
+// on the device.  The host never reads a scalar during a solve: the loop
+// body is captured once into a CUDA graph, replayed in chunks, and every
+// kernel of a finished solve returns at once.  The host only polls the
+// status word between chunks.
+#include <algorithm>
+#include <cstring>
+
+#include "spmv.cuh"
+
+namespace mtjg {
+
+int precond_apply_dev(mtjg_precond *M, const double *b, double *x, const int *status);
+
+constexpr int kPcIdentity = 0, kPcJacobi = 1, kPcExternal = 2;
+
+struct MonPtrs {
+    SysState *st;
+    MonCfgDev mon;
+    double *hr;
+    int *hi;
+    int *num_running;
+    __device__ __forceinline__ void finish(SysState &t, int code) const
+    {
+        t.status = code;
+        t.gate = code == ST_RUNNING ? ST_RUNNING : 1;
+        if (code != ST_RUNNING) atomicSub(num_running, 1);
+    }
+    __device__ __forceinline__ int check(SysState &t, int sys, double r) const
+    {
+        return monitor_check(t, mon, r, hr + (size_t)sys * mon.hist_cap, hi + (size_t)sys * mon.hist_cap);
+    }
+};
+
+// ================================================================== CG
+// S/CG.java:58-87.  pc == kPcExternal (ILU/ICC): z = M r runs as its own
+// kernels between the monitor test and CgDot.
+template <bool S>
+struct CgInit {  // r = b - A x (A.multAdd(-1, x, r.set(b)), :64); fused z = M r and r.z
+    const double *b;
+    double *r, *z;
+    const double *invdiag;
+    int pc;
+    MonPtrs m;
+    static constexpr bool kReduce = true;
+    __device__ bool active(int) const { return true; }
+    __device__ double init(int, int) const { return 0.0; }
+    __device__ void row(int i, int, double d, Acc &a) const
+    {
+        const double rr = b[i] - d;
+        r[i] = rr;
+        norm_add<S>(a, rr, m.mon.norm);
+        if (pc == kPcJacobi) {
+            const double zz = rr * invdiag[i];
+            z[i] = zz;
+            a.v[2] = fmac<S>(rr, zz, a.v[2]);
+        } else if (pc == kPcIdentity) {
+            a.v[2] = fmac<S>(rr, rr, a.v[2]);
+        }
+    }
+    __device__ void scalar(int sys, const Acc &s)
+    {
+        SysState &t = m.st[sys];
+        t.iter = 0;
+        const int c = m.check(t, sys, norm_finish(s.v, m.mon.norm));
+        if (c == ST_RUNNING && pc != kPcExternal) t.rho = s.v[2];
+        m.finish(t, c);
+    }
+};
+
+template <bool S>
+struct CgP {  // p = z (first) or p = beta*p + z (p.scale(beta).add(z), :70-75)
+    double *p;
+    const double *z;
+    SysState *st;
+    static constexpr bool kReduce = false;
+    __device__ bool active(int sys) const { return st[sys].status == ST_RUNNING; }
+    __device__ void row(int i, int sys, Acc &) const
+    {
+        const SysState &t = st[sys];
+        p[i] = t.iter == 0 ? z[i] : fmac<S>(p[i], t.beta, z[i]);
+    }
+    __device__ void scalar(int, const Acc &) {}
+};
+
+template <bool S>
+struct CgQ {  // q = A p; alpha = rho / p.q (:77-78)
+    const double *p;
+    double *q;
+    SysState *st;
+    static constexpr bool kReduce = true;
+    __device__ bool active(int sys) const { return st[sys].status == ST_RUNNING; }
+    __device__ double init(int, int) const { return 0.0; }
+    __device__ void row(int i, int, double d, Acc &a) const
+    {
+        const double qq = d != 0.0 ? d : 0.0;
+        q[i] = qq;
+        a.v[2] = fmac<S>(p[i], qq, a.v[2]);
+    }
+    __device__ void scalar(int sys, const Acc &s)
+    {
+        SysState &t = st[sys];
+        t.alpha = t.rho / s.v[2];
+    }
+};
+
+template <bool S>
+struct CgUpd {  // x += alpha p; r -= alpha q; next monitor test; fused z = M r, r.z (:80-83, :66-68)
+    double *x, *r, *z;
+    const double *p, *q, *invdiag;
+    int pc;
+    MonPtrs m;
+    static constexpr bool kReduce = true;
+    __device__ bool active(int sys) const { return m.st[sys].status == ST_RUNNING; }
+    __device__ void row(int i, int sys, Acc &a) const
+    {
+        const double al = m.st[sys].alpha;
+        double rr = r[i];
+        if (al != 0) {
+            x[i] = fmac<S>(al, p[i], x[i]);
+            rr = fmac<S>(-al, q[i], rr);
+            r[i] = rr;
+        }
+        norm_add<S>(a, rr, m.mon.norm);
+        if (pc == kPcJacobi) {
+            const double zz = rr * invdiag[i];
+            z[i] = zz;
+            a.v[2] = fmac<S>(rr, zz, a.v[2]);
+        } else if (pc == kPcIdentity) {
+            a.v[2] = fmac<S>(rr, rr, a.v[2]);
+        }
+    }
+    __device__ void scalar(int sys, const Acc &s)
+    {
+        SysState &t = m.st[sys];
+        t.rho_1 = t.rho;
+        t.iter++;
+        const int c = m.check(t, sys, norm_finish(s.v, m.mon.norm));
+        if (c == ST_RUNNING && pc != kPcExternal) {
+            t.rho = s.v[2];
+            t.beta = t.rho / t.rho_1;
+        }
+        m.finish(t, c);
+    }
+};
+
+template <bool S>
+struct CgDot {  // rho = r.z after an external preconditioner (:68, :73)
+    const double *r, *z;
+    SysState *st;
+    static constexpr bool kReduce = true;
+    __device__ bool active(int sys) const { return st[sys].status == ST_RUNNING; }
+    __device__ void row(int i, int, Acc &a) const { a.v[2] = fmac<S>(r[i], z[i], a.v[2]); }
+    __device__ void scalar(int sys, const Acc &s)
+    {
+        SysState &t = st[sys];
+        t.rho = s.v[2];
+        if (t.iter > 0) t.beta = t.rho / t.rho_1;
+    }
+};
+
+// ============================================================ BiCGstab
+// S/BiCGstab.java:65-116
+__device__ __forceinline__ void bicg_breakdown(SysState &t, int &c)
+{
+    if (t.rho_1 == 0) {
+        c = MTJG_NOT_CONVERGED_BREAKDOWN;
+        t.detail = 1;
+    } else if (t.omega == 0) {
+        c = MTJG_NOT_CONVERGED_BREAKDOWN;
+        t.detail = 2;
+    }
+}
+
+template <bool S>
+struct BiInit {  // r = b - A x; rtilde = r (:71-72); first test; rho_1 = rtilde.r (:75)
+    const double *b;
+    double *r, *rt;
+    MonPtrs m;
+    static constexpr bool kReduce = true;
+    __device__ bool active(int) const { return true; }
+    __device__ double init(int, int) const { return 0.0; }
+    __device__ void row(int i, int, double d, Acc &a) const
+    {
+        const double rr = b[i] - d;
+        r[i] = rr;
+        rt[i] = rr;
+        norm_add<S>(a, rr, m.mon.norm);
+        a.v[2] = fmac<S>(rr, rr, a.v[2]);
+    }
+    __device__ void scalar(int sys, const Acc &s)
+    {
+        SysState &t = m.st[sys];
+        t.iter = 0;
+        int c = m.check(t, sys, norm_finish(s.v, m.mon.norm));
+        if (c == ST_RUNNING) {
+            t.rho_1 = s.v[2];
+            bicg_breakdown(t, c);
+        }
+        m.finish(t, c);
+    }
+};
+
+template <bool S>
+struct BiP {  // p = r (first) or p = r + beta (p - omega v) (:85-95); fused phat = M p
+    double *p, *phat;
+    const double *r, *v, *invdiag;
+    int pc;
+    SysState *st;
+    static constexpr bool kReduce = false;
+    __device__ bool active(int sys) const { return st[sys].status == ST_RUNNING; }
+    __device__ void row(int i, int sys, Acc &) const
+    {
+        const SysState &t = st[sys];
+        double pp;
+        if (t.iter == 0) {
+            pp = r[i];
+        } else {
+            const double tmp = fmac<S>(-t.omega, v[i], p[i]);
+            pp = t.beta != 0 ? fmac<S>(t.beta, tmp, r[i]) : r[i];
+        }
+        p[i] = pp;
+        if (pc == kPcJacobi) phat[i] = pp * invdiag[i];
+    }
+    __device__ void scalar(int, const Acc &) {}
+};
+
+template <bool S>
+struct BiV {  // v = A phat; alpha = rho_1 / rtilde.v (:98-99)
+    double *v;
+    const double *rt;
+    SysState *st;
+    static constexpr bool kReduce = true;
+    __device__ bool active(int sys) const { return st[sys].status == ST_RUNNING; }
+    __device__ double init(int, int) const { return 0.0; }
+    __device__ void row(int i, int, double d, Acc &a) const
+    {
+        const double vv = d != 0.0 ? d : 0.0;
+        v[i] = vv;
+        a.v[2] = fmac<S>(rt[i], vv, a.v[2]);
+    }
+    __device__ void scalar(int sys, const Acc &s)
+    {
+        SysState &t = st[sys];
+        t.alpha = t.rho_1 / s.v[2];
+    }
+};
+
+template <bool S>
+struct BiS {  // s = r - alpha v; x += alpha phat; test on s (:100-104); fused shat = M s
+    double *s, *x, *shat;
+    const double *r, *v, *phat, *invdiag;
+    int pc;
+    MonPtrs m;
+    static constexpr bool kReduce = true;
+    __device__ bool active(int sys) const { return m.st[sys].status == ST_RUNNING; }
+    __device__ void row(int i, int sys, Acc &a) const
+    {
+        const double al = m.st[sys].alpha;
+        double ss = r[i];
+        if (al != 0) {
+            ss = fmac<S>(-al, v[i], ss);
+            x[i] = fmac<S>(al, phat[i], x[i]);
+        }
+        s[i] = ss;
+        norm_add<S>(a, ss, m.mon.norm);
+        if (pc == kPcJacobi) shat[i] = ss * invdiag[i];
+    }
+    __device__ void scalar(int sys, const Acc &sm)
+    {
+        SysState &t = m.st[sys];
+        m.finish(t, m.check(t, sys, norm_finish(sm.v, m.mon.norm)));
+    }
+};
+
+template <bool S>
+struct BiT {  // t = A shat; omega = t.s / t.t (:107-108)
+    double *t;
+    const double *s;
+    SysState *st;
+    static constexpr bool kReduce = true;
+    __device__ bool active(int sys) const { return st[sys].status == ST_RUNNING; }
+    __device__ double init(int, int) const { return 0.0; }
+    __device__ void row(int i, int, double d, Acc &a) const
+    {
+        const double tt = d != 0.0 ? d : 0.0;
+        t[i] = tt;
+        a.v[2] = fmac<S>(tt, s[i], a.v[2]);
+        a.v[3] = fmac<S>(tt, tt, a.v[3]);
+    }
+    __device__ void scalar(int sys, const Acc &sm)
+    {
+        SysState &q = st[sys];
+        q.omega = sm.v[2] / sm.v[3];
+    }
+};
+
+template <bool S>
+struct BiR {  // x += omega shat; r = s - omega t (:109-110); next test; rho_1, breakdown, beta
+    double *x, *r;
+    const double *s, *shat, *t, *rt;
+    MonPtrs m;
+    static constexpr bool kReduce = true;
+    __device__ bool active(int sys) const { return m.st[sys].status == ST_RUNNING; }
+    __device__ void row(int i, int sys, Acc &a) const
+    {
+        const double w = m.st[sys].omega;
+        double rr = s[i];
+        if (w != 0) {
+            x[i] = fmac<S>(w, shat[i], x[i]);
+            rr = fmac<S>(-w, t[i], rr);
+        }
+        r[i] = rr;
+        norm_add<S>(a, rr, m.mon.norm);
+        a.v[2] = fmac<S>(rt[i], rr, a.v[2]);
+    }
+    __device__ void scalar(int sys, const Acc &sm)
+    {
+        SysState &q = m.st[sys];
+        q.rho_2 = q.rho_1;
+        q.iter++;
+        int c = m.check(q, sys, norm_finish(sm.v, m.mon.norm));
+        if (c == ST_RUNNING) {
+            q.rho_1 = sm.v[2];
+            bicg_breakdown(q, c);
+            if (c == ST_RUNNING) q.beta = (q.rho_1 / q.rho_2) * (q.alpha / q.omega);
+        }
+        m.finish(q, c);
+    }
+};
+
+// =============================================================== GMRES
+// S/GMRES.java:127-176, GivensRotation M/GivensRotation.java:42-92.  The
+// scalar work (Hessenberg column, rotations, triangular solve) runs on one
+// thread with every product and sum rounded separately, as in Java.
+struct GmData {
+    double *H;   // (restart+1) x restart, column-major, ld = restart+1
+    double *s;   // restart+1
+    double *gc, *gs;  // rotations
+    int restart;
+};
+
+__device__ __forceinline__ double jmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double jadd(double a, double b) { return __dadd_rn(a, b); }
+
+__device__ void givens_make(double x, double y, double &c, double &s)
+{
+    const double roe = fabs(x) > fabs(y) ? x : y;
+    const double scale = jadd(fabs(x), fabs(y));
+    if (scale != 0) {
+        const double xs = x / scale, ys = y / scale;
+        double r = jmul(scale, sqrt(jadd(jmul(xs, xs), jmul(ys, ys))));
+        if (roe < 0) r = -r;
+        c = x / r;
+        s = y / r;
+    } else {
+        c = 1;
+        s = 0;
+    }
+}
+
+__device__ __forceinline__ void givens_apply(double c, double s, double &a1, double &a2)
+{
+    const double temp = jadd(jmul(c, a1), jmul(s, a2));
+    a2 = jadd(jmul(-s, a1), jmul(c, a2));
+    a1 = temp;
+}
+
+// residual phase: u = b - A x
+struct GmU {
+    const double *b;
+    double *u;
+    SysState *st;
+    bool always;
+    static constexpr bool kReduce = false;
+    __device__ bool active(int sys) const { return always || st[sys].status == ST_RUNNING; }
+    __device__ double init(int, int) const { return 0.0; }
+    __device__ void row(int i, int, double d, Acc &) const { u[i] = b[i] - d; }
+    __device__ void scalar(int, const Acc &) {}
+};
+
+// inner step product u = A v_i (A.mult, :146), while the inner loop runs
+struct GmAv {
+    double *u;
+    SysState *st;
+    static constexpr bool kReduce = false;
+    __device__ bool active(int sys) const { return st[sys].gate == ST_RUNNING; }
+    __device__ double init(int, int) const { return 0.0; }
+    __device__ void row(int i, int, double d, Acc &) const { u[i] = d != 0.0 ? d : 0.0; }
+    __device__ void scalar(int, const Acc &) {}
+};
+
+// norms of r = M u: the monitor's norm and ||r||2; outer test (:133, :137,
+// :172); on running, a new cycle: s = [normr, 0...], inner test on |s_0| (:144)
+template <bool S>
+struct GmNorm {
+    const double *r;
+    MonPtrs m;
+    GmData g;
+    bool first;
+    static constexpr bool kReduce = true;
+    __device__ bool active(int sys) const { return first || m.st[sys].status == ST_RUNNING; }
+    __device__ void row(int i, int, Acc &a) const
+    {
+        const double rr = r[i];
+        norm_add<S>(a, rr, m.mon.norm);
+        a.v[2] = fmac<S>(rr, rr, a.v[2]);
+    }
+    __device__ void scalar(int sys, const Acc &sm)
+    {
+        SysState &t = m.st[sys];
+        if (first) t.iter = 0;
+        else t.iter++;
+        t.normr = sqrt(sm.v[2]);
+        int c = m.check(t, sys, norm_finish(sm.v, m.mon.norm));
+        if (c == ST_RUNNING) {
+            for (int k = 0; k <= g.restart; ++k) g.s[k] = 0.0;
+            g.s[0] = t.normr;
+            t.inner = 0;
+            t.inner_done = 0;
+            t.scratch[0] = 1 / t.normr;  // v[0].set(1 / normr, r)
+            if (g.restart > 0) {
+                c = m.check(t, sys, fabs(g.s[0]));
+                if (c == ST_DONE) {
+                    t.inner_done = 1;
+                    c = ST_RUNNING;
+                }
+            } else {
+                t.inner_done = 1;
+            }
+        }
+        m.finish(t, c);
+        if (c == ST_RUNNING && t.inner_done) t.gate = 1;
+    }
+};
+
+// v_{k} = alpha * w (DenseVector.set(alpha, y): alpha == 0 zeroes, M/DenseVector.java:216-231)
+template <bool S>
+struct GmScale {
+    double *v;
+    const double *w;
+    SysState *st;
+    bool gated;  // use the inner gate (v_{i+1}) or the status (v_0)
+    static constexpr bool kReduce = false;
+    __device__ bool active(int sys) const { return gated ? st[sys].gate == ST_RUNNING : st[sys].status == ST_RUNNING; }
+    __device__ void row(int i, int sys, Acc &) const
+    {
+        const double al = st[sys].scratch[0];
+        v[i] = al == 0 ? 0.0 : al * w[i];
+    }
+    __device__ void scalar(int, const Acc &) {}
+};
+
+// Modified Gram-Schmidt pass k of inner step i (:149-153): w -= H[k-1,i] v_{k-1}
+// (k > 0), then H[k,i] = w.v_k (k <= i) or H[i+1,i] = ||w||2 (k == i+1);
+// the last pass also rotates column i and s and runs the next inner test.
+template <bool S>
+struct GmMgs {
+    double *w;
+    const double *vprev, *vk;
+    int i, k;
+    MonPtrs m;
+    GmData g;
+    static constexpr bool kReduce = true;
+    __device__ bool active(int sys) const { return m.st[sys].gate == ST_RUNNING; }
+    __device__ void row(int r, int, Acc &a) const
+    {
+        double wr = w[r];
+        if (k > 0) {
+            const double h = g.H[(k - 1) + (size_t)i * (g.restart + 1)];
+            if (-h != 0) {
+                wr = fmac<S>(-h, vprev[r], wr);
+                w[r] = wr;
+            }
+        }
+        if (k <= i) a.v[2] = fmac<S>(wr, vk[r], a.v[2]);
+        else a.v[2] = fmac<S>(wr, wr, a.v[2]);
+    }
+    __device__ void scalar(int sys, const Acc &sm)
+    {
+        SysState &t = m.st[sys];
+        const int ld = g.restart + 1;
+        double *Hc = g.H + (size_t)i * ld;
+        if (k <= i) {
+            Hc[k] = sm.v[2];
+            return;
+        }
+        Hc[i + 1] = sqrt(sm.v[2]);
+        t.scratch[0] = 1. / Hc[i + 1];
+        for (int q = 0; q < i; ++q) givens_apply(g.gc[q], g.gs[q], Hc[q], Hc[q + 1]);
+        givens_make(Hc[i], Hc[i + 1], g.gc[i], g.gs[i]);
+        givens_apply(g.gc[i], g.gs[i], Hc[i], Hc[i + 1]);
+        givens_apply(g.gc[i], g.gs[i], g.s[i], g.s[i + 1]);
+        t.iter++;
+        t.inner = i + 1;
+        int c = ST_RUNNING;
+        if (i + 1 < g.restart) {
+            c = m.check(t, sys, fabs(g.s[i + 1]));
+            if (c == ST_DONE) {
+                t.inner_done = 1;
+                c = ST_RUNNING;
+            }
+        } else {
+            t.inner_done = 1;
+        }
+        m.finish(t, c);
+        if (c == ST_RUNNING && t.inner_done) t.gate = 1;
+    }
+};
+
+// new UpperTriangDenseMatrix(H, i, false).solve(s, s) (:166): LAPACK dtrtrs
+// semantics -- info = first zero diagonal (MatrixSingularException), else the
+// reference dtrsm column sweep k = i-1..0 skipping zero entries of s.
+__global__ void k_gmres_trsv(SysState *st, GmData g, int *num_running)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    SysState &t = st[0];
+    if (t.status != ST_RUNNING) return;
+    const int n = t.inner, ld = g.restart + 1;
+    for (int k = 0; k < n; ++k)
+        if (g.H[k + (size_t)k * ld] == 0) {
+            t.status = MTJG_ERR_SINGULAR;
+            t.gate = 1;
+            atomicSub(num_running, 1);
+            return;
+        }
+    for (int k = n - 1; k >= 0; --k) {
+        if (g.s[k] != 0) {
+            g.s[k] = g.s[k] / g.H[k + (size_t)k * ld];
+            for (int q = 0; q < k; ++q) g.s[q] = jadd(g.s[q], -jmul(g.s[k], g.H[q + (size_t)k * ld]));
+        }
+    }
+}
+
+// x += s_j v_j for j < i, in order (:167-168)
+template <bool S>
+struct GmX {
+    double *x;
+    const double *V;
+    size_t ldv;
+    GmData g;
+    SysState *st;
+    static constexpr bool kReduce = false;
+    __device__ bool active(int sys) const { return st[sys].status == ST_RUNNING; }
+    __device__ void row(int r, int sys, Acc &) const
+    {
+        const int n = st[sys].inner;
+        double xr = x[r];
+        for (int j = 0; j < n; ++j) {
+            const double sj = g.s[j];
+            if (sj != 0) xr = fmac<S>(sj, V[(size_t)j * ldv + r], xr);
+        }
+        x[r] = xr;
+    }
+    __device__ void scalar(int, const Acc &) {}
+};
+
+}  // namespace mtjg
+
+using namespace mtjg;
+
+// ================================================================ handle
+struct mtjg_solver {
+    mtjg_ctx *ctx = nullptr;
+    int kind = MTJG_CG;
+    int n = 0;
+    int restart = 30;
+    mtjg_precond *M = nullptr;
+    mtjg_monitor mon{};
+    SysState *st = nullptr;
+    double *hist_r = nullptr;
+    int *hist_it = nullptr;
+    int hist_alloc = 0;
+    std::vector<double *> vecs;
+    double *V = nullptr;
+    GmData gm{};
+    // graph of one chunk of the loop body
+    cudaGraphExec_t gexec = nullptr;
+    const mtjg_csr *g_A = nullptr;
+    const mtjg_precond *g_M = nullptr;
+    int g_numerics = -1;
+    int g_norm = -1;
+    int64_t g_version = 0;
+    int g_kernels = 0;
+    int chunk = 16;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    SysState last{};
+    int last_valid = 0;
+};
+
+namespace {
+
+enum { V_B = 0, V_X, V_R, V_Z, V_P, V_Q, V_RT, V_PH, V_S, V_SH, V_T, V_V, V_U, V_W, V_COUNT };
+
+MonCfgDev mon_dev(const mtjg_solver *S)
+{
+    MonCfgDev c;
+    c.max_iter = S->mon.max_iter;
+    c.norm = S->mon.norm;
+    c.hist_cap = S->mon.history_cap;
+    c.pad = 0;
+    c.rtol = S->mon.rtol;
+    c.atol = S->mon.atol;
+    c.dtol = S->mon.dtol;
+    return c;
+}
+
+int pc_mode(const mtjg_solver *S)
+{
+    if (!S->M || S->M->kind == MTJG_PC_IDENTITY) return kPcIdentity;
+    if (S->M->kind == MTJG_PC_JACOBI) return kPcJacobi;
+    return kPcExternal;
+}
+
+template <bool STRICT>
+struct Phases {
+    mtjg_solver *S;
+    mtjg_csr *A;
+    MonPtrs mp() const
+    {
+        return MonPtrs{S->st, mon_dev(S), S->hist_r, S->hist_it, A->num_running};
+    }
+    CsrArgs csr() const { return CsrArgs{A->rowptr, A->colind, A->val}; }
+    RedCtx rc() const { return red_ctx(A, A->tiles); }
+    double *v(int k) const { return S->vecs[k]; }
+    const double *invdiag() const { return S->M && S->M->kind == MTJG_PC_JACOBI ? S->M->invdiag : nullptr; }
+    int norm() const { return S->mon.norm; }
+
+    // apply M (b -> x) with a gate word; identity with x == b does nothing
+    int pc(const double *b, double *x, const int *gate)
+    {
+        if (!S->M || S->M->kind == MTJG_PC_IDENTITY) {
+            if (x == b) return MTJG_OK;
+            mtjg_precond tmp;
+            tmp.ctx = S->ctx;
+            tmp.kind = MTJG_PC_IDENTITY;
+            tmp.n = S->n;
+            return precond_apply_dev(&tmp, b, x, gate);
+        }
+        return precond_apply_dev(S->M, b, x, gate);
+    }
+
+#define PH_CHECK(e)                                                \
+    do {                                                           \
+        cudaError_t e__ = (e);                                     \
+        if (e__ != cudaSuccess) return cuda_fail(e__, "solver phase"); \
+    } while (0)
+
+    // ---- CG
+    int cg_init()
+    {
+        const int pcm = pc_mode(S);
+        double *z = pcm == kPcIdentity ? v(V_R) : v(V_Z);
+        PH_CHECK(launch_spmv(S->ctx, csr(), A->tiles, v(V_X),
+                             CgInit<STRICT>{v(V_B), v(V_R), z, invdiag(), pcm, mp()}, rc(), norm()));
+        return MTJG_OK;
+    }
+    int cg_body()
+    {
+        const int pcm = pc_mode(S);
+        double *z = pcm == kPcIdentity ? v(V_R) : v(V_Z);
+        if (pcm == kPcExternal) {
+            int st = pc(v(V_R), z, &S->st->status);
+            if (st != MTJG_OK) return st;
+            PH_CHECK(launch_rows(S->ctx, A->tiles, CgDot<STRICT>{v(V_R), z, S->st}, rc(), norm()));
+        }
+        PH_CHECK(launch_rows(S->ctx, A->tiles, CgP<STRICT>{v(V_P), z, S->st}, rc(), norm()));
+        PH_CHECK(launch_spmv(S->ctx, csr(), A->tiles, v(V_P), CgQ<STRICT>{v(V_P), v(V_Q), S->st}, rc(), norm()));
+        PH_CHECK(launch_rows(S->ctx, A->tiles,
+                             CgUpd<STRICT>{v(V_X), v(V_R), z, v(V_P), v(V_Q), invdiag(), pcm, mp()}, rc(), norm()));
+        return MTJG_OK;
+    }
+
+    // ---- BiCGstab
+    int bi_init()
+    {
+        PH_CHECK(launch_spmv(S->ctx, csr(), A->tiles, v(V_X), BiInit<STRICT>{v(V_B), v(V_R), v(V_RT), mp()}, rc(),
+                             norm()));
+        return MTJG_OK;
+    }
+    int bi_body()
+    {
+        const int pcm = pc_mode(S);
+        double *phat = pcm == kPcIdentity ? v(V_P) : v(V_PH);
+        double *shat = pcm == kPcIdentity ? v(V_S) : v(V_SH);
+        PH_CHECK(launch_rows(S->ctx, A->tiles,
+                             BiP<STRICT>{v(V_P), phat, v(V_R), v(V_V), invdiag(), pcm, S->st}, rc(), norm()));
+        if (pcm == kPcExternal) {
+            int st = pc(v(V_P), phat, &S->st->status);
+            if (st != MTJG_OK) return st;
+        }
+        PH_CHECK(launch_spmv(S->ctx, csr(), A->tiles, phat, BiV<STRICT>{v(V_V), v(V_RT), S->st}, rc(), norm()));
+        PH_CHECK(launch_rows(S->ctx, A->tiles,
+                             BiS<STRICT>{v(V_S), v(V_X), shat, v(V_R), v(V_V), phat, invdiag(), pcm, mp()}, rc(),
+                             norm()));
+        if (pcm == kPcExternal) {
+            int st = pc(v(V_S), shat, &S->st->status);
+            if (st != MTJG_OK) return st;
+        }
+        PH_CHECK(launch_spmv(S->ctx, csr(), A->tiles, shat, BiT<STRICT>{v(V_T), v(V_S), S->st}, rc(), norm()));
+        PH_CHECK(launch_rows(S->ctx, A->tiles,
+                             BiR<STRICT>{v(V_X), v(V_R), v(V_S), shat, v(V_T), v(V_RT), mp()}, rc(), norm()));
+        return MTJG_OK;
+    }
+
+    // ---- GMRES
+    double *basis(int k) const { return S->V + (size_t)k * (size_t)S->n; }
+    int gm_residual(bool first)
+    {
+        const int pcm = pc_mode(S);
+        double *u = v(V_U);
+        double *r = pcm == kPcIdentity ? u : v(V_R);
+        PH_CHECK(launch_spmv(S->ctx, csr(), A->tiles, v(V_X), GmU{v(V_B), u, S->st, first}, rc(), norm()));
+        if (pcm != kPcIdentity) {
+            int st = pc(u, r, first ? nullptr : &S->st->status);
+            if (st != MTJG_OK) return st;
+        }
+        PH_CHECK(launch_rows(S->ctx, A->tiles, GmNorm<STRICT>{r, mp(), S->gm, first}, rc(), norm()));
+        return MTJG_OK;
+    }
+    int gm_init() { return gm_residual(true); }
+    int gm_body()
+    {
+        const int pcm = pc_mode(S);
+        double *u = v(V_U);
+        double *r = pcm == kPcIdentity ? u : v(V_R);
+        double *w = pcm == kPcIdentity ? u : v(V_W);
+        // v_0 = r / normr
+        PH_CHECK(launch_rows(S->ctx, A->tiles, GmScale<STRICT>{basis(0), r, S->st, false}, rc(), norm()));
+        for (int i = 0; i < S->restart; ++i) {
+            PH_CHECK(launch_spmv(S->ctx, csr(), A->tiles, basis(i), GmAv{u, S->st}, rc(), norm()));
+            if (pcm != kPcIdentity) {
+                int st = pc(u, w, &S->st->gate);
+                if (st != MTJG_OK) return st;
+            }
+            for (int k = 0; k <= i + 1; ++k) {
+                const double *vprev = k > 0 ? basis(k - 1) : nullptr;
+                const double *vk = k <= i ? basis(k) : nullptr;
+                PH_CHECK(launch_rows(S->ctx, A->tiles, GmMgs<STRICT>{w, vprev, vk, i, k, mp(), S->gm}, rc(),
+                                     norm()));
+            }
+            PH_CHECK(launch_rows(S->ctx, A->tiles, GmScale<STRICT>{basis(i + 1), w, S->st, true}, rc(), norm()));
+        }
+        k_gmres_trsv<<<1, 32, 0, S->ctx->stream>>>(S->st, S->gm, A->num_running);
+        S->ctx->launches++;
+        PH_CHECK(cudaGetLastError());
+        PH_CHECK(launch_rows(S->ctx, A->tiles, GmX<STRICT>{v(V_X), S->V, (size_t)S->n, S->gm, S->st}, rc(), norm()));
+        return gm_residual(false);
+    }
+};
+
+}  // namespace
+
+// ======================================================== orchestration
+namespace {
+
+void drop_graph(mtjg_solver *S)
+{
+    if (S->gexec) cudaGraphExecDestroy(S->gexec);
+    S->gexec = nullptr;
+    S->g_A = nullptr;
+    S->g_M = nullptr;
+}
+
+template <bool STRICT>
+int run_phase(mtjg_solver *S, mtjg_csr *A, bool init)
+{
+    Phases<STRICT> ph{S, A};
+    if (S->kind == MTJG_CG) return init ? ph.cg_init() : ph.cg_body();
+    if (S->kind == MTJG_BICGSTAB) return init ? ph.bi_init() : ph.bi_body();
+    return init ? ph.gm_init() : ph.gm_body();
+}
+
+int phase(mtjg_solver *S, mtjg_csr *A, bool init)
+{
+    return S->ctx->numerics == MTJG_NUMERICS_STRICT ? run_phase<true>(S, A, init) : run_phase<false>(S, A, init);
+}
+
+int capture(mtjg_solver *S, mtjg_csr *A)
+{
+    mtjg_ctx *ctx = S->ctx;
+    drop_graph(S);
+    const int64_t before = ctx->launches;
+    cudaGraph_t g = nullptr;
+    MTJG_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    int st = MTJG_OK;
+    const int reps = S->kind == MTJG_GMRES ? 1 : S->chunk;
+    for (int c = 0; c < reps && st == MTJG_OK; ++c) st = phase(S, A, false);
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    if (st != MTJG_OK) {
+        if (g) cudaGraphDestroy(g);
+        ctx->launches = before;
+        return st;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&S->gexec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+    S->g_kernels = (int)(ctx->launches - before);
+    ctx->launches = before;
+    S->g_A = A;
+    S->g_M = S->M;
+    S->g_numerics = ctx->numerics;
+    S->g_norm = S->mon.norm;
+    S->g_version = S->M ? S->M->version : 0;
+    return MTJG_OK;
+}
+
+int map_status(int st) { return st == ST_DONE ? MTJG_OK : st; }
+
+// vectors b and x are in the solver's buffers
+int run(mtjg_solver *S, mtjg_csr *A, mtjg_result *res)
+{
+    mtjg_ctx *ctx = S->ctx;
+    SysState init;
+    std::memset(&init, 0, sizeof(init));
+    init.status = ST_RUNNING;
+    init.gate = ST_RUNNING;
+    init.rho_1 = init.rho_2 = init.alpha = init.beta = init.omega = 1.0;
+    MTJG_CUDA(cudaMemcpyAsync(S->st, &init, sizeof(init), cudaMemcpyHostToDevice, ctx->stream));
+    const int one = 1;
+    MTJG_CUDA(cudaMemcpyAsync(A->num_running, &one, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    MTJG_CUDA(cudaMemsetAsync(A->cnt, 0, sizeof(unsigned) * 4, ctx->stream));
+    MTJG_CUDA(cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream));
+    int st = phase(S, A, true);
+    if (st != MTJG_OK) return st;
+    const bool stale = !S->gexec || S->g_A != A || S->g_M != S->M || S->g_numerics != ctx->numerics ||
+                       S->g_norm != S->mon.norm || S->g_version != (S->M ? S->M->version : 0);
+    if (stale) {
+        st = capture(S, A);
+        if (st != MTJG_OK) return st;
+    }
+    int *pin = ctx->h_pinned;
+    MTJG_CUDA(cudaMemcpyAsync(pin, A->num_running, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    MTJG_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (pin[0] != 0) {
+        // two chunks in flight: launch k+1, then wait for the status copied after k
+        int k = 0;
+        MTJG_CUDA(cudaGraphLaunch(S->gexec, ctx->stream));
+        ctx->launches += S->g_kernels;
+        MTJG_CUDA(cudaMemcpyAsync(pin + 0, A->num_running, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        MTJG_CUDA(cudaMemcpyAsync(pin + 2, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        MTJG_CUDA(cudaEventRecord(S->ev[0], ctx->stream));
+        for (;;) {
+            const int nx = (k + 1) & 1;
+            MTJG_CUDA(cudaGraphLaunch(S->gexec, ctx->stream));
+            ctx->launches += S->g_kernels;
+            MTJG_CUDA(cudaMemcpyAsync(pin + nx, A->num_running, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+            MTJG_CUDA(cudaMemcpyAsync(pin + 2 + nx, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+            MTJG_CUDA(cudaEventRecord(S->ev[nx], ctx->stream));
+            MTJG_CUDA(cudaEventSynchronize(S->ev[k & 1]));
+            if (pin[k & 1] == 0 || pin[2 + (k & 1)] != 0) break;
+            // every chunk advances the iteration count by at least one, so a
+            // solve that is still running after maxIter + 16 chunks is stuck
+            if (++k > (int64_t)std::max(0, S->mon.max_iter) + 16) {
+                MTJG_CUDA(cudaStreamSynchronize(ctx->stream));
+                return fail(MTJG_ERR_DEVICE_TIMEOUT, "solve did not finish within maxIter iterations");
+            }
+        }
+    }
+    MTJG_CUDA(cudaMemcpyAsync(&S->last, S->st, sizeof(SysState), cudaMemcpyDeviceToHost, ctx->stream));
+    int flag = 0;
+    MTJG_CUDA(cudaMemcpyAsync(&flag, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    MTJG_CUDA(cudaStreamSynchronize(ctx->stream));
+    S->last_valid = 1;
+    if (flag) {
+        cudaMemset(ctx->d_flag, 0, sizeof(int));
+        return fail(MTJG_ERR_DEVICE_TIMEOUT, "a bounded wait in a device kernel gave up during the solve");
+    }
+    const int code = map_status(S->last.status);
+    if (res) {
+        res->status = code;
+        res->iterations = S->last.iter;
+        res->residual = S->last.residual;
+        res->detail = S->last.detail;
+        res->history_len = S->last.hist_len;
+    }
+    if (code == MTJG_NOT_CONVERGED_BREAKDOWN)
+        set_error(S->last.detail == 1 ? "Breakdown: rho" : "Breakdown: omega");
+    else if (code == MTJG_NOT_CONVERGED_ITERATIONS)
+        set_error("Iterations");
+    else if (code == MTJG_NOT_CONVERGED_DIVERGENCE)
+        set_error("Divergence");
+    else if (code == MTJG_ERR_SINGULAR)
+        set_error("MatrixSingularException in the GMRES triangular solve");
+    return code;
+}
+
+// n == 0: every vector is empty, every norm is 0.  The first test converges
+// when atol > 0; otherwise MTJ loops without effect until maxIter.
+int run_empty(mtjg_solver *S, mtjg_result *res)
+{
+    std::memset(&S->last, 0, sizeof(S->last));
+    const bool conv = 0.0 < std::max(S->mon.rtol * 0.0, S->mon.atol);
+    S->last.status = conv ? ST_DONE : (S->mon.max_iter <= 0 ? MTJG_NOT_CONVERGED_ITERATIONS
+                                                            : MTJG_NOT_CONVERGED_ITERATIONS);
+    S->last.iter = conv ? 0 : std::max(0, S->mon.max_iter);
+    S->last.hist_len = 1;
+    S->last_valid = 1;
+    if (S->hist_r && S->mon.history_cap > 0) {
+        const double z = 0.0;
+        const int it = 0;
+        cudaMemcpy(S->hist_r, &z, sizeof(double), cudaMemcpyHostToDevice);
+        cudaMemcpy(S->hist_it, &it, sizeof(int), cudaMemcpyHostToDevice);
+    }
+    if (res) {
+        res->status = map_status(S->last.status);
+        res->iterations = S->last.iter;
+        res->residual = 0.0;
+        res->detail = 0;
+        res->history_len = 1;
+    }
+    return map_status(S->last.status);
+}
+
+int check_sizes(mtjg_solver *S, mtjg_csr *A)
+{
+    // AbstractIterativeSolver.checkSizes, S/AbstractIterativeSolver.java:70-77
+    if (!A) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL matrix");
+    if (A->ctx != S->ctx) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "matrix and solver use different contexts");
+    if (A->n != A->m) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "!A.isSquare()");
+    if (S->n != A->n) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "b.size() != A.numRows()");
+    if (S->M && S->M->n != A->n) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "preconditioner size differs from A");
+    if (S->M && !S->M->ready) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "preconditioner setMatrix has not been called");
+    return MTJG_OK;
+}
+
+}  // namespace
+
+extern "C" int mtjg_solver_create(mtjg_ctx *ctx, int kind, int n, int restart, mtjg_solver **out)
+{
+    if (!ctx || !out) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL argument");
+    *out = nullptr;
+    if (kind < MTJG_CG || kind > MTJG_GMRES) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "unknown solver kind");
+    if (n < 0) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "negative size");
+    if (kind == MTJG_GMRES && restart <= 0) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "restart must be a positive integer");
+    MTJG_CUDA(cudaSetDevice(ctx->device));
+    mtjg_solver *S = new mtjg_solver();
+    S->ctx = ctx;
+    ctx_retain(ctx);
+    S->kind = kind;
+    S->n = n;
+    S->restart = kind == MTJG_GMRES ? restart : 0;
+    mtjg_monitor_defaults(&S->mon);
+    S->vecs.assign(V_COUNT, nullptr);
+    std::vector<int> need;
+    if (kind == MTJG_CG) need = {V_B, V_X, V_R, V_Z, V_P, V_Q};
+    else if (kind == MTJG_BICGSTAB) need = {V_B, V_X, V_R, V_RT, V_P, V_PH, V_S, V_SH, V_T, V_V};
+    else need = {V_B, V_X, V_R, V_U, V_W};
+    const size_t nb = sizeof(double) * (size_t)std::max(1, n);
+    bool ok = cudaMalloc(&S->st, sizeof(SysState)) == cudaSuccess;
+    for (int k : need) ok = ok && cudaMalloc(&S->vecs[k], nb) == cudaSuccess;
+    if (kind == MTJG_GMRES) {
+        const size_t ld = (size_t)restart + 1;
+        ok = ok && cudaMalloc(&S->V, nb * ld) == cudaSuccess;
+        ok = ok && cudaMalloc(&S->gm.H, sizeof(double) * ld * (size_t)restart) == cudaSuccess;
+        ok = ok && cudaMalloc(&S->gm.s, sizeof(double) * ld) == cudaSuccess;
+        ok = ok && cudaMalloc(&S->gm.gc, sizeof(double) * ld) == cudaSuccess;
+        ok = ok && cudaMalloc(&S->gm.gs, sizeof(double) * ld) == cudaSuccess;
+        if (ok) {
+            cudaMemset(S->V, 0, nb * ld);
+            cudaMemset(S->gm.H, 0, sizeof(double) * ld * (size_t)restart);
+        }
+        S->gm.restart = restart;
+    }
+    ok = ok && cudaEventCreateWithFlags(&S->ev[0], cudaEventDisableTiming) == cudaSuccess;
+    ok = ok && cudaEventCreateWithFlags(&S->ev[1], cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+        mtjg_solver_destroy(S);
+        return fail(MTJG_ERR_OUT_OF_MEMORY, "cudaMalloc failed for the solver's work vectors");
+    }
+    *out = S;
+    return MTJG_OK;
+}
+
+extern "C" int mtjg_solver_destroy(mtjg_solver *S)
+{
+    if (!S) return MTJG_OK;
+    cudaSetDevice(S->ctx->device);
+    cudaStreamSynchronize(S->ctx->stream);
+    drop_graph(S);
+    for (double *p : S->vecs) cudaFree(p);
+    cudaFree(S->V);
+    cudaFree(S->gm.H);
+    cudaFree(S->gm.s);
+    cudaFree(S->gm.gc);
+    cudaFree(S->gm.gs);
+    cudaFree(S->st);
+    cudaFree(S->hist_r);
+    cudaFree(S->hist_it);
+    if (S->ev[0]) cudaEventDestroy(S->ev[0]);
+    if (S->ev[1]) cudaEventDestroy(S->ev[1]);
+    mtjg_ctx *ctx = S->ctx;
+    delete S;
+    ctx_release(ctx);
+    return MTJG_OK;
+}
+
+extern "C" int mtjg_solver_set_precond(mtjg_solver *S, mtjg_precond *M)
+{
+    if (!S) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL solver");
+    if (M && M->ctx != S->ctx) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "preconditioner uses another context");
+    if (M && M->n != S->n) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "preconditioner size differs from the solver's");
+    S->M = M;
+    drop_graph(S);
+    return MTJG_OK;
+}
+
+extern "C" int mtjg_solver_set_monitor(mtjg_solver *S, const mtjg_monitor *mon)
+{
+    if (!S || !mon) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL argument");
+    if (mon->norm < MTJG_NORM_ONE || mon->norm > MTJG_NORM_INFINITY || mon->history_cap < 0)
+        return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "bad monitor settings");
+    MTJG_CUDA(cudaSetDevice(S->ctx->device));
+    MTJG_CUDA(cudaStreamSynchronize(S->ctx->stream));
+    if (mon->history_cap > S->hist_alloc) {
+        cudaFree(S->hist_r);
+        cudaFree(S->hist_it);
+        S->hist_r = nullptr;
+        S->hist_it = nullptr;
+        S->hist_alloc = 0;
+        MTJG_CUDA(cudaMalloc(&S->hist_r, sizeof(double) * (size_t)mon->history_cap));
+        MTJG_CUDA(cudaMalloc(&S->hist_it, sizeof(int) * (size_t)mon->history_cap));
+        S->hist_alloc = mon->history_cap;
+    }
+    S->mon = *mon;
+    drop_graph(S);
+    return MTJG_OK;
+}
+
+extern "C" int mtjg_solver_solve(mtjg_solver *S, mtjg_csr *A, const double *b, double *x, mtjg_result *res)
+{
+    if (!S) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL solver");
+    int st = check_sizes(S, A);
+    if (st != MTJG_OK) return st;
+    if (S->n == 0) return run_empty(S, res);
+    if (!b || !x) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL vector");
+    mtjg_ctx *ctx = S->ctx;
+    MTJG_CUDA(cudaSetDevice(ctx->device));
+    const size_t nb = sizeof(double) * (size_t)S->n;
+    MTJG_CUDA(cudaMemcpyAsync(S->vecs[V_B], b, nb, cudaMemcpyHostToDevice, ctx->stream));
+    MTJG_CUDA(cudaMemcpyAsync(S->vecs[V_X], x, nb, cudaMemcpyHostToDevice, ctx->stream));
+    st = run(S, A, res);
+    if (st == MTJG_ERR_CUDA || st == MTJG_ERR_OUT_OF_MEMORY || st == MTJG_ERR_DEVICE_TIMEOUT) return st;
+    MTJG_CUDA(cudaMemcpyAsync(x, S->vecs[V_X], nb, cudaMemcpyDeviceToHost, ctx->stream));
+    MTJG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return st;
+}
+
+extern "C" int mtjg_solver_solve_dev(mtjg_solver *S, mtjg_csr *A, const double *db, double *dx, mtjg_result *res)
+{
+    if (!S) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL solver");
+    int st = check_sizes(S, A);
+    if (st != MTJG_OK) return st;
+    if (S->n == 0) return run_empty(S, res);
+    if (!db || !dx) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL vector");
+    mtjg_ctx *ctx = S->ctx;
+    MTJG_CUDA(cudaSetDevice(ctx->device));
+    const size_t nb = sizeof(double) * (size_t)S->n;
+    MTJG_CUDA(cudaMemcpyAsync(S->vecs[V_B], db, nb, cudaMemcpyDeviceToDevice, ctx->stream));
+    MTJG_CUDA(cudaMemcpyAsync(S->vecs[V_X], dx, nb, cudaMemcpyDeviceToDevice, ctx->stream));
+    st = run(S, A, res);
+    if (st == MTJG_ERR_CUDA || st == MTJG_ERR_OUT_OF_MEMORY || st == MTJG_ERR_DEVICE_TIMEOUT) return st;
+    MTJG_CUDA(cudaMemcpyAsync(dx, S->vecs[V_X], nb, cudaMemcpyDeviceToDevice, ctx->stream));
+    MTJG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return st;
+}
+
+extern "C" int mtjg_solver_history(mtjg_solver *S, double *resid, int *iters, int cap, int *len)
+{
+    if (!S) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL solver");
+    const int have = S->last_valid ? std::min(S->last.hist_len, S->mon.history_cap) : 0;
+    if (len) *len = have;
+    const int m = std::min(have, cap);
+    if (m > 0) {
+        MTJG_CUDA(cudaSetDevice(S->ctx->device));
+        if (resid) MTJG_CUDA(cudaMemcpy(resid, S->hist_r, sizeof(double) * (size_t)m, cudaMemcpyDeviceToHost));
+        if (iters) MTJG_CUDA(cudaMemcpy(iters, S->hist_it, sizeof(int) * (size_t)m, cudaMemcpyDeviceToHost));
+    }
+    return MTJG_OK;
+}

@@ -1,0 +1,540 @@
+// spmv.cu -- device CSR (CompRowMatrix) handles and their products.
+#include <algorithm>
+#include <cstring>
+
+#include "spmv.cuh"
+
+namespace mtjg {
+
+// ------------------------------------------------------------------ tiles
+int choose_vec(int64_t nnz, int64_t n)
+{
+    if (n <= 0) return 1;
+    double avg = (double)nnz / (double)n;
+    if (avg <= 12.0) return 1;
+    if (avg <= 48.0) return 4;
+    return 32;
+}
+
+void plan_tiles(const int *rowptr, int row_begin, int row_end, int vec, std::vector<int> &tile_row,
+                std::vector<unsigned char> &tile_long)
+{
+    const int rows_cap = kTileRows / vec;
+    int r = row_begin;
+    while (r < row_end) {
+        tile_row.push_back(r);
+        int len0 = rowptr[r + 1] - rowptr[r];
+        if (len0 > kTileNnz) {
+            tile_long.push_back(1);
+            r += 1;
+            continue;
+        }
+        int nz = len0, rows = 1;
+        r += 1;
+        while (r < row_end && rows < rows_cap) {
+            int len = rowptr[r + 1] - rowptr[r];
+            if (nz + len > kTileNnz) break;
+            nz += len;
+            rows++;
+            r++;
+        }
+        tile_long.push_back(0);
+    }
+}
+
+int upload_tiles(TileSet &ts, const std::vector<int> &tile_row, const std::vector<unsigned char> &tile_long,
+                 const std::vector<int> *tile_sys, const std::vector<int> &sys_tile, int vec)
+{
+    free_tiles(ts);
+    ts.num_tiles = (int)tile_long.size();
+    ts.num_sys = (int)sys_tile.size() - 1;
+    ts.vec = vec;
+    ts.h_tile_row = tile_row;
+    MTJG_CUDA(cudaMalloc(&ts.tile_row, sizeof(int) * tile_row.size()));
+    MTJG_CUDA(cudaMemcpy(ts.tile_row, tile_row.data(), sizeof(int) * tile_row.size(), cudaMemcpyHostToDevice));
+    MTJG_CUDA(cudaMalloc(&ts.tile_long, std::max<size_t>(1, tile_long.size())));
+    if (!tile_long.empty())
+        MTJG_CUDA(cudaMemcpy(ts.tile_long, tile_long.data(), tile_long.size(), cudaMemcpyHostToDevice));
+    MTJG_CUDA(cudaMalloc(&ts.sys_tile, sizeof(int) * sys_tile.size()));
+    MTJG_CUDA(cudaMemcpy(ts.sys_tile, sys_tile.data(), sizeof(int) * sys_tile.size(), cudaMemcpyHostToDevice));
+    if (tile_sys) {
+        MTJG_CUDA(cudaMalloc(&ts.tile_sys, sizeof(int) * std::max<size_t>(1, tile_sys->size())));
+        if (!tile_sys->empty())
+            MTJG_CUDA(cudaMemcpy(ts.tile_sys, tile_sys->data(), sizeof(int) * tile_sys->size(),
+                                 cudaMemcpyHostToDevice));
+    }
+    return MTJG_OK;
+}
+
+void free_tiles(TileSet &ts)
+{
+    cudaFree(ts.tile_row);
+    cudaFree(ts.tile_sys);
+    cudaFree(ts.sys_tile);
+    cudaFree(ts.tile_long);
+    ts.tile_row = ts.tile_sys = ts.sys_tile = nullptr;
+    ts.tile_long = nullptr;
+    ts.num_tiles = 0;
+}
+
+// ------------------------------------------------------------------- scan
+constexpr int kScanChunk = 2048;
+
+__global__ void k_scan_chunks(const int *in, int n, int *chunk_sum)
+{
+    __shared__ int sm[kBlock / 32];
+    const int c = blockIdx.x;
+    const int base = c * kScanChunk;
+    int s = 0;
+    for (int i = base + threadIdx.x; i < base + kScanChunk && i < n; i += blockDim.x) s += in[i];
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sm[w];
+        chunk_sum[c] = t;
+    }
+}
+
+// single block: exclusive scan of the chunk sums in place, total at [nc]
+__global__ void k_scan_top(int *chunk_sum, int nc)
+{
+    __shared__ int carry;
+    __shared__ int sm[kBlock];
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < nc; base += blockDim.x) {
+        int i = base + threadIdx.x;
+        int v = i < nc ? chunk_sum[i] : 0;
+        sm[threadIdx.x] = v;
+        __syncthreads();
+        for (int off = 1; off < (int)blockDim.x; off <<= 1) {
+            int add = threadIdx.x >= (unsigned)off ? sm[threadIdx.x - off] : 0;
+            __syncthreads();
+            sm[threadIdx.x] += add;
+            __syncthreads();
+        }
+        if (i < nc) chunk_sum[i] = carry + sm[threadIdx.x] - v;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += sm[blockDim.x - 1];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) chunk_sum[nc] = carry;
+}
+
+__global__ void k_scan_apply(const int *in, int n, const int *chunk_off, int *out)
+{
+    __shared__ int sm[kBlock];
+    __shared__ int carry;
+    const int c = blockIdx.x;
+    const int base = c * kScanChunk;
+    if (threadIdx.x == 0) carry = chunk_off[c];
+    __syncthreads();
+    for (int b = base; b < base + kScanChunk && b < n; b += blockDim.x) {
+        int i = b + threadIdx.x;
+        int v = i < n ? in[i] : 0;
+        sm[threadIdx.x] = v;
+        __syncthreads();
+        for (int off = 1; off < (int)blockDim.x; off <<= 1) {
+            int add = threadIdx.x >= (unsigned)off ? sm[threadIdx.x - off] : 0;
+            __syncthreads();
+            sm[threadIdx.x] += add;
+            __syncthreads();
+        }
+        if (i < n) out[i] = carry + sm[threadIdx.x] - v;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += sm[blockDim.x - 1];
+        __syncthreads();
+    }
+    if (c == (int)gridDim.x - 1 && threadIdx.x == 0) out[n] = chunk_off[gridDim.x];
+}
+
+int exclusive_scan(mtjg_ctx *ctx, const int *in, int *out, int n)
+{
+    if (n == 0) {
+        MTJG_CUDA(cudaMemsetAsync(out, 0, sizeof(int), ctx->stream));
+        return MTJG_OK;
+    }
+    int nc = (n + kScanChunk - 1) / kScanChunk;
+    int *cs = nullptr;
+    MTJG_CUDA(cudaMalloc(&cs, sizeof(int) * (nc + 1)));
+    k_scan_chunks<<<nc, kBlock, 0, ctx->stream>>>(in, n, cs);
+    k_scan_top<<<1, kBlock, 0, ctx->stream>>>(cs, nc);
+    k_scan_apply<<<nc, kBlock, 0, ctx->stream>>>(in, n, cs, out);
+    ctx->launches += 3;
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(cs);
+    if (e != cudaSuccess) return cuda_fail(e, "exclusive_scan");
+    return MTJG_OK;
+}
+
+// -------------------------------------------------------------- transpose
+__global__ void k_tr_count(int n, const int *rowptr, const int *colind, int mode, int *cnt)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+            int c = colind[k];
+            if (mode == 0 || (mode == 1 && c > i) || (mode == 2 && c < i))atomicAdd(&cnt[c], 1);
+        }
+}
+
+__global__ void k_tr_fill(int n, const int *rowptr, const int *colind, const double *val, int mode,
+                          const int *t_rowptr, int *cursor, int *t_colind, double *t_val)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+            int c = colind[k];
+            if (mode == 0 || (mode == 1 && c > i) || (mode == 2 && c < i)){
+                int pos = t_rowptr[c] + atomicAdd(&cursor[c], 1);
+                t_colind[pos] = i;
+                t_val[pos] = val[k];
+            }
+        }
+}
+
+// each transposed row sorted by source row (insertion sort; rows are short)
+__global__ void k_tr_sort(int m, const int *t_rowptr, int *t_colind, double *t_val)
+{
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < m; c += gridDim.x * blockDim.x) {
+        int b = t_rowptr[c], e = t_rowptr[c + 1];
+        for (int p = b + 1; p < e; ++p) {
+            int key = t_colind[p];
+            double v = t_val[p];
+            int q = p - 1;
+            while (q >= b && t_colind[q] > key) {
+                t_colind[q + 1] = t_colind[q];
+                t_val[q + 1] = t_val[q];
+                --q;
+            }
+            t_colind[q + 1] = key;
+            t_val[q + 1] = v;
+        }
+    }
+}
+
+int csr_transpose(mtjg_ctx *ctx, int n, int m, const int *rowptr, const int *colind, const double *val,
+                  int mode, int **t_rowptr, int **t_colind, double **t_val, int64_t *t_nnz)
+{
+    int *cnt = nullptr, *cursor = nullptr, *trp = nullptr, *tci = nullptr;
+    double *tv = nullptr;
+    const int grid = std::max(1, std::min((n + kBlock - 1) / kBlock, ctx->num_sms * 8));
+    MTJG_CUDA(cudaMalloc(&cnt, sizeof(int) * (size_t)std::max(1, m)));
+    MTJG_CUDA(cudaMalloc(&cursor, sizeof(int) * (size_t)std::max(1, m)));
+    MTJG_CUDA(cudaMalloc(&trp, sizeof(int) * (size_t)(m + 1)));
+    MTJG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int) * (size_t)std::max(1, m), ctx->stream));
+    MTJG_CUDA(cudaMemsetAsync(cursor, 0, sizeof(int) * (size_t)std::max(1, m), ctx->stream));
+    if (n > 0) {
+        k_tr_count<<<grid, kBlock, 0, ctx->stream>>>(n, rowptr, colind, mode, cnt);
+        ctx->launches++;
+    }
+    int st = exclusive_scan(ctx, cnt, trp, m);
+    if (st != MTJG_OK) return st;
+    int total = 0;
+    MTJG_CUDA(cudaMemcpy(&total, trp + m, sizeof(int), cudaMemcpyDeviceToHost));
+    MTJG_CUDA(cudaMalloc(&tci, sizeof(int) * (size_t)(total + 4)));
+    MTJG_CUDA(cudaMalloc(&tv, sizeof(double) * (size_t)(total + 2)));
+    MTJG_CUDA(cudaMemsetAsync(tci, 0xff, sizeof(int) * (size_t)(total + 4), ctx->stream));
+    MTJG_CUDA(cudaMemsetAsync(tv, 0, sizeof(double) * (size_t)(total + 2), ctx->stream));
+    if (n > 0) {
+        k_tr_fill<<<grid, kBlock, 0, ctx->stream>>>(n, rowptr, colind, val, mode, trp, cursor, tci, tv);
+        ctx->launches++;
+    }
+    if (m > 0) {
+        const int gm = std::max(1, std::min((m + kBlock - 1) / kBlock, ctx->num_sms * 8));
+        k_tr_sort<<<gm, kBlock, 0, ctx->stream>>>(m, trp, tci, tv);
+        ctx->launches++;
+    }
+    MTJG_CUDA(cudaStreamSynchronize(ctx->stream));
+    cudaFree(cnt);
+    cudaFree(cursor);
+    *t_rowptr = trp;
+    *t_colind = tci;
+    *t_val = tv;
+    *t_nnz = total;
+    return MTJG_OK;
+}
+
+// ----------------------------------------------------------- epilogues
+// CompRowMatrix.mult: y = Ax, a zero sum stored as +0 (y.zero() and the
+// "if (dot != 0)" test, S/CompRowMatrix.java:299,309-311).
+struct EpiMult {
+    double *y;
+    static constexpr bool kReduce = false;
+    __device__ bool active(int) const { return true; }
+    __device__ double init(int, int) const { return 0.0; }
+    __device__ void row(int r, int, double d, Acc &) const { y[r] = d != 0.0 ? d : 0.0; }
+    __device__ void scalar(int, const Acc &) {}
+};
+
+// CompRowMatrix.multAdd: y_i += alpha * dot (S/CompRowMatrix.java:343)
+template <bool S>
+struct EpiMultAdd {
+    double *y;
+    double alpha;
+    static constexpr bool kReduce = false;
+    __device__ bool active(int) const { return true; }
+    __device__ double init(int, int) const { return 0.0; }
+    __device__ void row(int r, int, double d, Acc &) const { y[r] = fmac<S>(alpha, d, y[r]); }
+    __device__ void scalar(int, const Acc &) {}
+};
+
+// transMult on the transpose: y_c = sum over ascending source rows, from 0
+// (the scatter of S/CompRowMatrix.java:359-363 in gather form).
+struct EpiSet {
+    double *y;
+    static constexpr bool kReduce = false;
+    __device__ bool active(int) const { return true; }
+    __device__ double init(int, int) const { return 0.0; }
+    __device__ void row(int r, int, double d, Acc &) const { y[r] = d; }
+    __device__ void scalar(int, const Acc &) {}
+};
+
+// transMultAdd (S/CompRowMatrix.java:378-387): y scaled by 1/alpha, the
+// products added onto it in ascending source row order, then scaled by alpha.
+struct EpiTransMultAdd {
+    double *y;
+    double alpha, inv;
+    static constexpr bool kReduce = false;
+    __device__ bool active(int) const { return true; }
+    __device__ double init(int r, int) const { return y[r] * inv; }
+    __device__ void row(int r, int, double d, Acc &) const { y[r] = d * alpha; }
+    __device__ void scalar(int, const Acc &) {}
+};
+
+}  // namespace mtjg
+
+using namespace mtjg;
+
+// ------------------------------------------------------------- handle ops
+static int csr_validate(int n, int m, const int *rowptr, const int *colind)
+{
+    if (n < 0 || m < 0) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "negative matrix dimension");
+    if (!rowptr) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "rowptr is NULL");
+    if (rowptr[0] != 0) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "rowptr[0] != 0");
+    for (int i = 0; i < n; ++i) {
+        if (rowptr[i + 1] < rowptr[i]) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "rowptr is not nondecreasing");
+        for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+            int c = colind[k];
+            if (c < 0 || c >= m)
+                return fail(MTJG_ERR_ILLEGAL_ARGUMENT,
+                            "nz[" + std::to_string(i) + "][" + std::to_string(k - rowptr[i]) + "]=" +
+                                std::to_string(c) + ", which is not a valid column index");
+            if (k > rowptr[i] && colind[k - 1] >= c)
+                return fail(MTJG_ERR_ILLEGAL_ARGUMENT,
+                            "column indices of row " + std::to_string(i) + " are not strictly ascending");
+        }
+    }
+    return MTJG_OK;
+}
+
+extern "C" int mtjg_csr_upload(mtjg_ctx *ctx, int n, int m, const int *rowptr, const int *colind,
+                               const double *val, mtjg_csr **out)
+{
+    if (!ctx || !out) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL argument");
+    *out = nullptr;
+    int st = csr_validate(n, m, rowptr, colind);
+    if (st != MTJG_OK) return st;
+    MTJG_CUDA(cudaSetDevice(ctx->device));
+    const int64_t nnz = rowptr[n];
+    mtjg_csr *A = new mtjg_csr();
+    A->ctx = ctx;
+    ctx_retain(ctx);
+    A->n = n;
+    A->m = m;
+    A->nnz = nnz;
+    A->h_rowptr.assign(rowptr, rowptr + n + 1);
+    auto bail = [&](int code) {
+        mtjg_csr_destroy(A);
+        return code;
+    };
+    if (cudaMalloc(&A->rowptr, sizeof(int) * (size_t)(n + 1)) != cudaSuccess ||
+        cudaMalloc(&A->colind, sizeof(int) * (size_t)(nnz + 4)) != cudaSuccess ||
+        cudaMalloc(&A->val, sizeof(double) * (size_t)(nnz + 2)) != cudaSuccess ||
+        cudaMalloc(&A->d_x, sizeof(double) * (size_t)std::max(1, std::max(n, m))) != cudaSuccess ||
+        cudaMalloc(&A->d_y, sizeof(double) * (size_t)std::max(1, std::max(n, m))) != cudaSuccess)
+        return bail(fail(MTJG_ERR_OUT_OF_MEMORY, "cudaMalloc failed for the CSR matrix"));
+    cudaMemset(A->colind, 0xff, sizeof(int) * (size_t)(nnz + 4));
+    cudaMemset(A->val, 0, sizeof(double) * (size_t)(nnz + 2));
+    if (cudaMemcpy(A->rowptr, rowptr, sizeof(int) * (size_t)(n + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
+        (nnz && cudaMemcpy(A->colind, colind, sizeof(int) * (size_t)nnz, cudaMemcpyHostToDevice) != cudaSuccess) ||
+        (nnz && cudaMemcpy(A->val, val, sizeof(double) * (size_t)nnz, cudaMemcpyHostToDevice) != cudaSuccess))
+        return bail(fail(MTJG_ERR_CUDA, "copying the CSR matrix to the device failed"));
+    // tiles
+    const int vec = choose_vec(nnz, n);
+    std::vector<int> tile_row;
+    std::vector<unsigned char> tile_long;
+    plan_tiles(rowptr, 0, n, vec, tile_row, tile_long);
+    tile_row.push_back(n);
+    std::vector<int> sys_tile = {0, (int)tile_long.size()};
+    st = upload_tiles(A->tiles, tile_row, tile_long, nullptr, sys_tile, vec);
+    if (st != MTJG_OK) return bail(st);
+    const size_t nt = std::max<size_t>(1, tile_long.size());
+    if (cudaMalloc(&A->part, sizeof(double) * nt * kParts) != cudaSuccess ||
+        cudaMalloc(&A->cnt, sizeof(unsigned) * 4) != cudaSuccess ||
+        cudaMalloc(&A->num_running, sizeof(int) * 4) != cudaSuccess)
+        return bail(fail(MTJG_ERR_OUT_OF_MEMORY, "cudaMalloc failed for reduction scratch"));
+    cudaMemset(A->cnt, 0, sizeof(unsigned) * 4);
+    cudaMemset(A->num_running, 0, sizeof(int) * 4);
+    *out = A;
+    return MTJG_OK;
+}
+
+extern "C" int mtjg_csr_update_values(mtjg_csr *A, const double *val)
+{
+    if (!A || (!val && A->nnz)) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL argument");
+    MTJG_CUDA(cudaSetDevice(A->ctx->device));
+    MTJG_CUDA(cudaStreamSynchronize(A->ctx->stream));
+    if (A->nnz) MTJG_CUDA(cudaMemcpy(A->val, val, sizeof(double) * (size_t)A->nnz, cudaMemcpyHostToDevice));
+    // the transpose holds old values: rebuild on next use
+    cudaFree(A->t_rowptr);
+    cudaFree(A->t_colind);
+    cudaFree(A->t_val);
+    A->t_rowptr = A->t_colind = nullptr;
+    A->t_val = nullptr;
+    free_tiles(A->t_tiles);
+    return MTJG_OK;
+}
+
+extern "C" int mtjg_csr_destroy(mtjg_csr *A)
+{
+    if (!A) return MTJG_OK;
+    if (A->ctx) cudaSetDevice(A->ctx->device);
+    if (A->ctx) cudaStreamSynchronize(A->ctx->stream);
+    cudaFree(A->rowptr);
+    cudaFree(A->colind);
+    cudaFree(A->val);
+    cudaFree(A->t_rowptr);
+    cudaFree(A->t_colind);
+    cudaFree(A->t_val);
+    cudaFree(A->part);
+    cudaFree(A->cnt);
+    cudaFree(A->num_running);
+    cudaFree(A->d_x);
+    cudaFree(A->d_y);
+    free_tiles(A->tiles);
+    free_tiles(A->t_tiles);
+    mtjg_ctx *ctx = A->ctx;
+    delete A;
+    ctx_release(ctx);
+    return MTJG_OK;
+}
+
+extern "C" int mtjg_csr_dims(const mtjg_csr *A, int *n, int *m, int64_t *nnz)
+{
+    if (!A) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL matrix");
+    if (n) *n = A->n;
+    if (m) *m = A->m;
+    if (nnz) *nnz = A->nnz;
+    return MTJG_OK;
+}
+
+static int ensure_transpose(mtjg_csr *A)
+{
+    if (A->t_rowptr) return MTJG_OK;
+    mtjg_ctx *ctx = A->ctx;
+    int64_t tnnz = 0;
+    int st = csr_transpose(ctx, A->n, A->m, A->rowptr, A->colind, A->val, 0, &A->t_rowptr, &A->t_colind,
+                           &A->t_val, &tnnz);
+    if (st != MTJG_OK) return st;
+    std::vector<int> trp(A->m + 1);
+    MTJG_CUDA(cudaMemcpy(trp.data(), A->t_rowptr, sizeof(int) * (size_t)(A->m + 1), cudaMemcpyDeviceToHost));
+    const int vec = choose_vec(tnnz, A->m);
+    std::vector<int> tile_row;
+    std::vector<unsigned char> tile_long;
+    plan_tiles(trp.data(), 0, A->m, vec, tile_row, tile_long);
+    tile_row.push_back(A->m);
+    std::vector<int> sys_tile = {0, (int)tile_long.size()};
+    return upload_tiles(A->t_tiles, tile_row, tile_long, nullptr, sys_tile, vec);
+}
+
+static int check_err_flag(mtjg_ctx *ctx)
+{
+    int flag = 0;
+    MTJG_CUDA(cudaMemcpy(&flag, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag) {
+        cudaMemset(ctx->d_flag, 0, sizeof(int));
+        return fail(MTJG_ERR_DEVICE_TIMEOUT, "a bounded wait in a device kernel gave up");
+    }
+    return MTJG_OK;
+}
+
+// op: 0 mult, 1 multAdd, 2 transMult, 3 transMultAdd.  Device pointers.
+static int csr_product_dev(mtjg_csr *A, int op, double alpha, const double *dx, double *dy)
+{
+    mtjg_ctx *ctx = A->ctx;
+    const bool strict = ctx->numerics == MTJG_NUMERICS_STRICT;
+    RedCtx rc = red_ctx(A, A->tiles);
+    cudaError_t e = cudaSuccess;
+    if (op == 0) {
+        e = launch_spmv(ctx, CsrArgs{A->rowptr, A->colind, A->val}, A->tiles, dx, EpiMult{dy}, rc, MTJG_NORM_TWO);
+    } else if (op == 1) {
+        if (strict)
+            e = launch_spmv(ctx, CsrArgs{A->rowptr, A->colind, A->val}, A->tiles, dx, EpiMultAdd<true>{dy, alpha},
+                            rc, MTJG_NORM_TWO);
+        else
+            e = launch_spmv(ctx, CsrArgs{A->rowptr, A->colind, A->val}, A->tiles, dx,
+                            EpiMultAdd<false>{dy, alpha}, rc, MTJG_NORM_TWO);
+    } else {
+        int st = ensure_transpose(A);
+        if (st != MTJG_OK) return st;
+        RedCtx trc = red_ctx(A, A->t_tiles);
+        if (op == 2)
+            e = launch_spmv(ctx, CsrArgs{A->t_rowptr, A->t_colind, A->t_val}, A->t_tiles, dx, EpiSet{dy}, trc,
+                            MTJG_NORM_TWO);
+        else
+            e = launch_spmv(ctx, CsrArgs{A->t_rowptr, A->t_colind, A->t_val}, A->t_tiles, dx,
+                            EpiTransMultAdd{dy, alpha, 1. / alpha}, trc, MTJG_NORM_TWO);
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "CSR product launch");
+    return MTJG_OK;
+}
+
+static int csr_product_host(mtjg_csr *A, int op, double alpha, const double *x, double *y)
+{
+    if (!A || !x || !y) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL argument");
+    mtjg_ctx *ctx = A->ctx;
+    MTJG_CUDA(cudaSetDevice(ctx->device));
+    const bool trans = op >= 2;
+    const int nx = trans ? A->n : A->m, ny = trans ? A->m : A->n;
+    MTJG_CUDA(cudaMemcpyAsync(A->d_x, x, sizeof(double) * (size_t)nx, cudaMemcpyHostToDevice, ctx->stream));
+    if (op == 1 || op == 3)
+        MTJG_CUDA(cudaMemcpyAsync(A->d_y, y, sizeof(double) * (size_t)ny, cudaMemcpyHostToDevice, ctx->stream));
+    int st = csr_product_dev(A, op, alpha, A->d_x, A->d_y);
+    if (st != MTJG_OK) return st;
+    MTJG_CUDA(cudaMemcpyAsync(y, A->d_y, sizeof(double) * (size_t)ny, cudaMemcpyDeviceToHost, ctx->stream));
+    MTJG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return check_err_flag(ctx);
+}
+
+extern "C" int mtjg_csr_mult(mtjg_csr *A, const double *x, double *y) { return csr_product_host(A, 0, 0.0, x, y); }
+extern "C" int mtjg_csr_mult_add(mtjg_csr *A, double alpha, const double *x, double *y)
+{
+    return csr_product_host(A, 1, alpha, x, y);
+}
+extern "C" int mtjg_csr_trans_mult(mtjg_csr *A, const double *x, double *y)
+{
+    return csr_product_host(A, 2, 0.0, x, y);
+}
+extern "C" int mtjg_csr_trans_mult_add(mtjg_csr *A, double alpha, const double *x, double *y)
+{
+    return csr_product_host(A, 3, alpha, x, y);
+}
+extern "C" int mtjg_csr_mult_dev(mtjg_csr *A, const double *dx, double *dy)
+{
+    if (!A || !dx || !dy) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL argument");
+    MTJG_CUDA(cudaSetDevice(A->ctx->device));
+    return csr_product_dev(A, 0, 0.0, dx, dy);
+}
+extern "C" int mtjg_csr_mult_add_dev(mtjg_csr *A, double alpha, const double *dx, double *dy)
+{
+    if (!A || !dx || !dy) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL argument");
+    MTJG_CUDA(cudaSetDevice(A->ctx->device));
+    return csr_product_dev(A, 1, alpha, dx, dy);
+}
+extern "C" int mtjg_csr_trans_mult_dev(mtjg_csr *A, const double *dx, double *dy)
+{
+    if (!A || !dx || !dy) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL argument");
+    MTJG_CUDA(cudaSetDevice(A->ctx->device));
+    return csr_product_dev(A, 2, 0.0, dx, dy);
+}

@@ -1,0 +1,522 @@
+"""Host-side mirror of MTJ's ``no.uib.cipr.matrix.sparse`` iterative API.
+
+Same class and method names, argument meaning and error behaviour as the
+reference (citations are files of the reference project, S/ =
+src/main/java/no/uib/cipr/matrix/sparse/, M/ = src/main/java/no/uib/cipr/matrix/):
+
+  CompRowMatrix               S/CompRowMatrix.java   (device CSR)
+  DiagonalPreconditioner      S/DiagonalPreconditioner.java
+  ILU, ICC                    S/ILU.java, S/ICC.java
+  CG, BiCGstab, GMRES         S/CG.java, S/BiCGstab.java, S/GMRES.java
+  DefaultIterationMonitor     S/DefaultIterationMonitor.java
+  IterativeSolverNotConvergedException, NotConvergedException.Reason
+
+Vectors are float64 numpy arrays (the DenseVector analogue); ``solve``
+overwrites ``x`` in place and returns it, as IterativeSolver.solve does.
+Everything computes on the GPU through libmtjg.so.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+import sys
+
+import numpy as np
+
+from . import _lib as L
+
+
+# ---------------------------------------------------------------- errors
+class IllegalArgumentException(ValueError):
+    pass
+
+
+class IndexOutOfBoundsException(IndexError):
+    pass
+
+
+class MatrixSingularException(RuntimeError):
+    """M/MatrixSingularException.java (GMRES's triangular solve)."""
+
+
+class CudaError(RuntimeError):
+    pass
+
+
+class NotConvergedException(Exception):
+    class Reason(enum.Enum):  # M/NotConvergedException.java:33-49
+        Iterations = 1
+        Divergence = 2
+        Breakdown = 3
+
+
+class IterativeSolverNotConvergedException(NotConvergedException):
+    """S/IterativeSolverNotConvergedException.java: reason, residual, iterations."""
+
+    def __init__(self, reason, residual, iterations, message=""):
+        super().__init__(f"{reason.name}{': ' + message if message else ''} "
+                         f"(residual={residual}, iterations={iterations})")
+        self.reason = reason
+        self._r = residual
+        self._it = iterations
+        self.message = message
+
+    def getReason(self):
+        return self.reason
+
+    def getResidual(self):
+        return self._r
+
+    def getIterations(self):
+        return self._it
+
+
+def _raise(code: int, what: str = ""):
+    if code == L.OK:
+        return
+    msg = L.last_error()
+    if code in (L.ERR_ILLEGAL_ARGUMENT,):
+        raise IllegalArgumentException(msg)
+    if code == L.ERR_INDEX_OUT_OF_BOUNDS:
+        raise IndexOutOfBoundsException(msg)
+    if code in (L.ERR_ZERO_PIVOT, L.ERR_ZERO_DIAGONAL, L.ERR_MISSING_DIAGONAL):
+        raise RuntimeError(msg)
+    if code == L.ERR_SINGULAR:
+        raise MatrixSingularException(msg)
+    raise CudaError(f"{what}: code {code}: {msg}")
+
+
+# --------------------------------------------------------------- context
+class Context:
+    """One CUDA device and stream (all objects made with it share them)."""
+
+    def __init__(self, device: int = 0, numerics: int = L.NUMERICS_FAST):
+        self._lib = L.load()
+        h = C.c_void_p()
+        _raise(self._lib.mtjg_ctx_create(device, C.byref(h)), "mtjg_ctx_create")
+        self.h = h
+        self.setNumerics(numerics)
+
+    def setNumerics(self, numerics: int):
+        _raise(self._lib.mtjg_ctx_set_numerics(self.h, numerics), "set_numerics")
+        self.numerics = numerics
+
+    def launchCount(self) -> int:
+        return int(self._lib.mtjg_ctx_launch_count(self.h))
+
+    def synchronize(self):
+        _raise(self._lib.mtjg_ctx_synchronize(self.h), "synchronize")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.mtjg_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        # at interpreter shutdown the process is about to release the device
+        if sys.is_finalizing():
+            return
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default = None
+
+
+def default_context() -> Context:
+    global _default
+    if _default is None:
+        _default = Context(0)
+    return _default
+
+
+# ---------------------------------------------------------- CompRowMatrix
+class CompRowMatrix:
+    """CSR matrix resident on the device (S/CompRowMatrix.java).
+
+    ``CompRowMatrix(numRows, numColumns, rowptr, colind, data)`` takes MTJ's
+    0-based arrays (ascending columns per row); ``CompRowMatrix.fromDense``
+    builds the pattern of the nonzeros of a dense array.
+    """
+
+    def __init__(self, numRows, numColumns, rowptr, colind, data, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        self._lib = self.ctx._lib
+        self.rowptr = L.i32(rowptr)
+        self.colind = L.i32(colind)
+        self.data = L.f64(data)
+        self.n, self.m = int(numRows), int(numColumns)
+        if len(self.rowptr) != self.n + 1:
+            raise IllegalArgumentException("rowptr.length != numRows + 1")
+        nnz = int(self.rowptr[-1]) if self.n >= 0 else 0
+        if len(self.colind) < nnz or len(self.data) < nnz:
+            raise IllegalArgumentException("colind/data shorter than rowptr[numRows]")
+        h = C.c_void_p()
+        _raise(self._lib.mtjg_csr_upload(self.ctx.h, self.n, self.m, L.iptr(self.rowptr), L.iptr(self.colind),
+                                         L.dptr(self.data), C.byref(h)), "csr_upload")
+        self.h = h
+
+    @classmethod
+    def fromDense(cls, A, ctx=None, keep_zeros_on_diagonal=True):
+        A = np.asarray(A, dtype=np.float64)
+        n, m = A.shape
+        rows, cols, vals = [], [], []
+        rp = [0]
+        for i in range(n):
+            for j in range(m):
+                if A[i, j] != 0 or (keep_zeros_on_diagonal and i == j):
+                    cols.append(j)
+                    vals.append(A[i, j])
+            rp.append(len(cols))
+        return cls(n, m, np.array(rp), np.array(cols, dtype=np.int32), np.array(vals), ctx)
+
+    def numRows(self):
+        return self.n
+
+    def numColumns(self):
+        return self.m
+
+    def isSquare(self):
+        return self.n == self.m
+
+    def getRowPointers(self):
+        return self.rowptr
+
+    def getColumnIndices(self):
+        return self.colind
+
+    def getData(self):
+        return self.data
+
+    def setData(self, data):
+        """New values with the same pattern."""
+        self.data = L.f64(data)
+        _raise(self._lib.mtjg_csr_update_values(self.h, L.dptr(self.data)), "update_values")
+
+    def _vec(self, v, size, name):
+        v = L.f64(v)
+        if v.shape != (size,):
+            raise IndexOutOfBoundsException(f"{name}.size != {size}")
+        return v
+
+    def mult(self, x, y=None):
+        """y = A x (S/CompRowMatrix.java:295-314)."""
+        x = self._vec(x, self.m, "x")
+        out = np.empty(self.n) if y is None else y
+        _raise(self._lib.mtjg_csr_mult(self.h, L.dptr(x), L.dptr(out)), "mult")
+        return out
+
+    def multAdd(self, alpha, x, y):
+        """y = alpha A x + y, in place (S/CompRowMatrix.java:330-347)."""
+        x = self._vec(x, self.m, "x")
+        if y.dtype != np.float64 or not y.flags.c_contiguous or y.shape != (self.n,):
+            raise IllegalArgumentException("y must be a contiguous float64 vector of numRows")
+        _raise(self._lib.mtjg_csr_mult_add(self.h, float(alpha), L.dptr(x), L.dptr(y)), "multAdd")
+        return y
+
+    def transMult(self, x, y=None):
+        """y = A' x (S/CompRowMatrix.java:350-366)."""
+        x = self._vec(x, self.n, "x")
+        out = np.empty(self.m) if y is None else y
+        _raise(self._lib.mtjg_csr_trans_mult(self.h, L.dptr(x), L.dptr(out)), "transMult")
+        return out
+
+    def transMultAdd(self, alpha, x, y):
+        """y = alpha A' x + y, in place (S/CompRowMatrix.java:369-388)."""
+        x = self._vec(x, self.n, "x")
+        if y.dtype != np.float64 or not y.flags.c_contiguous or y.shape != (self.m,):
+            raise IllegalArgumentException("y must be a contiguous float64 vector of numColumns")
+        _raise(self._lib.mtjg_csr_trans_mult_add(self.h, float(alpha), L.dptr(x), L.dptr(y)), "transMultAdd")
+        return y
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.mtjg_csr_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        # at interpreter shutdown the process is about to release the device
+        if sys.is_finalizing():
+            return
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# -------------------------------------------------------- preconditioners
+class Preconditioner:
+    """S/Preconditioner.java: setMatrix(A), apply(b, x), transApply(b, x)."""
+
+    kind = L.PC_IDENTITY
+
+    def __init__(self, n: int, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        self._lib = self.ctx._lib
+        self.n = int(n)
+        h = C.c_void_p()
+        _raise(self._lib.mtjg_precond_create(self.ctx.h, self.kind, self.n, C.byref(h)), "precond_create")
+        self.h = h
+        self.error_row = 0
+
+    def setMatrix(self, A: CompRowMatrix):
+        row = C.c_int(0)
+        code = self._lib.mtjg_precond_set_matrix(self.h, A.h, C.byref(row))
+        self.error_row = row.value
+        _raise(code, "setMatrix")
+
+    def apply(self, b, x=None):
+        b = L.f64(b)
+        out = np.empty(self.n) if x is None else x
+        _raise(self._lib.mtjg_precond_apply(self.h, L.dptr(b), L.dptr(out)), "apply")
+        return out
+
+    def transApply(self, b, x=None):
+        b = L.f64(b)
+        out = np.empty(self.n) if x is None else x
+        _raise(self._lib.mtjg_precond_trans_apply(self.h, L.dptr(b), L.dptr(out)), "transApply")
+        return out
+
+    def values(self) -> np.ndarray:
+        """The factored values (ILU/ICC data array; Jacobi inverse diagonal)."""
+        ln = C.c_int64(0)
+        _raise(self._lib.mtjg_precond_values(self.h, None, 0, C.byref(ln)), "values")
+        out = np.empty(ln.value)
+        if ln.value:
+            _raise(self._lib.mtjg_precond_values(self.h, L.dptr(out), ln.value, C.byref(ln)), "values")
+        return out
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.mtjg_precond_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        # at interpreter shutdown the process is about to release the device
+        if sys.is_finalizing():
+            return
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class IdentityPreconditioner(Preconditioner):
+    kind = L.PC_IDENTITY
+
+
+class DiagonalPreconditioner(Preconditioner):
+    """new DiagonalPreconditioner(n) (S/DiagonalPreconditioner.java:43-45)."""
+
+    kind = L.PC_JACOBI
+
+
+class ILU(Preconditioner):
+    """new ILU(CompRowMatrix LU) (S/ILU.java:54-62): LU gives the size."""
+
+    kind = L.PC_ILU
+
+    def __init__(self, LU, ctx=None):
+        n = LU.numRows() if hasattr(LU, "numRows") else int(LU)
+        if hasattr(LU, "isSquare") and not LU.isSquare():
+            raise IllegalArgumentException("ILU only applies to square matrices")
+        super().__init__(n, ctx or getattr(LU, "ctx", None))
+
+
+class ICC(Preconditioner):
+    """new ICC(CompRowMatrix R) (S/ICC.java:57-65)."""
+
+    kind = L.PC_ICC
+
+    def __init__(self, R, ctx=None):
+        n = R.numRows() if hasattr(R, "numRows") else int(R)
+        if hasattr(R, "isSquare") and not R.isSquare():
+            raise IllegalArgumentException("ICC only applies to square matrices")
+        super().__init__(n, ctx or getattr(R, "ctx", None))
+
+
+# --------------------------------------------------------------- monitor
+class Norm(enum.IntEnum):  # M/Vector.java:159-182
+    One = L.NORM_ONE
+    Two = L.NORM_TWO
+    TwoRobust = L.NORM_TWO_ROBUST
+    Infinity = L.NORM_INFINITY
+
+
+class IterationReporter:
+    """S/IterationReporter.java: monitor(r, i) per convergence test."""
+
+    def monitor(self, r, i):
+        pass
+
+
+class DefaultIterationMonitor:
+    """S/DefaultIterationMonitor.java (defaults 100000, 1e-5, 1e-50, 1e+5).
+
+    The reporter is replayed after the solve from the residual history that
+    the device records at every convergence test; per-iteration x is not
+    available to it.
+    """
+
+    def __init__(self, maxIter=100000, rtol=1e-5, atol=1e-50, dtol=1e+5):
+        self.maxIter, self.rtol, self.atol, self.dtol = int(maxIter), float(rtol), float(atol), float(dtol)
+        self.normType = Norm.Two
+        self.reporter = None
+        self.history_cap = 0
+        self._iter = 0
+        self._residual = 0.0
+
+    def setMaxIterations(self, m):
+        self.maxIter = int(m)
+
+    def setRelativeTolerance(self, r):
+        self.rtol = float(r)
+
+    def setAbsoluteTolerance(self, a):
+        self.atol = float(a)
+
+    def setDivergenceTolerance(self, d):
+        self.dtol = float(d)
+
+    def setNormType(self, t):
+        self.normType = Norm(t)
+
+    def getNormType(self):
+        return self.normType
+
+    def setIterationReporter(self, reporter, history_cap=None):
+        self.reporter = reporter
+        if history_cap is None:
+            history_cap = self.maxIter * 2 + 64
+        self.history_cap = int(history_cap)
+
+    def getIterationReporter(self):
+        return self.reporter
+
+    def iterations(self):
+        return self._iter
+
+    def residual(self):
+        return self._residual
+
+    def _struct(self) -> L.Monitor:
+        return L.Monitor(self.maxIter, self.rtol, self.atol, self.dtol, int(self.normType), self.history_cap)
+
+
+# --------------------------------------------------------------- solvers
+class AbstractIterativeSolver:
+    """S/AbstractIterativeSolver.java: identity preconditioner and default
+    monitor until set."""
+
+    kind = L.CG
+
+    def __init__(self, template, restart=0, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        self._lib = self.ctx._lib
+        self.n = len(template) if not isinstance(template, int) else template
+        h = C.c_void_p()
+        _raise(self._lib.mtjg_solver_create(self.ctx.h, self.kind, self.n, restart, C.byref(h)), "solver_create")
+        self.h = h
+        self.M = IdentityPreconditioner(self.n, self.ctx)
+        self.iter = DefaultIterationMonitor()
+        self._mon_key = None
+        self.history = (np.empty(0), np.empty(0, dtype=np.int32))
+
+    def setPreconditioner(self, M: Preconditioner):
+        self.M = M
+        _raise(self._lib.mtjg_solver_set_precond(self.h, M.h), "set_precond")
+
+    def getPreconditioner(self):
+        return self.M
+
+    def setIterationMonitor(self, mon: DefaultIterationMonitor):
+        self.iter = mon
+
+    def getIterationMonitor(self):
+        return self.iter
+
+    def _sync_monitor(self):
+        s = self.iter._struct()
+        key = (s.max_iter, s.rtol, s.atol, s.dtol, s.norm, s.history_cap)
+        if key != self._mon_key:
+            _raise(self._lib.mtjg_solver_set_monitor(self.h, C.byref(s)), "set_monitor")
+            self._mon_key = key
+
+    def solve(self, A: CompRowMatrix, b, x):
+        """IterativeSolver.solve(A, b, x) (S/IterativeSolver.java:30-44)."""
+        if not A.isSquare():
+            raise IllegalArgumentException("!A.isSquare()")
+        b = L.f64(b)
+        if b.shape != (A.numRows(),):
+            raise IllegalArgumentException("b.size() != A.numRows()")
+        if not isinstance(x, np.ndarray) or x.dtype != np.float64 or not x.flags.c_contiguous:
+            raise IllegalArgumentException("x must be a contiguous float64 numpy vector")
+        if x.shape != b.shape:
+            raise IllegalArgumentException("b.size() != x.size()")
+        self._sync_monitor()
+        res = L.Result()
+        code = self._lib.mtjg_solver_solve(self.h, A.h, L.dptr(b), L.dptr(x), C.byref(res))
+        self.iter._iter = res.iterations
+        self.iter._residual = res.residual
+        self.last_result = res
+        self._replay()
+        if code in (L.NOT_CONVERGED_ITERATIONS, L.NOT_CONVERGED_DIVERGENCE, L.NOT_CONVERGED_BREAKDOWN):
+            reason = NotConvergedException.Reason(code)
+            msg = {1: "rho", 2: "omega"}.get(res.detail, "") if code == L.NOT_CONVERGED_BREAKDOWN else ""
+            raise IterativeSolverNotConvergedException(reason, res.residual, res.iterations, msg)
+        _raise(code, "solve")
+        return x
+
+    def _replay(self):
+        cap = self.iter.history_cap
+        if cap <= 0:
+            self.history = (np.empty(0), np.empty(0, dtype=np.int32))
+            return
+        r = np.empty(cap)
+        it = np.empty(cap, dtype=np.int32)
+        ln = C.c_int(0)
+        _raise(self._lib.mtjg_solver_history(self.h, L.dptr(r), L.iptr(it), cap, C.byref(ln)), "history")
+        self.history = (r[: ln.value].copy(), it[: ln.value].copy())
+        if self.iter.reporter is not None:
+            for rv, iv in zip(*self.history):
+                self.iter.reporter.monitor(float(rv), int(iv))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.mtjg_solver_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        # at interpreter shutdown the process is about to release the device
+        if sys.is_finalizing():
+            return
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class CG(AbstractIterativeSolver):
+    """S/CG.java"""
+
+    kind = L.CG
+
+
+class BiCGstab(AbstractIterativeSolver):
+    """S/BiCGstab.java"""
+
+    kind = L.BICGSTAB
+
+
+class GMRES(AbstractIterativeSolver):
+    """S/GMRES.java; restart defaults to 30 (:84-86)."""
+
+    kind = L.GMRES
+
+    def __init__(self, template, restart=30, ctx=None):
+        if restart <= 0:
+            raise IllegalArgumentException("restart must be a positive integer")
+        super().__init__(template, restart, ctx)
+        self.restart = restart

@@ -1,0 +1,727 @@
+/*
+ * mtj_oracle.c -- CPU restatement of MTJ's preconditioned Krylov path.
+ *
+ * TEST INFRASTRUCTURE ONLY (the checker, never the product): see
+ * mtj_oracle.h.  Build with -ffp-contract=off; Java never fuses a*b+c.
+ */
+#include "mtj_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ---------------------------------------------------------------- helpers */
+
+/* java.lang.Math.max for doubles: NaN wins, otherwise the larger value. */
+static double jmax(double a, double b)
+{
+    if (a != a) return a;
+    if (b != b) return b;
+    return a >= b ? a : b;
+}
+
+/* java.util.Arrays.binarySearch(int[], from, to, key) as used through
+ * S/Arrays.java:119-121: index if found, negative otherwise. */
+static int jbinsearch(const int *a, int from, int to, int key)
+{
+    int lo = from, hi = to - 1;
+    while (lo <= hi) {
+        int mid = (int)(((unsigned)lo + (unsigned)hi) >> 1);
+        int v = a[mid];
+        if (v < key) lo = mid + 1;
+        else if (v > key) hi = mid - 1;
+        else return mid;
+    }
+    return -(lo + 1);
+}
+
+/* ------------------------------------------------------- CompRowMatrix */
+
+/* CompRowMatrix.mult(Vector,Vector), S/CompRowMatrix.java:295-314:
+ * y.zero(); row sums in ascending entry order; stored only if != 0. */
+void or_mult(int n, const int *rowptr, const int *colind, const double *val,
+             const double *x, double *y)
+{
+    for (int i = 0; i < n; ++i) y[i] = 0.0;
+    for (int i = 0; i < n; ++i) {
+        double dot = 0;
+        for (int j = rowptr[i]; j < rowptr[i + 1]; j++)
+            dot += val[j] * x[colind[j]];
+        if (dot != 0) y[i] = dot;
+    }
+}
+
+/* CompRowMatrix.multAdd, S/CompRowMatrix.java:330-347: y_i += alpha*dot. */
+void or_mult_add(int n, const int *rowptr, const int *colind, const double *val,
+                 double alpha, const double *x, double *y)
+{
+    for (int i = 0; i < n; ++i) {
+        double dot = 0;
+        for (int j = rowptr[i]; j < rowptr[i + 1]; ++j)
+            dot += val[j] * x[colind[j]];
+        y[i] += alpha * dot;
+    }
+}
+
+/* CompRowMatrix.transMult, S/CompRowMatrix.java:350-366: scatter form. */
+void or_trans_mult(int n, int m, const int *rowptr, const int *colind,
+                   const double *val, const double *x, double *y)
+{
+    for (int i = 0; i < m; ++i) y[i] = 0.0;
+    for (int i = 0; i < n; ++i)
+        for (int j = rowptr[i]; j < rowptr[i + 1]; ++j)
+            y[colind[j]] += val[j] * x[i];
+}
+
+/* CompRowMatrix.transMultAdd, S/CompRowMatrix.java:369-388: y scaled by
+ * 1/alpha, scatter-added, then scaled by alpha (alpha == 0 gives Inf/NaN,
+ * as in the reference). */
+void or_trans_mult_add(int n, int m, const int *rowptr, const int *colind,
+                       const double *val, double alpha, const double *x, double *y)
+{
+    double inv = 1. / alpha;
+    for (int i = 0; i < m; ++i) y[i] *= inv;
+    for (int i = 0; i < n; ++i)
+        for (int j = rowptr[i]; j < rowptr[i + 1]; ++j)
+            y[colind[j]] += val[j] * x[i];
+    for (int i = 0; i < m; ++i) y[i] *= alpha;
+}
+
+/* ---------------------------------------------------------- DenseVector */
+
+/* DenseVector.dot, M/DenseVector.java:267-279 */
+double or_dot(int n, const double *x, const double *y)
+{
+    double dot = 0.;
+    for (int i = 0; i < n; ++i) dot += x[i] * y[i];
+    return dot;
+}
+
+/* AbstractVector.norm dispatch M/AbstractVector.java:180-190 onto
+ * DenseVector.norm1/norm2/norm2_robust/normInf, M/DenseVector.java:282-318 */
+double or_norm(int n, const double *x, int type)
+{
+    if (type == OR_NORM_ONE) {
+        double sum = 0;
+        for (int i = 0; i < n; ++i) sum += fabs(x[i]);
+        return sum;
+    } else if (type == OR_NORM_TWO) {
+        double norm = 0;
+        for (int i = 0; i < n; ++i) norm += x[i] * x[i];
+        return sqrt(norm);
+    } else if (type == OR_NORM_TWO_ROBUST) {
+        double scale = 0, ssq = 1;
+        for (int i = 0; i < n; ++i)
+            if (x[i] != 0) {
+                double absxi = fabs(x[i]);
+                if (scale < absxi) {
+                    ssq = 1 + ssq * (scale / absxi) * (scale / absxi);
+                    scale = absxi;
+                } else
+                    ssq += (absxi / scale) * (absxi / scale);
+            }
+        return scale * sqrt(ssq);
+    } else {
+        double max = 0;
+        for (int i = 0; i < n; ++i) max = jmax(fabs(x[i]), max);
+        return max;
+    }
+}
+
+/* DenseVector.set(alpha, y), M/DenseVector.java:216-231 (alpha==0 zeroes) */
+static void vset_a(int n, double *d, double alpha, const double *y)
+{
+    if (alpha == 0) { for (int i = 0; i < n; ++i) d[i] = 0.0; return; }
+    for (int i = 0; i < n; ++i) d[i] = alpha * y[i];
+}
+
+/* DenseVector.add(alpha, y), M/DenseVector.java:249-264 (alpha==0 no-op) */
+static void vadd_a(int n, double *d, double alpha, const double *y)
+{
+    if (alpha == 0) return;
+    for (int i = 0; i < n; i++) d[i] += alpha * y[i];
+}
+
+/* DenseVector.add(y), M/DenseVector.java:234-246 */
+static void vadd(int n, double *d, const double *y)
+{
+    for (int i = 0; i < n; i++) d[i] += y[i];
+}
+
+/* DenseVector.scale, M/DenseVector.java:196-200 */
+static void vscale(int n, double *d, double alpha)
+{
+    for (int i = 0; i < n; ++i) d[i] *= alpha;
+}
+
+/* ------------------------------------------------------ iteration monitor */
+
+typedef struct mon_state {
+    const or_monitor *cfg;
+    int iter;
+    double initR;
+    double residual;
+    double *hist_r;
+    int *hist_it;
+    int hist_cap;
+    int hist_len;
+} mon_state;
+
+/* AbstractIterationMonitor.converged(double), S/AbstractIterationMonitor.java
+ * :81-93 (reporter hook, then residual, then convergedI) and
+ * DefaultIterationMonitor.convergedI, S/DefaultIterationMonitor.java:133-156.
+ * Returns -1 while running, OR_OK when converged, or a not-converged code. */
+static int mon_check(mon_state *m, double r)
+{
+    if (m->hist_len < m->hist_cap) {
+        m->hist_r[m->hist_len] = r;
+        m->hist_it[m->hist_len] = m->iter;
+    }
+    m->hist_len++;
+    m->residual = r;
+    if (m->iter == 0) m->initR = r;
+    if (r < jmax(m->cfg->rtol * m->initR, m->cfg->atol)) return OR_OK;
+    if (r > m->cfg->dtol * m->initR) return OR_NC_DIVERGENCE;
+    if (m->iter >= m->cfg->max_iter) return OR_NC_ITERATIONS;
+    if (r != r) return OR_NC_DIVERGENCE;
+    return -1;
+}
+
+static int mon_check_vec(mon_state *m, int n, const double *r)
+{
+    return mon_check(m, or_norm(n, r, m->cfg->norm));
+}
+
+/* ------------------------------------------------------- preconditioners */
+
+struct or_pc {
+    int kind;
+    int n;
+    /* Jacobi */
+    double *invdiag;
+    /* ILU / ICC: private CSR copy factored in place + diagonal positions */
+    int *rowptr, *colind, *diagind;
+    double *data;
+    int nnz;
+    double *y; /* the temporary vector of ILU/ICC apply */
+};
+
+or_pc *or_pc_new(int kind, int n)
+{
+    or_pc *pc = (or_pc *)calloc(1, sizeof(or_pc));
+    pc->kind = kind;
+    pc->n = n;
+    pc->y = (double *)calloc((size_t)(n > 0 ? n : 1), sizeof(double));
+    if (kind == OR_PC_JACOBI)
+        pc->invdiag = (double *)calloc((size_t)(n > 0 ? n : 1), sizeof(double));
+    return pc;
+}
+
+void or_pc_free(or_pc *pc)
+{
+    if (!pc) return;
+    free(pc->invdiag);
+    free(pc->rowptr);
+    free(pc->colind);
+    free(pc->diagind);
+    free(pc->data);
+    free(pc->y);
+    free(pc);
+}
+
+/* ILU.findDiagonalIndices S/ILU.java:127-140 / ICC S/ICC.java:141-154 */
+static int find_diag(or_pc *pc, int *detail)
+{
+    int n = pc->n;
+    pc->diagind = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    for (int k = 0; k < n; ++k) {
+        pc->diagind[k] = jbinsearch(pc->colind, pc->rowptr[k], pc->rowptr[k + 1], k);
+        if (pc->diagind[k] < 0) { *detail = k + 1; return OR_ERR_MISSING_DIAGONAL; }
+    }
+    return OR_OK;
+}
+
+/* ILU.factor, S/ILU.java:86-125, including the read of colind[l] after the
+ * scan has left row k (l == rowptr[k+1]), which may update the first entry
+ * of row k+1 when the pattern is structurally nonsymmetric. */
+static int ilu_factor(or_pc *pc, int *detail)
+{
+    int n = pc->n;
+    const int *colind = pc->colind, *rowptr = pc->rowptr, *diagind = pc->diagind;
+    double *data = pc->data;
+    for (int k = 1; k < n; ++k)
+        for (int i = rowptr[k]; i < diagind[k]; ++i) {
+            int index = colind[i];
+            double LUii = data[diagind[index]];
+            if (LUii == 0) { *detail = i + 1; return OR_ERR_ZERO_PIVOT; }
+            double LUki = (data[i] /= LUii);
+            for (int j = diagind[index] + 1, l = rowptr[k] + 1; j < rowptr[index + 1]; ++j) {
+                while (l < rowptr[k + 1] && colind[l] < colind[j]) l++;
+                if (colind[l] == colind[j]) data[l] -= LUki * data[j];
+            }
+        }
+    return OR_OK;
+}
+
+/* ICC.factor, S/ICC.java:85-139, literally: dense row workspace and a scan
+ * over every earlier row.  O(n^2); used on small cases to pin the fast one. */
+static int icc_factor_literal(or_pc *pc, int *detail)
+{
+    int n = pc->n;
+    const int *colind = pc->colind, *rowptr = pc->rowptr, *diagind = pc->diagind;
+    double *data = pc->data;
+    double *Rk = (double *)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
+    for (int k = 0; k < n; ++k) {
+        for (int c = 0; c < n; ++c) Rk[c] = 0;
+        for (int i = rowptr[k]; i < rowptr[k + 1]; ++i) Rk[colind[i]] = data[i];
+        for (int i = 0; i < k; ++i) {
+            double Rii = data[diagind[i]];
+            if (Rii == 0) { free(Rk); *detail = i + 1; return OR_ERR_ZERO_PIVOT; }
+            double Rki = Rk[i] / Rii;
+            if (Rki == 0) continue;
+            for (int j = diagind[i] + 1; j < rowptr[i + 1]; ++j)
+                Rk[colind[j]] -= Rki * data[j];
+        }
+        if (Rk[k] == 0) { free(Rk); *detail = k + 1; return OR_ERR_ZERO_DIAGONAL; }
+        double sqRkk = sqrt(Rk[k]);
+        for (int i = diagind[k]; i < rowptr[k + 1]; ++i) data[i] = Rk[colind[i]] / sqRkk;
+    }
+    free(Rk);
+    return OR_OK;
+}
+
+/* min-heap of column indices for the reach-based ICC */
+typedef struct { int *a; int len, cap; } iheap;
+static void hpush(iheap *h, int v)
+{
+    if (h->len == h->cap) {
+        h->cap = h->cap ? 2 * h->cap : 64;
+        h->a = (int *)realloc(h->a, sizeof(int) * (size_t)h->cap);
+    }
+    int i = h->len++;
+    while (i > 0) {
+        int p = (i - 1) / 2;
+        if (h->a[p] <= v) break;
+        h->a[i] = h->a[p];
+        i = p;
+    }
+    h->a[i] = v;
+}
+static int hpop(iheap *h)
+{
+    int top = h->a[0], v = h->a[--h->len], i = 0;
+    for (;;) {
+        int c = 2 * i + 1;
+        if (c >= h->len) break;
+        if (c + 1 < h->len && h->a[c + 1] < h->a[c]) c++;
+        if (h->a[c] >= v) break;
+        h->a[i] = h->a[c];
+        i = c;
+    }
+    if (h->len) h->a[i] = v;
+    return top;
+}
+
+/* ICC.factor restated over the reach of each row: the literal loop visits
+ * every i < k but only changes Rk through rows i whose Rk[i] is nonzero, and
+ * Rk[i] can only become nonzero by being in row k's pattern or by an update
+ * from a visited row.  Visiting exactly those columns in ascending order
+ * performs the same floating-point operations in the same order.  Rows whose
+ * diagonal became NaN (a negative pivot) make 0/NaN != 0, so the literal loop
+ * applies them to every later row; they are added to every reach. */
+static int icc_factor_reach(or_pc *pc, int *detail)
+{
+    int n = pc->n;
+    const int *colind = pc->colind, *rowptr = pc->rowptr, *diagind = pc->diagind;
+    double *data = pc->data;
+    double *Rk = (double *)calloc((size_t)(n > 0 ? n : 1), sizeof(double));
+    unsigned char *mark = (unsigned char *)calloc((size_t)(n > 0 ? n : 1), 1);
+    int *touched = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    int *nanrows = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    int nnan = 0;
+    iheap h = {0, 0, 0};
+    int st = OR_OK;
+    for (int k = 0; k < n && st == OR_OK; ++k) {
+        int nt = 0;
+        for (int i = rowptr[k]; i < rowptr[k + 1]; ++i) {
+            int c = colind[i];
+            Rk[c] = data[i];
+            if (!mark[c]) { mark[c] = 1; touched[nt++] = c; if (c < k) hpush(&h, c); }
+        }
+        for (int q = 0; q < nnan; ++q) {
+            int c = nanrows[q];
+            if (!mark[c]) { mark[c] = 1; touched[nt++] = c; hpush(&h, c); }
+        }
+        while (h.len) {
+            int i = hpop(&h);
+            double Rii = data[diagind[i]];
+            if (Rii == 0) { *detail = i + 1; st = OR_ERR_ZERO_PIVOT; break; }
+            double Rki = Rk[i] / Rii;
+            if (Rki == 0) continue;
+            for (int j = diagind[i] + 1; j < rowptr[i + 1]; ++j) {
+                int c = colind[j];
+                Rk[c] -= Rki * data[j];
+                if (!mark[c]) { mark[c] = 1; touched[nt++] = c; if (c < k) hpush(&h, c); }
+            }
+        }
+        if (st == OR_OK) {
+            if (Rk[k] == 0) { *detail = k + 1; st = OR_ERR_ZERO_DIAGONAL; }
+            else {
+                double sqRkk = sqrt(Rk[k]);
+                for (int i = diagind[k]; i < rowptr[k + 1]; ++i) data[i] = Rk[colind[i]] / sqRkk;
+                if (data[diagind[k]] != data[diagind[k]]) nanrows[nnan++] = k;
+            }
+        }
+        for (int t = 0; t < nt; ++t) { Rk[touched[t]] = 0; mark[touched[t]] = 0; }
+        h.len = 0;
+    }
+    free(h.a);
+    free(Rk);
+    free(mark);
+    free(touched);
+    free(nanrows);
+    return st;
+}
+
+int or_pc_set_matrix(or_pc *pc, int n, const int *rowptr, const int *colind,
+                     const double *val, int *detail)
+{
+    int dummy;
+    if (!detail) detail = &dummy;
+    *detail = 0;
+    if (n != pc->n) return OR_ERR_ILLEGAL_ARGUMENT;
+    if (pc->kind == OR_PC_IDENTITY) return OR_OK;
+    if (pc->kind == OR_PC_JACOBI) {
+        /* DiagonalPreconditioner.setMatrix, S/DiagonalPreconditioner.java:64-76,
+         * with CompRowMatrix.get (binary search) S/CompRowMatrix.java:407-417 */
+        for (int i = 0; i < n; ++i) {
+            int idx = jbinsearch(colind, rowptr[i], rowptr[i + 1], i);
+            double d = idx >= 0 ? val[idx] : 0.0;
+            if (d == 0) { *detail = i + 1; return OR_ERR_ZERO_DIAGONAL; }
+            pc->invdiag[i] = 1 / d;
+        }
+        return OR_OK;
+    }
+    /* ILU/ICC: LU.set(A) / R.set(A) copies A into the private CSR
+     * (S/ILU.java:80-84, S/ICC.java:79-83) */
+    int nnz = rowptr[n];
+    free(pc->rowptr); free(pc->colind); free(pc->data); free(pc->diagind);
+    pc->diagind = NULL;
+    pc->nnz = nnz;
+    pc->rowptr = (int *)malloc(sizeof(int) * (size_t)(n + 1));
+    pc->colind = (int *)malloc(sizeof(int) * (size_t)(nnz > 0 ? nnz : 1));
+    pc->data = (double *)malloc(sizeof(double) * (size_t)(nnz > 0 ? nnz : 1));
+    memcpy(pc->rowptr, rowptr, sizeof(int) * (size_t)(n + 1));
+    if (nnz) {
+        memcpy(pc->colind, colind, sizeof(int) * (size_t)nnz);
+        memcpy(pc->data, val, sizeof(double) * (size_t)nnz);
+    }
+    int st = find_diag(pc, detail);
+    if (st != OR_OK) return st;
+    if (pc->kind == OR_PC_ILU) return ilu_factor(pc, detail);
+    if (pc->kind == OR_PC_ICC_LITERAL) return icc_factor_literal(pc, detail);
+    return icc_factor_reach(pc, detail);
+}
+
+int or_pc_values(const or_pc *pc, double *out, int cap)
+{
+    if (pc->kind == OR_PC_JACOBI) {
+        int m = pc->n < cap ? pc->n : cap;
+        memcpy(out, pc->invdiag, sizeof(double) * (size_t)m);
+        return pc->n;
+    }
+    if (!pc->data) return 0;
+    int m = pc->nnz < cap ? pc->nnz : cap;
+    memcpy(out, pc->data, sizeof(double) * (size_t)m);
+    return pc->nnz;
+}
+
+/* UnitLowerCompRowMatrix.solve, S/UnitLowerCompRowMatrix.java:49-67 */
+static void lower_solve(const or_pc *pc, const double *b, double *x)
+{
+    for (int i = 0; i < pc->n; ++i) {
+        double sum = 0;
+        for (int j = pc->rowptr[i]; j < pc->diagind[i]; ++j)
+            sum += pc->data[j] * x[pc->colind[j]];
+        x[i] = b[i] - sum;
+    }
+}
+
+/* UnitLowerCompRowMatrix.transSolve, S/UnitLowerCompRowMatrix.java:70-86 */
+static void lower_trans_solve(const or_pc *pc, const double *b, double *x)
+{
+    if (x != b) memcpy(x, b, sizeof(double) * (size_t)pc->n);
+    for (int i = pc->n - 1; i >= 0; --i)
+        for (int j = pc->rowptr[i]; j < pc->diagind[i]; ++j)
+            x[pc->colind[j]] -= pc->data[j] * x[i];
+}
+
+/* UpperCompRowMatrix.solve, S/UpperCompRowMatrix.java:49-67 */
+static void upper_solve(const or_pc *pc, const double *b, double *x)
+{
+    for (int i = pc->n - 1; i >= 0; --i) {
+        double sum = 0;
+        for (int j = pc->diagind[i] + 1; j < pc->rowptr[i + 1]; ++j)
+            sum += pc->data[j] * x[pc->colind[j]];
+        x[i] = (b[i] - sum) / pc->data[pc->diagind[i]];
+    }
+}
+
+/* UpperCompRowMatrix.transSolve, S/UpperCompRowMatrix.java:70-90 */
+static void upper_trans_solve(const or_pc *pc, const double *b, double *x)
+{
+    if (x != b) memcpy(x, b, sizeof(double) * (size_t)pc->n);
+    for (int i = 0; i < pc->n; ++i) {
+        x[i] /= pc->data[pc->diagind[i]];
+        for (int j = pc->diagind[i] + 1; j < pc->rowptr[i + 1]; ++j)
+            x[pc->colind[j]] -= pc->data[j] * x[i];
+    }
+}
+
+void or_pc_apply(or_pc *pc, const double *b, double *x)
+{
+    int n = pc->n;
+    switch (pc->kind) {
+    case OR_PC_IDENTITY: /* S/AbstractIterativeSolver.java:82-96 */
+        if (x != b) memcpy(x, b, sizeof(double) * (size_t)n);
+        break;
+    case OR_PC_JACOBI: /* S/DiagonalPreconditioner.java:47-58 */
+        for (int i = 0; i < n; ++i) x[i] = b[i] * pc->invdiag[i];
+        break;
+    case OR_PC_ILU: /* S/ILU.java:64-70 */
+        lower_solve(pc, b, pc->y);
+        upper_solve(pc, pc->y, x);
+        break;
+    default: /* ICC.apply S/ICC.java:67-73 */
+        upper_trans_solve(pc, b, pc->y);
+        upper_solve(pc, pc->y, x);
+        break;
+    }
+}
+
+void or_pc_trans_apply(or_pc *pc, const double *b, double *x)
+{
+    if (pc->kind == OR_PC_ILU) { /* S/ILU.java:72-78 */
+        upper_trans_solve(pc, b, pc->y);
+        lower_trans_solve(pc, pc->y, x);
+    } else {
+        or_pc_apply(pc, b, x);
+    }
+}
+
+/* ---------------------------------------------------------------- solvers */
+
+static void pc_apply_or_identity(or_pc *pc, int n, const double *b, double *x)
+{
+    if (pc) or_pc_apply(pc, b, x);
+    else if (x != b) memcpy(x, b, sizeof(double) * (size_t)n);
+}
+
+/* CG.solve, S/CG.java:58-87 */
+static int cg_solve(int n, const int *rp, const int *ci, const double *v, or_pc *pc,
+                    const double *b, double *x, mon_state *m, int *detail)
+{
+    (void)detail;
+    double alpha = 0, beta = 0, rho = 0, rho_1 = 0;
+    double *p = calloc((size_t)n + 1, 8), *z = calloc((size_t)n + 1, 8);
+    double *q = calloc((size_t)n + 1, 8), *r = calloc((size_t)n + 1, 8);
+    memcpy(r, b, sizeof(double) * (size_t)n);
+    or_mult_add(n, rp, ci, v, -1, x, r);
+    int st;
+    for (m->iter = 0; (st = mon_check_vec(m, n, r)) < 0; m->iter++) {
+        pc_apply_or_identity(pc, n, r, z);
+        rho = or_dot(n, r, z);
+        if (m->iter == 0)
+            memcpy(p, z, sizeof(double) * (size_t)n);
+        else {
+            beta = rho / rho_1;
+            vscale(n, p, beta);
+            vadd(n, p, z);
+        }
+        or_mult(n, rp, ci, v, p, q);
+        alpha = rho / or_dot(n, p, q);
+        vadd_a(n, x, alpha, p);
+        vadd_a(n, r, -alpha, q);
+        rho_1 = rho;
+    }
+    free(p); free(z); free(q); free(r);
+    return st;
+}
+
+/* BiCGstab.solve, S/BiCGstab.java:65-116 */
+static int bicgstab_solve(int n, const int *rp, const int *ci, const double *v, or_pc *pc,
+                          const double *b, double *x, mon_state *m, int *detail)
+{
+    double rho_1 = 1, rho_2 = 1, alpha = 1, beta = 1, omega = 1;
+    size_t sz = (size_t)n + 1;
+    double *p = calloc(sz, 8), *s = calloc(sz, 8), *phat = calloc(sz, 8), *shat = calloc(sz, 8);
+    double *t = calloc(sz, 8), *vv = calloc(sz, 8), *temp = calloc(sz, 8), *r = calloc(sz, 8);
+    double *rtilde = calloc(sz, 8);
+    memcpy(r, b, sizeof(double) * (size_t)n);
+    or_mult_add(n, rp, ci, v, -1, x, r);
+    memcpy(rtilde, r, sizeof(double) * (size_t)n);
+    int st;
+    for (m->iter = 0; (st = mon_check_vec(m, n, r)) < 0; m->iter++) {
+        rho_1 = or_dot(n, rtilde, r);
+        if (rho_1 == 0) { st = OR_NC_BREAKDOWN; *detail = 1; break; }
+        if (omega == 0) { st = OR_NC_BREAKDOWN; *detail = 2; break; }
+        if (m->iter == 0)
+            memcpy(p, r, sizeof(double) * (size_t)n);
+        else {
+            beta = (rho_1 / rho_2) * (alpha / omega);
+            vset_a(n, temp, -omega, vv);
+            vadd(n, temp, p);
+            memcpy(p, r, sizeof(double) * (size_t)n);
+            vadd_a(n, p, beta, temp);
+        }
+        pc_apply_or_identity(pc, n, p, phat);
+        or_mult(n, rp, ci, v, phat, vv);
+        alpha = rho_1 / or_dot(n, rtilde, vv);
+        memcpy(s, r, sizeof(double) * (size_t)n);
+        vadd_a(n, s, -alpha, vv);
+        vadd_a(n, x, alpha, phat);
+        st = mon_check_vec(m, n, s);
+        if (st >= 0) break;
+        pc_apply_or_identity(pc, n, s, shat);
+        or_mult(n, rp, ci, v, shat, t);
+        omega = or_dot(n, t, s) / or_dot(n, t, t);
+        vadd_a(n, x, omega, shat);
+        memcpy(r, s, sizeof(double) * (size_t)n);
+        vadd_a(n, r, -omega, t);
+        rho_2 = rho_1;
+    }
+    free(p); free(s); free(phat); free(shat); free(t); free(vv); free(temp); free(r); free(rtilde);
+    return st;
+}
+
+/* GivensRotation(x, y), M/GivensRotation.java:42-58 */
+static void givens(double x, double y, double *c, double *s)
+{
+    double roe = fabs(x) > fabs(y) ? x : y;
+    double scale = fabs(x) + fabs(y);
+    if (scale != 0) {
+        double xs = x / scale;
+        double ys = y / scale;
+        double r = scale * sqrt(xs * xs + ys * ys);
+        if (roe < 0) r *= -1;
+        *c = x / r;
+        *s = y / r;
+    } else {
+        *c = 1;
+        *s = 0;
+    }
+}
+
+/* GivensRotation.apply on two entries, M/GivensRotation.java:72-92 */
+static void givens_apply(double c, double s, double *a1, double *a2)
+{
+    double temp = c * *a1 + s * *a2;
+    *a2 = -s * *a1 + c * *a2;
+    *a1 = temp;
+}
+
+/* UpperTriangDenseMatrix(H, i, false).solve(s, s), S/GMRES.java:166 ->
+ * M/AbstractTriangDenseMatrix.java:228-257 -> LAPACK dtrtrs('U','N','N').
+ * dtrtrs reports info = k when A(k,k) == 0 (checked first, k ascending),
+ * otherwise solves with dtrsm; the netlib reference dtrsm for one right-hand
+ * side, Left/Upper/NoTrans/NonUnit, walks k = n..1: when b(k) != 0,
+ * b(k) /= A(k,k) and b(i) -= b(k)*A(i,k) for i < k. */
+static int dtrtrs_upper(int nn, const double *H, int ld, double *b)
+{
+    for (int k = 0; k < nn; ++k)
+        if (H[k + (size_t)k * ld] == 0) return k + 1;
+    for (int k = nn - 1; k >= 0; --k) {
+        if (b[k] != 0) {
+            b[k] = b[k] / H[k + (size_t)k * ld];
+            for (int i = 0; i < k; ++i) b[i] = b[i] - b[k] * H[i + (size_t)k * ld];
+        }
+    }
+    return 0;
+}
+
+/* GMRES.solve, S/GMRES.java:127-176 (restart from GMRES(template, restart),
+ * :99-125).  The reference also computes M.apply(b, u) at :134; u is
+ * overwritten before any read, so that dead call is not repeated here. */
+static int gmres_solve(int restart, int n, const int *rp, const int *ci, const double *v,
+                       or_pc *pc, const double *b, double *x, mon_state *m, int *detail)
+{
+    (void)detail;
+    size_t sz = (size_t)n + 1;
+    int ld = restart + 1;
+    double *w = calloc(sz, 8), *u = calloc(sz, 8), *r = calloc(sz, 8);
+    double *s = calloc((size_t)restart + 1, 8);
+    double *H = calloc((size_t)(restart + 1) * (size_t)restart, 8);
+    double *rc = calloc((size_t)restart + 1, 8), *rs = calloc((size_t)restart + 1, 8);
+    double **V = malloc(sizeof(double *) * (size_t)(restart + 1));
+    for (int i = 0; i <= restart; ++i) V[i] = calloc(sz, 8);
+
+    memcpy(u, b, sizeof(double) * (size_t)n);
+    or_mult_add(n, rp, ci, v, -1, x, u);
+    pc_apply_or_identity(pc, n, u, r);
+    double normr = or_norm(n, r, OR_NORM_TWO);
+
+    int st;
+    for (m->iter = 0; (st = mon_check_vec(m, n, r)) < 0; m->iter++) {
+        vset_a(n, V[0], 1 / normr, r);
+        for (int k = 0; k <= restart; ++k) s[k] = 0;
+        s[0] = normr;
+        int i = 0;
+        for (; i < restart; i++, m->iter++) {
+            st = mon_check(m, fabs(s[i]));
+            if (st > 0) goto done;     /* exception out of the inner loop */
+            if (st == OR_OK) break;
+            or_mult(n, rp, ci, v, V[i], u);
+            pc_apply_or_identity(pc, n, u, w);
+            for (int k = 0; k <= i; k++) {
+                H[k + (size_t)i * ld] = or_dot(n, w, V[k]);
+                vadd_a(n, w, -H[k + (size_t)i * ld], V[k]);
+            }
+            H[i + 1 + (size_t)i * ld] = or_norm(n, w, OR_NORM_TWO);
+            vset_a(n, V[i + 1], 1. / H[i + 1 + (size_t)i * ld], w);
+            for (int k = 0; k < i; ++k)
+                givens_apply(rc[k], rs[k], &H[k + (size_t)i * ld], &H[k + 1 + (size_t)i * ld]);
+            givens(H[i + (size_t)i * ld], H[i + 1 + (size_t)i * ld], &rc[i], &rs[i]);
+            givens_apply(rc[i], rs[i], &H[i + (size_t)i * ld], &H[i + 1 + (size_t)i * ld]);
+            givens_apply(rc[i], rs[i], &s[i], &s[i + 1]);
+        }
+        if (dtrtrs_upper(i, H, ld, s) != 0) { st = OR_ERR_SINGULAR; goto done; }
+        for (int j = 0; j < i; j++) vadd_a(n, x, s[j], V[j]);
+        memcpy(u, b, sizeof(double) * (size_t)n);
+        or_mult_add(n, rp, ci, v, -1, x, u);
+        pc_apply_or_identity(pc, n, u, r);
+        normr = or_norm(n, r, OR_NORM_TWO);
+    }
+done:
+    for (int i = 0; i <= restart; ++i) free(V[i]);
+    free(V); free(w); free(u); free(r); free(s); free(H); free(rc); free(rs);
+    return st;
+}
+
+int or_solve(int kind, int restart, int n, const int *rowptr, const int *colind,
+             const double *val, or_pc *pc, const double *b, double *x,
+             const or_monitor *mon, or_result *res,
+             double *hist_r, int *hist_it, int hist_cap)
+{
+    mon_state m;
+    memset(&m, 0, sizeof(m));
+    m.cfg = mon;
+    m.hist_r = hist_r;
+    m.hist_it = hist_it;
+    m.hist_cap = hist_r && hist_it ? hist_cap : 0;
+    int detail = 0, st;
+    if (pc && pc->n != n) return OR_ERR_ILLEGAL_ARGUMENT;
+    if (kind == OR_CG) st = cg_solve(n, rowptr, colind, val, pc, b, x, &m, &detail);
+    else if (kind == OR_BICGSTAB) st = bicgstab_solve(n, rowptr, colind, val, pc, b, x, &m, &detail);
+    else {
+        if (restart <= 0) return OR_ERR_ILLEGAL_ARGUMENT;
+        st = gmres_solve(restart, n, rowptr, colind, val, pc, b, x, &m, &detail);
+    }
+    if (res) {
+        res->status = st;
+        res->iterations = m.iter;
+        res->residual = m.residual;
+        res->detail = detail;
+        res->history_len = m.hist_len;
+    }
+    return st;
+}

@@ -1,0 +1,341 @@
+"""A second, independent restatement of MTJ's Krylov path in pure Python.
+
+Python floats are IEEE doubles and Python never fuses a*b+c, so each
+expression rounds exactly as the Java source does.  Small cases only: it is
+the cross-check that pins the C oracle (oracle/mtj_oracle.c) bit for bit.
+References are files of the reference project (S/ = .../matrix/sparse/,
+M/ = .../matrix/).
+"""
+from __future__ import annotations
+
+import bisect
+import math
+
+
+class NotConverged(Exception):
+    def __init__(self, code, iters, resid, detail=0):
+        super().__init__(code)
+        self.code, self.iters, self.resid, self.detail = code, iters, resid, detail
+
+
+class Singular(Exception):
+    pass
+
+
+def jmax(a, b):
+    if a != a:
+        return a
+    if b != b:
+        return b
+    return a if a >= b else b
+
+
+def mult(rp, ci, v, x):
+    """CompRowMatrix.mult, S/CompRowMatrix.java:295-314."""
+    n = len(rp) - 1
+    y = [0.0] * n
+    for i in range(n):
+        s = 0.0
+        for k in range(rp[i], rp[i + 1]):
+            s = s + v[k] * x[ci[k]]
+        if s != 0:
+            y[i] = s
+    return y
+
+
+def mult_add(rp, ci, v, alpha, x, y):
+    """CompRowMatrix.multAdd, S/CompRowMatrix.java:330-347."""
+    y = list(y)
+    for i in range(len(rp) - 1):
+        s = 0.0
+        for k in range(rp[i], rp[i + 1]):
+            s = s + v[k] * x[ci[k]]
+        y[i] = y[i] + alpha * s
+    return y
+
+
+def dot(x, y):
+    s = 0.0
+    for a, b in zip(x, y):
+        s = s + a * b
+    return s
+
+
+def norm2(x):
+    s = 0.0
+    for a in x:
+        s = s + a * a
+    return math.sqrt(s)
+
+
+class Monitor:
+    """DefaultIterationMonitor, S/DefaultIterationMonitor.java:133-156."""
+
+    def __init__(self, max_iter, rtol, atol=1e-50, dtol=1e5):
+        self.max_iter, self.rtol, self.atol, self.dtol = max_iter, rtol, atol, dtol
+        self.iter = 0
+        self.initR = 0.0
+        self.residual = 0.0
+        self.hist = []
+
+    def converged(self, r):
+        self.hist.append((r, self.iter))
+        self.residual = r
+        if self.iter == 0:
+            self.initR = r
+        if r < jmax(self.rtol * self.initR, self.atol):
+            return True
+        if r > self.dtol * self.initR:
+            raise NotConverged(2, self.iter, r)
+        if self.iter >= self.max_iter:
+            raise NotConverged(1, self.iter, r)
+        if r != r:
+            raise NotConverged(2, self.iter, r)
+        return False
+
+
+def jacobi(rp, ci, v):
+    """DiagonalPreconditioner.setMatrix, S/DiagonalPreconditioner.java:64-76."""
+    n = len(rp) - 1
+    inv = [0.0] * n
+    for i in range(n):
+        cols = ci[rp[i]:rp[i + 1]]
+        j = bisect.bisect_left(cols, i)
+        d = v[rp[i] + j] if j < len(cols) and cols[j] == i else 0.0
+        if d == 0:
+            raise RuntimeError(f"Zero diagonal on row {i + 1}")
+        inv[i] = 1 / d
+    return lambda b: [b[i] * inv[i] for i in range(n)]
+
+
+def diag_positions(rp, ci):
+    out = []
+    for k in range(len(rp) - 1):
+        cols = ci[rp[k]:rp[k + 1]]
+        j = bisect.bisect_left(cols, k)
+        if j >= len(cols) or cols[j] != k:
+            raise RuntimeError(f"Missing diagonal entry on row {k + 1}")
+        out.append(rp[k] + j)
+    return out
+
+
+def ilu_factor(rp, ci, v):
+    """ILU.factor, S/ILU.java:86-125 (with its scan past the row end)."""
+    n = len(rp) - 1
+    data = list(v)
+    cix = list(ci) + [-1]  # an index past the last row reads nothing that matches
+    dg = diag_positions(rp, ci)
+    for k in range(1, n):
+        for i in range(rp[k], dg[k]):
+            index = cix[i]
+            piv = data[dg[index]]
+            if piv == 0:
+                raise RuntimeError(f"Zero pivot encountered on row {i + 1} during ILU process")
+            data[i] = data[i] / piv
+            lki = data[i]
+            l = rp[k] + 1
+            for j in range(dg[index] + 1, rp[index + 1]):
+                while l < rp[k + 1] and cix[l] < cix[j]:
+                    l += 1
+                if cix[l] == cix[j]:
+                    data[l] = data[l] - lki * data[j]
+    return data, dg
+
+
+def ilu_apply(rp, ci, data, dg, b):
+    """ILU.apply (S/ILU.java:64-70): unit-lower then upper gather solves."""
+    n = len(rp) - 1
+    y = [0.0] * n
+    for i in range(n):
+        s = 0.0
+        for k in range(rp[i], dg[i]):
+            s = s + data[k] * y[ci[k]]
+        y[i] = b[i] - s
+    x = [0.0] * n
+    for i in range(n - 1, -1, -1):
+        s = 0.0
+        for k in range(dg[i] + 1, rp[i + 1]):
+            s = s + data[k] * x[ci[k]]
+        x[i] = (y[i] - s) / data[dg[i]]
+    return x
+
+
+def icc_factor(rp, ci, v):
+    """ICC.factor, S/ICC.java:85-139, literally (O(n^2))."""
+    n = len(rp) - 1
+    data = list(v)
+    dg = diag_positions(rp, ci)
+    for k in range(n):
+        Rk = [0.0] * n
+        for e in range(rp[k], rp[k + 1]):
+            Rk[ci[e]] = data[e]
+        for i in range(k):
+            Rii = data[dg[i]]
+            if Rii == 0:
+                raise RuntimeError("zero pivot")
+            Rki = Rk[i] / Rii
+            if Rki == 0:
+                continue
+            for j in range(dg[i] + 1, rp[i + 1]):
+                Rk[ci[j]] = Rk[ci[j]] - Rki * data[j]
+        if Rk[k] == 0:
+            raise RuntimeError("zero diagonal")
+        sq = math.sqrt(Rk[k])
+        for e in range(dg[k], rp[k + 1]):
+            data[e] = Rk[ci[e]] / sq
+    return data, dg
+
+
+def icc_apply(rp, ci, data, dg, b):
+    """ICC.apply (S/ICC.java:67-73): R' scatter solve then R gather solve."""
+    n = len(rp) - 1
+    y = list(b)
+    for i in range(n):
+        y[i] = y[i] / data[dg[i]]
+        for k in range(dg[i] + 1, rp[i + 1]):
+            y[ci[k]] = y[ci[k]] - data[k] * y[i]
+    x = [0.0] * n
+    for i in range(n - 1, -1, -1):
+        s = 0.0
+        for k in range(dg[i] + 1, rp[i + 1]):
+            s = s + data[k] * x[ci[k]]
+        x[i] = (y[i] - s) / data[dg[i]]
+    return x
+
+
+def cg(rp, ci, v, b, x, M, mon):
+    """CG.solve, S/CG.java:58-87."""
+    n = len(b)
+    x = list(x)
+    r = mult_add(rp, ci, v, -1.0, x, b)
+    p = [0.0] * n
+    rho_1 = 0.0
+    mon.iter = 0
+    while not mon.converged(norm2(r)):
+        z = M(r)
+        rho = dot(r, z)
+        if mon.iter == 0:
+            p = list(z)
+        else:
+            beta = rho / rho_1
+            p = [p[i] * beta for i in range(n)]
+            p = [p[i] + z[i] for i in range(n)]
+        q = mult(rp, ci, v, p)
+        alpha = rho / dot(p, q)
+        if alpha != 0:
+            x = [x[i] + alpha * p[i] for i in range(n)]
+            r = [r[i] + (-alpha) * q[i] for i in range(n)]
+        rho_1 = rho
+        mon.iter += 1
+    return x
+
+
+def bicgstab(rp, ci, v, b, x, M, mon):
+    """BiCGstab.solve, S/BiCGstab.java:65-116."""
+    n = len(b)
+    x = list(x)
+    rho_1 = rho_2 = alpha = beta = omega = 1.0
+    r = mult_add(rp, ci, v, -1.0, x, b)
+    rt = list(r)
+    p = [0.0] * n
+    vv = [0.0] * n
+    mon.iter = 0
+    while not mon.converged(norm2(r)):
+        rho_1 = dot(rt, r)
+        if rho_1 == 0:
+            raise NotConverged(3, mon.iter, mon.residual, 1)
+        if omega == 0:
+            raise NotConverged(3, mon.iter, mon.residual, 2)
+        if mon.iter == 0:
+            p = list(r)
+        else:
+            beta = (rho_1 / rho_2) * (alpha / omega)
+            temp = [(-omega) * vv[i] for i in range(n)]
+            temp = [temp[i] + p[i] for i in range(n)]
+            p = list(r) if beta == 0 else [r[i] + beta * temp[i] for i in range(n)]
+        phat = M(p)
+        vv = mult(rp, ci, v, phat)
+        alpha = rho_1 / dot(rt, vv)
+        s = list(r) if alpha == 0 else [r[i] + (-alpha) * vv[i] for i in range(n)]
+        if alpha != 0:
+            x = [x[i] + alpha * phat[i] for i in range(n)]
+        if mon.converged(norm2(s)):
+            return x
+        shat = M(s)
+        t = mult(rp, ci, v, shat)
+        omega = dot(t, s) / dot(t, t)
+        if omega != 0:
+            x = [x[i] + omega * shat[i] for i in range(n)]
+        r = list(s) if omega == 0 else [s[i] + (-omega) * t[i] for i in range(n)]
+        rho_2 = rho_1
+        mon.iter += 1
+    return x
+
+
+def _givens(a, b):
+    """GivensRotation(x, y), M/GivensRotation.java:42-58."""
+    roe = a if abs(a) > abs(b) else b
+    scale = abs(a) + abs(b)
+    if scale != 0:
+        xs, ys = a / scale, b / scale
+        r = scale * math.sqrt(xs * xs + ys * ys)
+        if roe < 0:
+            r *= -1
+        return a / r, b / r
+    return 1.0, 0.0
+
+
+def _rot(c, s, a1, a2):
+    return c * a1 + s * a2, -s * a1 + c * a2
+
+
+def gmres(rp, ci, v, b, x, M, mon, restart=30):
+    """GMRES.solve, S/GMRES.java:127-176 with dtrtrs per the netlib reference."""
+    n = len(b)
+    x = list(x)
+    H = [[0.0] * restart for _ in range(restart + 1)]
+    rots = [None] * (restart + 1)
+    u = mult_add(rp, ci, v, -1.0, x, b)
+    r = M(u)
+    normr = norm2(r)
+    mon.iter = 0
+    while not mon.converged(norm2(r)):
+        a = 1 / normr
+        V = [[0.0] * n if a == 0 else [a * r[j] for j in range(n)]]
+        s = [0.0] * (restart + 1)
+        s[0] = normr
+        i = 0
+        while i < restart and not mon.converged(abs(s[i])):
+            u = mult(rp, ci, v, V[i])
+            w = M(u)
+            for k in range(i + 1):
+                H[k][i] = dot(w, V[k])
+                h = -H[k][i]
+                if h != 0:
+                    w = [w[j] + h * V[k][j] for j in range(n)]
+            H[i + 1][i] = norm2(w)
+            a = 1. / H[i + 1][i]
+            V.append([0.0] * n if a == 0 else [a * w[j] for j in range(n)])
+            for k in range(i):
+                H[k][i], H[k + 1][i] = _rot(rots[k][0], rots[k][1], H[k][i], H[k + 1][i])
+            rots[i] = _givens(H[i][i], H[i + 1][i])
+            H[i][i], H[i + 1][i] = _rot(rots[i][0], rots[i][1], H[i][i], H[i + 1][i])
+            s[i], s[i + 1] = _rot(rots[i][0], rots[i][1], s[i], s[i + 1])
+            i += 1
+            mon.iter += 1
+        for k in range(i):
+            if H[k][k] == 0:
+                raise Singular()
+        for k in range(i - 1, -1, -1):
+            if s[k] != 0:
+                s[k] = s[k] / H[k][k]
+                for q in range(k):
+                    s[q] = s[q] - s[k] * H[q][k]
+        for j in range(i):
+            if s[j] != 0:
+                x = [x[t] + s[j] * V[j][t] for t in range(n)]
+        u = mult_add(rp, ci, v, -1.0, x, b)
+        r = M(u)
+        normr = norm2(r)
+        mon.iter += 1
+    return x

@@ -1,0 +1,403 @@
+"""GPU library vs the oracle: CSR products, preconditioners, solvers.
+
+Tolerances: STRICT numerics are bit-exact for products, factors and
+triangular solves (Java's rounding); FAST numerics (fused multiply-add) are
+within 1e-13 of the row's magnitude sum(|a_ij x_j|) for a product.  Solvers
+must match the oracle's iteration count within +-2 and its relative residual
+history r_k / r_0 within 1e-10 over the common prefix, the bar MTJ's drop-in
+states.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from helpers import dense_to_csr, nonsingular_system, pentadiagonal, spd_system, tridiagonal
+from mtjg import sparse, workloads
+
+pytestmark = pytest.mark.gpu
+
+FAST, STRICT = 0, 1
+
+
+@pytest.fixture(params=[FAST, STRICT], ids=["fast", "strict"])
+def numerics(request, ctx):
+    ctx.setNumerics(request.param)
+    yield request.param
+    ctx.setNumerics(FAST)
+
+
+def _mats():
+    out = {}
+    out["poisson2d_20"] = workloads.poisson2d(20)
+    out["poisson3d_12"] = workloads.poisson3d(12)
+    out["convdiff3d_10"] = workloads.convdiff3d(10)
+    out["laplacian_3000"] = workloads.laplacian(3000, 7)
+    rng = np.random.default_rng(3)
+    n, m, rp, ci, v = dense_to_csr(rng.random((90, 70)) * (rng.random((90, 70)) < 0.6), keep_diag=False)
+    out["rect_dense_rows"] = (n, rp, ci, v, m)
+    return out
+
+
+MATS = _mats()
+
+
+def _unpack(t):
+    if len(t) == 5:
+        n, rp, ci, v, m = t
+        return n, m, rp, ci, v
+    n, rp, ci, v = t
+    return n, n, rp, ci, v
+
+
+def _row_scale(n, rp, ci, v, x):
+    s = np.zeros(n)
+    for i in range(n):
+        s[i] = np.sum(np.abs(v[rp[i]:rp[i + 1]] * x[ci[rp[i]:rp[i + 1]]]))
+    return s
+
+
+@pytest.mark.parametrize("name", sorted(MATS))
+def test_products(ctx, numerics, name):
+    n, m, rp, ci, v = _unpack(MATS[name])
+    A = sparse.CompRowMatrix(n, m, rp, ci, v, ctx)
+    Ao = O.Csr(n, m, rp, ci, v)
+    x = workloads.uniform(m, 11)
+    xt = workloads.uniform(n, 12)
+    y0 = workloads.uniform(n, 13)
+    yt0 = workloads.uniform(m, 14)
+    got = {
+        "mult": A.mult(x),
+        "multAdd": A.multAdd(-0.75, x, y0.copy()),
+        "transMult": A.transMult(xt),
+        "transMultAdd": A.transMultAdd(1.5, xt, yt0.copy()),
+    }
+    want = {
+        "mult": O.mult(Ao, x),
+        "multAdd": O.mult_add(Ao, -0.75, x, y0),
+        "transMult": O.trans_mult(Ao, xt),
+        "transMultAdd": O.trans_mult_add(Ao, 1.5, xt, yt0),
+    }
+    if numerics == STRICT:
+        for k in got:
+            assert np.array_equal(got[k], want[k]), k
+    else:
+        sc = _row_scale(n, rp, ci, v, x)
+        assert np.all(np.abs(got["mult"] - want["mult"]) <= 1e-13 * sc + 1e-300)
+        assert np.all(np.abs(got["multAdd"] - want["multAdd"]) <= 1e-13 * (0.75 * sc + np.abs(y0)) + 1e-300)
+        for k in ("transMult", "transMultAdd"):
+            assert np.allclose(got[k], want[k], rtol=1e-12, atol=1e-12), k
+
+
+def test_mult_zero_sum_is_positive_zero(ctx):
+    # CompRowMatrix.mult stores a row sum only when it is != 0: -0.0 becomes +0.0
+    n, m, rp, ci, v = dense_to_csr(np.array([[1.0, 1.0], [0.0, 2.0]]))
+    A = sparse.CompRowMatrix(n, m, rp, ci, v, ctx)
+    y = A.mult(np.array([-0.0, -0.0]))
+    assert np.all(np.signbit(y) == False)  # noqa: E712
+
+
+def test_long_row_and_empty_rows(ctx, numerics):
+    rng = np.random.default_rng(5)
+    n, m = 40, 9000
+    rows = []
+    for i in range(n):
+        if i == 3:
+            cols = np.arange(0, m, 2)  # 4500 entries: longer than one tile
+        elif i % 7 == 0:
+            cols = np.array([], dtype=np.int64)  # empty row
+        else:
+            cols = np.sort(rng.choice(m, size=int(rng.integers(1, 40)), replace=False))
+        rows.append(cols)
+    rp = np.zeros(n + 1, dtype=np.int32)
+    rp[1:] = np.cumsum([len(c) for c in rows])
+    ci = np.concatenate(rows).astype(np.int32)
+    v = rng.standard_normal(len(ci))
+    A = sparse.CompRowMatrix(n, m, rp, ci, v, ctx)
+    Ao = O.Csr(n, m, rp, ci, v)
+    x = workloads.uniform(m, 21)
+    y = A.mult(x)
+    yo = O.mult(Ao, x)
+    if numerics == STRICT:
+        assert np.array_equal(y, yo)
+    else:
+        assert np.all(np.abs(y - yo) <= 1e-13 * _row_scale(n, rp, ci, v, x) + 1e-300)
+
+
+def test_upload_rejects_bad_columns(ctx):
+    with pytest.raises(sparse.IllegalArgumentException):
+        sparse.CompRowMatrix(2, 2, [0, 1, 2], [0, 5], [1.0, 1.0], ctx)
+    with pytest.raises(sparse.IllegalArgumentException):
+        sparse.CompRowMatrix(2, 3, [0, 2, 2], [1, 0], [1.0, 1.0], ctx)
+
+
+# ------------------------------------------------------------ preconditioners
+def _pc_pair(kind, okind, n, rp, ci, v, ctx):
+    A = sparse.CompRowMatrix(n, n, rp, ci, v, ctx)
+    M = {sparse.DiagonalPreconditioner.kind: sparse.DiagonalPreconditioner,
+         sparse.ILU.kind: sparse.ILU, sparse.ICC.kind: sparse.ICC}[kind](n, ctx)
+    M.setMatrix(A)
+    Mo = O.Precond(okind, n)
+    assert Mo.set_matrix(O.Csr(n, n, rp, ci, v)) == 0
+    return A, M, Mo
+
+
+PC_CASES = [
+    ("poisson2d_16", lambda: workloads.poisson2d(16)),
+    ("convdiff3d_8", lambda: workloads.convdiff3d(8)),
+    ("laplacian_2000", lambda: workloads.laplacian(2000, 3)),
+]
+
+
+@pytest.mark.parametrize("case", PC_CASES, ids=[c[0] for c in PC_CASES])
+@pytest.mark.parametrize("kind", ["jacobi", "ilu", "icc"])
+def test_preconditioner_factor_and_apply(ctx, numerics, case, kind):
+    n, rp, ci, v = case[1]()
+    if kind == "icc" and case[0].startswith("convdiff"):
+        pytest.skip("ICC needs a symmetric matrix")
+    k, ok = {"jacobi": (sparse.DiagonalPreconditioner.kind, O.PC_JACOBI),
+             "ilu": (sparse.ILU.kind, O.PC_ILU), "icc": (sparse.ICC.kind, O.PC_ICC)}[kind]
+    A, M, Mo = _pc_pair(k, ok, n, rp, ci, v, ctx)
+    assert np.array_equal(M.values(), Mo.values())  # factors are always bit-exact
+    b = workloads.uniform(n, 31)
+    x = M.apply(b)
+    xo = Mo.apply(b)
+    if numerics == STRICT:
+        assert np.array_equal(x, xo)
+    else:
+        assert np.allclose(x, xo, rtol=1e-12, atol=1e-14)
+    xt = M.transApply(b)
+    xto = Mo.trans_apply(b)
+    if numerics == STRICT:
+        assert np.array_equal(xt, xto)
+    else:
+        assert np.allclose(xt, xto, rtol=1e-12, atol=1e-14)
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_ilu_random_nonsymmetric_patterns(ctx, seed):
+    # reference-test shaped matrices; structurally nonsymmetric patterns
+    # exercise MTJ's read past the end of a row in ILU.factor
+    rng = np.random.default_rng(100 + seed)
+    n = int(rng.integers(1, 60))
+    A = nonsingular_system(n, int(rng.integers(1, min(10, n) + 1)), rng)
+    n, _, rp, ci, v = dense_to_csr(A)
+    _, M, Mo = _pc_pair(sparse.ILU.kind, O.PC_ILU, n, rp, ci, v, ctx)
+    assert np.array_equal(M.values(), Mo.values())
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_icc_random_spd(ctx, seed):
+    rng = np.random.default_rng(200 + seed)
+    n = int(rng.integers(1, 60))
+    A = spd_system(n, int(rng.integers(1, min(10, n) + 1)), rng)
+    n, _, rp, ci, v = dense_to_csr(A)
+    _, M, Mo = _pc_pair(sparse.ICC.kind, O.PC_ICC, n, rp, ci, v, ctx)
+    assert np.array_equal(M.values(), Mo.values())
+
+
+@pytest.mark.parametrize("n", range(1, 11))
+@pytest.mark.parametrize("shape", ["tri", "penta"])
+@pytest.mark.parametrize("kind", ["ilu", "icc"])
+def test_incomplete_factorization_exact_on_banded(ctx, n, shape, kind):
+    # TS/IncompleteFactorizationTestAbstract.java:31-69 + TS/ILUTest, TS/ICCTest
+    Ad = tridiagonal(n) if shape == "tri" else pentadiagonal(n)
+    n, _, rp, ci, v = dense_to_csr(Ad)
+    A = sparse.CompRowMatrix(n, n, rp, ci, v, ctx)
+    M = (sparse.ILU if kind == "ilu" else sparse.ICC)(A)
+    M.setMatrix(A)
+    x = np.ones(n)
+    b = A.mult(x)
+    x = M.apply(b)
+    r = A.multAdd(-1, x, b.copy())
+    assert np.linalg.norm(r) <= 1e-5
+
+
+def test_setup_errors(ctx):
+    # missing diagonal (S/ILU.java:134-136)
+    n, _, rp, ci, v = dense_to_csr(np.array([[1.0, 2.0], [3.0, 0.0]]), keep_diag=False)
+    A = sparse.CompRowMatrix(n, n, rp, ci, v, ctx)
+    M = sparse.ILU(A)
+    with pytest.raises(RuntimeError, match="Missing diagonal entry on row 2"):
+        M.setMatrix(A)
+    # zero diagonal (S/DiagonalPreconditioner.java:71-72)
+    n, _, rp, ci, v = dense_to_csr(np.array([[1.0, 2.0], [3.0, 0.0]]), keep_diag=True)
+    A = sparse.CompRowMatrix(n, n, rp, ci, v, ctx)
+    J = sparse.DiagonalPreconditioner(n, ctx)
+    with pytest.raises(RuntimeError, match="Zero diagonal on row 2"):
+        J.setMatrix(A)
+    # zero pivot (S/ILU.java:105-107): MTJ prints the entry index + 1
+    Ad = np.array([[0.0, 1.0], [1.0, 1.0]])
+    n, _, rp, ci, v = dense_to_csr(Ad)
+    A = sparse.CompRowMatrix(n, n, rp, ci, v, ctx)
+    M = sparse.ILU(A)
+    Mo = O.Precond(O.PC_ILU, n)
+    st = Mo.set_matrix(O.Csr(n, n, rp, ci, v))
+    assert st == O.ERR_ZERO_PIVOT
+    with pytest.raises(RuntimeError, match=f"Zero pivot encountered on row {Mo.detail} "):
+        M.setMatrix(A)
+
+
+# ----------------------------------------------------------------- solvers
+SOLVERS = {"cg": (sparse.CG, O.CG), "bicgstab": (sparse.BiCGstab, O.BICGSTAB), "gmres": (sparse.GMRES, O.GMRES)}
+PCS = {"identity": (None, None), "jacobi": (sparse.DiagonalPreconditioner, O.PC_JACOBI),
+       "ilu": (sparse.ILU, O.PC_ILU), "icc": (sparse.ICC, O.PC_ICC)}
+
+
+def _solve_both(ctx, sname, pname, n, rp, ci, v, b, x0, max_iter=2000, rtol=1e-10, atol=1e-50, dtol=1e5,
+                norm=1, restart=30):
+    A = sparse.CompRowMatrix(n, n, rp, ci, v, ctx)
+    Ao = O.Csr(n, n, rp, ci, v)
+    cls, okind = SOLVERS[sname]
+    solver = cls(n, restart=restart, ctx=ctx) if sname == "gmres" else cls(n, ctx=ctx)
+    pcls, pk = PCS[pname]
+    pco = None
+    if pcls is not None:
+        M = pcls(n, ctx) if pcls is sparse.DiagonalPreconditioner else pcls(A)
+        M.setMatrix(A)
+        solver.setPreconditioner(M)
+        pco = O.Precond(pk, n)
+        assert pco.set_matrix(Ao) == 0
+    mon = sparse.DefaultIterationMonitor(max_iter, rtol, atol, dtol)
+    mon.setNormType(norm)
+    mon.setIterationReporter(sparse.IterationReporter(), history_cap=4 * max_iter + 64)
+    solver.setIterationMonitor(mon)
+    x = np.array(x0, dtype=np.float64, copy=True)
+    exc = None
+    try:
+        solver.solve(A, b, x)
+    except sparse.IterativeSolverNotConvergedException as e:
+        exc = e
+    xo, res, hr, hi = O.solve(okind, Ao, b, x0, pco, max_iter=max_iter, rtol=rtol, atol=atol, dtol=dtol,
+                              norm_type=norm, restart=restart)
+    return x, exc, solver, xo, res, hr, hi
+
+
+def _compare_histories(solver, hr, hi):
+    """Largest difference of the relative residuals r_k / r_0 (the quantity
+    the monitor tests against rtol) over the common prefix of the two
+    residual histories.  A near-converged residual carries rounding noise of
+    order eps * |b| in any implementation, so the difference is measured on
+    the scale of r_0, not of r_k."""
+    gr, gi = solver.history
+    k = min(len(gr), len(hr))
+    assert k > 0
+    # iteration numbers passed to the reporter agree over the common prefix
+    assert np.array_equal(gi[:k], hi[:k])
+    r0 = max(abs(hr[0]), 1e-300)
+    return float(np.max(np.abs(gr[:k] - hr[:k])) / r0)
+
+
+SOLVE_CASES = [
+    ("cg", "identity", "poisson2d", 24),
+    ("cg", "jacobi", "poisson2d", 24),
+    ("cg", "icc", "poisson2d", 24),
+    ("cg", "ilu", "poisson2d", 24),
+    ("bicgstab", "identity", "convdiff3d", 10),
+    ("bicgstab", "jacobi", "convdiff3d", 10),
+    ("bicgstab", "ilu", "convdiff3d", 10),
+    ("gmres", "identity", "convdiff3d", 10),
+    ("gmres", "jacobi", "convdiff3d", 10),
+    ("gmres", "ilu", "convdiff3d", 10),
+    ("gmres", "ilu", "poisson2d", 24),
+]
+
+
+@pytest.mark.parametrize("case", SOLVE_CASES, ids=["-".join(map(str, c)) for c in SOLVE_CASES])
+def test_solver_matches_oracle(ctx, numerics, case):
+    sname, pname, mat, N = case
+    n, rp, ci, v = getattr(workloads, mat)(N)
+    xt = workloads.uniform(n, 1)
+    b = O.mult(O.Csr(n, n, rp, ci, v), xt)
+    x, exc, solver, xo, res, hr, hi = _solve_both(ctx, sname, pname, n, rp, ci, v, b, np.zeros(n))
+    assert exc is None and res.status == 0, (exc, res.status)
+    it = solver.getIterationMonitor().iterations()
+    assert abs(it - res.iterations) <= 2, (it, res.iterations)
+    rel = _compare_histories(solver, hr, hi)
+    assert rel <= 1e-10, rel
+    assert np.max(np.abs(x - xo)) <= 1e-8 * max(1.0, np.max(np.abs(xo)))
+
+
+@pytest.mark.parametrize("seed", range(6))
+@pytest.mark.parametrize("sname", ["cg", "bicgstab", "gmres"])
+@pytest.mark.parametrize("pname", ["identity", "jacobi", "ilu"])
+def test_reference_style_random_systems(ctx, seed, sname, pname):
+    # TS/IterativeSolverTestAbstract.java:140-168 (solve and repeat 5 times,
+    # x recovered within 1e-4), with the preconditioner actually installed
+    rng = np.random.default_rng(1000 * seed + hash(sname + pname) % 997)
+    n = int(rng.integers(1, 51))
+    bw = int(rng.integers(1, min(10, n) + 1))
+    Ad = spd_system(n, bw, rng) if sname == "cg" else nonsingular_system(n, bw, rng)
+    n, _, rp, ci, v = dense_to_csr(Ad)
+    A = sparse.CompRowMatrix(n, n, rp, ci, v, ctx)
+    cls = SOLVERS[sname][0]
+    solver = cls(n, ctx=ctx)
+    pcls = PCS[pname][0]
+    if pcls is not None:
+        M = pcls(n, ctx) if pcls is sparse.DiagonalPreconditioner else pcls(A)
+        M.setMatrix(A)
+        solver.setPreconditioner(M)
+    for _ in range(5):
+        xt = rng.random(n)
+        b = Ad @ xt
+        x = rng.random(n)
+        solver.solve(A, b, x)
+        assert np.max(np.abs(x - xt)) <= 1e-4
+
+
+def test_not_converged_iterations_matches_oracle(ctx):
+    n, rp, ci, v = workloads.poisson2d(24)
+    b = workloads.uniform(n, 2)
+    x, exc, solver, xo, res, hr, hi = _solve_both(ctx, "cg", "jacobi", n, rp, ci, v, b, np.zeros(n), max_iter=7)
+    assert res.status == O.NC_ITERATIONS
+    assert exc is not None and exc.getReason() == sparse.NotConvergedException.Reason.Iterations
+    assert exc.getIterations() == res.iterations == 7
+    assert abs(exc.getResidual() - res.residual) <= 1e-10 * res.residual
+    assert np.allclose(x, xo, rtol=1e-10, atol=1e-12)
+
+
+def test_nan_rhs_is_divergence(ctx):
+    n, rp, ci, v = workloads.poisson2d(8)
+    b = np.ones(n)
+    b[3] = np.nan
+    x, exc, solver, xo, res, hr, hi = _solve_both(ctx, "cg", "identity", n, rp, ci, v, b, np.zeros(n))
+    assert res.status == O.NC_DIVERGENCE
+    assert exc is not None and exc.getReason() == sparse.NotConvergedException.Reason.Divergence
+    assert exc.getIterations() == res.iterations
+
+
+def test_bicgstab_breakdown(ctx):
+    # rtilde.r becomes exactly 0 after one iteration on this 2x2 system, so
+    # the next iteration throws Breakdown "rho" (S/BiCGstab.java:77-79)
+    Ad = np.array([[-1.0, -1.0], [-1.0, 0.0]])
+    n, _, rp, ci, v = dense_to_csr(Ad)
+    b = np.array([1.0, 0.0])
+    x, exc, solver, xo, res, hr, hi = _solve_both(ctx, "bicgstab", "identity", n, rp, ci, v, b, np.zeros(n))
+    assert res.status == O.NC_BREAKDOWN
+    assert exc is not None and exc.getReason() == sparse.NotConvergedException.Reason.Breakdown
+    assert exc.message == {1: "rho", 2: "omega"}[res.detail]
+    assert exc.getIterations() == res.iterations
+
+
+def test_gmres_singular_hessenberg(ctx):
+    # zero matrix: the Hessenberg diagonal is 0 -> MatrixSingularException
+    n = 5
+    rp = np.arange(n + 1, dtype=np.int32)
+    ci = np.arange(n, dtype=np.int32)
+    v = np.zeros(n)
+    b = np.ones(n)
+    A = sparse.CompRowMatrix(n, n, rp, ci, v, ctx)
+    solver = sparse.GMRES(n, ctx=ctx)
+    xo, res, _, _ = O.solve(O.GMRES, O.Csr(n, n, rp, ci, v), b, np.zeros(n))
+    assert res.status == O.ERR_SINGULAR
+    with pytest.raises(sparse.MatrixSingularException):
+        solver.solve(A, b, np.zeros(n))
+
+
+@pytest.mark.parametrize("norm", [0, 2, 3])
+def test_other_norms(ctx, norm):
+    n, rp, ci, v = workloads.poisson2d(16)
+    b = workloads.uniform(n, 4)
+    x, exc, solver, xo, res, hr, hi = _solve_both(ctx, "cg", "jacobi", n, rp, ci, v, b, np.zeros(n), norm=norm)
+    assert exc is None and res.status == 0
+    assert abs(solver.getIterationMonitor().iterations() - res.iterations) <= 2
+    assert _compare_histories(solver, hr, hi) <= 1e-10

@@ -1,0 +1,210 @@
+"""Pins the oracle (CPU restatement of MTJ) on the CPU.
+
+1. Against the reference's own test properties (the reference ships no
+   golden vectors): TS/ILUTest + TS/ICCTest exact solves on tri/penta-diagonal
+   systems (TS/IncompleteFactorizationTestAbstract.java:31-69), CompRowMatrix
+   products against dense loops (T/MatrixTestAbstract.java:582-675), solvers
+   recovering x within 1e-4 (TS/IterativeSolverTestAbstract.java:140-168).
+2. Bit for bit against an independent pure-Python restatement (tests/pyref.py)
+   on small cases: products, ILU/ICC factors, residual histories and iterates
+   of CG / BiCGstab / GMRES.
+3. The reach-based ICC against the literal O(n^2) ICC, bit for bit.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+import pyref
+from helpers import dense_to_csr, nonsingular_system, pentadiagonal, spd_system, tridiagonal
+
+
+def _csr(Ad):
+    n, m, rp, ci, v = dense_to_csr(Ad)
+    return n, m, rp, ci, v, O.Csr(n, m, rp, ci, v)
+
+
+# ---------------------------------------------------- reference properties
+@pytest.mark.parametrize("n", range(1, 11))
+@pytest.mark.parametrize("shape", ["tri", "penta"])
+@pytest.mark.parametrize("kind", [O.PC_ILU, O.PC_ICC, O.PC_ICC_LITERAL])
+def test_incomplete_factorizations_solve_banded_exactly(n, shape, kind):
+    Ad = tridiagonal(n) if shape == "tri" else pentadiagonal(n)
+    n, m, rp, ci, v, A = _csr(Ad)
+    pc = O.Precond(kind, n)
+    assert pc.set_matrix(A) == O.OK
+    x = np.ones(n)
+    b = O.mult(A, x)
+    x = pc.apply(b)
+    r = O.mult_add(A, -1.0, x, b)
+    assert O.norm(r, O.NORM_TWO_ROBUST) <= 1e-5
+
+
+@pytest.mark.parametrize("seed", range(10))
+def test_products_against_dense(seed):
+    rng = np.random.default_rng(seed)
+    n, m = int(rng.integers(1, 101)), int(rng.integers(1, 101))
+    Ad = rng.random((n, m)) * (rng.random((n, m)) < 0.3)
+    _, _, rp, ci, v, A = _csr(Ad)
+    x, y, xt, yt = rng.random(m), rng.random(n), rng.random(n), rng.random(m)
+    assert np.allclose(O.mult(A, x), Ad @ x, rtol=1e-12, atol=1e-12)
+    assert np.allclose(O.mult_add(A, 0.5, x, y), y + 0.5 * (Ad @ x), rtol=1e-12, atol=1e-12)
+    assert np.allclose(O.trans_mult(A, xt), Ad.T @ xt, rtol=1e-12, atol=1e-12)
+    assert np.allclose(O.trans_mult_add(A, 2.0, xt, yt), yt + 2.0 * (Ad.T @ xt), rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("seed", range(8))
+@pytest.mark.parametrize("kind,pk", [(O.CG, O.PC_IDENTITY), (O.CG, O.PC_JACOBI), (O.CG, O.PC_ICC),
+                                     (O.BICGSTAB, O.PC_IDENTITY), (O.BICGSTAB, O.PC_ILU),
+                                     (O.GMRES, O.PC_IDENTITY), (O.GMRES, O.PC_JACOBI), (O.GMRES, O.PC_ILU)])
+def test_solvers_recover_x(seed, kind, pk):
+    rng = np.random.default_rng(seed * 31 + kind * 7 + pk)
+    n = int(rng.integers(1, 51))
+    bw = int(rng.integers(1, min(10, n) + 1))
+    Ad = spd_system(n, bw, rng) if kind == O.CG or pk == O.PC_ICC else nonsingular_system(n, bw, rng)
+    n, _, rp, ci, v, A = _csr(Ad)
+    pc = None
+    if pk != O.PC_IDENTITY:
+        pc = O.Precond(pk, n)
+        assert pc.set_matrix(A) == O.OK
+    for _ in range(5):  # testRepeatSolve
+        xt = rng.random(n)
+        b = Ad @ xt
+        x, res, _, _ = O.solve(kind, A, b, rng.random(n), pc)
+        assert res.status == O.OK
+        assert np.max(np.abs(x - xt)) <= 1e-4
+
+
+# ------------------------------------------------- independent restatement
+def _py_system(seed, spd):
+    rng = np.random.default_rng(seed)
+    n = int(rng.integers(2, 30))
+    bw = int(rng.integers(1, min(6, n) + 1))
+    Ad = spd_system(n, bw, rng) if spd else nonsingular_system(n, bw, rng)
+    n, _, rp, ci, v, A = _csr(Ad)
+    return n, list(map(int, rp)), list(map(int, ci)), list(map(float, v)), A, rng
+
+
+@pytest.mark.parametrize("seed", range(20))
+def test_products_bitwise(seed):
+    n, rp, ci, v, A, rng = _py_system(seed, False)
+    x = list(rng.standard_normal(n))
+    y = list(rng.standard_normal(n))
+    assert np.array_equal(O.mult(A, x), np.array(pyref.mult(rp, ci, v, x)))
+    assert np.array_equal(O.mult_add(A, -1.0, x, y), np.array(pyref.mult_add(rp, ci, v, -1.0, x, y)))
+
+
+@pytest.mark.parametrize("seed", range(20))
+def test_ilu_factor_bitwise(seed):
+    n, rp, ci, v, A, rng = _py_system(seed, False)
+    pc = O.Precond(O.PC_ILU, n)
+    assert pc.set_matrix(A) == O.OK
+    data, dg = pyref.ilu_factor(rp, ci, v)
+    assert np.array_equal(pc.values(), np.array(data))
+    b = list(rng.standard_normal(n))
+    assert np.array_equal(pc.apply(b), np.array(pyref.ilu_apply(rp, ci, data, dg, b)))
+
+
+@pytest.mark.parametrize("seed", range(20))
+@pytest.mark.parametrize("kind", [O.PC_ICC, O.PC_ICC_LITERAL])
+def test_icc_factor_bitwise(seed, kind):
+    n, rp, ci, v, A, rng = _py_system(seed, True)
+    pc = O.Precond(kind, n)
+    assert pc.set_matrix(A) == O.OK
+    data, dg = pyref.icc_factor(rp, ci, v)
+    assert np.array_equal(pc.values(), np.array(data))
+    b = list(rng.standard_normal(n))
+    assert np.array_equal(pc.apply(b), np.array(pyref.icc_apply(rp, ci, data, dg, b)))
+
+
+def _py_solve(name, rp, ci, v, b, x0, M, mon):
+    fn = {"cg": pyref.cg, "bicgstab": pyref.bicgstab, "gmres": pyref.gmres}[name]
+    try:
+        x = fn(rp, ci, v, b, x0, M, mon)
+        return x, 0, 0
+    except pyref.NotConverged as e:
+        return None, e.code, e.detail
+    except pyref.Singular:
+        return None, O.ERR_SINGULAR, 0
+
+
+@pytest.mark.parametrize("seed", range(10))
+@pytest.mark.parametrize("name,pk", [("cg", O.PC_IDENTITY), ("cg", O.PC_JACOBI), ("cg", O.PC_ICC),
+                                     ("bicgstab", O.PC_IDENTITY), ("bicgstab", O.PC_JACOBI),
+                                     ("bicgstab", O.PC_ILU), ("gmres", O.PC_IDENTITY), ("gmres", O.PC_ILU)])
+@pytest.mark.parametrize("max_iter", [3, 500])
+def test_solver_histories_bitwise(seed, name, pk, max_iter):
+    spd = name == "cg" or pk == O.PC_ICC
+    n, rp, ci, v, A, rng = _py_system(seed + 50, spd)
+    b = list(rng.standard_normal(n))
+    x0 = list(rng.standard_normal(n))
+    pc = None
+    M = lambda r: list(r)  # noqa: E731
+    if pk != O.PC_IDENTITY:
+        pc = O.Precond(pk, n)
+        assert pc.set_matrix(A) == O.OK
+        if pk == O.PC_JACOBI:
+            M = pyref.jacobi(rp, ci, v)
+        elif pk == O.PC_ILU:
+            data, dg = pyref.ilu_factor(rp, ci, v)
+            M = lambda r: pyref.ilu_apply(rp, ci, data, dg, r)  # noqa: E731
+        else:
+            data, dg = pyref.icc_factor(rp, ci, v)
+            M = lambda r: pyref.icc_apply(rp, ci, data, dg, r)  # noqa: E731
+    kind = {"cg": O.CG, "bicgstab": O.BICGSTAB, "gmres": O.GMRES}[name]
+    restart = 4 if name == "gmres" else 30  # exercise restarts
+    mon = pyref.Monitor(max_iter, 1e-10)
+    xp, code, detail = _py_solve(name, rp, ci, v, b, x0, M, mon) if name != "gmres" else \
+        _gm(rp, ci, v, b, x0, M, mon, restart)
+    xo, res, hr, hi = O.solve(kind, A, np.array(b), np.array(x0), pc, max_iter=max_iter, rtol=1e-10,
+                              restart=restart)
+    assert res.status == code and res.detail == detail
+    assert res.iterations == mon.iter
+    assert np.array_equal(hr, np.array([h[0] for h in mon.hist]))
+    assert np.array_equal(hi, np.array([h[1] for h in mon.hist]))
+    if code == 0:
+        assert np.array_equal(xo, np.array(xp))
+
+
+def _gm(rp, ci, v, b, x0, M, mon, restart):
+    try:
+        return pyref.gmres(rp, ci, v, b, x0, M, mon, restart), 0, 0
+    except pyref.NotConverged as e:
+        return None, e.code, e.detail
+    except pyref.Singular:
+        return None, O.ERR_SINGULAR, 0
+
+
+# ------------------------------------------------------- ICC reach vs literal
+@pytest.mark.parametrize("seed", range(15))
+def test_icc_reach_equals_literal(seed):
+    rng = np.random.default_rng(700 + seed)
+    n = int(rng.integers(1, 120))
+    Ad = spd_system(n, int(rng.integers(1, min(8, n) + 1)), rng)
+    n, _, rp, ci, v, A = _csr(Ad)
+    a, b = O.Precond(O.PC_ICC, n), O.Precond(O.PC_ICC_LITERAL, n)
+    assert a.set_matrix(A) == b.set_matrix(A) == O.OK
+    assert np.array_equal(a.values(), b.values())
+
+
+def test_icc_reach_equals_literal_on_stencils():
+    import sys
+    from mtjg import workloads  # noqa: F401  (host-only generator library)
+    for gen, N in (("poisson2d", 14), ("poisson3d", 6)):
+        n, rp, ci, v = getattr(workloads, gen)(N)
+        A = O.Csr(n, n, rp, ci, v)
+        a, b = O.Precond(O.PC_ICC, n), O.Precond(O.PC_ICC_LITERAL, n)
+        assert a.set_matrix(A) == b.set_matrix(A) == O.OK
+        assert np.array_equal(a.values(), b.values()), gen
+    assert sys is not None
+
+
+def test_icc_negative_pivot_propagates_like_literal():
+    # a symmetric indefinite matrix: a NaN diagonal appears and MTJ's literal
+    # loop then applies that row to every later row
+    Ad = np.array([[1.0, 2.0, 0.0, 0.0], [2.0, 1.0, 0.0, 0.0], [0.0, 0.0, 3.0, 1.0], [0.0, 0.0, 1.0, 3.0]])
+    n, _, rp, ci, v, A = _csr(Ad)
+    a, b = O.Precond(O.PC_ICC, n), O.Precond(O.PC_ICC_LITERAL, n)
+    assert a.set_matrix(A) == b.set_matrix(A)
+    va, vb = a.values(), b.values()
+    assert np.array_equal(np.isnan(va), np.isnan(vb))
+    assert np.array_equal(va[~np.isnan(va)], vb[~np.isnan(vb)])
