@@ -250,6 +250,34 @@ def run_gpu(args):
     return out
 
 
+def spmv_only(args):
+    """CompRowMatrix.mult on the 3D Poisson matrix, `spmv_reps` launches."""
+    from mtjg import _lib as L
+    from mtjg import sparse, workloads
+
+    lib = L.load()
+    ctx = sparse.Context(0)
+    n, rp, ci, v = workloads.poisson3d(args.grid)
+    A = sparse.CompRowMatrix(n, n, rp, ci, v, ctx)
+    xt = workloads.uniform(n, SEED)
+    dx, dy = C.c_void_p(), C.c_void_p()
+    lib.mtjg_dev_alloc(ctx.h, 8 * n, C.byref(dx))
+    lib.mtjg_dev_alloc(ctx.h, 8 * n, C.byref(dy))
+    lib.mtjg_memcpy_h2d(ctx.h, dx, xt.ctypes.data_as(C.c_void_p), 8 * n)
+    for _ in range(args.warmup):
+        lib.mtjg_csr_mult_dev(A.h, dx, dy)
+    lib.mtjg_ctx_event_record(ctx.h, 0)
+    for _ in range(args.spmv_reps):
+        lib.mtjg_csr_mult_dev(A.h, dx, dy)
+    lib.mtjg_ctx_event_record(ctx.h, 1)
+    ms = C.c_float()
+    lib.mtjg_ctx_event_elapsed(ctx.h, 0, 1, C.byref(ms))
+    us = 1e3 * ms.value / args.spmv_reps
+    nnz = int(rp[-1])
+    by = 12 * nnz + 4 * (n + 1) + 16 * n
+    return {"workload": f"CSR product, 3D Poisson {args.grid}^3", "us": us, "bytes": by, "gbs": by / us / 1e3}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -261,7 +289,12 @@ def main():
     ap.add_argument("--cpu-sample-iters", type=int, default=40)
     ap.add_argument("--cpu-procs", type=int, default=0, help="0: all host cores")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--only-spmv", action="store_true",
+                    help="run only the CSR product loop (for profiling the product kernel)")
     args = ap.parse_args()
+    if args.only_spmv:
+        print(json.dumps(spmv_only(args)))
+        return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     cfg = {"workload": f"CG + DiagonalPreconditioner, 3D 7-point Poisson {args.grid}^3, rtol 1e-10, x0 = 0",

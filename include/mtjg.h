@@ -102,6 +102,7 @@ typedef struct mtjg_result {
     double residual;
     int detail;
     int history_len;   /* convergence tests made (may exceed history_cap) */
+    int inner_iterations;  /* mixed precision: FP32 inner iterations of all refinement steps */
 } mtjg_result;
 
 typedef struct mtjg_ctx mtjg_ctx;
@@ -139,6 +140,15 @@ MTJG_API int mtjg_memcpy_d2h(mtjg_ctx *ctx, void *dst, const void *src, int64_t 
 MTJG_API int mtjg_csr_upload(mtjg_ctx *ctx, int num_rows, int num_cols,
                              const int *rowptr, const int *colind, const double *val,
                              mtjg_csr **out);
+/* A batch of independent square systems as one block-diagonal CSR: system s
+ * owns rows [sys_rows[s], sys_rows[s+1]) and references only columns in that
+ * range (checked).  Solving it with a CG or BiCGstab solver of size
+ * sys_rows[num_systems] runs every system in the same launches, each with
+ * its own scalars and DefaultIterationMonitor; a system's results do not
+ * depend on the other systems of the batch.  No reference counterpart: MTJ
+ * solves one system per call (IterativeSolver.solve, S/IterativeSolver.java:30-44). */
+MTJG_API int mtjg_batch_upload(mtjg_ctx *ctx, int num_systems, const int *sys_rows, const int *rowptr,
+                               const int *colind, const double *val, mtjg_csr **out);
 /* New values, same pattern (CompRowMatrix.set on the data array). */
 MTJG_API int mtjg_csr_update_values(mtjg_csr *A, const double *val);
 MTJG_API int mtjg_csr_destroy(mtjg_csr *A);
@@ -192,9 +202,23 @@ MTJG_API int mtjg_solver_solve(mtjg_solver *S, mtjg_csr *A, const double *b, dou
                                mtjg_result *res);
 MTJG_API int mtjg_solver_solve_dev(mtjg_solver *S, mtjg_csr *A, const double *db,
                                    double *dx, mtjg_result *res);
+/* Mixed precision for CG with the identity or Jacobi preconditioner (also
+ * batched).  The solve becomes iterative refinement in the shape of MTJ's IR
+ * (S/IR.java:57-70): the outer loop keeps x, the true residual r = b - A x
+ * and the monitor's test in FP64, exactly as DefaultIterationMonitor sees
+ * them, and each correction comes from an inner CG whose matrix values,
+ * vectors, products and preconditioner are FP32, run until its residual
+ * falls by inner_rtol or for inner_max_iter iterations.  iterations() then
+ * counts refinement steps; mtjg_result.inner_iterations the inner ones.
+ * enable = 0 restores the FP64 solver.  No counterpart in the reference. */
+MTJG_API int mtjg_solver_set_mixed(mtjg_solver *S, int enable, double inner_rtol, int inner_max_iter);
 /* Residual history of the last solve: the (residual, iteration) pairs passed
  * to IterationReporter.monitor, oldest first (up to history_cap). */
 MTJG_API int mtjg_solver_history(mtjg_solver *S, double *resid, int *iters, int cap, int *len);
+/* Per-system outcome and residual history of the last batched solve (the
+ * aggregate mtjg_result reports the first system that did not converge). */
+MTJG_API int mtjg_solver_batch_results(mtjg_solver *S, mtjg_result *out, int count);
+MTJG_API int mtjg_solver_batch_history(mtjg_solver *S, int sys, double *resid, int *iters, int cap, int *len);
 MTJG_API int mtjg_solver_destroy(mtjg_solver *S);
 
 #ifdef __cplusplus

@@ -132,43 +132,46 @@ __device__ __forceinline__ void block_reduce(Acc &a, int type, Acc *sm /* [kBloc
     __syncthreads();
 }
 
-// Finishes one tile: block-reduce the per-thread partials, store them as the
-// tile's partial, and if this was the last tile of system `sys` to arrive,
-// reduce that system's tile partials in tile order and run op.scalar(sys, sums)
-// on thread 0.
-template <class Op>
-__device__ __forceinline__ void tile_finish(Acc &a, int tile, int sys, Op &op, const RedCtx &rc,
-                                            int type, Acc *sm, int *s_last)
+// Stores one tile's partial: block-reduce the per-thread partials (fixed
+// order) and write them to the tile's slot.  No fence: see tiles_arrive.
+__device__ __forceinline__ void tile_partial(Acc &a, int tile, const RedCtx &rc, int type, Acc *sm)
 {
     block_reduce(a, type, sm);
     if (threadIdx.x == 0) {
 #pragma unroll
         for (int i = 0; i < kParts; ++i) rc.part[(size_t)tile * kParts + i] = a.v[i];
-        __threadfence();
-        const int t0 = rc.sys_tile[sys], t1 = rc.sys_tile[sys + 1];
-        unsigned prev = atomicAdd(&rc.cnt[sys], 1u);
-        *s_last = (prev == (unsigned)(t1 - t0 - 1));
     }
-    __syncthreads();
-    if (*s_last) {
-        __threadfence();
-        const int t0 = rc.sys_tile[sys], t1 = rc.sys_tile[sys + 1];
-        Acc s;
-        acc_zero(s);
-        for (int t = t0 + (int)threadIdx.x; t < t1; t += blockDim.x) {
-            Acc o;
+}
+
+// The reduction of a phase finishes in k_finalize (a launch of its own after
+// the phase's kernel): block s sums system s's tile partials in tile order
+// (thread t takes tiles t, t+B, t+2B, ... with eight loads in flight, then
+// the fixed block tree) and thread 0 runs op.scalar(s, sums).  No atomics
+// and no fences: the launch boundary orders the partial stores before it.
+template <class Op>
+__global__ void __launch_bounds__(kBlock) k_finalize(Op op, RedCtx rc, int type)
+{
+    __shared__ Acc sm[kBlock / 32];
+    const int sys = blockIdx.x;
+    if (!op.active(sys)) return;
+    const int t0 = rc.sys_tile[sys], t1 = rc.sys_tile[sys + 1];
+    const int stride = blockDim.x;
+    Acc s;
+    acc_zero(s);
+    for (int base = t0 + (int)threadIdx.x; base < t1; base += 8 * stride) {
+        Acc o[8];
 #pragma unroll
-            for (int i = 0; i < kParts; ++i) o.v[i] = __ldcg(rc.part + (size_t)t * kParts + i);
-            acc_merge(s, o, type);
+        for (int u = 0; u < 8; ++u) {
+            const int t = base + u * stride;
+#pragma unroll
+            for (int i = 0; i < kParts; ++i) o[u].v[i] = t < t1 ? rc.part[(size_t)t * kParts + i] : 0.0;
         }
-        block_reduce(s, type, sm);
-        if (threadIdx.x == 0) {
-            op.scalar(sys, s);
-            rc.cnt[sys] = 0u;
-            __threadfence();
-        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+            if (base + u * stride < t1) acc_merge(s, o[u], type);
     }
-    __syncthreads();
+    block_reduce(s, type, sm);
+    if (threadIdx.x == 0) op.scalar(sys, s);
 }
 
 // ------------------------------------------------------------ monitor

@@ -32,14 +32,15 @@ void ctx_release(mtjg_ctx *ctx);
     } while (0)
 
 // ------------------------------------------------------------ tiling
-// Rows are cut into tiles of at most kTileRows/vec rows and kTileNnz entries
-// (one long row may exceed kTileNnz; it forms a tile of its own).  Every
-// kernel walks the same tiles, so per-tile partial sums, and therefore every
-// reduction, do not depend on the grid size or on the other systems of a
+// For CSR products, rows are cut into tiles of at most kTileRows/vec rows
+// and kTileNnz entries (one long row may exceed kTileNnz; it forms a tile of
+// its own).  Row kernels use tiles of kBlock rows.  Tiles never straddle two
+// systems of a batch, and reductions are sums of per-tile partials in tile
+// order, so no result depends on the grid size or on the other systems of a
 // batch.
 constexpr int kBlock = 256;
 constexpr int kTileRows = 256;
-constexpr int kTileNnz = 2816;
+constexpr int kTileNnz = 2048;
 constexpr int kParts = 4;             // partial-sum slots per tile
 
 // device status of a system (SysState::status)
@@ -65,6 +66,12 @@ struct SysState {
     double alpha, beta, omega;
     double normr;   // GMRES: ||r||2 of the running cycle
     double scratch[3];
+    // mixed precision (outer FP64 refinement around an FP32 inner CG)
+    int phase;      // 0: the outer step is due, 1: inner iterations run
+    int pending;    // 1: the inner correction still has to be added to x
+    int in_iter;    // iterations of the running inner solve
+    int in_total;   // inner iterations of the whole solve
+    double in_rho, in_rho_1, in_alpha, in_beta, in_r0;
 };
 
 struct MonCfgDev {
@@ -89,9 +96,12 @@ struct TileSet {
     int num_sys = 1;
     int vec = 1;
     int *tile_row = nullptr;   // device [num_tiles + 1]
+    int *tile_nz = nullptr;    // device [num_tiles + 1]: rowptr at each tile's first row
     int *tile_sys = nullptr;   // device [num_tiles] (nullptr: all system 0)
     int *sys_tile = nullptr;   // device [num_sys + 1]
-    unsigned char *tile_long = nullptr;  // device [num_tiles]: 1 = single long row
+    // device [num_tiles]: (lanes per row << 1) | 1 if the tile is a single long row
+    unsigned char *tile_flags = nullptr;
+    int vec_mask = 0;          // OR of the lanes-per-row classes of the tiles
     std::vector<int> h_tile_row;
 };
 
@@ -127,11 +137,15 @@ struct mtjg_csr {
     int *colind = nullptr;     // device [nnz + 4] (padded for 16-byte bulk copies)
     double *val = nullptr;     // device [nnz + 2]
     std::vector<int> h_rowptr; // host copy (tiling, validation)
-    mtjg::TileSet tiles;
+    std::vector<int> sys_rows; // batch: first row of each system (+ end); empty for one system
+    mtjg::TileSet tiles;       // product tiles
+    mtjg::TileSet rtiles;      // row-kernel tiles (kBlock rows)
     // transpose (built on first transMult): CSR of A'
     int *t_rowptr = nullptr, *t_colind = nullptr;
     double *t_val = nullptr;
     mtjg::TileSet t_tiles;
+    // FP32 copy of the values (mixed precision), built on first use
+    float *val32 = nullptr;
     // reduction scratch sized for this matrix's tiles
     double *part = nullptr;
     unsigned *cnt = nullptr;

@@ -1,11 +1,11 @@
 // solver.cu -- CG, BiCGstab and GMRES(m) (S/CG.java, S/BiCGstab.java,
 // S/GMRES.java) as fused device phases.
 //
-// Every phase is one kernel over the matrix's row tiles: a CSR product with
-// a fused epilogue or a row kernel, whose per-tile partial sums are reduced
-// in tile order by the last tile to finish; that tile also runs the phase's
-// scalar step (alpha, beta, omega, Givens rotations, the iteration monitor)
-// on the device.  The host never reads a scalar during a solve: the loop
+// Every phase is one kernel over the matrix's tiles: a CSR product with a
+// fused epilogue or a row kernel, whose per-tile partial sums a small
+// finalize launch reduces in tile order before running the phase's scalar
+// step (alpha, beta, omega, Givens rotations, the iteration monitor) on the
+// device.  The host never reads a scalar during a solve: the loop
 // body is captured once into a CUDA graph, replayed in chunks, and every
 // kernel of a finished solve returns at once.  The host only polls the
 // status word between chunks.
@@ -49,9 +49,10 @@ struct CgInit {  // r = b - A x (A.multAdd(-1, x, r.set(b)), :64); fused z = M r
     int pc;
     MonPtrs m;
     static constexpr bool kReduce = true;
+    static constexpr bool kNeedsXr = false;
     __device__ bool active(int) const { return true; }
     __device__ double init(int, int) const { return 0.0; }
-    __device__ void row(int i, int, double d, Acc &a) const
+    __device__ void row(int i, int, double d, double, Acc &a) const
     {
         const double rr = b[i] - d;
         r[i] = rr;
@@ -80,6 +81,7 @@ struct CgP {  // p = z (first) or p = beta*p + z (p.scale(beta).add(z), :70-75)
     const double *z;
     SysState *st;
     static constexpr bool kReduce = false;
+    static constexpr bool kNeedsXr = false;
     __device__ bool active(int sys) const { return st[sys].status == ST_RUNNING; }
     __device__ void row(int i, int sys, Acc &) const
     {
@@ -95,13 +97,14 @@ struct CgQ {  // q = A p; alpha = rho / p.q (:77-78)
     double *q;
     SysState *st;
     static constexpr bool kReduce = true;
+    static constexpr bool kNeedsXr = true;  // p_i arrives with the row's diagonal gather
     __device__ bool active(int sys) const { return st[sys].status == ST_RUNNING; }
     __device__ double init(int, int) const { return 0.0; }
-    __device__ void row(int i, int, double d, Acc &a) const
+    __device__ void row(int i, int, double d, double pi, Acc &a) const
     {
         const double qq = d != 0.0 ? d : 0.0;
         q[i] = qq;
-        a.v[2] = fmac<S>(p[i], qq, a.v[2]);
+        a.v[2] = fmac<S>(pi, qq, a.v[2]);
     }
     __device__ void scalar(int sys, const Acc &s)
     {
@@ -117,6 +120,7 @@ struct CgUpd {  // x += alpha p; r -= alpha q; next monitor test; fused z = M r,
     int pc;
     MonPtrs m;
     static constexpr bool kReduce = true;
+    static constexpr bool kNeedsXr = false;
     __device__ bool active(int sys) const { return m.st[sys].status == ST_RUNNING; }
     __device__ void row(int i, int sys, Acc &a) const
     {
@@ -155,6 +159,7 @@ struct CgDot {  // rho = r.z after an external preconditioner (:68, :73)
     const double *r, *z;
     SysState *st;
     static constexpr bool kReduce = true;
+    static constexpr bool kNeedsXr = false;
     __device__ bool active(int sys) const { return st[sys].status == ST_RUNNING; }
     __device__ void row(int i, int, Acc &a) const { a.v[2] = fmac<S>(r[i], z[i], a.v[2]); }
     __device__ void scalar(int sys, const Acc &s)
@@ -184,9 +189,10 @@ struct BiInit {  // r = b - A x; rtilde = r (:71-72); first test; rho_1 = rtilde
     double *r, *rt;
     MonPtrs m;
     static constexpr bool kReduce = true;
+    static constexpr bool kNeedsXr = false;
     __device__ bool active(int) const { return true; }
     __device__ double init(int, int) const { return 0.0; }
-    __device__ void row(int i, int, double d, Acc &a) const
+    __device__ void row(int i, int, double d, double, Acc &a) const
     {
         const double rr = b[i] - d;
         r[i] = rr;
@@ -214,6 +220,7 @@ struct BiP {  // p = r (first) or p = r + beta (p - omega v) (:85-95); fused pha
     int pc;
     SysState *st;
     static constexpr bool kReduce = false;
+    static constexpr bool kNeedsXr = false;
     __device__ bool active(int sys) const { return st[sys].status == ST_RUNNING; }
     __device__ void row(int i, int sys, Acc &) const
     {
@@ -237,9 +244,10 @@ struct BiV {  // v = A phat; alpha = rho_1 / rtilde.v (:98-99)
     const double *rt;
     SysState *st;
     static constexpr bool kReduce = true;
+    static constexpr bool kNeedsXr = false;
     __device__ bool active(int sys) const { return st[sys].status == ST_RUNNING; }
     __device__ double init(int, int) const { return 0.0; }
-    __device__ void row(int i, int, double d, Acc &a) const
+    __device__ void row(int i, int, double d, double, Acc &a) const
     {
         const double vv = d != 0.0 ? d : 0.0;
         v[i] = vv;
@@ -259,6 +267,7 @@ struct BiS {  // s = r - alpha v; x += alpha phat; test on s (:100-104); fused s
     int pc;
     MonPtrs m;
     static constexpr bool kReduce = true;
+    static constexpr bool kNeedsXr = false;
     __device__ bool active(int sys) const { return m.st[sys].status == ST_RUNNING; }
     __device__ void row(int i, int sys, Acc &a) const
     {
@@ -285,9 +294,10 @@ struct BiT {  // t = A shat; omega = t.s / t.t (:107-108)
     const double *s;
     SysState *st;
     static constexpr bool kReduce = true;
+    static constexpr bool kNeedsXr = false;
     __device__ bool active(int sys) const { return st[sys].status == ST_RUNNING; }
     __device__ double init(int, int) const { return 0.0; }
-    __device__ void row(int i, int, double d, Acc &a) const
+    __device__ void row(int i, int, double d, double, Acc &a) const
     {
         const double tt = d != 0.0 ? d : 0.0;
         t[i] = tt;
@@ -307,6 +317,7 @@ struct BiR {  // x += omega shat; r = s - omega t (:109-110); next test; rho_1, 
     const double *s, *shat, *t, *rt;
     MonPtrs m;
     static constexpr bool kReduce = true;
+    static constexpr bool kNeedsXr = false;
     __device__ bool active(int sys) const { return m.st[sys].status == ST_RUNNING; }
     __device__ void row(int i, int sys, Acc &a) const
     {
@@ -379,9 +390,10 @@ struct GmU {
     SysState *st;
     bool always;
     static constexpr bool kReduce = false;
+    static constexpr bool kNeedsXr = false;
     __device__ bool active(int sys) const { return always || st[sys].status == ST_RUNNING; }
     __device__ double init(int, int) const { return 0.0; }
-    __device__ void row(int i, int, double d, Acc &) const { u[i] = b[i] - d; }
+    __device__ void row(int i, int, double d, double, Acc &) const { u[i] = b[i] - d; }
     __device__ void scalar(int, const Acc &) {}
 };
 
@@ -390,9 +402,10 @@ struct GmAv {
     double *u;
     SysState *st;
     static constexpr bool kReduce = false;
+    static constexpr bool kNeedsXr = false;
     __device__ bool active(int sys) const { return st[sys].gate == ST_RUNNING; }
     __device__ double init(int, int) const { return 0.0; }
-    __device__ void row(int i, int, double d, Acc &) const { u[i] = d != 0.0 ? d : 0.0; }
+    __device__ void row(int i, int, double d, double, Acc &) const { u[i] = d != 0.0 ? d : 0.0; }
     __device__ void scalar(int, const Acc &) {}
 };
 
@@ -405,6 +418,7 @@ struct GmNorm {
     GmData g;
     bool first;
     static constexpr bool kReduce = true;
+    static constexpr bool kNeedsXr = false;
     __device__ bool active(int sys) const { return first || m.st[sys].status == ST_RUNNING; }
     __device__ void row(int i, int, Acc &a) const
     {
@@ -448,6 +462,7 @@ struct GmScale {
     SysState *st;
     bool gated;  // use the inner gate (v_{i+1}) or the status (v_0)
     static constexpr bool kReduce = false;
+    static constexpr bool kNeedsXr = false;
     __device__ bool active(int sys) const { return gated ? st[sys].gate == ST_RUNNING : st[sys].status == ST_RUNNING; }
     __device__ void row(int i, int sys, Acc &) const
     {
@@ -468,6 +483,7 @@ struct GmMgs {
     MonPtrs m;
     GmData g;
     static constexpr bool kReduce = true;
+    static constexpr bool kNeedsXr = false;
     __device__ bool active(int sys) const { return m.st[sys].gate == ST_RUNNING; }
     __device__ void row(int r, int, Acc &a) const
     {
@@ -547,6 +563,7 @@ struct GmX {
     GmData g;
     SysState *st;
     static constexpr bool kReduce = false;
+    static constexpr bool kNeedsXr = false;
     __device__ bool active(int sys) const { return st[sys].status == ST_RUNNING; }
     __device__ void row(int r, int sys, Acc &) const
     {
@@ -561,6 +578,163 @@ struct GmX {
     __device__ void scalar(int, const Acc &) {}
 };
 
+// ===================================================== mixed precision
+// Iterative refinement around an FP32 CG (the loop of S/IR.java:57-70 with
+// the inner solve in the role of the preconditioner).  Per system, `phase`
+// says whether the FP64 outer step (x += d, r = b - A x, monitor test) is due
+// or inner FP32 iterations run; every kernel is gated on it, so systems of a
+// batch move through their own refinement steps independently.
+struct MixCfg {
+    double in_rtol;
+    int in_max;
+};
+
+// x += d (the FP32 correction, widened exactly); iter.next() of the outer loop
+struct MxX {
+    double *x;
+    const float *d;
+    SysState *st;
+    static constexpr bool kReduce = true;
+    static constexpr bool kNeedsXr = false;
+    __device__ bool active(int sys) const
+    {
+        const SysState &t = st[sys];
+        return t.status == ST_RUNNING && t.phase == 0 && t.pending;
+    }
+    __device__ void row(int i, int, Acc &) const { x[i] = x[i] + (double)d[i]; }
+    __device__ void scalar(int sys, const Acc &)
+    {
+        SysState &t = st[sys];
+        t.pending = 0;
+        t.iter++;
+    }
+};
+
+// r = b - A x in FP64, the monitor's test on it, then the inner system's
+// right-hand side rin = (float) r, d = 0 and z = M rin in FP32
+struct MxOuter {
+    const double *b;
+    float *rin, *z, *d;
+    const float *invdiag;
+    int pc;
+    MonPtrs m;
+    static constexpr bool kReduce = true;
+    static constexpr bool kNeedsXr = false;
+    __device__ bool active(int sys) const
+    {
+        const SysState &t = m.st[sys];
+        return t.status == ST_RUNNING && t.phase == 0 && !t.pending;
+    }
+    __device__ double init(int, int) const { return 0.0; }
+    __device__ void row(int i, int, double dd, double, Acc &a) const
+    {
+        const double rr = b[i] - dd;
+        norm_add<false>(a, rr, m.mon.norm);
+        const float rf = (float)rr;
+        rin[i] = rf;
+        d[i] = 0.0f;
+        float zf = rf;
+        if (pc == kPcJacobi) {
+            zf = rf * invdiag[i];
+            z[i] = zf;
+        }
+        a.v[2] += (double)(rf * zf);
+        a.v[3] += (double)(rf * rf);
+    }
+    __device__ void scalar(int sys, const Acc &s)
+    {
+        SysState &t = m.st[sys];
+        const int c = m.check(t, sys, norm_finish(s.v, m.mon.norm));
+        if (c == ST_RUNNING) {
+            t.phase = 1;
+            t.pending = 1;
+            t.in_iter = 0;
+            t.in_rho = s.v[2];
+            t.in_r0 = sqrt(s.v[3]);
+        }
+        m.finish(t, c);
+    }
+};
+
+struct MxP {  // p = z (first) or p = beta p + z, FP32
+    float *p;
+    const float *z;
+    SysState *st;
+    static constexpr bool kReduce = false;
+    static constexpr bool kNeedsXr = false;
+    __device__ bool active(int sys) const { return st[sys].status == ST_RUNNING && st[sys].phase == 1; }
+    __device__ void row(int i, int sys, Acc &) const
+    {
+        const SysState &t = st[sys];
+        p[i] = t.in_iter == 0 ? z[i] : fmaf(p[i], (float)t.in_beta, z[i]);
+    }
+    __device__ void scalar(int, const Acc &) {}
+};
+
+struct MxQ {  // q = A32 p (FP32 row sums); alpha = rho / p.q
+    float *q;
+    SysState *st;
+    static constexpr bool kReduce = true;
+    static constexpr bool kNeedsXr = true;
+    __device__ bool active(int sys) const { return st[sys].status == ST_RUNNING && st[sys].phase == 1; }
+    __device__ float init(int, int) const { return 0.0f; }
+    __device__ void row(int i, int, float dd, float pi, Acc &a) const
+    {
+        q[i] = dd;
+        a.v[2] += (double)(pi * dd);
+    }
+    __device__ void scalar(int sys, const Acc &s)
+    {
+        SysState &t = st[sys];
+        t.in_alpha = t.in_rho / s.v[2];
+    }
+};
+
+struct MxUpd {  // d += alpha p; rin -= alpha q; z = M rin; inner stopping test
+    float *d, *rin, *z;
+    const float *p, *q, *invdiag;
+    int pc;
+    SysState *st;
+    MixCfg cfg;
+    static constexpr bool kReduce = true;
+    static constexpr bool kNeedsXr = false;
+    __device__ bool active(int sys) const { return st[sys].status == ST_RUNNING && st[sys].phase == 1; }
+    __device__ void row(int i, int sys, Acc &a) const
+    {
+        const float al = (float)st[sys].in_alpha;
+        d[i] = fmaf(al, p[i], d[i]);
+        const float rf = fmaf(-al, q[i], rin[i]);
+        rin[i] = rf;
+        float zf = rf;
+        if (pc == kPcJacobi) {
+            zf = rf * invdiag[i];
+            z[i] = zf;
+        }
+        a.v[2] += (double)(rf * zf);
+        a.v[3] += (double)(rf * rf);
+    }
+    __device__ void scalar(int sys, const Acc &s)
+    {
+        SysState &t = st[sys];
+        t.in_iter++;
+        t.in_total++;
+        const double rn = sqrt(s.v[3]);
+        if (!(rn > cfg.in_rtol * t.in_r0) || t.in_iter >= cfg.in_max) {
+            t.phase = 0;  // the correction in d goes to x in the next outer step
+        } else {
+            t.in_rho_1 = t.in_rho;
+            t.in_rho = s.v[2];
+            t.in_beta = t.in_rho / t.in_rho_1;
+        }
+    }
+};
+
+__global__ void k_to_f32(int64_t n, const double *a, float *b)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+
 }  // namespace mtjg
 
 using namespace mtjg;
@@ -573,10 +747,19 @@ struct mtjg_solver {
     int restart = 30;
     mtjg_precond *M = nullptr;
     mtjg_monitor mon{};
-    SysState *st = nullptr;
-    double *hist_r = nullptr;
+    SysState *st = nullptr;     // one per system of the matrix being solved
+    int st_alloc = 0;
+    double *hist_r = nullptr;   // history_cap entries per system
     int *hist_it = nullptr;
-    int hist_alloc = 0;
+    int64_t hist_alloc = 0;
+    int num_sys = 1;            // systems of the last solve
+    std::vector<SysState> last_all;
+    // mixed precision
+    bool mixed = false;
+    MixCfg mix{1e-4, 1000};
+    std::vector<float *> v32;   // d, rin, z, p, q
+    float *invdiag32 = nullptr;
+    int64_t inv32_version = -1;
     std::vector<double *> vecs;
     double *V = nullptr;
     GmData gm{};
@@ -668,11 +851,11 @@ struct Phases {
         if (pcm == kPcExternal) {
             int st = pc(v(V_R), z, &S->st->status);
             if (st != MTJG_OK) return st;
-            PH_CHECK(launch_rows(S->ctx, A->tiles, CgDot<STRICT>{v(V_R), z, S->st}, rc(), norm()));
+            PH_CHECK(launch_rows(S->ctx, A->rtiles, CgDot<STRICT>{v(V_R), z, S->st}, rc(), norm()));
         }
-        PH_CHECK(launch_rows(S->ctx, A->tiles, CgP<STRICT>{v(V_P), z, S->st}, rc(), norm()));
+        PH_CHECK(launch_rows(S->ctx, A->rtiles, CgP<STRICT>{v(V_P), z, S->st}, rc(), norm()));
         PH_CHECK(launch_spmv(S->ctx, csr(), A->tiles, v(V_P), CgQ<STRICT>{v(V_P), v(V_Q), S->st}, rc(), norm()));
-        PH_CHECK(launch_rows(S->ctx, A->tiles,
+        PH_CHECK(launch_rows(S->ctx, A->rtiles,
                              CgUpd<STRICT>{v(V_X), v(V_R), z, v(V_P), v(V_Q), invdiag(), pcm, mp()}, rc(), norm()));
         return MTJG_OK;
     }
@@ -689,14 +872,14 @@ struct Phases {
         const int pcm = pc_mode(S);
         double *phat = pcm == kPcIdentity ? v(V_P) : v(V_PH);
         double *shat = pcm == kPcIdentity ? v(V_S) : v(V_SH);
-        PH_CHECK(launch_rows(S->ctx, A->tiles,
+        PH_CHECK(launch_rows(S->ctx, A->rtiles,
                              BiP<STRICT>{v(V_P), phat, v(V_R), v(V_V), invdiag(), pcm, S->st}, rc(), norm()));
         if (pcm == kPcExternal) {
             int st = pc(v(V_P), phat, &S->st->status);
             if (st != MTJG_OK) return st;
         }
         PH_CHECK(launch_spmv(S->ctx, csr(), A->tiles, phat, BiV<STRICT>{v(V_V), v(V_RT), S->st}, rc(), norm()));
-        PH_CHECK(launch_rows(S->ctx, A->tiles,
+        PH_CHECK(launch_rows(S->ctx, A->rtiles,
                              BiS<STRICT>{v(V_S), v(V_X), shat, v(V_R), v(V_V), phat, invdiag(), pcm, mp()}, rc(),
                              norm()));
         if (pcm == kPcExternal) {
@@ -704,7 +887,7 @@ struct Phases {
             if (st != MTJG_OK) return st;
         }
         PH_CHECK(launch_spmv(S->ctx, csr(), A->tiles, shat, BiT<STRICT>{v(V_T), v(V_S), S->st}, rc(), norm()));
-        PH_CHECK(launch_rows(S->ctx, A->tiles,
+        PH_CHECK(launch_rows(S->ctx, A->rtiles,
                              BiR<STRICT>{v(V_X), v(V_R), v(V_S), shat, v(V_T), v(V_RT), mp()}, rc(), norm()));
         return MTJG_OK;
     }
@@ -721,7 +904,7 @@ struct Phases {
             int st = pc(u, r, first ? nullptr : &S->st->status);
             if (st != MTJG_OK) return st;
         }
-        PH_CHECK(launch_rows(S->ctx, A->tiles, GmNorm<STRICT>{r, mp(), S->gm, first}, rc(), norm()));
+        PH_CHECK(launch_rows(S->ctx, A->rtiles, GmNorm<STRICT>{r, mp(), S->gm, first}, rc(), norm()));
         return MTJG_OK;
     }
     int gm_init() { return gm_residual(true); }
@@ -732,7 +915,7 @@ struct Phases {
         double *r = pcm == kPcIdentity ? u : v(V_R);
         double *w = pcm == kPcIdentity ? u : v(V_W);
         // v_0 = r / normr
-        PH_CHECK(launch_rows(S->ctx, A->tiles, GmScale<STRICT>{basis(0), r, S->st, false}, rc(), norm()));
+        PH_CHECK(launch_rows(S->ctx, A->rtiles, GmScale<STRICT>{basis(0), r, S->st, false}, rc(), norm()));
         for (int i = 0; i < S->restart; ++i) {
             PH_CHECK(launch_spmv(S->ctx, csr(), A->tiles, basis(i), GmAv{u, S->st}, rc(), norm()));
             if (pcm != kPcIdentity) {
@@ -742,15 +925,15 @@ struct Phases {
             for (int k = 0; k <= i + 1; ++k) {
                 const double *vprev = k > 0 ? basis(k - 1) : nullptr;
                 const double *vk = k <= i ? basis(k) : nullptr;
-                PH_CHECK(launch_rows(S->ctx, A->tiles, GmMgs<STRICT>{w, vprev, vk, i, k, mp(), S->gm}, rc(),
+                PH_CHECK(launch_rows(S->ctx, A->rtiles, GmMgs<STRICT>{w, vprev, vk, i, k, mp(), S->gm}, rc(),
                                      norm()));
             }
-            PH_CHECK(launch_rows(S->ctx, A->tiles, GmScale<STRICT>{basis(i + 1), w, S->st, true}, rc(), norm()));
+            PH_CHECK(launch_rows(S->ctx, A->rtiles, GmScale<STRICT>{basis(i + 1), w, S->st, true}, rc(), norm()));
         }
         k_gmres_trsv<<<1, 32, 0, S->ctx->stream>>>(S->st, S->gm, A->num_running);
         S->ctx->launches++;
         PH_CHECK(cudaGetLastError());
-        PH_CHECK(launch_rows(S->ctx, A->tiles, GmX<STRICT>{v(V_X), S->V, (size_t)S->n, S->gm, S->st}, rc(), norm()));
+        PH_CHECK(launch_rows(S->ctx, A->rtiles, GmX<STRICT>{v(V_X), S->V, (size_t)S->n, S->gm, S->st}, rc(), norm()));
         return gm_residual(false);
     }
 };
@@ -768,9 +951,61 @@ void drop_graph(mtjg_solver *S)
     S->g_M = nullptr;
 }
 
+// Mixed precision: the body is one outer step then kInnerPerBody inner
+// iterations; systems whose inner solve ends early idle until the next body.
+constexpr int kInnerPerBody = 8;
+
+int mixed_body(mtjg_solver *S, mtjg_csr *A)
+{
+    mtjg_ctx *ctx = S->ctx;
+    const int pcm = pc_mode(S);
+    float *d = S->v32[0], *rin = S->v32[1], *z = pcm == kPcIdentity ? S->v32[1] : S->v32[2];
+    float *p = S->v32[3], *q = S->v32[4];
+    const RedCtx rc = red_ctx(A, A->tiles);
+    const MonPtrs mp{S->st, mon_dev(S), S->hist_r, S->hist_it, A->num_running};
+    const int norm = S->mon.norm;
+    cudaError_t e = launch_rows(ctx, A->rtiles, MxX{S->vecs[V_X], d, S->st}, rc, norm);
+    if (e == cudaSuccess)
+        e = launch_spmv(ctx, CsrArgs{A->rowptr, A->colind, A->val}, A->tiles, (const double *)S->vecs[V_X],
+                        MxOuter{S->vecs[V_B], rin, z, d, S->invdiag32, pcm, mp}, rc, norm);
+    for (int k = 0; k < kInnerPerBody && e == cudaSuccess; ++k) {
+        e = launch_rows(ctx, A->rtiles, MxP{p, z, S->st}, rc, norm);
+        if (e == cudaSuccess)
+            e = launch_spmv(ctx, CsrArgsT<float>{A->rowptr, A->colind, A->val32}, A->tiles, (const float *)p,
+                            MxQ{q, S->st}, rc, norm);
+        if (e == cudaSuccess)
+            e = launch_rows(ctx, A->rtiles, MxUpd{d, rin, z, p, q, S->invdiag32, pcm, S->st, S->mix}, rc, norm);
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "mixed-precision phase");
+    return MTJG_OK;
+}
+
+// FP32 copies the mixed solver reads: the matrix values and the inverse diagonal
+int mixed_prepare(mtjg_solver *S, mtjg_csr *A)
+{
+    mtjg_ctx *ctx = S->ctx;
+    const int grid = ctx->num_sms * 8;
+    if (!A->val32) {
+        MTJG_CUDA(cudaMalloc(&A->val32, sizeof(float) * (size_t)(A->nnz + 4)));
+        MTJG_CUDA(cudaMemsetAsync(A->val32, 0, sizeof(float) * (size_t)(A->nnz + 4), ctx->stream));
+        if (A->nnz) k_to_f32<<<grid, kBlock, 0, ctx->stream>>>(A->nnz, A->val, A->val32);
+        ctx->launches++;
+        drop_graph(S);
+    }
+    if (S->M && S->M->kind == MTJG_PC_JACOBI && S->inv32_version != S->M->version) {
+        if (!S->invdiag32) MTJG_CUDA(cudaMalloc(&S->invdiag32, sizeof(float) * (size_t)std::max(1, S->n)));
+        if (S->n) k_to_f32<<<grid, kBlock, 0, ctx->stream>>>(S->n, S->M->invdiag, S->invdiag32);
+        ctx->launches++;
+        S->inv32_version = S->M->version;
+    }
+    MTJG_CUDA(cudaGetLastError());
+    return MTJG_OK;
+}
+
 template <bool STRICT>
 int run_phase(mtjg_solver *S, mtjg_csr *A, bool init)
 {
+    if (S->mixed) return init ? MTJG_OK : mixed_body(S, A);
     Phases<STRICT> ph{S, A};
     if (S->kind == MTJG_CG) return init ? ph.cg_init() : ph.cg_body();
     if (S->kind == MTJG_BICGSTAB) return init ? ph.bi_init() : ph.bi_body();
@@ -790,7 +1025,7 @@ int capture(mtjg_solver *S, mtjg_csr *A)
     cudaGraph_t g = nullptr;
     MTJG_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     int st = MTJG_OK;
-    const int reps = S->kind == MTJG_GMRES ? 1 : S->chunk;
+    const int reps = S->kind == MTJG_GMRES ? 1 : S->mixed ? 2 : S->chunk;
     for (int c = 0; c < reps && st == MTJG_OK; ++c) st = phase(S, A, false);
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
     if (st != MTJG_OK) {
@@ -814,21 +1049,56 @@ int capture(mtjg_solver *S, mtjg_csr *A)
 
 int map_status(int st) { return st == ST_DONE ? MTJG_OK : st; }
 
+// Device state for `ns` systems: scalars and monitor histories.
+int ensure_state(mtjg_solver *S, int ns)
+{
+    if (ns > S->st_alloc) {
+        cudaFree(S->st);
+        S->st = nullptr;
+        S->st_alloc = 0;
+        MTJG_CUDA(cudaMalloc(&S->st, sizeof(SysState) * (size_t)ns));
+        S->st_alloc = ns;
+        drop_graph(S);
+    }
+    const int64_t need = (int64_t)ns * S->mon.history_cap;
+    if (need > S->hist_alloc) {
+        cudaFree(S->hist_r);
+        cudaFree(S->hist_it);
+        S->hist_r = nullptr;
+        S->hist_it = nullptr;
+        S->hist_alloc = 0;
+        MTJG_CUDA(cudaMalloc(&S->hist_r, sizeof(double) * (size_t)need));
+        MTJG_CUDA(cudaMalloc(&S->hist_it, sizeof(int) * (size_t)need));
+        S->hist_alloc = need;
+        drop_graph(S);
+    }
+    return MTJG_OK;
+}
+
 // vectors b and x are in the solver's buffers
 int run(mtjg_solver *S, mtjg_csr *A, mtjg_result *res)
 {
     mtjg_ctx *ctx = S->ctx;
+    const int ns = A->tiles.num_sys;
+    int st = ensure_state(S, ns);
+    if (st != MTJG_OK) return st;
+    S->num_sys = ns;
     SysState init;
     std::memset(&init, 0, sizeof(init));
     init.status = ST_RUNNING;
     init.gate = ST_RUNNING;
     init.rho_1 = init.rho_2 = init.alpha = init.beta = init.omega = 1.0;
-    MTJG_CUDA(cudaMemcpyAsync(S->st, &init, sizeof(init), cudaMemcpyHostToDevice, ctx->stream));
-    const int one = 1;
-    MTJG_CUDA(cudaMemcpyAsync(A->num_running, &one, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
-    MTJG_CUDA(cudaMemsetAsync(A->cnt, 0, sizeof(unsigned) * 4, ctx->stream));
+    S->last_all.assign(ns, init);
+    if (S->mixed) {
+        st = mixed_prepare(S, A);
+        if (st != MTJG_OK) return st;
+    }
+    MTJG_CUDA(cudaMemcpyAsync(S->st, S->last_all.data(), sizeof(SysState) * (size_t)ns, cudaMemcpyHostToDevice,
+                              ctx->stream));
+    MTJG_CUDA(cudaMemcpyAsync(A->num_running, &S->num_sys, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    MTJG_CUDA(cudaMemsetAsync(A->cnt, 0, sizeof(unsigned) * (size_t)ns, ctx->stream));
     MTJG_CUDA(cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream));
-    int st = phase(S, A, true);
+    st = phase(S, A, true);
     if (st != MTJG_OK) return st;
     const bool stale = !S->gexec || S->g_A != A || S->g_M != S->M || S->g_numerics != ctx->numerics ||
                        S->g_norm != S->mon.norm || S->g_version != (S->M ? S->M->version : 0);
@@ -864,15 +1134,23 @@ int run(mtjg_solver *S, mtjg_csr *A, mtjg_result *res)
             }
         }
     }
-    MTJG_CUDA(cudaMemcpyAsync(&S->last, S->st, sizeof(SysState), cudaMemcpyDeviceToHost, ctx->stream));
+    MTJG_CUDA(cudaMemcpyAsync(S->last_all.data(), S->st, sizeof(SysState) * (size_t)ns, cudaMemcpyDeviceToHost,
+                              ctx->stream));
     int flag = 0;
     MTJG_CUDA(cudaMemcpyAsync(&flag, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     MTJG_CUDA(cudaStreamSynchronize(ctx->stream));
+    S->last = S->last_all[0];
     S->last_valid = 1;
     if (flag) {
         cudaMemset(ctx->d_flag, 0, sizeof(int));
         return fail(MTJG_ERR_DEVICE_TIMEOUT, "a bounded wait in a device kernel gave up during the solve");
     }
+    // a batch reports its first system that did not converge (else system 0)
+    for (const SysState &q : S->last_all)
+        if (q.status != ST_DONE) {
+            S->last = q;
+            break;
+        }
     const int code = map_status(S->last.status);
     if (res) {
         res->status = code;
@@ -880,6 +1158,7 @@ int run(mtjg_solver *S, mtjg_csr *A, mtjg_result *res)
         res->residual = S->last.residual;
         res->detail = S->last.detail;
         res->history_len = S->last.hist_len;
+        res->inner_iterations = S->last.in_total;
     }
     if (code == MTJG_NOT_CONVERGED_BREAKDOWN)
         set_error(S->last.detail == 1 ? "Breakdown: rho" : "Breakdown: omega");
@@ -915,6 +1194,7 @@ int run_empty(mtjg_solver *S, mtjg_result *res)
         res->residual = 0.0;
         res->detail = 0;
         res->history_len = 1;
+        res->inner_iterations = 0;
     }
     return map_status(S->last.status);
 }
@@ -928,6 +1208,15 @@ int check_sizes(mtjg_solver *S, mtjg_csr *A)
     if (S->n != A->n) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "b.size() != A.numRows()");
     if (S->M && S->M->n != A->n) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "preconditioner size differs from A");
     if (S->M && !S->M->ready) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "preconditioner setMatrix has not been called");
+    if (S->mixed && (S->kind != MTJG_CG ||
+                     (S->M && S->M->kind != MTJG_PC_IDENTITY && S->M->kind != MTJG_PC_JACOBI)))
+        return fail(MTJG_ERR_UNSUPPORTED, "mixed precision supports CG with the identity or Jacobi preconditioner");
+    if (A->tiles.num_sys > 1) {
+        if (S->kind == MTJG_GMRES)
+            return fail(MTJG_ERR_UNSUPPORTED, "batched solves support CG and BiCGstab");
+        if (S->M && S->M->kind != MTJG_PC_IDENTITY && S->M->kind != MTJG_PC_JACOBI)
+            return fail(MTJG_ERR_UNSUPPORTED, "batched solves support the identity and Jacobi preconditioners");
+    }
     return MTJG_OK;
 }
 
@@ -954,7 +1243,7 @@ extern "C" int mtjg_solver_create(mtjg_ctx *ctx, int kind, int n, int restart, m
     else if (kind == MTJG_BICGSTAB) need = {V_B, V_X, V_R, V_RT, V_P, V_PH, V_S, V_SH, V_T, V_V};
     else need = {V_B, V_X, V_R, V_U, V_W};
     const size_t nb = sizeof(double) * (size_t)std::max(1, n);
-    bool ok = cudaMalloc(&S->st, sizeof(SysState)) == cudaSuccess;
+    bool ok = ensure_state(S, 1) == MTJG_OK;
     for (int k : need) ok = ok && cudaMalloc(&S->vecs[k], nb) == cudaSuccess;
     if (kind == MTJG_GMRES) {
         const size_t ld = (size_t)restart + 1;
@@ -986,6 +1275,8 @@ extern "C" int mtjg_solver_destroy(mtjg_solver *S)
     cudaStreamSynchronize(S->ctx->stream);
     drop_graph(S);
     for (double *p : S->vecs) cudaFree(p);
+    for (float *p : S->v32) cudaFree(p);
+    cudaFree(S->invdiag32);
     cudaFree(S->V);
     cudaFree(S->gm.H);
     cudaFree(S->gm.s);
@@ -1019,18 +1310,61 @@ extern "C" int mtjg_solver_set_monitor(mtjg_solver *S, const mtjg_monitor *mon)
         return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "bad monitor settings");
     MTJG_CUDA(cudaSetDevice(S->ctx->device));
     MTJG_CUDA(cudaStreamSynchronize(S->ctx->stream));
-    if (mon->history_cap > S->hist_alloc) {
-        cudaFree(S->hist_r);
-        cudaFree(S->hist_it);
-        S->hist_r = nullptr;
-        S->hist_it = nullptr;
-        S->hist_alloc = 0;
-        MTJG_CUDA(cudaMalloc(&S->hist_r, sizeof(double) * (size_t)mon->history_cap));
-        MTJG_CUDA(cudaMalloc(&S->hist_it, sizeof(int) * (size_t)mon->history_cap));
-        S->hist_alloc = mon->history_cap;
-    }
     S->mon = *mon;
     drop_graph(S);
+    return ensure_state(S, std::max(1, S->num_sys));
+}
+
+extern "C" int mtjg_solver_set_mixed(mtjg_solver *S, int enable, double inner_rtol, int inner_max_iter)
+{
+    if (!S) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL solver");
+    if (enable && S->kind != MTJG_CG) return fail(MTJG_ERR_UNSUPPORTED, "mixed precision supports CG");
+    if (enable && (!(inner_rtol > 0.0 && inner_rtol < 1.0) || inner_max_iter <= 0))
+        return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "inner_rtol must lie in (0, 1) and inner_max_iter be positive");
+    MTJG_CUDA(cudaSetDevice(S->ctx->device));
+    MTJG_CUDA(cudaStreamSynchronize(S->ctx->stream));
+    if (enable && S->v32.empty()) {
+        S->v32.assign(5, nullptr);
+        for (auto &p : S->v32)
+            if (cudaMalloc(&p, sizeof(float) * (size_t)std::max(1, S->n)) != cudaSuccess)
+                return fail(MTJG_ERR_OUT_OF_MEMORY, "cudaMalloc failed for the FP32 work vectors");
+    }
+    S->mixed = enable != 0;
+    if (enable) S->mix = MixCfg{inner_rtol, inner_max_iter};
+    drop_graph(S);
+    return MTJG_OK;
+}
+
+extern "C" int mtjg_solver_batch_results(mtjg_solver *S, mtjg_result *out, int count)
+{
+    if (!S || (!out && count > 0)) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL argument");
+    if (!S->last_valid) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "no solve has run");
+    const int m = std::min(count, (int)S->last_all.size());
+    for (int i = 0; i < m; ++i) {
+        const SysState &q = S->last_all[i];
+        out[i].status = map_status(q.status);
+        out[i].iterations = q.iter;
+        out[i].residual = q.residual;
+        out[i].detail = q.detail;
+        out[i].history_len = q.hist_len;
+        out[i].inner_iterations = q.in_total;
+    }
+    return MTJG_OK;
+}
+
+extern "C" int mtjg_solver_batch_history(mtjg_solver *S, int sys, double *resid, int *iters, int cap, int *len)
+{
+    if (!S) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL solver");
+    if (sys < 0 || sys >= (int)S->last_all.size()) return fail(MTJG_ERR_INDEX_OUT_OF_BOUNDS, "system index");
+    const int have = std::min(S->last_all[sys].hist_len, S->mon.history_cap);
+    if (len) *len = have;
+    const int m = std::min(have, cap);
+    if (m > 0) {
+        const size_t off = (size_t)sys * (size_t)S->mon.history_cap;
+        MTJG_CUDA(cudaSetDevice(S->ctx->device));
+        if (resid) MTJG_CUDA(cudaMemcpy(resid, S->hist_r + off, sizeof(double) * (size_t)m, cudaMemcpyDeviceToHost));
+        if (iters) MTJG_CUDA(cudaMemcpy(iters, S->hist_it + off, sizeof(int) * (size_t)m, cudaMemcpyDeviceToHost));
+    }
     return MTJG_OK;
 }
 

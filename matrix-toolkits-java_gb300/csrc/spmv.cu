@@ -17,7 +17,7 @@ int choose_vec(int64_t nnz, int64_t n)
 }
 
 void plan_tiles(const int *rowptr, int row_begin, int row_end, int vec, std::vector<int> &tile_row,
-                std::vector<unsigned char> &tile_long)
+                std::vector<unsigned char> &tile_flags)
 {
     const int rows_cap = kTileRows / vec;
     int r = row_begin;
@@ -25,7 +25,7 @@ void plan_tiles(const int *rowptr, int row_begin, int row_end, int vec, std::vec
         tile_row.push_back(r);
         int len0 = rowptr[r + 1] - rowptr[r];
         if (len0 > kTileNnz) {
-            tile_long.push_back(1);
+            tile_flags.push_back((unsigned char)((vec << 1) | 1));
             r += 1;
             continue;
         }
@@ -38,23 +38,39 @@ void plan_tiles(const int *rowptr, int row_begin, int row_end, int vec, std::vec
             rows++;
             r++;
         }
-        tile_long.push_back(0);
+        tile_flags.push_back((unsigned char)(vec << 1));
     }
 }
 
-int upload_tiles(TileSet &ts, const std::vector<int> &tile_row, const std::vector<unsigned char> &tile_long,
-                 const std::vector<int> *tile_sys, const std::vector<int> &sys_tile, int vec)
+void plan_row_tiles(int row_begin, int row_end, std::vector<int> &tile_row, std::vector<unsigned char> &tile_flags)
+{
+    for (int r = row_begin; r < row_end; r += kBlock) {
+        tile_row.push_back(r);
+        tile_flags.push_back((unsigned char)(1 << 1));
+    }
+}
+
+int upload_tiles(TileSet &ts, const std::vector<int> &tile_row, const std::vector<unsigned char> &tile_flags,
+                 const std::vector<int> *tile_sys, const std::vector<int> &sys_tile, int vec, const int *rowptr)
 {
     free_tiles(ts);
-    ts.num_tiles = (int)tile_long.size();
+    ts.num_tiles = (int)tile_flags.size();
     ts.num_sys = (int)sys_tile.size() - 1;
     ts.vec = vec;
+    ts.vec_mask = 0;
+    for (unsigned char f : tile_flags) ts.vec_mask |= f >> 1;
     ts.h_tile_row = tile_row;
     MTJG_CUDA(cudaMalloc(&ts.tile_row, sizeof(int) * tile_row.size()));
     MTJG_CUDA(cudaMemcpy(ts.tile_row, tile_row.data(), sizeof(int) * tile_row.size(), cudaMemcpyHostToDevice));
-    MTJG_CUDA(cudaMalloc(&ts.tile_long, std::max<size_t>(1, tile_long.size())));
-    if (!tile_long.empty())
-        MTJG_CUDA(cudaMemcpy(ts.tile_long, tile_long.data(), tile_long.size(), cudaMemcpyHostToDevice));
+    if (rowptr) {
+        std::vector<int> nz(tile_row.size());
+        for (size_t i = 0; i < tile_row.size(); ++i) nz[i] = rowptr[tile_row[i]];
+        MTJG_CUDA(cudaMalloc(&ts.tile_nz, sizeof(int) * nz.size()));
+        MTJG_CUDA(cudaMemcpy(ts.tile_nz, nz.data(), sizeof(int) * nz.size(), cudaMemcpyHostToDevice));
+    }
+    MTJG_CUDA(cudaMalloc(&ts.tile_flags, std::max<size_t>(1, tile_flags.size())));
+    if (!tile_flags.empty())
+        MTJG_CUDA(cudaMemcpy(ts.tile_flags, tile_flags.data(), tile_flags.size(), cudaMemcpyHostToDevice));
     MTJG_CUDA(cudaMalloc(&ts.sys_tile, sizeof(int) * sys_tile.size()));
     MTJG_CUDA(cudaMemcpy(ts.sys_tile, sys_tile.data(), sizeof(int) * sys_tile.size(), cudaMemcpyHostToDevice));
     if (tile_sys) {
@@ -69,11 +85,12 @@ int upload_tiles(TileSet &ts, const std::vector<int> &tile_row, const std::vecto
 void free_tiles(TileSet &ts)
 {
     cudaFree(ts.tile_row);
+    cudaFree(ts.tile_nz);
     cudaFree(ts.tile_sys);
     cudaFree(ts.sys_tile);
-    cudaFree(ts.tile_long);
-    ts.tile_row = ts.tile_sys = ts.sys_tile = nullptr;
-    ts.tile_long = nullptr;
+    cudaFree(ts.tile_flags);
+    ts.tile_row = ts.tile_nz = ts.tile_sys = ts.sys_tile = nullptr;
+    ts.tile_flags = nullptr;
     ts.num_tiles = 0;
 }
 
@@ -221,7 +238,7 @@ int csr_transpose(mtjg_ctx *ctx, int n, int m, const int *rowptr, const int *col
     const int grid = std::max(1, std::min((n + kBlock - 1) / kBlock, ctx->num_sms * 8));
     MTJG_CUDA(cudaMalloc(&cnt, sizeof(int) * (size_t)std::max(1, m)));
     MTJG_CUDA(cudaMalloc(&cursor, sizeof(int) * (size_t)std::max(1, m)));
-    MTJG_CUDA(cudaMalloc(&trp, sizeof(int) * (size_t)(m + 1)));
+    MTJG_CUDA(cudaMalloc(&trp, sizeof(int) * (size_t)(m + 1 + kRowptrPad)));
     MTJG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int) * (size_t)std::max(1, m), ctx->stream));
     MTJG_CUDA(cudaMemsetAsync(cursor, 0, sizeof(int) * (size_t)std::max(1, m), ctx->stream));
     if (n > 0) {
@@ -232,6 +249,10 @@ int csr_transpose(mtjg_ctx *ctx, int n, int m, const int *rowptr, const int *col
     if (st != MTJG_OK) return st;
     int total = 0;
     MTJG_CUDA(cudaMemcpy(&total, trp + m, sizeof(int), cudaMemcpyDeviceToHost));
+    {
+        const int pad[kRowptrPad] = {total, total, total, total};
+        MTJG_CUDA(cudaMemcpy(trp + m + 1, pad, sizeof(pad), cudaMemcpyHostToDevice));
+    }
     MTJG_CUDA(cudaMalloc(&tci, sizeof(int) * (size_t)(total + 4)));
     MTJG_CUDA(cudaMalloc(&tv, sizeof(double) * (size_t)(total + 2)));
     MTJG_CUDA(cudaMemsetAsync(tci, 0xff, sizeof(int) * (size_t)(total + 4), ctx->stream));
@@ -261,9 +282,10 @@ int csr_transpose(mtjg_ctx *ctx, int n, int m, const int *rowptr, const int *col
 struct EpiMult {
     double *y;
     static constexpr bool kReduce = false;
+    static constexpr bool kNeedsXr = false;
     __device__ bool active(int) const { return true; }
     __device__ double init(int, int) const { return 0.0; }
-    __device__ void row(int r, int, double d, Acc &) const { y[r] = d != 0.0 ? d : 0.0; }
+    __device__ void row(int r, int, double d, double, Acc &) const { y[r] = d != 0.0 ? d : 0.0; }
     __device__ void scalar(int, const Acc &) {}
 };
 
@@ -273,9 +295,10 @@ struct EpiMultAdd {
     double *y;
     double alpha;
     static constexpr bool kReduce = false;
+    static constexpr bool kNeedsXr = false;
     __device__ bool active(int) const { return true; }
     __device__ double init(int, int) const { return 0.0; }
-    __device__ void row(int r, int, double d, Acc &) const { y[r] = fmac<S>(alpha, d, y[r]); }
+    __device__ void row(int r, int, double d, double, Acc &) const { y[r] = fmac<S>(alpha, d, y[r]); }
     __device__ void scalar(int, const Acc &) {}
 };
 
@@ -284,9 +307,10 @@ struct EpiMultAdd {
 struct EpiSet {
     double *y;
     static constexpr bool kReduce = false;
+    static constexpr bool kNeedsXr = false;
     __device__ bool active(int) const { return true; }
     __device__ double init(int, int) const { return 0.0; }
-    __device__ void row(int r, int, double d, Acc &) const { y[r] = d; }
+    __device__ void row(int r, int, double d, double, Acc &) const { y[r] = d; }
     __device__ void scalar(int, const Acc &) {}
 };
 
@@ -296,9 +320,10 @@ struct EpiTransMultAdd {
     double *y;
     double alpha, inv;
     static constexpr bool kReduce = false;
+    static constexpr bool kNeedsXr = false;
     __device__ bool active(int) const { return true; }
     __device__ double init(int r, int) const { return y[r] * inv; }
-    __device__ void row(int r, int, double d, Acc &) const { y[r] = d * alpha; }
+    __device__ void row(int r, int, double d, double, Acc &) const { y[r] = d * alpha; }
     __device__ void scalar(int, const Acc &) {}
 };
 
@@ -328,13 +353,27 @@ static int csr_validate(int n, int m, const int *rowptr, const int *colind)
     return MTJG_OK;
 }
 
-extern "C" int mtjg_csr_upload(mtjg_ctx *ctx, int n, int m, const int *rowptr, const int *colind,
-                               const double *val, mtjg_csr **out)
+// Uploads a CSR; with sys_rows (num_sys + 1 row offsets) it is a batch of
+// independent systems whose tiles are planned system by system.
+static int csr_upload_impl(mtjg_ctx *ctx, int n, int m, const int *rowptr, const int *colind, const double *val,
+                           int num_sys, const int *sys_rows, mtjg_csr **out)
 {
     if (!ctx || !out) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL argument");
     *out = nullptr;
     int st = csr_validate(n, m, rowptr, colind);
     if (st != MTJG_OK) return st;
+    if (sys_rows) {
+        if (sys_rows[0] != 0 || sys_rows[num_sys] != n)
+            return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "system row offsets must run from 0 to the number of rows");
+        for (int s = 0; s < num_sys; ++s) {
+            const int r0 = sys_rows[s], r1 = sys_rows[s + 1];
+            if (r1 < r0) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "system row offsets must be nondecreasing");
+            for (int i = r0; i < r1; ++i)
+                if (rowptr[i + 1] > rowptr[i] && (colind[rowptr[i]] < r0 || colind[rowptr[i + 1] - 1] >= r1))
+                    return fail(MTJG_ERR_ILLEGAL_ARGUMENT,
+                                "system " + std::to_string(s) + " references a column outside its rows");
+        }
+    }
     MTJG_CUDA(cudaSetDevice(ctx->device));
     const int64_t nnz = rowptr[n];
     mtjg_csr *A = new mtjg_csr();
@@ -348,7 +387,7 @@ extern "C" int mtjg_csr_upload(mtjg_ctx *ctx, int n, int m, const int *rowptr, c
         mtjg_csr_destroy(A);
         return code;
     };
-    if (cudaMalloc(&A->rowptr, sizeof(int) * (size_t)(n + 1)) != cudaSuccess ||
+    if (cudaMalloc(&A->rowptr, sizeof(int) * (size_t)(n + 1 + kRowptrPad)) != cudaSuccess ||
         cudaMalloc(&A->colind, sizeof(int) * (size_t)(nnz + 4)) != cudaSuccess ||
         cudaMalloc(&A->val, sizeof(double) * (size_t)(nnz + 2)) != cudaSuccess ||
         cudaMalloc(&A->d_x, sizeof(double) * (size_t)std::max(1, std::max(n, m))) != cudaSuccess ||
@@ -360,24 +399,59 @@ extern "C" int mtjg_csr_upload(mtjg_ctx *ctx, int n, int m, const int *rowptr, c
         (nnz && cudaMemcpy(A->colind, colind, sizeof(int) * (size_t)nnz, cudaMemcpyHostToDevice) != cudaSuccess) ||
         (nnz && cudaMemcpy(A->val, val, sizeof(double) * (size_t)nnz, cudaMemcpyHostToDevice) != cudaSuccess))
         return bail(fail(MTJG_ERR_CUDA, "copying the CSR matrix to the device failed"));
-    // tiles
+    {
+        // bulk copies of a tile's row pointers may read up to 3 entries past rowptr[n]
+        const int pad[kRowptrPad] = {rowptr[n], rowptr[n], rowptr[n], rowptr[n]};
+        if (cudaMemcpy(A->rowptr + n + 1, pad, sizeof(pad), cudaMemcpyHostToDevice) != cudaSuccess)
+            return bail(fail(MTJG_ERR_CUDA, "copying the CSR matrix to the device failed"));
+    }
+    // tiles, system by system (tiles never straddle two systems); each
+    // system's lanes per row follow its own entries per row, so its tiles and
+    // its results do not depend on the rest of a batch
     const int vec = choose_vec(nnz, n);
-    std::vector<int> tile_row;
-    std::vector<unsigned char> tile_long;
-    plan_tiles(rowptr, 0, n, vec, tile_row, tile_long);
+    std::vector<int> tile_row, rtile_row, tile_sys, rtile_sys, sys_tile = {0}, rsys_tile = {0};
+    std::vector<unsigned char> tile_flags, rtile_flags;
+    const int ns = sys_rows ? num_sys : 1;
+    for (int s = 0; s < ns; ++s) {
+        const int r0 = sys_rows ? sys_rows[s] : 0, r1 = sys_rows ? sys_rows[s + 1] : n;
+        const int vs = choose_vec((int64_t)rowptr[r1] - rowptr[r0], r1 - r0);
+        plan_tiles(rowptr, r0, r1, vs, tile_row, tile_flags);
+        plan_row_tiles(r0, r1, rtile_row, rtile_flags);
+        tile_sys.resize(tile_flags.size(), s);
+        rtile_sys.resize(rtile_flags.size(), s);
+        sys_tile.push_back((int)tile_flags.size());
+        rsys_tile.push_back((int)rtile_flags.size());
+    }
     tile_row.push_back(n);
-    std::vector<int> sys_tile = {0, (int)tile_long.size()};
-    st = upload_tiles(A->tiles, tile_row, tile_long, nullptr, sys_tile, vec);
+    rtile_row.push_back(n);
+    st = upload_tiles(A->tiles, tile_row, tile_flags, sys_rows ? &tile_sys : nullptr, sys_tile, vec, rowptr);
     if (st != MTJG_OK) return bail(st);
-    const size_t nt = std::max<size_t>(1, tile_long.size());
+    st = upload_tiles(A->rtiles, rtile_row, rtile_flags, sys_rows ? &rtile_sys : nullptr, rsys_tile, 1, nullptr);
+    if (st != MTJG_OK) return bail(st);
+    const size_t nt = std::max<size_t>(1, std::max(tile_flags.size(), rtile_flags.size()));
     if (cudaMalloc(&A->part, sizeof(double) * nt * kParts) != cudaSuccess ||
-        cudaMalloc(&A->cnt, sizeof(unsigned) * 4) != cudaSuccess ||
+        cudaMalloc(&A->cnt, sizeof(unsigned) * (size_t)std::max(4, ns)) != cudaSuccess ||
         cudaMalloc(&A->num_running, sizeof(int) * 4) != cudaSuccess)
         return bail(fail(MTJG_ERR_OUT_OF_MEMORY, "cudaMalloc failed for reduction scratch"));
-    cudaMemset(A->cnt, 0, sizeof(unsigned) * 4);
+    cudaMemset(A->cnt, 0, sizeof(unsigned) * (size_t)std::max(4, ns));
     cudaMemset(A->num_running, 0, sizeof(int) * 4);
+    if (sys_rows) A->sys_rows.assign(sys_rows, sys_rows + num_sys + 1);
     *out = A;
     return MTJG_OK;
+}
+
+extern "C" int mtjg_csr_upload(mtjg_ctx *ctx, int n, int m, const int *rowptr, const int *colind,
+                               const double *val, mtjg_csr **out)
+{
+    return csr_upload_impl(ctx, n, m, rowptr, colind, val, 1, nullptr, out);
+}
+
+extern "C" int mtjg_batch_upload(mtjg_ctx *ctx, int num_systems, const int *sys_rows, const int *rowptr,
+                                 const int *colind, const double *val, mtjg_csr **out)
+{
+    if (num_systems <= 0 || !sys_rows) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "a batch needs at least one system");
+    const int n = sys_rows[num_systems];
+    return csr_upload_impl(ctx, n, n, rowptr, colind, val, num_systems, sys_rows, out);
 }
 
 extern "C" int mtjg_csr_update_values(mtjg_csr *A, const double *val)
@@ -393,6 +467,8 @@ extern "C" int mtjg_csr_update_values(mtjg_csr *A, const double *val)
     A->t_rowptr = A->t_colind = nullptr;
     A->t_val = nullptr;
     free_tiles(A->t_tiles);
+    cudaFree(A->val32);  // the FP32 copy too
+    A->val32 = nullptr;
     return MTJG_OK;
 }
 
@@ -407,12 +483,14 @@ extern "C" int mtjg_csr_destroy(mtjg_csr *A)
     cudaFree(A->t_rowptr);
     cudaFree(A->t_colind);
     cudaFree(A->t_val);
+    cudaFree(A->val32);
     cudaFree(A->part);
     cudaFree(A->cnt);
     cudaFree(A->num_running);
     cudaFree(A->d_x);
     cudaFree(A->d_y);
     free_tiles(A->tiles);
+    free_tiles(A->rtiles);
     free_tiles(A->t_tiles);
     mtjg_ctx *ctx = A->ctx;
     delete A;
@@ -441,11 +519,11 @@ static int ensure_transpose(mtjg_csr *A)
     MTJG_CUDA(cudaMemcpy(trp.data(), A->t_rowptr, sizeof(int) * (size_t)(A->m + 1), cudaMemcpyDeviceToHost));
     const int vec = choose_vec(tnnz, A->m);
     std::vector<int> tile_row;
-    std::vector<unsigned char> tile_long;
-    plan_tiles(trp.data(), 0, A->m, vec, tile_row, tile_long);
+    std::vector<unsigned char> tile_flags;
+    plan_tiles(trp.data(), 0, A->m, vec, tile_row, tile_flags);
     tile_row.push_back(A->m);
-    std::vector<int> sys_tile = {0, (int)tile_long.size()};
-    return upload_tiles(A->t_tiles, tile_row, tile_long, nullptr, sys_tile, vec);
+    std::vector<int> sys_tile = {0, (int)tile_flags.size()};
+    return upload_tiles(A->t_tiles, tile_row, tile_flags, nullptr, sys_tile, vec, trp.data());
 }
 
 static int check_err_flag(mtjg_ctx *ctx)

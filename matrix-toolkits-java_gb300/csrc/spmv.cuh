@@ -1,15 +1,21 @@
 // spmv.cuh -- tiled CSR product and tiled row kernels.
 //
-// k_spmv: persistent CTAs walk the row tiles of a CSR matrix.  The values
-// and column indices of the next tile are brought into shared memory by one
-// thread with two cp.async.bulk copies completing on an mbarrier, while the
-// block computes the current tile (two stages).  Each row is summed from
-// shared memory in ascending entry order (vec == 1: one thread per row, the
-// order of CompRowMatrix.mult, S/CompRowMatrix.java:304-312) or by a group of
-// `vec` lanes with a fixed butterfly (vec > 1).  x is gathered through the
-// read-only path (L1/L2).  The epilogue object gives the starting value of a
-// row sum (init) and decides what a finished row sum becomes (y = Ax,
-// y += alpha*Ax, r = b - Ax, fused dot products, ...).
+// k_spmv: persistent CTAs walk the product tiles of a CSR matrix.  The row
+// pointers, values and column indices of the next tile are brought into
+// shared memory by one thread with three cp.async.bulk copies completing on
+// an mbarrier, while the block computes the current tile (two stages).  Each
+// row is summed from shared memory in ascending entry order (vec == 1: one
+// thread per row, the order of CompRowMatrix.mult, S/CompRowMatrix.java:304-312)
+// or by a group of `vec` lanes with a fixed butterfly (vec > 1).  x is
+// gathered through the read-only path (L1/L2).  The epilogue object gives the
+// starting value of a row sum (init) and decides what a finished row sum
+// becomes (y = Ax, y += alpha*Ax, r = b - Ax, fused dot products, ...).
+//
+// k_rows: one block per row tile (kBlock rows, one row per thread); enough
+// blocks are resident to keep HBM busy without any loop per thread.
+//
+// A phase with a reduction stores one partial per tile; k_finalize (dev.cuh)
+// then reduces each system's partials in tile order and runs the scalar step.
 #pragma once
 
 #include "dev.cuh"
@@ -18,44 +24,50 @@ namespace mtjg {
 
 constexpr int kValCap = kTileNnz + 2;     // doubles per stage (+2: 16-byte rounding)
 constexpr int kColCap = kTileNnz + 8;     // ints per stage (+8: 16-byte rounding at both ends)
+constexpr int kRowCap = kTileRows + 1 + 8;  // row pointers per stage
 constexpr int kValBytes = ((kValCap * 8 + 15) / 16) * 16;
 constexpr int kColBytes = ((kColCap * 4 + 15) / 16) * 16;
-constexpr int kStageBytes = kValBytes + kColBytes;
+constexpr int kRowBytes = ((kRowCap * 4 + 15) / 16) * 16;
+constexpr int kStageBytes = kValBytes + kColBytes + kRowBytes;
 constexpr int kSpmvSmem = 2 * kStageBytes;
-constexpr int kSpmvCtasPerSm = 3;
+constexpr int kSpmvCtasPerSm = 4;
 constexpr long long kWaitLimit = 1LL << 22;
+// row pointer arrays handed to k_spmv carry this many padding entries
+constexpr int kRowptrPad = 4;
 
 struct TileArgs {
     int num_tiles;
     const int *tile_row;
+    const int *tile_nz;
     const int *tile_sys;
-    const unsigned char *tile_long;
+    const unsigned char *tile_flags;
 };
 
-struct CsrArgs {
+template <class T>
+struct CsrArgsT {
     const int *rowptr;
     const int *colind;
-    const double *val;
+    const T *val;
 };
+using CsrArgs = CsrArgsT<double>;
 
 __device__ __forceinline__ int tile_system(const TileArgs &ta, int t)
 {
     return ta.tile_sys ? ta.tile_sys[t] : 0;
 }
 
-template <int VEC, bool S, class Epi>
+template <int VEC, bool S, class T, class Epi>
 __global__ void __launch_bounds__(kBlock, kSpmvCtasPerSm)
-    k_spmv(CsrArgs A, TileArgs ta, const double *__restrict__ x, Epi epi, RedCtx rc, int normtype,
-           int *err)
+    k_spmv(CsrArgsT<T> A, TileArgs ta, const T *__restrict__ x, Epi epi, RedCtx rc, int normtype, int *err)
 {
+    constexpr int kVA = 16 / (int)sizeof(T);  // values per 16 bytes
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ Acc red_sm[kBlock / 32];
-    __shared__ int s_last;
-    __shared__ double s_long[kBlock / 32];
+    __shared__ T s_long[kBlock / 32];
 
     const int tid = threadIdx.x;
-    const int G = gridDim.x, T = ta.num_tiles;
+    const int G = gridDim.x, NT = ta.num_tiles;
     if (tid == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
@@ -63,77 +75,96 @@ __global__ void __launch_bounds__(kBlock, kSpmvCtasPerSm)
     }
     __syncthreads();
 
-    auto sval = [&](int s) { return reinterpret_cast<double *>(smem + s * kStageBytes); };
+    auto sval = [&](int s) { return reinterpret_cast<T *>(smem + s * kStageBytes); };
     auto scol = [&](int s) { return reinterpret_cast<int *>(smem + s * kStageBytes + kValBytes); };
-    auto active = [&](int t) { return epi.active(tile_system(ta, t)); };
+    auto srow = [&](int s) { return reinterpret_cast<int *>(smem + s * kStageBytes + kValBytes + kColBytes); };
+    // a launch takes the tiles of its lanes-per-row class (STRICT: all tiles)
+    auto active = [&](int t) { return (S || (ta.tile_flags[t] >> 1) == VEC) && epi.active(tile_system(ta, t)); };
     auto issue = [&](int t, int s) {
+        const int nz0 = ta.tile_nz[t], nz1 = ta.tile_nz[t + 1];
         const int r0 = ta.tile_row[t], r1 = ta.tile_row[t + 1];
-        const int nz0 = A.rowptr[r0], nz1 = A.rowptr[r1];
-        const int v0 = nz0 & ~1, v1 = (nz1 + 1) & ~1;
+        const int v0 = nz0 & ~(kVA - 1), v1 = (nz1 + kVA - 1) & ~(kVA - 1);
         const int c0 = nz0 & ~3, c1 = (nz1 + 3) & ~3;
-        const unsigned vb = (unsigned)(v1 - v0) * 8u, cb = (unsigned)(c1 - c0) * 4u;
+        const int p0 = r0 & ~3, p1 = (r1 + 1 + 3) & ~3;
+        const unsigned vb = (unsigned)(v1 - v0) * (unsigned)sizeof(T), cb = (unsigned)(c1 - c0) * 4u,
+                       pb = (unsigned)(p1 - p0) * 4u;
         fence_proxy_async();
-        mbar_arrive_expect_tx(&bar[s], vb + cb);
+        mbar_arrive_expect_tx(&bar[s], vb + cb + pb);
         if (vb) bulk_g2s(sval(s), A.val + v0, vb, &bar[s]);
         if (cb) bulk_g2s(scol(s), A.colind + c0, cb, &bar[s]);
+        bulk_g2s(srow(s), A.rowptr + p0, pb, &bar[s]);
     };
 
     unsigned phase[2] = {0u, 0u};
     int s = 0;
     int t = blockIdx.x;
-    if (tid == 0 && t < T && !ta.tile_long[t] && active(t)) issue(t, 0);
-    for (; t < T; t += G) {
+    if (tid == 0 && t < NT && !(ta.tile_flags[t] & 1) && active(t)) issue(t, 0);
+    for (; t < NT; t += G) {
         const int tn = t + G;
-        if (tid == 0 && tn < T && !ta.tile_long[tn] && active(tn)) issue(tn, s ^ 1);
+        if (tid == 0 && tn < NT && !(ta.tile_flags[tn] & 1) && active(tn)) issue(tn, s ^ 1);
         if (active(t)) {
             const int sys = tile_system(ta, t);
             const int r0 = ta.tile_row[t], r1 = ta.tile_row[t + 1];
             Acc acc;
             acc_zero(acc);
-            if (!ta.tile_long[t]) {
+            if (!(ta.tile_flags[t] & 1)) {
                 const bool ok = mbar_wait_bounded(&bar[s], phase[s], kWaitLimit);
                 if (__syncthreads_or(!ok)) {
                     // a copy never completed: report, drain what is in flight, stop
                     if (tid == 0) atomicExch(err, 1);
                     mbar_wait_bounded(&bar[s], phase[s], kWaitLimit);
-                    if (tn < T && !ta.tile_long[tn] && active(tn))
+                    if (tn < NT && !(ta.tile_flags[tn] & 1) && active(tn))
                         mbar_wait_bounded(&bar[s ^ 1], phase[s ^ 1], kWaitLimit);
                     return;
                 }
                 phase[s] ^= 1u;
-                const double *sv = sval(s);
+                const T *sv = sval(s);
                 const int *sc = scol(s);
-                const int nzb = A.rowptr[r0];
-                const int vo = nzb & ~1, co = nzb & ~3;
+                const int *sr = srow(s);
+                const int nzb = ta.tile_nz[t];
+                const int vo = nzb & ~(kVA - 1), co = nzb & ~3, po = r0 & ~3;
                 if constexpr (VEC == 1) {
                     for (int r = r0 + tid; r < r1; r += kBlock) {
-                        const int b = A.rowptr[r], e = A.rowptr[r + 1];
-                        double sum = epi.init(r, sys);
-#pragma unroll 4
-                        for (int k = b; k < e; ++k) sum = fmac<S>(sv[k - vo], __ldg(x + sc[k - co]), sum);
-                        epi.row(r, sys, sum, acc);
+                        const int b = sr[r - po], e = sr[r + 1 - po];
+                        T sum = epi.init(r, sys);
+                        T xr = T(0);
+                        bool diag = false;
+#pragma unroll 8
+                        for (int k = b; k < e; ++k) {
+                            const int c = sc[k - co];
+                            const T xv = __ldg(x + c);
+                            if (c == r) {
+                                xr = xv;
+                                diag = true;
+                            }
+                            sum = fmac<S>(sv[k - vo], xv, sum);
+                        }
+                        if constexpr (Epi::kNeedsXr) {
+                            if (!diag) xr = __ldg(x + r);
+                        }
+                        epi.row(r, sys, sum, xr, acc);
                     }
                 } else {
                     const int g = tid / VEC, l = tid % VEC;
                     for (int base = r0; base < r1; base += kBlock / VEC) {
                         const int r = base + g;
-                        double sum = 0.0;
+                        T sum = T(0);
                         if (r < r1 && l == 0) sum = epi.init(r, sys);
                         if (r < r1) {
-                            const int b = A.rowptr[r], e = A.rowptr[r + 1];
+                            const int b = sr[r - po], e = sr[r + 1 - po];
                             for (int k = b + l; k < e; k += VEC)
                                 sum = fmac<S>(sv[k - vo], __ldg(x + sc[k - co]), sum);
                         }
 #pragma unroll
                         for (int off = VEC / 2; off > 0; off >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off, VEC);
-                        if (r < r1 && l == 0) epi.row(r, sys, sum, acc);
+                        if (r < r1 && l == 0) epi.row(r, sys, sum, Epi::kNeedsXr ? __ldg(x + r) : T(0), acc);
                     }
                 }
             } else {
                 // a single row longer than a stage: straight from global memory
                 const int r = r0;
                 const int b = A.rowptr[r], e = A.rowptr[r + 1];
-                double sum = tid == 0 ? epi.init(r, sys) : 0.0;
+                T sum = tid == 0 ? epi.init(r, sys) : T(0);
                 if constexpr (S) {
                     if (tid == 0)
                         for (int k = b; k < e; ++k) sum = fmac<S>(A.val[k], __ldg(x + A.colind[k]), sum);
@@ -149,47 +180,48 @@ __global__ void __launch_bounds__(kBlock, kSpmvCtasPerSm)
                     }
                     __syncthreads();
                 }
-                if (tid == 0) epi.row(r, sys, sum, acc);
+                if (tid == 0) epi.row(r, sys, sum, Epi::kNeedsXr ? __ldg(x + r) : T(0), acc);
             }
-            if constexpr (Epi::kReduce) tile_finish(acc, t, sys, epi, rc, normtype, red_sm, &s_last);
+            if constexpr (Epi::kReduce) tile_partial(acc, t, rc, normtype, red_sm);
         }
         __syncthreads();
         s ^= 1;
     }
 }
 
-// Row kernel: persistent CTAs walk the same tiles and apply op.row to every
-// row of active systems; per-tile partials as in k_spmv.
+// Row kernel: block b handles row tile b, one row per thread.
 template <class Op>
 __global__ void __launch_bounds__(kBlock) k_rows(TileArgs ta, Op op, RedCtx rc, int normtype)
 {
     __shared__ Acc red_sm[kBlock / 32];
-    __shared__ int s_last;
-    for (int t = blockIdx.x; t < ta.num_tiles; t += gridDim.x) {
-        const int sys = tile_system(ta, t);
-        if (!op.active(sys)) continue;
-        Acc acc;
-        acc_zero(acc);
-        const int r0 = ta.tile_row[t], r1 = ta.tile_row[t + 1];
-        for (int r = r0 + (int)threadIdx.x; r < r1; r += kBlock) op.row(r, sys, acc);
-        if constexpr (Op::kReduce) tile_finish(acc, t, sys, op, rc, normtype, red_sm, &s_last);
-    }
+    const int t = blockIdx.x;
+    const int sys = tile_system(ta, t);
+    if (!op.active(sys)) return;
+    Acc acc;
+    acc_zero(acc);
+    const int r = ta.tile_row[t] + (int)threadIdx.x;
+    if (r < ta.tile_row[t + 1]) op.row(r, sys, acc);
+    if constexpr (Op::kReduce) tile_partial(acc, t, rc, normtype, red_sm);
 }
-
-}  // namespace mtjg
-
-namespace mtjg {
 
 inline TileArgs tile_args(const TileSet &ts)
 {
-    return TileArgs{ts.num_tiles, ts.tile_row, ts.tile_sys, ts.tile_long};
+    return TileArgs{ts.num_tiles, ts.tile_row, ts.tile_nz, ts.tile_sys, ts.tile_flags};
 }
 
-template <int VEC, bool S, class Epi>
-cudaError_t launch_spmv_t(mtjg_ctx *ctx, CsrArgs A, const TileSet &ts, const double *x, const Epi &epi,
+template <class Op>
+cudaError_t launch_finalize(mtjg_ctx *ctx, const TileSet &ts, const Op &op, const RedCtx &rc, int normtype)
+{
+    k_finalize<Op><<<ts.num_sys, kBlock, 0, ctx->stream>>>(op, rc, normtype);
+    ctx->launches++;
+    return cudaGetLastError();
+}
+
+template <int VEC, bool S, class T, class Epi>
+cudaError_t launch_spmv_t(mtjg_ctx *ctx, CsrArgsT<T> A, const TileSet &ts, const T *x, const Epi &epi,
                           const RedCtx &rc, int normtype)
 {
-    auto k = k_spmv<VEC, S, Epi>;
+    auto k = k_spmv<VEC, S, T, Epi>;
     static bool attr_set = false;
     if (!attr_set) {
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kSpmvSmem);
@@ -204,26 +236,40 @@ cudaError_t launch_spmv_t(mtjg_ctx *ctx, CsrArgs A, const TileSet &ts, const dou
 
 // Chooses the lanes-per-row variant of the tiles and the rounding mode of
 // the context.  STRICT always sums one row per thread in entry order.
-template <class Epi>
-cudaError_t launch_spmv(mtjg_ctx *ctx, CsrArgs A, const TileSet &ts, const double *x, const Epi &epi,
+template <class T, class Epi>
+cudaError_t launch_spmv(mtjg_ctx *ctx, CsrArgsT<T> A, const TileSet &ts, const T *x, const Epi &epi,
                         const RedCtx &rc, int normtype)
 {
     if (ts.num_tiles == 0) return cudaSuccess;
-    if (ctx->numerics == MTJG_NUMERICS_STRICT) return launch_spmv_t<1, true>(ctx, A, ts, x, epi, rc, normtype);
-    if (ts.vec >= 32) return launch_spmv_t<32, false>(ctx, A, ts, x, epi, rc, normtype);
-    if (ts.vec >= 4) return launch_spmv_t<4, false>(ctx, A, ts, x, epi, rc, normtype);
-    return launch_spmv_t<1, false>(ctx, A, ts, x, epi, rc, normtype);
+    RedCtx r = rc;
+    r.sys_tile = ts.sys_tile;  // partial slots are this tiling's tiles
+    cudaError_t e = cudaSuccess;
+    if (ctx->numerics == MTJG_NUMERICS_STRICT) {
+        e = launch_spmv_t<1, true, T>(ctx, A, ts, x, epi, r, normtype);
+    } else {
+        // one launch per lanes-per-row class present (a batch may mix
+        // classes; every system's tiles belong to one class)
+        if (ts.vec_mask & 1) e = launch_spmv_t<1, false, T>(ctx, A, ts, x, epi, r, normtype);
+        if (e == cudaSuccess && (ts.vec_mask & 4)) e = launch_spmv_t<4, false, T>(ctx, A, ts, x, epi, r, normtype);
+        if (e == cudaSuccess && (ts.vec_mask & 32))
+            e = launch_spmv_t<32, false, T>(ctx, A, ts, x, epi, r, normtype);
+    }
+    if (e == cudaSuccess && Epi::kReduce) e = launch_finalize(ctx, ts, epi, r, normtype);
+    return e;
 }
 
+// Row kernels run on the row tiles (one block per tile).
 template <class Op>
 cudaError_t launch_rows(mtjg_ctx *ctx, const TileSet &ts, const Op &op, const RedCtx &rc, int normtype)
 {
     if (ts.num_tiles == 0) return cudaSuccess;
-    int cap = ctx->num_sms * 8;
-    int grid = ts.num_tiles < cap ? ts.num_tiles : cap;
-    k_rows<Op><<<grid, kBlock, 0, ctx->stream>>>(tile_args(ts), op, rc, normtype);
+    RedCtx r = rc;
+    r.sys_tile = ts.sys_tile;  // partial slots are this tiling's tiles
+    k_rows<Op><<<ts.num_tiles, kBlock, 0, ctx->stream>>>(tile_args(ts), op, r, normtype);
     ctx->launches++;
-    return cudaGetLastError();
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && Op::kReduce) e = launch_finalize(ctx, ts, op, r, normtype);
+    return e;
 }
 
 inline RedCtx red_ctx(const mtjg_csr *A, const TileSet &ts)
@@ -231,21 +277,25 @@ inline RedCtx red_ctx(const mtjg_csr *A, const TileSet &ts)
     return RedCtx{A->part, A->cnt, ts.sys_tile, A->num_running};
 }
 
-// Builds the row tiles of rows [row_begin, row_end) of a CSR (host row
-// pointers) and appends them to `tile_row` (first rows) / `tile_long`.
+// Appends the product tiles of rows [row_begin, row_end) of a CSR (host row
+// pointers) to `tile_row` (first rows) / `tile_flags`.
 void plan_tiles(const int *rowptr, int row_begin, int row_end, int vec, std::vector<int> &tile_row,
-                std::vector<unsigned char> &tile_long);
+                std::vector<unsigned char> &tile_flags);
+// Appends row-kernel tiles (kBlock rows) of rows [row_begin, row_end).
+void plan_row_tiles(int row_begin, int row_end, std::vector<int> &tile_row, std::vector<unsigned char> &tile_flags);
 int choose_vec(int64_t nnz, int64_t n);
 // Uploads a host tiling (tile_row has num_tiles+1 entries) for `num_sys`
-// systems whose tile ranges are sys_tile (num_sys+1 entries).
-int upload_tiles(TileSet &ts, const std::vector<int> &tile_row, const std::vector<unsigned char> &tile_long,
-                 const std::vector<int> *tile_sys, const std::vector<int> &sys_tile, int vec);
+// systems whose tile ranges are sys_tile (num_sys+1 entries); rowptr gives
+// each tile's first entry (nullptr for row tiles).
+int upload_tiles(TileSet &ts, const std::vector<int> &tile_row, const std::vector<unsigned char> &tile_flags,
+                 const std::vector<int> *tile_sys, const std::vector<int> &sys_tile, int vec, const int *rowptr);
 void free_tiles(TileSet &ts);
 // Device exclusive scan of n ints into out[0..n] (out[n] = total).
 int exclusive_scan(mtjg_ctx *ctx, const int *in, int *out, int n);
 // Device transpose of selected entries of a CSR: mode 0 = all entries,
-// mode 1 = strictly upper entries (column > row), mode 2 = strictly lower.  Rows of the result list
-// their entries in ascending source row order.
+// mode 1 = strictly upper entries (column > row), mode 2 = strictly lower.
+// Rows of the result list their entries in ascending source row order; the
+// row pointer array carries kRowptrPad padding entries.
 int csr_transpose(mtjg_ctx *ctx, int n, int m, const int *rowptr, const int *colind, const double *val,
                   int mode, int **t_rowptr, int **t_colind, double **t_val, int64_t *t_nnz);
 

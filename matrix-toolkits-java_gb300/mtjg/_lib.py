@@ -45,7 +45,7 @@ class Monitor(C.Structure):
 
 class Result(C.Structure):
     _fields_ = [("status", C.c_int), ("iterations", C.c_int), ("residual", C.c_double),
-                ("detail", C.c_int), ("history_len", C.c_int)]
+                ("detail", C.c_int), ("history_len", C.c_int), ("inner_iterations", C.c_int)]
 
 
 _vp = C.c_void_p
@@ -94,6 +94,10 @@ PROTOTYPES = {
     "mtjg_solver_solve_dev": (C.c_int, [_vp, _vp, _vp, _vp, C.POINTER(Result)]),
     "mtjg_solver_history": (C.c_int, [_vp, _dp, _ip, C.c_int, _ip]),
     "mtjg_solver_destroy": (C.c_int, [_vp]),
+    "mtjg_batch_upload": (C.c_int, [_vp, C.c_int, _ip, _ip, _ip, _dp, C.POINTER(_vp)]),
+    "mtjg_solver_set_mixed": (C.c_int, [_vp, C.c_int, C.c_double, C.c_int]),
+    "mtjg_solver_batch_results": (C.c_int, [_vp, C.POINTER(Result), C.c_int]),
+    "mtjg_solver_batch_history": (C.c_int, [_vp, C.c_int, _dp, _ip, C.c_int, _ip]),
 }
 
 _lib = None

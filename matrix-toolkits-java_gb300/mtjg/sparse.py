@@ -246,6 +246,53 @@ class CompRowMatrix:
             pass
 
 
+def block_diagonal(systems):
+    """Concatenates CSR systems [(n, rowptr, colind, data), ...] into one
+    block-diagonal CSR; returns (sys_rows, rowptr, colind, data)."""
+    sizes = [int(s[0]) for s in systems]
+    sys_rows = np.zeros(len(systems) + 1, dtype=np.int64)
+    sys_rows[1:] = np.cumsum(sizes)
+    nnzs = [int(s[1][-1]) for s in systems]
+    nz_off = np.zeros(len(systems) + 1, dtype=np.int64)
+    nz_off[1:] = np.cumsum(nnzs)
+    if sys_rows[-1] >= 2 ** 31 or nz_off[-1] >= 2 ** 31:
+        raise IllegalArgumentException("batch exceeds 32-bit row or entry indices")
+    rowptr = np.empty(int(sys_rows[-1]) + 1, dtype=np.int32)
+    colind = np.empty(int(nz_off[-1]), dtype=np.int32)
+    data = np.empty(int(nz_off[-1]), dtype=np.float64)
+    for k, (n, rp, ci, v) in enumerate(systems):
+        r0, z0 = int(sys_rows[k]), int(nz_off[k])
+        rowptr[r0:r0 + n] = np.asarray(rp[:n], dtype=np.int64) + z0
+        colind[z0:z0 + nnzs[k]] = np.asarray(ci[:nnzs[k]], dtype=np.int64) + r0
+        data[z0:z0 + nnzs[k]] = v[:nnzs[k]]
+    rowptr[-1] = int(nz_off[-1])
+    return sys_rows.astype(np.int32), rowptr, colind, data
+
+
+class BatchCompRowMatrix(CompRowMatrix):
+    """A batch of independent square systems held as one block-diagonal CSR
+    on the device (mtjg_batch_upload).  A CG or BiCGstab solver of the total
+    size solves all systems in the same launches; ``solveBatch`` returns each
+    system's outcome.  No counterpart in the reference, which solves one
+    system per call."""
+
+    def __init__(self, systems, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        self._lib = self.ctx._lib
+        self.sys_rows, self.rowptr, self.colind, self.data = block_diagonal(systems)
+        self.n = self.m = int(self.sys_rows[-1])
+        h = C.c_void_p()
+        _raise(self._lib.mtjg_batch_upload(self.ctx.h, len(systems), L.iptr(self.sys_rows), L.iptr(self.rowptr),
+                                           L.iptr(self.colind), L.dptr(self.data), C.byref(h)), "batch_upload")
+        self.h = h
+
+    def numSystems(self):
+        return len(self.sys_rows) - 1
+
+    def systemRows(self, s):
+        return int(self.sys_rows[s]), int(self.sys_rows[s + 1])
+
+
 # -------------------------------------------------------- preconditioners
 class Preconditioner:
     """S/Preconditioner.java: setMatrix(A), apply(b, x), transApply(b, x)."""
@@ -437,6 +484,16 @@ class AbstractIterativeSolver:
     def getIterationMonitor(self):
         return self.iter
 
+    def setMixedPrecision(self, enable=True, inner_rtol=1e-4, inner_max_iter=1000):
+        """CG only: FP32 inner solves inside FP64 iterative refinement
+        (mtjg_solver_set_mixed).  iterations() then counts refinement steps."""
+        _raise(self._lib.mtjg_solver_set_mixed(self.h, 1 if enable else 0, float(inner_rtol), int(inner_max_iter)),
+               "set_mixed")
+
+    def innerIterations(self):
+        r = getattr(self, "last_result", None)
+        return r.inner_iterations if r is not None else 0
+
     def _sync_monitor(self):
         s = self.iter._struct()
         key = (s.max_iter, s.rtol, s.atol, s.dtol, s.norm, s.history_cap)
@@ -468,6 +525,31 @@ class AbstractIterativeSolver:
             raise IterativeSolverNotConvergedException(reason, res.residual, res.iterations, msg)
         _raise(code, "solve")
         return x
+
+    def solveBatch(self, A: BatchCompRowMatrix, b, x):
+        """Solves every system of a batch; x is overwritten in place.  Returns
+        one (status, iterations, residual) per system and raises only for
+        errors that are not a system's own convergence failure."""
+        b = L.f64(b)
+        if b.shape != (A.numRows(),) or x.shape != b.shape or x.dtype != np.float64 or not x.flags.c_contiguous:
+            raise IllegalArgumentException("b and x must be float64 vectors of the batch's total size")
+        self._sync_monitor()
+        res = L.Result()
+        code = self._lib.mtjg_solver_solve(self.h, A.h, L.dptr(b), L.dptr(x), C.byref(res))
+        if code not in (L.OK, L.NOT_CONVERGED_ITERATIONS, L.NOT_CONVERGED_DIVERGENCE, L.NOT_CONVERGED_BREAKDOWN):
+            _raise(code, "solveBatch")
+        ns = A.numSystems()
+        out = (L.Result * ns)()
+        _raise(self._lib.mtjg_solver_batch_results(self.h, out, ns), "batch_results")
+        return [(r.status, r.iterations, r.residual) for r in out]
+
+    def batchHistory(self, s):
+        cap = self.iter.history_cap
+        r = np.empty(max(cap, 1))
+        it = np.empty(max(cap, 1), dtype=np.int32)
+        ln = C.c_int(0)
+        _raise(self._lib.mtjg_solver_batch_history(self.h, s, L.dptr(r), L.iptr(it), cap, C.byref(ln)), "history")
+        return r[: ln.value].copy(), it[: ln.value].copy()
 
     def _replay(self):
         cap = self.iter.history_cap

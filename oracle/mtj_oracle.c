@@ -89,9 +89,37 @@ void or_trans_mult_add(int n, int m, const int *rowptr, const int *colind,
 
 /* ---------------------------------------------------------- DenseVector */
 
+/* Summation order of dot products and two-norms: 0 = MTJ's sequential loop
+ * (the restatement); B > 0 = blocks of B entries summed sequentially, then
+ * the block sums combined pairwise.  B > 0 exists only to measure how far a
+ * solver's residual history moves when nothing but the order of these sums
+ * changes. */
+static int g_sum_order = 0;
+
+void or_set_sum_order(int mode) { g_sum_order = mode; }
+
+static double blocked_sum_sq(int n, const double *x, const double *y)
+{
+    const int B = g_sum_order;
+    int nb = (n + B - 1) / B;
+    double *part = (double *)malloc(sizeof(double) * (size_t)(nb > 0 ? nb : 1));
+    for (int b = 0; b < nb; ++b) {
+        double s = 0.;
+        int e = (b + 1) * B < n ? (b + 1) * B : n;
+        for (int i = b * B; i < e; ++i) s += x[i] * y[i];
+        part[b] = s;
+    }
+    for (int w = 1; w < nb; w *= 2)
+        for (int b = 0; b + w < nb; b += 2 * w) part[b] += part[b + w];
+    double r = nb ? part[0] : 0.;
+    free(part);
+    return r;
+}
+
 /* DenseVector.dot, M/DenseVector.java:267-279 */
 double or_dot(int n, const double *x, const double *y)
 {
+    if (g_sum_order > 0) return blocked_sum_sq(n, x, y);
     double dot = 0.;
     for (int i = 0; i < n; ++i) dot += x[i] * y[i];
     return dot;
@@ -106,6 +134,7 @@ double or_norm(int n, const double *x, int type)
         for (int i = 0; i < n; ++i) sum += fabs(x[i]);
         return sum;
     } else if (type == OR_NORM_TWO) {
+        if (g_sum_order > 0) return sqrt(blocked_sum_sq(n, x, x));
         double norm = 0;
         for (int i = 0; i < n; ++i) norm += x[i] * x[i];
         return sqrt(norm);

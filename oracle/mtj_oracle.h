@@ -71,6 +71,10 @@ void or_trans_mult_add(int n, int m, const int *rowptr, const int *colind,
 /* DenseVector (M/DenseVector.java) */
 double or_dot(int n, const double *x, const double *y);
 double or_norm(int n, const double *x, int type);
+/* 0 (default): MTJ's sequential sums.  B > 0: sums of B-entry blocks combined
+ * pairwise, used only to measure a solver's sensitivity to the order of its
+ * reductions. */
+void or_set_sum_order(int mode);
 
 /* Preconditioners (S/DiagonalPreconditioner.java, S/ILU.java, S/ICC.java) */
 typedef struct or_pc or_pc;

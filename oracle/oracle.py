@@ -79,8 +79,25 @@ def lib():
         l.or_pc_values.argtypes = [C.c_void_p, _dp, C.c_int]
         l.or_solve.argtypes = [C.c_int, C.c_int, C.c_int, _ip, _ip, _dp, C.c_void_p, _dp, _dp,
                                C.POINTER(Monitor), C.POINTER(Result), _dp, _ip, C.c_int]
+        l.or_set_sum_order.argtypes = [C.c_int]
         _lib = l
     return _lib
+
+
+class sum_order:
+    """Context manager: run the oracle with dot products and norms summed in
+    blocks of `block` entries combined pairwise, instead of MTJ's sequential
+    sums, to measure how much a solver's history depends on the order of its
+    reductions alone."""
+
+    def __init__(self, block=256):
+        self.mode = int(block)
+
+    def __enter__(self):
+        lib().or_set_sum_order(self.mode)
+
+    def __exit__(self, *a):
+        lib().or_set_sum_order(0)
 
 
 def _d(a):

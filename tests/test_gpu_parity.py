@@ -313,8 +313,31 @@ def test_solver_matches_oracle(ctx, numerics, case):
     it = solver.getIterationMonitor().iterations()
     assert abs(it - res.iterations) <= 2, (it, res.iterations)
     rel = _compare_histories(solver, hr, hi)
-    assert rel <= 1e-10, rel
+    bar = 1e-10
+    if sname == "bicgstab":
+        # BiCGstab's history moves by more than 1e-10 of r_0 under a mere
+        # change of the order of its dot products (measured on the oracle
+        # itself); the GPU must stay inside four times that envelope
+        bar = max(bar, 4.0 * _order_envelope(sname, pname, n, rp, ci, v, b))
+    assert rel <= bar, (rel, bar)
     assert np.max(np.abs(x - xo)) <= 1e-8 * max(1.0, np.max(np.abs(xo)))
+
+
+def _order_envelope(sname, pname, n, rp, ci, v, b):
+    Ao = O.Csr(n, n, rp, ci, v)
+    pco = None
+    if PCS[pname][1] is not None:
+        pco = O.Precond(PCS[pname][1], n)
+        pco.set_matrix(Ao)
+    kind = SOLVERS[sname][1]
+    _, _, h_seq, _ = O.solve(kind, Ao, b, np.zeros(n), pco, max_iter=2000, rtol=1e-10)
+    env = 0.0
+    for block in (16, 64, 256, 1024):
+        with O.sum_order(block):
+            _, _, h_blk, _ = O.solve(kind, Ao, b, np.zeros(n), pco, max_iter=2000, rtol=1e-10)
+        k = min(len(h_seq), len(h_blk))
+        env = max(env, float(np.max(np.abs(h_seq[:k] - h_blk[:k])) / h_seq[0]))
+    return env
 
 
 @pytest.mark.parametrize("seed", range(6))
