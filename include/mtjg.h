@@ -127,7 +127,9 @@ MTJG_API int64_t mtjg_ctx_launch_count(mtjg_ctx *ctx);
  * elapsed milliseconds between two recorded slots (synchronizes on b). */
 MTJG_API int mtjg_ctx_event_record(mtjg_ctx *ctx, int slot);
 MTJG_API int mtjg_ctx_event_elapsed(mtjg_ctx *ctx, int a, int b, float *ms);
-/* Device scratch: n doubles, for callers that keep vectors on the GPU. */
+/* Device memory of `bytes` bytes on ctx's device (cudaMalloc), for callers
+ * that keep vectors on the GPU; copies below are ordered on ctx's stream and
+ * return when done. */
 MTJG_API int mtjg_dev_alloc(mtjg_ctx *ctx, int64_t bytes, void **dptr);
 MTJG_API int mtjg_dev_free(mtjg_ctx *ctx, void *dptr);
 MTJG_API int mtjg_memcpy_h2d(mtjg_ctx *ctx, void *dst, const void *src, int64_t bytes);
@@ -220,6 +222,59 @@ MTJG_API int mtjg_solver_history(mtjg_solver *S, double *resid, int *iters, int 
 MTJG_API int mtjg_solver_batch_results(mtjg_solver *S, mtjg_result *out, int count);
 MTJG_API int mtjg_solver_batch_history(mtjg_solver *S, int sys, double *resid, int *iters, int cap, int *len);
 MTJG_API int mtjg_solver_destroy(mtjg_solver *S);
+
+/* ---- Serving ------------------------------------------------------------
+ * A continuous-batching solve server.  No counterpart in the reference,
+ * which solves one system per IterativeSolver.solve call.  Matrices are
+ * registered once and stay resident (CSR, FP32 values, Jacobi diagonal).
+ * Requests (matrix, b, x0) queue on the host; a scheduler thread admits each
+ * into a free slot as soon as a slot and a segment of the pooled vector
+ * workspace are free (admission by device-memory footprint: 40 bytes per row),
+ * runs a chunk of mixed-precision CG + Jacobi iterations over every admitted
+ * system at once, and retires finished systems between chunks, so requests
+ * that arrive while others are on the GPU join the running batch.  A
+ * system's result does not depend on the other systems in flight.  The
+ * server runs on a context and stream of its own, on ctx's device; ctx stays
+ * free for other work.  mtjg_server_destroy abandons unfinished requests.   */
+typedef struct mtjg_server mtjg_server;
+
+typedef struct mtjg_server_config {
+    int max_systems;       /* concurrent systems on the device */
+    int64_t pool_rows;     /* rows of pooled vector workspace (< 2^31) */
+    int max_iter;          /* refinement steps (DefaultIterationMonitor maxIter) */
+    double rtol, atol, dtol;
+    double inner_rtol;     /* FP32 inner CG: residual decrease per refinement step */
+    int inner_max_iter;
+} mtjg_server_config;
+
+typedef struct mtjg_server_result {
+    int64_t ticket;
+    int matrix;
+    mtjg_result result;
+    double latency_s;      /* submission to result on the host */
+    double queue_s;        /* submission to admission */
+} mtjg_server_result;
+
+MTJG_API void mtjg_server_config_defaults(mtjg_server_config *cfg);
+MTJG_API int mtjg_server_create(mtjg_ctx *ctx, const mtjg_server_config *cfg, mtjg_server **out);
+/* Registers a resident SPD matrix (0-based CSR, sorted columns, with a
+ * nonzero diagonal); *matrix_id identifies it in submissions. */
+MTJG_API int mtjg_server_add_matrix(mtjg_server *S, int n, const int *rowptr, const int *colind,
+                                    const double *val, int *matrix_id);
+/* Queues a solve of A x = b (x0 may be NULL for zeros).  b and x0 are copied;
+ * x_out receives the solution and must stay valid until the request is
+ * reported by mtjg_server_poll. */
+MTJG_API int mtjg_server_submit(mtjg_server *S, int matrix_id, const double *b, const double *x0,
+                                double *x_out, int64_t *ticket);
+/* Finished requests since the last poll (non-blocking). */
+MTJG_API int mtjg_server_poll(mtjg_server *S, mtjg_server_result *out, int cap, int *count);
+/* Waits until every submitted request has finished (or the timeout). */
+MTJG_API int mtjg_server_drain(mtjg_server *S, double timeout_s);
+/* Chunks run, requests admitted, largest number of systems in flight, and
+ * the server's clock (seconds since creation). */
+MTJG_API int mtjg_server_stats(mtjg_server *S, int64_t *chunks, int64_t *admitted, int64_t *max_active,
+                               double *clock_s);
+MTJG_API int mtjg_server_destroy(mtjg_server *S);
 
 #ifdef __cplusplus
 }

@@ -126,7 +126,7 @@ extern "C" int mtjg_ctx_synchronize(mtjg_ctx *c)
     return MTJG_OK;
 }
 
-extern "C" int64_t mtjg_ctx_launch_count(mtjg_ctx *c) { return c ? c->launches : 0; }
+extern "C" int64_t mtjg_ctx_launch_count(mtjg_ctx *c) { return c ? c->launches.load() : 0; }
 
 extern "C" int mtjg_ctx_event_record(mtjg_ctx *c, int slot)
 {

@@ -100,79 +100,144 @@ __device__ __forceinline__ double norm_finish(const double *v, int type)
     return v[0];
 }
 
-__device__ __forceinline__ void acc_merge(Acc &a, const Acc &b, int type)
+// Slot masks: bit i set = Acc slot i carries a value.  Slots 0/1 hold a norm
+// (slot 1 only for TWO_ROBUST); slots 2/3 plain sums.  Reductions touch only
+// the slots a phase uses: every FP64 add or compare spent on an idle slot is
+// an issue slot of GB300's narrow FP64 pipe.
+constexpr int kSlotNorm = 1, kSlotD2 = 4, kSlotD3 = 8;
+
+// Op::kSlots when the op declares it, else every slot.
+template <class Op, class = void>
+struct OpSlots {
+    static constexpr int value = kSlotNorm | kSlotD2 | kSlotD3;
+};
+template <class Op>
+struct OpSlots<Op, decltype((void)Op::kSlots)> {
+    static constexpr int value = Op::kSlots;
+};
+
+template <int SLOTS>
+__device__ __forceinline__ void acc_merge_m(Acc &a, const Acc &b, int type)
 {
-    norm_merge(a.v[0], a.v[1], b.v[0], b.v[1], type);
-#pragma unroll
-    for (int i = 2; i < kParts; ++i) a.v[i] += b.v[i];
+    if constexpr ((SLOTS & kSlotNorm) != 0) {
+        if (type == MTJG_NORM_ONE || type == MTJG_NORM_TWO) a.v[0] += b.v[0];
+        else norm_merge(a.v[0], a.v[1], b.v[0], b.v[1], type);
+    }
+    if constexpr ((SLOTS & kSlotD2) != 0) a.v[2] += b.v[2];
+    if constexpr ((SLOTS & kSlotD3) != 0) a.v[3] += b.v[3];
 }
 
+__device__ __forceinline__ void acc_merge(Acc &a, const Acc &b, int type)
+{
+    acc_merge_m<kSlotNorm | kSlotD2 | kSlotD3>(a, b, type);
+}
+
+template <int SLOTS>
 __device__ __forceinline__ void acc_shfl_down(Acc &a, int off, int type)
 {
     Acc o;
-#pragma unroll
-    for (int i = 0; i < kParts; ++i) o.v[i] = __shfl_down_sync(0xffffffffu, a.v[i], off);
-    acc_merge(a, o, type);
+    if constexpr ((SLOTS & kSlotNorm) != 0) {
+        o.v[0] = __shfl_down_sync(0xffffffffu, a.v[0], off);
+        o.v[1] = type == MTJG_NORM_TWO_ROBUST ? __shfl_down_sync(0xffffffffu, a.v[1], off) : 0.0;
+    }
+    if constexpr ((SLOTS & kSlotD2) != 0) o.v[2] = __shfl_down_sync(0xffffffffu, a.v[2], off);
+    if constexpr ((SLOTS & kSlotD3) != 0) o.v[3] = __shfl_down_sync(0xffffffffu, a.v[3], off);
+    acc_merge_m<SLOTS>(a, o, type);
 }
 
-// Block-wide fixed-order reduction; result valid in thread 0.
-__device__ __forceinline__ void block_reduce(Acc &a, int type, Acc *sm /* [kBlock/32] */)
+// Block-wide fixed-order reduction of the slots in SLOTS; result valid in
+// thread 0.  Every thread parks its slots in shared memory; warp 0 alone
+// then sums them (lane l takes entries l, l+32, ..., sequentially) and
+// finishes with a 5-level butterfly.  That costs about a quarter of the
+// FP64 instructions of a shuffle tree run in every warp.
+template <int SLOTS>
+__device__ __forceinline__ void block_reduce(Acc &a, int type, double *sm /* [kParts * kBlock] */)
 {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) acc_shfl_down(a, off, type);
-    if (lane == 0) sm[wid] = a;
+    constexpr bool kN = (SLOTS & kSlotNorm) != 0, k2 = (SLOTS & kSlotD2) != 0, k3 = (SLOTS & kSlotD3) != 0;
+    const int tid = threadIdx.x, lane = tid & 31, nt = blockDim.x;
+    const bool robust = type == MTJG_NORM_TWO_ROBUST;
+    if constexpr (kN) {
+        sm[tid] = a.v[0];
+        if (robust) sm[kBlock + tid] = a.v[1];
+    }
+    if constexpr (k2) sm[2 * kBlock + tid] = a.v[2];
+    if constexpr (k3) sm[3 * kBlock + tid] = a.v[3];
     __syncthreads();
-    if (wid == 0) {
-        if (lane < (int)(blockDim.x >> 5)) a = sm[lane];
-        else acc_zero(a);
+    if (tid < 32 && SLOTS != 0) {
+        Acc o;
+        if constexpr (kN) {
+            a.v[0] = sm[lane];
+            a.v[1] = robust ? sm[kBlock + lane] : 0.0;
+        }
+        if constexpr (k2) a.v[2] = sm[2 * kBlock + lane];
+        if constexpr (k3) a.v[3] = sm[3 * kBlock + lane];
+        for (int i = lane + 32; i < nt; i += 32) {
+            if constexpr (kN) {
+                o.v[0] = sm[i];
+                o.v[1] = robust ? sm[kBlock + i] : 0.0;
+            }
+            if constexpr (k2) o.v[2] = sm[2 * kBlock + i];
+            if constexpr (k3) o.v[3] = sm[3 * kBlock + i];
+            acc_merge_m<SLOTS>(a, o, type);
+        }
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) acc_shfl_down(a, off, type);
+        for (int off = 16; off > 0; off >>= 1) acc_shfl_down<SLOTS>(a, off, type);
     }
     __syncthreads();
 }
 
-// Stores one tile's partial: block-reduce the per-thread partials (fixed
-// order) and write them to the tile's slot.  No fence: see tiles_arrive.
-__device__ __forceinline__ void tile_partial(Acc &a, int tile, const RedCtx &rc, int type, Acc *sm)
+// Stores one group's partial: block-reduce the per-thread partials (fixed
+// order) and write the used slots to the group's entry.
+template <int SLOTS>
+__device__ __forceinline__ void group_partial(Acc &a, int group, const RedCtx &rc, int type, double *sm)
 {
-    block_reduce(a, type, sm);
+    block_reduce<SLOTS>(a, type, sm);
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int i = 0; i < kParts; ++i) rc.part[(size_t)tile * kParts + i] = a.v[i];
+        for (int i = 0; i < kParts; ++i)
+            if (SLOTS & (i < 2 ? kSlotNorm : (1 << i))) rc.part[(size_t)group * kParts + i] = a.v[i];
     }
 }
 
 // The reduction of a phase finishes in k_finalize (a launch of its own after
-// the phase's kernel): block s sums system s's tile partials in tile order
-// (thread t takes tiles t, t+B, t+2B, ... with eight loads in flight, then
+// the phase's kernel): block s sums system s's group partials in group order
+// (thread t takes groups t, t+B, t+2B, ... with four loads in flight, then
 // the fixed block tree) and thread 0 runs op.scalar(s, sums).  No atomics
 // and no fences: the launch boundary orders the partial stores before it.
+//
+// Kernel templates and their launchers live in an unnamed namespace: without
+// relocatable device code every translation unit carries its own device
+// image, so each one instantiates (and sets attributes on) its own kernels.
+namespace {
 template <class Op>
 __global__ void __launch_bounds__(kBlock) k_finalize(Op op, RedCtx rc, int type)
 {
-    __shared__ Acc sm[kBlock / 32];
+    constexpr int SLOTS = OpSlots<Op>::value;
+    __shared__ double sm[kParts * kBlock];
     const int sys = blockIdx.x;
     if (!op.active(sys)) return;
-    const int t0 = rc.sys_tile[sys], t1 = rc.sys_tile[sys + 1];
+    const int g0 = rc.sys_group[sys], g1 = rc.sys_group[sys + 1];
     const int stride = blockDim.x;
     Acc s;
     acc_zero(s);
-    for (int base = t0 + (int)threadIdx.x; base < t1; base += 8 * stride) {
-        Acc o[8];
+    for (int base = g0 + (int)threadIdx.x; base < g1; base += 4 * stride) {
+        Acc o[4];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            const int t = base + u * stride;
+        for (int u = 0; u < 4; ++u) {
+            const int g = base + u * stride;
 #pragma unroll
-            for (int i = 0; i < kParts; ++i) o[u].v[i] = t < t1 ? rc.part[(size_t)t * kParts + i] : 0.0;
+            for (int i = 0; i < kParts; ++i)
+                o[u].v[i] = (g < g1 && (SLOTS & (i < 2 ? kSlotNorm : (1 << i)))) ? rc.part[(size_t)g * kParts + i]
+                                                                                  : 0.0;
         }
 #pragma unroll
-        for (int u = 0; u < 8; ++u)
-            if (base + u * stride < t1) acc_merge(s, o[u], type);
+        for (int u = 0; u < 4; ++u)
+            if (base + u * stride < g1) acc_merge_m<SLOTS>(s, o[u], type);
     }
-    block_reduce(s, type, sm);
+    block_reduce<SLOTS>(s, type, sm);
     if (threadIdx.x == 0) op.scalar(sys, s);
 }
+}  // namespace
 
 // ------------------------------------------------------------ monitor
 // AbstractIterationMonitor.converged(double) + DefaultIterationMonitor.convergedI

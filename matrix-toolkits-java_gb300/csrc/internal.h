@@ -40,8 +40,16 @@ void ctx_release(mtjg_ctx *ctx);
 // batch.
 constexpr int kBlock = 256;
 constexpr int kTileRows = 256;
-constexpr int kTileNnz = 2048;
-constexpr int kParts = 4;             // partial-sum slots per tile
+constexpr int kTileNnz = 1792;        // 256 rows of a 7-point stencil
+constexpr int kParts = 4;             // partial-sum slots per group
+// A reduction group is what one block sums before a block-wide reduction:
+// up to kGroupTiles consecutive product tiles of one system, or one row tile
+// of kRowsPerThread * kBlock rows.  Few block-wide reductions matter on
+// GB300, whose FP64 pipe is narrow: a tree over 256 threads costs more FP64
+// issue slots than the vector work of 256 rows.
+constexpr int kGroupTiles = 8;        // at most; see group_size_for
+constexpr int kRowsPerThread = 2;
+constexpr int kRowTile = kBlock * kRowsPerThread;
 
 // device status of a system (SysState::status)
 enum : int {
@@ -82,23 +90,28 @@ struct MonCfgDev {
     double rtol, atol, dtol;
 };
 
-// Reduction context: per-tile partial sums, per-system arrival counters and
-// tile ranges (tiles of system s are [sys_tile[s], sys_tile[s+1])).
+// Reduction context: per-group partial sums and the group ranges of the
+// systems (groups of system s are [sys_group[s], sys_group[s+1])).
 struct RedCtx {
-    double *part;          // [num_tiles * kParts]
-    unsigned *cnt;         // [num_sys]
-    const int *sys_tile;   // [num_sys + 1]
+    double *part;          // [num_groups * kParts]
+    unsigned *cnt;         // [num_sys] (unused on the hot path)
+    const int *sys_group;  // [num_sys + 1]
     int *num_running;      // number of systems with status RUNNING
 };
 
 struct TileSet {
     int num_tiles = 0;
+    int num_groups = 0;
     int num_sys = 1;
     int vec = 1;
     int *tile_row = nullptr;   // device [num_tiles + 1]
     int *tile_nz = nullptr;    // device [num_tiles + 1]: rowptr at each tile's first row
+    int *tile_row_end = nullptr;  // device [num_tiles], served batches only (else tile_row + 1)
+    int *tile_nz_end = nullptr;   // device [num_tiles], served batches only (else tile_nz + 1)
     int *tile_sys = nullptr;   // device [num_tiles] (nullptr: all system 0)
-    int *sys_tile = nullptr;   // device [num_sys + 1]
+    int *group_tile = nullptr; // device [num_groups + 1]: first tile of each reduction group
+    int *sys_group = nullptr;  // device [num_sys + 1]
+    const struct SysDesc *sd = nullptr;  // device per-system matrices (served batches), else nullptr
     // device [num_tiles]: (lanes per row << 1) | 1 if the tile is a single long row
     unsigned char *tile_flags = nullptr;
     int vec_mask = 0;          // OR of the lanes-per-row classes of the tiles
@@ -124,7 +137,7 @@ struct mtjg_ctx {
     cudaEvent_t events[16] = {};
     int numerics = MTJG_NUMERICS_FAST;
     int num_sms = 0;
-    int64_t launches = 0;
+    std::atomic<int64_t> launches{0};  // kernels launched (a serving thread counts here too)
     int *d_flag = nullptr;          // device error flag (bounded waits)
     int *h_pinned = nullptr;        // pinned host words for status polling
 };

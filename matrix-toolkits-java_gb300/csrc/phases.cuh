@@ -1,0 +1,193 @@
+// phases.cuh -- solver phases shared by the solver (solver.cu) and the
+// serving engine (server.cu): the monitor plumbing and the mixed-precision
+// refinement phases.
+#pragma once
+
+#include "spmv.cuh"
+
+namespace mtjg {
+
+constexpr int kPcIdentity = 0, kPcJacobi = 1, kPcExternal = 2;
+
+// Mixed precision: inner iterations per outer step slot of a loop body.
+constexpr int kInnerPerBody = 8;
+
+struct MonPtrs {
+    SysState *st;
+    MonCfgDev mon;
+    double *hr;
+    int *hi;
+    int *num_running;
+    __device__ __forceinline__ void finish(SysState &t, int code) const
+    {
+        t.status = code;
+        t.gate = code == ST_RUNNING ? ST_RUNNING : 1;
+        if (code != ST_RUNNING) atomicSub(num_running, 1);
+    }
+    __device__ __forceinline__ int check(SysState &t, int sys, double r) const
+    {
+        return monitor_check(t, mon, r, hr + (size_t)sys * mon.hist_cap, hi + (size_t)sys * mon.hist_cap);
+    }
+};
+
+// ===================================================== mixed precision
+// Iterative refinement around an FP32 CG (the loop of S/IR.java:57-70 with
+// the inner solve in the role of the preconditioner).  Per system, `phase`
+// says whether the FP64 outer step (x += d, r = b - A x, monitor test) is due
+// or inner FP32 iterations run; every kernel is gated on it, so systems of a
+// batch move through their own refinement steps independently.
+struct MixCfg {
+    double in_rtol;
+    int in_max;
+};
+
+// x += d (the FP32 correction, widened exactly); iter.next() of the outer loop
+struct MxX {
+    double *x;
+    const float *d;
+    SysState *st;
+    static constexpr bool kReduce = true;
+    static constexpr bool kNeedsXr = false;
+    static constexpr int kSlots = 0;
+    __device__ bool active(int sys) const
+    {
+        const SysState &t = st[sys];
+        return t.status == ST_RUNNING && t.phase == 0 && t.pending;
+    }
+    __device__ void row(int i, int, Acc &) const { x[i] = x[i] + (double)d[i]; }
+    __device__ void scalar(int sys, const Acc &)
+    {
+        SysState &t = st[sys];
+        t.pending = 0;
+        t.iter++;
+    }
+};
+
+// r = b - A x in FP64, the monitor's test on it, then the inner system's
+// right-hand side rin = (float) r, d = 0 and z = M rin in FP32
+struct MxOuter {
+    const double *b;
+    float *rin, *z, *d;
+    const float *invdiag;
+    int pc;
+    MonPtrs m;
+    static constexpr bool kReduce = true;
+    static constexpr bool kNeedsXr = false;
+    __device__ bool active(int sys) const
+    {
+        const SysState &t = m.st[sys];
+        return t.status == ST_RUNNING && t.phase == 0 && !t.pending;
+    }
+    __device__ double init(int, int) const { return 0.0; }
+    __device__ void row(int i, int, double dd, double, Acc &a) const
+    {
+        const double rr = b[i] - dd;
+        norm_add<false>(a, rr, m.mon.norm);
+        const float rf = (float)rr;
+        rin[i] = rf;
+        d[i] = 0.0f;
+        float zf = rf;
+        if (pc == kPcJacobi) {
+            zf = rf * invdiag[i];
+            z[i] = zf;
+        }
+        a.v[2] += (double)(rf * zf);
+        a.v[3] += (double)(rf * rf);
+    }
+    __device__ void scalar(int sys, const Acc &s)
+    {
+        SysState &t = m.st[sys];
+        const int c = m.check(t, sys, norm_finish(s.v, m.mon.norm));
+        if (c == ST_RUNNING) {
+            t.phase = 1;
+            t.pending = 1;
+            t.in_iter = 0;
+            t.in_rho = s.v[2];
+            t.in_r0 = sqrt(s.v[3]);
+        }
+        m.finish(t, c);
+    }
+};
+
+struct MxP {  // p = z (first) or p = beta p + z, FP32
+    float *p;
+    const float *z;
+    SysState *st;
+    static constexpr bool kReduce = false;
+    static constexpr bool kNeedsXr = false;
+    __device__ bool active(int sys) const { return st[sys].status == ST_RUNNING && st[sys].phase == 1; }
+    __device__ void row(int i, int sys, Acc &) const
+    {
+        const SysState &t = st[sys];
+        p[i] = t.in_iter == 0 ? z[i] : fmaf(p[i], (float)t.in_beta, z[i]);
+    }
+    __device__ void scalar(int, const Acc &) {}
+};
+
+struct MxQ {  // q = A32 p (FP32 row sums); alpha = rho / p.q
+    float *q;
+    SysState *st;
+    static constexpr bool kReduce = true;
+    static constexpr bool kNeedsXr = true;
+    static constexpr int kSlots = kSlotD2;
+    __device__ bool active(int sys) const { return st[sys].status == ST_RUNNING && st[sys].phase == 1; }
+    __device__ float init(int, int) const { return 0.0f; }
+    __device__ void row(int i, int, float dd, float pi, Acc &a) const
+    {
+        q[i] = dd;
+        a.v[2] += (double)(pi * dd);
+    }
+    __device__ void scalar(int sys, const Acc &s)
+    {
+        SysState &t = st[sys];
+        t.in_alpha = t.in_rho / s.v[2];
+    }
+};
+
+struct MxUpd {  // d += alpha p; rin -= alpha q; z = M rin; inner stopping test
+    float *d, *rin, *z;
+    const float *p, *q, *invdiag;
+    int pc;
+    SysState *st;
+    MixCfg cfg;
+    static constexpr bool kReduce = true;
+    static constexpr bool kNeedsXr = false;
+    static constexpr int kSlots = kSlotD2 | kSlotD3;
+    __device__ bool active(int sys) const { return st[sys].status == ST_RUNNING && st[sys].phase == 1; }
+    __device__ void row(int i, int sys, Acc &a) const
+    {
+        const float al = (float)st[sys].in_alpha;
+        d[i] = fmaf(al, p[i], d[i]);
+        const float rf = fmaf(-al, q[i], rin[i]);
+        rin[i] = rf;
+        float zf = rf;
+        if (pc == kPcJacobi) {
+            zf = rf * invdiag[i];
+            z[i] = zf;
+        }
+        a.v[2] += (double)(rf * zf);
+        a.v[3] += (double)(rf * rf);
+    }
+    __device__ void scalar(int sys, const Acc &s)
+    {
+        SysState &t = st[sys];
+        t.in_iter++;
+        t.in_total++;
+        const double rn = sqrt(s.v[3]);
+        if (!(rn > cfg.in_rtol * t.in_r0) || t.in_iter >= cfg.in_max) {
+            t.phase = 0;  // the correction in d goes to x in the next outer step
+        } else {
+            t.in_rho_1 = t.in_rho;
+            t.in_rho = s.v[2];
+            t.in_beta = t.in_rho / t.in_rho_1;
+        }
+    }
+};
+
+static __global__ void k_to_f32(int64_t n, const double *a, float *b)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+
+}  // namespace mtjg

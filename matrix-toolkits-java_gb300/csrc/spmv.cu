@@ -44,18 +44,37 @@ void plan_tiles(const int *rowptr, int row_begin, int row_end, int vec, std::vec
 
 void plan_row_tiles(int row_begin, int row_end, std::vector<int> &tile_row, std::vector<unsigned char> &tile_flags)
 {
-    for (int r = row_begin; r < row_end; r += kBlock) {
+    for (int r = row_begin; r < row_end; r += kRowTile) {
         tile_row.push_back(r);
         tile_flags.push_back((unsigned char)(1 << 1));
     }
 }
 
 int upload_tiles(TileSet &ts, const std::vector<int> &tile_row, const std::vector<unsigned char> &tile_flags,
-                 const std::vector<int> *tile_sys, const std::vector<int> &sys_tile, int vec, const int *rowptr)
+                 const std::vector<int> *tile_sys, const std::vector<int> &sys_tile, int vec, const int *rowptr,
+                 int group_size)
 {
     free_tiles(ts);
     ts.num_tiles = (int)tile_flags.size();
     ts.num_sys = (int)sys_tile.size() - 1;
+    // reduction groups: runs of consecutive tiles inside each system.  A
+    // system of T tiles uses groups of min(group_size, T / 4096) tiles (at
+    // least 1): large systems amortise the block reduction over several
+    // tiles while keeping thousands of groups for the CTAs to share evenly;
+    // the size depends on the system alone, never on the rest of a batch.
+    std::vector<int> group_tile, sys_group = {0};
+    for (int s = 0; s < ts.num_sys; ++s) {
+        const int t0 = sys_tile[s], t1 = sys_tile[s + 1];
+        const int gs = std::max(1, std::min(group_size, (t1 - t0) / 4096));
+        for (int t = t0; t < t1; t += gs) group_tile.push_back(t);
+        sys_group.push_back((int)group_tile.size());
+    }
+    ts.num_groups = (int)group_tile.size();
+    group_tile.push_back(ts.num_tiles);
+    MTJG_CUDA(cudaMalloc(&ts.group_tile, sizeof(int) * group_tile.size()));
+    MTJG_CUDA(cudaMemcpy(ts.group_tile, group_tile.data(), sizeof(int) * group_tile.size(), cudaMemcpyHostToDevice));
+    MTJG_CUDA(cudaMalloc(&ts.sys_group, sizeof(int) * sys_group.size()));
+    MTJG_CUDA(cudaMemcpy(ts.sys_group, sys_group.data(), sizeof(int) * sys_group.size(), cudaMemcpyHostToDevice));
     ts.vec = vec;
     ts.vec_mask = 0;
     for (unsigned char f : tile_flags) ts.vec_mask |= f >> 1;
@@ -71,8 +90,6 @@ int upload_tiles(TileSet &ts, const std::vector<int> &tile_row, const std::vecto
     MTJG_CUDA(cudaMalloc(&ts.tile_flags, std::max<size_t>(1, tile_flags.size())));
     if (!tile_flags.empty())
         MTJG_CUDA(cudaMemcpy(ts.tile_flags, tile_flags.data(), tile_flags.size(), cudaMemcpyHostToDevice));
-    MTJG_CUDA(cudaMalloc(&ts.sys_tile, sizeof(int) * sys_tile.size()));
-    MTJG_CUDA(cudaMemcpy(ts.sys_tile, sys_tile.data(), sizeof(int) * sys_tile.size(), cudaMemcpyHostToDevice));
     if (tile_sys) {
         MTJG_CUDA(cudaMalloc(&ts.tile_sys, sizeof(int) * std::max<size_t>(1, tile_sys->size())));
         if (!tile_sys->empty())
@@ -87,11 +104,13 @@ void free_tiles(TileSet &ts)
     cudaFree(ts.tile_row);
     cudaFree(ts.tile_nz);
     cudaFree(ts.tile_sys);
-    cudaFree(ts.sys_tile);
+    cudaFree(ts.group_tile);
+    cudaFree(ts.sys_group);
     cudaFree(ts.tile_flags);
-    ts.tile_row = ts.tile_nz = ts.tile_sys = ts.sys_tile = nullptr;
+    ts.tile_row = ts.tile_nz = ts.tile_sys = ts.group_tile = ts.sys_group = nullptr;
     ts.tile_flags = nullptr;
     ts.num_tiles = 0;
+    ts.num_groups = 0;
 }
 
 // ------------------------------------------------------------------- scan
@@ -424,9 +443,10 @@ static int csr_upload_impl(mtjg_ctx *ctx, int n, int m, const int *rowptr, const
     }
     tile_row.push_back(n);
     rtile_row.push_back(n);
-    st = upload_tiles(A->tiles, tile_row, tile_flags, sys_rows ? &tile_sys : nullptr, sys_tile, vec, rowptr);
+    st = upload_tiles(A->tiles, tile_row, tile_flags, sys_rows ? &tile_sys : nullptr, sys_tile, vec, rowptr,
+                      kGroupTiles);
     if (st != MTJG_OK) return bail(st);
-    st = upload_tiles(A->rtiles, rtile_row, rtile_flags, sys_rows ? &rtile_sys : nullptr, rsys_tile, 1, nullptr);
+    st = upload_tiles(A->rtiles, rtile_row, rtile_flags, sys_rows ? &rtile_sys : nullptr, rsys_tile, 1, nullptr, 1);
     if (st != MTJG_OK) return bail(st);
     const size_t nt = std::max<size_t>(1, std::max(tile_flags.size(), rtile_flags.size()));
     if (cudaMalloc(&A->part, sizeof(double) * nt * kParts) != cudaSuccess ||
@@ -523,7 +543,7 @@ static int ensure_transpose(mtjg_csr *A)
     plan_tiles(trp.data(), 0, A->m, vec, tile_row, tile_flags);
     tile_row.push_back(A->m);
     std::vector<int> sys_tile = {0, (int)tile_flags.size()};
-    return upload_tiles(A->t_tiles, tile_row, tile_flags, nullptr, sys_tile, vec, trp.data());
+    return upload_tiles(A->t_tiles, tile_row, tile_flags, nullptr, sys_tile, vec, trp.data(), kGroupTiles);
 }
 
 static int check_err_flag(mtjg_ctx *ctx)

@@ -1,21 +1,24 @@
 // spmv.cuh -- tiled CSR product and tiled row kernels.
 //
-// k_spmv: persistent CTAs walk the product tiles of a CSR matrix.  The row
-// pointers, values and column indices of the next tile are brought into
-// shared memory by one thread with three cp.async.bulk copies completing on
-// an mbarrier, while the block computes the current tile (two stages).  Each
-// row is summed from shared memory in ascending entry order (vec == 1: one
-// thread per row, the order of CompRowMatrix.mult, S/CompRowMatrix.java:304-312)
-// or by a group of `vec` lanes with a fixed butterfly (vec > 1).  x is
-// gathered through the read-only path (L1/L2).  The epilogue object gives the
-// starting value of a row sum (init) and decides what a finished row sum
-// becomes (y = Ax, y += alpha*Ax, r = b - Ax, fused dot products, ...).
+// k_spmv: persistent CTAs walk reduction groups of product tiles (up to
+// kGroupTiles consecutive tiles of one system; CTA b takes groups b, b+G,
+// ...).  The row pointers, values and column indices of the next tile are
+// brought into shared memory by one thread with three cp.async.bulk copies
+// completing on an mbarrier, while the block computes the current tile (two
+// stages).  Each row is summed from shared memory in ascending entry order
+// (vec == 1: one thread per row, the order of CompRowMatrix.mult,
+// S/CompRowMatrix.java:304-312) or by a group of `vec` lanes with a fixed
+// butterfly (vec > 1).  x is gathered through the read-only path (L1/L2).
+// The epilogue object gives the starting value of a row sum (init) and
+// decides what a finished row sum becomes (y = Ax, y += alpha*Ax,
+// r = b - Ax, fused dot products, ...).
 //
-// k_rows: one block per row tile (kBlock rows, one row per thread); enough
-// blocks are resident to keep HBM busy without any loop per thread.
+// k_rows: one block per row tile (kRowTile rows, kRowsPerThread rows per
+// thread, strided for coalescing).
 //
-// A phase with a reduction stores one partial per tile; k_finalize (dev.cuh)
-// then reduces each system's partials in tile order and runs the scalar step.
+// A phase with a reduction accumulates per thread over a whole group, then
+// stores one block-reduced partial per group; k_finalize (dev.cuh) reduces
+// each system's partials in group order and runs the scalar step.
 #pragma once
 
 #include "dev.cuh"
@@ -35,12 +38,28 @@ constexpr long long kWaitLimit = 1LL << 22;
 // row pointer arrays handed to k_spmv carry this many padding entries
 constexpr int kRowptrPad = 4;
 
+// One system of a served batch: its own resident CSR (rows numbered from 0)
+// and the offset of its rows in the pooled vectors.
+struct SysDesc {
+    const int *rowptr;
+    const int *colind;
+    const double *val;
+    const float *val32;
+    int voff;
+    int pad;
+};
+
 struct TileArgs {
     int num_tiles;
-    const int *tile_row;
-    const int *tile_nz;
+    int num_groups;
+    const int *tile_row;      // tile t covers rows [tile_row[t], tile_row_end[t])
+    const int *tile_row_end;
+    const int *tile_nz;       // and entries [tile_nz[t], tile_nz_end[t])
+    const int *tile_nz_end;
     const int *tile_sys;
     const unsigned char *tile_flags;
+    const int *group_tile;
+    const SysDesc *sd;  // nullptr: one CSR (the kernel's argument), rows = vector indices
 };
 
 template <class T>
@@ -56,6 +75,9 @@ __device__ __forceinline__ int tile_system(const TileArgs &ta, int t)
     return ta.tile_sys ? ta.tile_sys[t] : 0;
 }
 
+// Kernels and launchers are private to each translation unit (see k_finalize).
+namespace {
+
 template <int VEC, bool S, class T, class Epi>
 __global__ void __launch_bounds__(kBlock, kSpmvCtasPerSm)
     k_spmv(CsrArgsT<T> A, TileArgs ta, const T *__restrict__ x, Epi epi, RedCtx rc, int normtype, int *err)
@@ -63,11 +85,11 @@ __global__ void __launch_bounds__(kBlock, kSpmvCtasPerSm)
     constexpr int kVA = 16 / (int)sizeof(T);  // values per 16 bytes
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t bar[2];
-    __shared__ Acc red_sm[kBlock / 32];
+    __shared__ double red_sm[kParts * kBlock];
     __shared__ T s_long[kBlock / 32];
 
     const int tid = threadIdx.x;
-    const int G = gridDim.x, NT = ta.num_tiles;
+    const int G = gridDim.x, NG = ta.num_groups;
     if (tid == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
@@ -78,11 +100,39 @@ __global__ void __launch_bounds__(kBlock, kSpmvCtasPerSm)
     auto sval = [&](int s) { return reinterpret_cast<T *>(smem + s * kStageBytes); };
     auto scol = [&](int s) { return reinterpret_cast<int *>(smem + s * kStageBytes + kValBytes); };
     auto srow = [&](int s) { return reinterpret_cast<int *>(smem + s * kStageBytes + kValBytes + kColBytes); };
-    // a launch takes the tiles of its lanes-per-row class (STRICT: all tiles)
-    auto active = [&](int t) { return (S || (ta.tile_flags[t] >> 1) == VEC) && epi.active(tile_system(ta, t)); };
+    // a launch takes the groups of its lanes-per-row class (STRICT: all)
+    auto group_active = [&](int g) {
+        const int t0 = ta.group_tile[g];
+        return (S || (ta.tile_flags[t0] >> 1) == VEC) && epi.active(tile_system(ta, t0));
+    };
+    auto next_group = [&](int g) {
+        while (g < NG && !group_active(g)) g += G;
+        return g;
+    };
+    auto staged = [&](int t) { return !(ta.tile_flags[t] & 1); };
+    // the CSR a tile reads and the vector offset of its rows
+    struct MatView {
+        const int *rowptr;
+        const int *colind;
+        const T *val;
+        int voff;
+    };
+    auto view = [&](int t) -> MatView {
+        if (ta.sd) {
+            const SysDesc &d = ta.sd[tile_system(ta, t)];
+            if constexpr (sizeof(T) == 8)
+                return MatView{d.rowptr, d.colind, reinterpret_cast<const T *>(d.val), d.voff};
+            else
+                return MatView{d.rowptr, d.colind, reinterpret_cast<const T *>(d.val32), d.voff};
+        }
+        return MatView{A.rowptr, A.colind, A.val, 0};
+    };
+    // tile t's row pointers, values and columns, rounded out to 16 bytes
+    // (the arrays carry the padding this reads past their ends)
     auto issue = [&](int t, int s) {
-        const int nz0 = ta.tile_nz[t], nz1 = ta.tile_nz[t + 1];
-        const int r0 = ta.tile_row[t], r1 = ta.tile_row[t + 1];
+        const MatView m = view(t);
+        const int nz0 = ta.tile_nz[t], nz1 = ta.tile_nz_end[t];
+        const int r0 = ta.tile_row[t], r1 = ta.tile_row_end[t];
         const int v0 = nz0 & ~(kVA - 1), v1 = (nz1 + kVA - 1) & ~(kVA - 1);
         const int c0 = nz0 & ~3, c1 = (nz1 + 3) & ~3;
         const int p0 = r0 & ~3, p1 = (r1 + 1 + 3) & ~3;
@@ -90,123 +140,150 @@ __global__ void __launch_bounds__(kBlock, kSpmvCtasPerSm)
                        pb = (unsigned)(p1 - p0) * 4u;
         fence_proxy_async();
         mbar_arrive_expect_tx(&bar[s], vb + cb + pb);
-        if (vb) bulk_g2s(sval(s), A.val + v0, vb, &bar[s]);
-        if (cb) bulk_g2s(scol(s), A.colind + c0, cb, &bar[s]);
-        bulk_g2s(srow(s), A.rowptr + p0, pb, &bar[s]);
+        if (vb) bulk_g2s(sval(s), m.val + v0, vb, &bar[s]);
+        if (cb) bulk_g2s(scol(s), m.colind + c0, cb, &bar[s]);
+        bulk_g2s(srow(s), m.rowptr + p0, pb, &bar[s]);
     };
 
     unsigned phase[2] = {0u, 0u};
     int s = 0;
-    int t = blockIdx.x;
-    if (tid == 0 && t < NT && !(ta.tile_flags[t] & 1) && active(t)) issue(t, 0);
-    for (; t < NT; t += G) {
-        const int tn = t + G;
-        if (tid == 0 && tn < NT && !(ta.tile_flags[tn] & 1) && active(tn)) issue(tn, s ^ 1);
-        if (active(t)) {
-            const int sys = tile_system(ta, t);
-            const int r0 = ta.tile_row[t], r1 = ta.tile_row[t + 1];
-            Acc acc;
-            acc_zero(acc);
-            if (!(ta.tile_flags[t] & 1)) {
-                const bool ok = mbar_wait_bounded(&bar[s], phase[s], kWaitLimit);
-                if (__syncthreads_or(!ok)) {
-                    // a copy never completed: report, drain what is in flight, stop
-                    if (tid == 0) atomicExch(err, 1);
-                    mbar_wait_bounded(&bar[s], phase[s], kWaitLimit);
-                    if (tn < NT && !(ta.tile_flags[tn] & 1) && active(tn))
-                        mbar_wait_bounded(&bar[s ^ 1], phase[s ^ 1], kWaitLimit);
-                    return;
-                }
-                phase[s] ^= 1u;
-                const T *sv = sval(s);
-                const int *sc = scol(s);
-                const int *sr = srow(s);
-                const int nzb = ta.tile_nz[t];
-                const int vo = nzb & ~(kVA - 1), co = nzb & ~3, po = r0 & ~3;
-                if constexpr (VEC == 1) {
-                    for (int r = r0 + tid; r < r1; r += kBlock) {
-                        const int b = sr[r - po], e = sr[r + 1 - po];
-                        T sum = epi.init(r, sys);
-                        T xr = T(0);
-                        bool diag = false;
+    // (g, t): the current group and tile; the walk is uniform over the block
+    int g = next_group(blockIdx.x);
+    int t = g < NG ? ta.group_tile[g] : 0;
+    if (tid == 0 && g < NG && staged(t)) issue(t, 0);
+    Acc acc;
+    acc_zero(acc);
+    while (g < NG) {
+        // the tile after t in this block's walk
+        int gn = g, tn = t + 1;
+        if (tn >= ta.group_tile[g + 1]) {
+            gn = next_group(g + G);
+            tn = gn < NG ? ta.group_tile[gn] : 0;
+        }
+        if (tid == 0 && gn < NG && staged(tn)) issue(tn, s ^ 1);
+        const int sys = tile_system(ta, t);
+        const int r0 = ta.tile_row[t], r1 = ta.tile_row_end[t];
+        // rows r are the matrix's own; vectors are indexed at vo + r
+        const MatView mv = view(t);
+        const T *xs = x + mv.voff;
+        const int vgo = mv.voff;
+        if (staged(t)) {
+            const bool ok = mbar_wait_bounded(&bar[s], phase[s], kWaitLimit);
+            if (__syncthreads_or(!ok)) {
+                // a copy never completed: report, drain what is in flight, stop
+                if (tid == 0) atomicExch(err, 1);
+                mbar_wait_bounded(&bar[s], phase[s], kWaitLimit);
+                if (gn < NG && staged(tn)) mbar_wait_bounded(&bar[s ^ 1], phase[s ^ 1], kWaitLimit);
+                return;
+            }
+            phase[s] ^= 1u;
+            const T *sv = sval(s);
+            const int *sc = scol(s);
+            const int *sr = srow(s);
+            const int nzb = ta.tile_nz[t];
+            const int vo = nzb & ~(kVA - 1), co = nzb & ~3, po = r0 & ~3;
+            if constexpr (VEC == 1) {
+                for (int r = r0 + tid; r < r1; r += kBlock) {
+                    const int b = sr[r - po], e = sr[r + 1 - po];
+                    T sum = epi.init(vgo + r, sys);
+                    T xr = T(0);
+                    bool diag = false;
 #pragma unroll 8
-                        for (int k = b; k < e; ++k) {
-                            const int c = sc[k - co];
-                            const T xv = __ldg(x + c);
-                            if (c == r) {
-                                xr = xv;
-                                diag = true;
-                            }
-                            sum = fmac<S>(sv[k - vo], xv, sum);
+                    for (int k = b; k < e; ++k) {
+                        const int c = sc[k - co];
+                        const T xv = __ldg(xs + c);
+                        if (c == r) {
+                            xr = xv;
+                            diag = true;
                         }
-                        if constexpr (Epi::kNeedsXr) {
-                            if (!diag) xr = __ldg(x + r);
-                        }
-                        epi.row(r, sys, sum, xr, acc);
+                        sum = fmac<S>(sv[k - vo], xv, sum);
                     }
-                } else {
-                    const int g = tid / VEC, l = tid % VEC;
-                    for (int base = r0; base < r1; base += kBlock / VEC) {
-                        const int r = base + g;
-                        T sum = T(0);
-                        if (r < r1 && l == 0) sum = epi.init(r, sys);
-                        if (r < r1) {
-                            const int b = sr[r - po], e = sr[r + 1 - po];
-                            for (int k = b + l; k < e; k += VEC)
-                                sum = fmac<S>(sv[k - vo], __ldg(x + sc[k - co]), sum);
-                        }
-#pragma unroll
-                        for (int off = VEC / 2; off > 0; off >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off, VEC);
-                        if (r < r1 && l == 0) epi.row(r, sys, sum, Epi::kNeedsXr ? __ldg(x + r) : T(0), acc);
+                    if constexpr (Epi::kNeedsXr) {
+                        if (!diag) xr = __ldg(xs + r);
                     }
+                    epi.row(vgo + r, sys, sum, xr, acc);
                 }
             } else {
-                // a single row longer than a stage: straight from global memory
-                const int r = r0;
-                const int b = A.rowptr[r], e = A.rowptr[r + 1];
-                T sum = tid == 0 ? epi.init(r, sys) : T(0);
-                if constexpr (S) {
-                    if (tid == 0)
-                        for (int k = b; k < e; ++k) sum = fmac<S>(A.val[k], __ldg(x + A.colind[k]), sum);
-                } else {
-                    for (int k = b + tid; k < e; k += kBlock) sum = fmac<S>(A.val[k], __ldg(x + A.colind[k]), sum);
-#pragma unroll
-                    for (int off = 16; off > 0; off >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, off);
-                    if ((tid & 31) == 0) s_long[tid >> 5] = sum;
-                    __syncthreads();
-                    if (tid == 0) {
-                        sum = s_long[0];
-                        for (int w = 1; w < kBlock / 32; ++w) sum += s_long[w];
+                const int gg = tid / VEC, l = tid % VEC;
+                for (int base = r0; base < r1; base += kBlock / VEC) {
+                    const int r = base + gg;
+                    T sum = T(0);
+                    if (r < r1 && l == 0) sum = epi.init(vgo + r, sys);
+                    if (r < r1) {
+                        const int b = sr[r - po], e = sr[r + 1 - po];
+                        for (int k = b + l; k < e; k += VEC) sum = fmac<S>(sv[k - vo], __ldg(xs + sc[k - co]), sum);
                     }
-                    __syncthreads();
+#pragma unroll
+                    for (int off = VEC / 2; off > 0; off >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off, VEC);
+                    if (r < r1 && l == 0) epi.row(vgo + r, sys, sum, Epi::kNeedsXr ? __ldg(xs + r) : T(0), acc);
                 }
-                if (tid == 0) epi.row(r, sys, sum, Epi::kNeedsXr ? __ldg(x + r) : T(0), acc);
             }
-            if constexpr (Epi::kReduce) tile_partial(acc, t, rc, normtype, red_sm);
+        } else {
+            // a single row longer than a stage: straight from global memory
+            const int r = r0;
+            const int b = mv.rowptr[r], e = mv.rowptr[r + 1];
+            T sum = tid == 0 ? epi.init(vgo + r, sys) : T(0);
+            if constexpr (S) {
+                if (tid == 0)
+                    for (int k = b; k < e; ++k) sum = fmac<S>(mv.val[k], __ldg(xs + mv.colind[k]), sum);
+            } else {
+                for (int k = b + tid; k < e; k += kBlock) sum = fmac<S>(mv.val[k], __ldg(xs + mv.colind[k]), sum);
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, off);
+                if ((tid & 31) == 0) s_long[tid >> 5] = sum;
+                __syncthreads();
+                if (tid == 0) {
+                    sum = s_long[0];
+                    for (int w = 1; w < kBlock / 32; ++w) sum += s_long[w];
+                }
+                __syncthreads();
+            }
+            if (tid == 0) epi.row(vgo + r, sys, sum, Epi::kNeedsXr ? __ldg(xs + r) : T(0), acc);
         }
-        __syncthreads();
+        if (gn != g) {
+            // the group is complete
+            if constexpr (Epi::kReduce) {
+                group_partial<OpSlots<Epi>::value>(acc, g, rc, normtype, red_sm);
+                acc_zero(acc);
+            }
+        }
+        __syncthreads();  // stage s is free for the copy issued next turn
         s ^= 1;
+        g = gn;
+        t = tn;
     }
 }
 
-// Row kernel: block b handles row tile b, one row per thread.
+// Row kernel: block b handles row tile b, kRowsPerThread rows per thread
+// (rows tid, tid + kBlock, ...), one partial per tile.
 template <class Op>
 __global__ void __launch_bounds__(kBlock) k_rows(TileArgs ta, Op op, RedCtx rc, int normtype)
 {
-    __shared__ Acc red_sm[kBlock / 32];
+    __shared__ double red_sm[kParts * kBlock];
     const int t = blockIdx.x;
     const int sys = tile_system(ta, t);
     if (!op.active(sys)) return;
     Acc acc;
     acc_zero(acc);
-    const int r = ta.tile_row[t] + (int)threadIdx.x;
-    if (r < ta.tile_row[t + 1]) op.row(r, sys, acc);
-    if constexpr (Op::kReduce) tile_partial(acc, t, rc, normtype, red_sm);
+    const int r0 = ta.tile_row[t], r1 = ta.tile_row_end[t];
+#pragma unroll 2
+    for (int r = r0 + (int)threadIdx.x; r < r1; r += kBlock) op.row(r, sys, acc);
+    if constexpr (Op::kReduce) group_partial<OpSlots<Op>::value>(acc, t, rc, normtype, red_sm);
 }
 
 inline TileArgs tile_args(const TileSet &ts)
 {
-    return TileArgs{ts.num_tiles, ts.tile_row, ts.tile_nz, ts.tile_sys, ts.tile_flags};
+    // contiguous tilings end each tile where the next one starts
+    return TileArgs{ts.num_tiles,
+                    ts.num_groups,
+                    ts.tile_row,
+                    ts.tile_row_end ? ts.tile_row_end : ts.tile_row + 1,
+                    ts.tile_nz,
+                    ts.tile_nz_end ? ts.tile_nz_end : (ts.tile_nz ? ts.tile_nz + 1 : nullptr),
+                    ts.tile_sys,
+                    ts.tile_flags,
+                    ts.group_tile,
+                    ts.sd};
 }
 
 template <class Op>
@@ -222,13 +299,16 @@ cudaError_t launch_spmv_t(mtjg_ctx *ctx, CsrArgsT<T> A, const TileSet &ts, const
                           const RedCtx &rc, int normtype)
 {
     auto k = k_spmv<VEC, S, T, Epi>;
-    static bool attr_set = false;
-    if (!attr_set) {
+    // the shared-memory opt-in is a per-device attribute of this kernel
+    static std::atomic<unsigned long long> attr_set{0};
+    const unsigned long long bit = 1ull << (ctx->device & 63);
+    if (!(attr_set.load() & bit)) {
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kSpmvSmem);
         if (e != cudaSuccess) return e;
-        attr_set = true;
+        attr_set.fetch_or(bit);
     }
-    int grid = ts.num_tiles < ctx->num_sms * kSpmvCtasPerSm ? ts.num_tiles : ctx->num_sms * kSpmvCtasPerSm;
+    const int cap = ctx->num_sms * kSpmvCtasPerSm;
+    const int grid = ts.num_groups < cap ? ts.num_groups : cap;
     k<<<grid, kBlock, kSpmvSmem, ctx->stream>>>(A, tile_args(ts), x, epi, rc, normtype, ctx->d_flag);
     ctx->launches++;
     return cudaGetLastError();
@@ -242,7 +322,7 @@ cudaError_t launch_spmv(mtjg_ctx *ctx, CsrArgsT<T> A, const TileSet &ts, const T
 {
     if (ts.num_tiles == 0) return cudaSuccess;
     RedCtx r = rc;
-    r.sys_tile = ts.sys_tile;  // partial slots are this tiling's tiles
+    r.sys_group = ts.sys_group;  // partial slots are this tiling's groups
     cudaError_t e = cudaSuccess;
     if (ctx->numerics == MTJG_NUMERICS_STRICT) {
         e = launch_spmv_t<1, true, T>(ctx, A, ts, x, epi, r, normtype);
@@ -258,13 +338,13 @@ cudaError_t launch_spmv(mtjg_ctx *ctx, CsrArgsT<T> A, const TileSet &ts, const T
     return e;
 }
 
-// Row kernels run on the row tiles (one block per tile).
+// Row kernels run on the row tiles (one block per tile, a tile is a group).
 template <class Op>
 cudaError_t launch_rows(mtjg_ctx *ctx, const TileSet &ts, const Op &op, const RedCtx &rc, int normtype)
 {
     if (ts.num_tiles == 0) return cudaSuccess;
     RedCtx r = rc;
-    r.sys_tile = ts.sys_tile;  // partial slots are this tiling's tiles
+    r.sys_group = ts.sys_group;
     k_rows<Op><<<ts.num_tiles, kBlock, 0, ctx->stream>>>(tile_args(ts), op, r, normtype);
     ctx->launches++;
     cudaError_t e = cudaGetLastError();
@@ -272,23 +352,27 @@ cudaError_t launch_rows(mtjg_ctx *ctx, const TileSet &ts, const Op &op, const Re
     return e;
 }
 
+}  // namespace
+
 inline RedCtx red_ctx(const mtjg_csr *A, const TileSet &ts)
 {
-    return RedCtx{A->part, A->cnt, ts.sys_tile, A->num_running};
+    return RedCtx{A->part, A->cnt, ts.sys_group, A->num_running};
 }
 
 // Appends the product tiles of rows [row_begin, row_end) of a CSR (host row
 // pointers) to `tile_row` (first rows) / `tile_flags`.
 void plan_tiles(const int *rowptr, int row_begin, int row_end, int vec, std::vector<int> &tile_row,
                 std::vector<unsigned char> &tile_flags);
-// Appends row-kernel tiles (kBlock rows) of rows [row_begin, row_end).
+// Appends row-kernel tiles (kRowTile rows) of rows [row_begin, row_end).
 void plan_row_tiles(int row_begin, int row_end, std::vector<int> &tile_row, std::vector<unsigned char> &tile_flags);
 int choose_vec(int64_t nnz, int64_t n);
-// Uploads a host tiling (tile_row has num_tiles+1 entries) for `num_sys`
-// systems whose tile ranges are sys_tile (num_sys+1 entries); rowptr gives
-// each tile's first entry (nullptr for row tiles).
+// Uploads a host tiling (tile_row has num_tiles+1 entries, sys_tile has
+// num_sys+1 tile offsets) and groups each system's tiles by group_size
+// consecutive tiles; rowptr gives each tile's first entry (nullptr for row
+// tiles).
 int upload_tiles(TileSet &ts, const std::vector<int> &tile_row, const std::vector<unsigned char> &tile_flags,
-                 const std::vector<int> *tile_sys, const std::vector<int> &sys_tile, int vec, const int *rowptr);
+                 const std::vector<int> *tile_sys, const std::vector<int> &sys_tile, int vec, const int *rowptr,
+                 int group_size);
 void free_tiles(TileSet &ts);
 // Device exclusive scan of n ints into out[0..n] (out[n] = total).
 int exclusive_scan(mtjg_ctx *ctx, const int *in, int *out, int n);

@@ -48,6 +48,17 @@ class Result(C.Structure):
                 ("detail", C.c_int), ("history_len", C.c_int), ("inner_iterations", C.c_int)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("max_systems", C.c_int), ("pool_rows", C.c_int64), ("max_iter", C.c_int),
+                ("rtol", C.c_double), ("atol", C.c_double), ("dtol", C.c_double),
+                ("inner_rtol", C.c_double), ("inner_max_iter", C.c_int)]
+
+
+class ServerResult(C.Structure):
+    _fields_ = [("ticket", C.c_int64), ("matrix", C.c_int), ("result", Result),
+                ("latency_s", C.c_double), ("queue_s", C.c_double)]
+
+
 _vp = C.c_void_p
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -96,6 +107,15 @@ PROTOTYPES = {
     "mtjg_solver_destroy": (C.c_int, [_vp]),
     "mtjg_batch_upload": (C.c_int, [_vp, C.c_int, _ip, _ip, _ip, _dp, C.POINTER(_vp)]),
     "mtjg_solver_set_mixed": (C.c_int, [_vp, C.c_int, C.c_double, C.c_int]),
+    "mtjg_server_config_defaults": (None, [C.POINTER(ServerConfig)]),
+    "mtjg_server_create": (C.c_int, [_vp, C.POINTER(ServerConfig), C.POINTER(_vp)]),
+    "mtjg_server_add_matrix": (C.c_int, [_vp, C.c_int, _ip, _ip, _dp, _ip]),
+    "mtjg_server_submit": (C.c_int, [_vp, C.c_int, _dp, _dp, _dp, C.POINTER(C.c_int64)]),
+    "mtjg_server_poll": (C.c_int, [_vp, C.POINTER(ServerResult), C.c_int, _ip]),
+    "mtjg_server_drain": (C.c_int, [_vp, C.c_double]),
+    "mtjg_server_stats": (C.c_int, [_vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                    C.POINTER(C.c_double)]),
+    "mtjg_server_destroy": (C.c_int, [_vp]),
     "mtjg_solver_batch_results": (C.c_int, [_vp, C.POINTER(Result), C.c_int]),
     "mtjg_solver_batch_history": (C.c_int, [_vp, C.c_int, _dp, _ip, C.c_int, _ip]),
 }

@@ -1,0 +1,105 @@
+"""Continuous-batching solve server (include/mtjg.h, mtjg_server_*).
+
+    srv = Server(max_systems=256, pool_rows=1 << 24)
+    mid = srv.addMatrix(n, rowptr, colind, data)      # resident on the device
+    t = srv.submit(mid, b)                            # returns a ticket
+    for r in srv.poll(): ...                          # finished requests
+    srv.drain(); srv.close()
+
+Each request is solved by mixed-precision CG + Jacobi (FP64 refinement,
+FP32 inner iterations) to `rtol` on the FP64 true residual.  No counterpart
+in the reference.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import sys
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as L
+from .sparse import Context, _raise, default_context
+
+
+@dataclass
+class Finished:
+    ticket: int
+    matrix: int
+    status: int
+    iterations: int
+    inner_iterations: int
+    residual: float
+    latency_s: float
+    queue_s: float
+    x: np.ndarray
+
+
+class Server:
+    def __init__(self, ctx: Context | None = None, max_systems=256, pool_rows=1 << 24, max_iter=100, rtol=1e-10,
+                 atol=1e-50, dtol=1e5, inner_rtol=1e-4, inner_max_iter=2000):
+        self.ctx = ctx or default_context()
+        self._lib = self.ctx._lib
+        cfg = L.ServerConfig()
+        self._lib.mtjg_server_config_defaults(C.byref(cfg))
+        cfg.max_systems, cfg.pool_rows, cfg.max_iter = int(max_systems), int(pool_rows), int(max_iter)
+        cfg.rtol, cfg.atol, cfg.dtol = float(rtol), float(atol), float(dtol)
+        cfg.inner_rtol, cfg.inner_max_iter = float(inner_rtol), int(inner_max_iter)
+        h = C.c_void_p()
+        _raise(self._lib.mtjg_server_create(self.ctx.h, C.byref(cfg), C.byref(h)), "server_create")
+        self.h = h
+        self._out = {}   # ticket -> (x, b) kept alive until the request finishes
+        self.sizes = {}
+
+    def addMatrix(self, n, rowptr, colind, data) -> int:
+        rp, ci, v = L.i32(rowptr), L.i32(colind), L.f64(data)
+        mid = C.c_int()
+        _raise(self._lib.mtjg_server_add_matrix(self.h, int(n), L.iptr(rp), L.iptr(ci), L.dptr(v), C.byref(mid)),
+               "add_matrix")
+        self.sizes[mid.value] = int(n)
+        return mid.value
+
+    def submit(self, mid: int, b, x0=None) -> int:
+        n = self.sizes[mid]
+        b = L.f64(b)
+        if b.shape != (n,):
+            raise ValueError("b has the wrong size")
+        x = np.zeros(n)
+        x0p = L.dptr(L.f64(x0)) if x0 is not None else None
+        t = C.c_int64()
+        _raise(self._lib.mtjg_server_submit(self.h, mid, L.dptr(b), x0p, L.dptr(x), C.byref(t)), "submit")
+        self._out[t.value] = (x, b)
+        return t.value
+
+    def poll(self, cap=1024):
+        out = (L.ServerResult * cap)()
+        k = C.c_int()
+        _raise(self._lib.mtjg_server_poll(self.h, out, cap, C.byref(k)), "poll")
+        res = []
+        for i in range(k.value):
+            r = out[i]
+            x, _ = self._out.pop(r.ticket)
+            res.append(Finished(r.ticket, r.matrix, r.result.status, r.result.iterations, r.result.inner_iterations,
+                                r.result.residual, r.latency_s, r.queue_s, x))
+        return res
+
+    def drain(self, timeout=600.0):
+        _raise(self._lib.mtjg_server_drain(self.h, float(timeout)), "drain")
+
+    def stats(self):
+        c, a, m, t = C.c_int64(), C.c_int64(), C.c_int64(), C.c_double()
+        _raise(self._lib.mtjg_server_stats(self.h, C.byref(c), C.byref(a), C.byref(m), C.byref(t)), "stats")
+        return {"chunks": c.value, "admitted": a.value, "max_active": m.value, "clock_s": t.value}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.mtjg_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        if sys.is_finalizing():
+            return
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,111 @@
+"""Continuous-batching server: results alone equal results in a mix, every
+request meets rtol on its FP64 true residual, admission honours the vector
+pool, and requests join a batch that is already running."""
+import time
+
+import numpy as np
+import pytest
+
+import oracle as O
+from mtjg import serve, workloads
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture
+def servers(ctx):
+    made = []
+
+    def make(**kw):
+        made.append(serve.Server(ctx, **kw))
+        return made[-1]
+
+    yield make
+    for s in made:  # also when a test fails: no scheduler thread outlives its test
+        s.close()
+
+
+def _library():
+    return [workloads.poisson2d(40), workloads.poisson2d(97), workloads.laplacian(1500, 3),
+            workloads.laplacian(12000, 4), workloads.poisson3d(14), workloads.laplacian(4000, 5)]
+
+
+def _rhs(mats, count, seed):
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for k in range(count):
+        m = int(rng.integers(0, len(mats)))
+        n = mats[m][0]
+        reqs.append((m, workloads.uniform(n, 1000 + k)))
+    return reqs
+
+
+def _solve_all(srv, mids, reqs, one_at_a_time):
+    out = {}
+    tickets = {}
+    for k, (m, b) in enumerate(reqs):
+        t = srv.submit(mids[m], b)
+        tickets[t] = k
+        if one_at_a_time:
+            srv.drain(120.0)
+            for r in srv.poll():
+                out[tickets[r.ticket]] = r
+    srv.drain(120.0)
+    for r in srv.poll():
+        out[tickets[r.ticket]] = r
+    return out
+
+
+def test_alone_equals_mix_and_converges(servers):
+    mats = _library()
+    reqs = _rhs(mats, 30, 7)
+    srv = servers(max_systems=64, pool_rows=1 << 20)
+    mids = [srv.addMatrix(*m) for m in mats]
+    alone = _solve_all(srv, mids, reqs, True)
+    mix = _solve_all(srv, mids, reqs, False)
+    st = srv.stats()
+    assert len(alone) == len(mix) == len(reqs)
+    assert st["max_active"] > 1  # the mix really ran together
+    for k, (m, b) in enumerate(reqs):
+        a, x = alone[k], mix[k]
+        assert a.status == 0 and x.status == 0
+        assert a.iterations == x.iterations and a.inner_iterations == x.inner_iterations
+        assert np.array_equal(a.x, x.x), k
+        n, rp, ci, v = mats[m]
+        r = O.mult_add(O.Csr(n, n, rp, ci, v), -1.0, x.x, b)
+        assert np.linalg.norm(r) < 1e-10 * np.linalg.norm(b)
+
+
+def test_admission_by_pool_footprint(servers):
+    mats = [workloads.laplacian(20000, 8), workloads.laplacian(20000, 9)]
+    srv = servers(max_systems=16, pool_rows=30000)  # room for one system at a time
+    mids = [srv.addMatrix(*m) for m in mats]
+    reqs = [(k % 2, workloads.uniform(20000, 50 + k)) for k in range(6)]
+    out = _solve_all(srv, mids, reqs, False)
+    st = srv.stats()
+    assert st["max_active"] == 1
+    assert all(out[k].status == 0 for k in range(6))
+
+
+def test_requests_join_a_running_batch(servers):
+    mats = [workloads.poisson2d(600), workloads.laplacian(3000, 2)]
+    srv = servers(max_systems=32, pool_rows=1 << 20)
+    mids = [srv.addMatrix(*m) for m in mats]
+    big = srv.submit(mids[0], workloads.uniform(360000, 1))
+    time.sleep(0.02)
+    assert srv.poll() == []  # the large solve (thousands of inner iterations) is still running
+    small = [srv.submit(mids[1], workloads.uniform(3000, 10 + k)) for k in range(8)]
+    srv.drain(120.0)
+    res = {r.ticket: r for r in srv.poll()}
+    st = srv.stats()
+    assert st["max_active"] >= 2
+    # the small requests were admitted while the large one was running and
+    # finished before it
+    assert all(res[t].latency_s < res[big].latency_s for t in small)
+    assert all(res[t].status == 0 for t in small + [big])
+
+
+def test_unknown_matrix_is_rejected(servers):
+    srv = servers(max_systems=4, pool_rows=1000)
+    with pytest.raises(KeyError):
+        srv.submit(5, np.zeros(3))
