@@ -169,6 +169,33 @@ MTJG_API int mtjg_csr_mult_dev(mtjg_csr *A, const double *dx, double *dy);
 MTJG_API int mtjg_csr_mult_add_dev(mtjg_csr *A, double alpha, const double *dx, double *dy);
 MTJG_API int mtjg_csr_trans_mult_dev(mtjg_csr *A, const double *dx, double *dy);
 
+/* y = alpha A x + y (as mtjg_csr_mult_add_dev) and the two-norm of the new y,
+ * written to dnorm[0] -- one norm per system, dnorm[s], for a batch from
+ * mtjg_batch_upload.  All pointers are device pointers; the call is
+ * asynchronous on A's context stream.  With alpha = -1 and y = b it is the
+ * residual step r = b - A x, |r| of an iterative refinement loop.  No
+ * counterpart in the reference.
+ *
+ * This call allocates nothing: its reduction scratch is a fixed 512 KB array
+ * in the library's device image.  It is for callers that may not allocate
+ * device memory once set up: hosts whose device memory is a fixed arena
+ * handed out at start-up (a JVM off-heap pool, a serving process with a
+ * memory budget), and loops that cannot afford cudaMalloc/cudaFree, which may
+ * synchronise the device.
+ *   - Limit: A's product tiling may have at most 16384 reduction groups (one
+ *     system up to about 33 million rows at 7 entries per row, or a batch of
+ *     at most 16384 systems); larger A gives MTJG_ERR_ILLEGAL_ARGUMENT.
+ *   - Nothing has to start at zero: partials are written before they are read
+ *     within the call, and each norm is stored, not accumulated.
+ *   - The scratch is one array per device, shared by all contexts and threads:
+ *     calls that overlap on one device (two streams, contexts or threads)
+ *     race and return wrong norms.  Calls in order on one stream are safe.
+ *   - The first call on each device looks the scratch's address up once
+ *     (with that device current).  A caller that captures streams makes one
+ *     call before capture begins, so this set-up is not inside a capture. */
+MTJG_API int mtjg_csr_mult_add_norm_noalloc(mtjg_csr *A, double alpha, const double *dx, double *dy,
+                                            double *dnorm);
+
 /* ---- Preconditioner ---------------------------------------------------- */
 /* new DiagonalPreconditioner(n) / new ILU(CompRowMatrix) / new ICC(CompRowMatrix),
  * S/DiagonalPreconditioner.java:43-45, S/ILU.java:54-62, S/ICC.java:57-65 */

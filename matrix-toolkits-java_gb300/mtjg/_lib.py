@@ -91,6 +91,7 @@ PROTOTYPES = {
     "mtjg_csr_mult_dev": (C.c_int, [_vp, _vp, _vp]),
     "mtjg_csr_mult_add_dev": (C.c_int, [_vp, C.c_double, _vp, _vp]),
     "mtjg_csr_trans_mult_dev": (C.c_int, [_vp, _vp, _vp]),
+    "mtjg_csr_mult_add_norm_noalloc": (C.c_int, [_vp, C.c_double, _vp, _vp, _vp]),
     "mtjg_precond_create": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(_vp)]),
     "mtjg_precond_set_matrix": (C.c_int, [_vp, _vp, _ip]),
     "mtjg_precond_apply": (C.c_int, [_vp, _dp, _dp]),
