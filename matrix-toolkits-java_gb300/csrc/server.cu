@@ -4,9 +4,17 @@
 // values, Jacobi inverse diagonals).  Requests (matrix, b, x0) queue on the
 // host; a scheduler thread admits them into free slots whenever a slot and
 // a contiguous segment of the pooled vector workspace are free (admission
-// by HBM footprint), runs a chunk of the mixed-precision CG phases over all
+// by HBM footprint), runs chunks of the mixed-precision CG phases over all
 // admitted systems at once, and retires finished systems between chunks, so
 // requests that arrive while others are on the GPU join the running batch.
+//
+// The scheduler keeps two chunks queued on its stream: while the GPU runs
+// chunk k+1, the host reads chunk k's statuses, retires finished systems,
+// admits new ones and rebuilds the tile tables.  Everything the host hands
+// to the device for chunk k+2 (b, x0, system states, tile tables) is staged
+// in pinned memory and copied on the same stream, so stream order puts it
+// after chunk k+1 without the host waiting for it.  A system admitted for
+// chunk k+2 is ignored in the status snapshot of chunk k+1.
 //
 // Each system's product tiles are its own matrix's tiles and its reduction
 // groups depend on that matrix alone, so its arithmetic -- and its result --
@@ -23,9 +31,6 @@
 #include "phases.cuh"
 
 namespace mtjg {
-
-int precond_apply_dev(mtjg_precond *M, const double *b, double *x, const int *status);
-
 namespace {
 
 struct ResMat {
@@ -48,9 +53,11 @@ struct Req {
     double t_submit = 0, t_admit = 0;
     int slot = -1;
     int voff = -1;
+    int64_t first_chunk = 0;      // the first chunk the system runs in
 };
 
-// device array that grows on demand
+// device array that grows on demand (with slack: regrowth frees, which
+// waits for the device)
 template <class T>
 struct DevBuf {
     T *p = nullptr;
@@ -61,11 +68,40 @@ struct DevBuf {
         cudaFree(p);
         p = nullptr;
         cap = 0;
-        MTJG_CUDA(cudaMalloc(&p, sizeof(T) * std::max<size_t>(n, 16)));
-        cap = std::max<size_t>(n, 16);
+        const size_t c = std::max<size_t>(n + n / 2, 1024);
+        MTJG_CUDA(cudaMalloc(&p, sizeof(T) * c));
+        cap = c;
         return MTJG_OK;
     }
     ~DevBuf() { cudaFree(p); }
+};
+
+// pinned host array that grows on demand
+template <class T>
+struct PinBuf {
+    T *p = nullptr;
+    size_t cap = 0;
+    int ensure(size_t n)
+    {
+        if (n <= cap) return MTJG_OK;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+        const size_t c = std::max<size_t>(n + n / 2, 1024);
+        MTJG_CUDA(cudaHostAlloc((void **)&p, sizeof(T) * c, cudaHostAllocDefault));
+        cap = c;
+        return MTJG_OK;
+    }
+    ~PinBuf()
+    {
+        if (p) cudaFreeHost(p);
+    }
+};
+
+// A finished system whose x is on its way to the pinned staging area.
+struct Retired {
+    Req *r;
+    mtjg_server_result out;
 };
 
 }  // namespace
@@ -74,26 +110,33 @@ struct DevBuf {
 using namespace mtjg;
 
 struct mtjg_server {
-    mtjg_ctx *ctx = nullptr;  // the server's own context (own stream), on the caller's device
+    mtjg_ctx *ctx = nullptr;   // the scheduler's own context (own stream), on the caller's device
+    mtjg_ctx *uctx = nullptr;  // matrix registration (own stream, so uploads never wait for chunks)
     mtjg_server_config cfg{};
     std::vector<ResMat *> mats;
     std::mutex mats_mu;
     // pooled vectors: row offsets [0, pool_rows)
     double *b64 = nullptr, *x64 = nullptr;
     float *d32 = nullptr, *rin = nullptr, *z32 = nullptr, *p32 = nullptr, *q32 = nullptr, *inv32 = nullptr;
+    // pinned staging at the same row offsets: b and x0 in, x out
+    double *h_b = nullptr, *h_x0 = nullptr, *h_x = nullptr;
     std::map<int, int> free_seg;  // start -> length
     // slots
     SysState *st = nullptr;       // device [max_systems]
     SysDesc *sd = nullptr;        // device [max_systems]
-    std::vector<SysState> h_st;
-    std::vector<SysDesc> h_sd;
+    std::vector<SysDesc> h_sd;    // the live table (host)
     std::vector<Req *> slot_req;
     int active = 0;
-    // tiles of the current composition
-    DevBuf<int> pt_row, pt_row_end, pt_nz, pt_nz_end, pt_sys, pt_group, pt_sysg;
-    DevBuf<unsigned char> pt_flags;
-    DevBuf<int> rt_row, rt_row_end, rt_sys, rt_group, rt_sysg;
-    DevBuf<unsigned char> rt_flags;
+    int64_t active_rows = 0;
+    // per chunk parity: status snapshot, error flag, staged uploads, events
+    SysState *h_snap[2] = {nullptr, nullptr};
+    int *h_flag[2] = {nullptr, nullptr};
+    SysState *h_init[2] = {nullptr, nullptr};
+    SysDesc *h_sdst[2] = {nullptr, nullptr};
+    PinBuf<int> h_tiles[2];
+    cudaEvent_t ev_start[2] = {}, ev_done[2] = {}, ev_ret[2] = {};
+    // tiles of the current composition (one device blob)
+    DevBuf<int> d_tiles;
     DevBuf<double> part;
     TileSet ptiles, rtiles;
     int *num_running = nullptr;
@@ -113,6 +156,7 @@ struct mtjg_server {
     std::chrono::steady_clock::time_point t0;
     // statistics
     int64_t chunks = 0, admitted = 0, retired = 0, max_active = 0;
+    double gpu_s = 0, host_s = 0, wait_s = 0, row_chunks = 0;
 
     double now() const
     {
@@ -153,79 +197,85 @@ void seg_free(mtjg_server *S, int start, int n)
     }
 }
 
-// Rebuilds the product and row tiles of the admitted systems (slot order).
-int rebuild_tiles(mtjg_server *S)
+// Rebuilds the product and row tiles of the admitted systems (slot order)
+// into the pinned blob of parity `par`, and queues its upload.
+int rebuild_tiles(mtjg_server *S, int par)
 {
     const int ns = S->cfg.max_systems;
-    std::vector<int> row, row_end, nz, nz_end, sys, group, sysg = {0};
-    std::vector<unsigned char> flags;
-    std::vector<int> rrow, rrow_end, rsys, rgroup, rsysg = {0};
-    std::vector<unsigned char> rflags;
-    int vec_mask = 0;
+    int NT = 0, NG = 0, NR = 0;
     for (int s = 0; s < ns; ++s) {
-        Req *r = S->slot_req[s];
+        const Req *r = S->slot_req[s];
+        if (!r) continue;
+        const int T = (int)r->mat->t_row.size();
+        NT += T;
+        const int gs = std::max(1, std::min(kGroupTiles, T / 4096));  // as for an uploaded CSR
+        NG += (T + gs - 1) / gs;
+        NR += (r->mat->n + kRowTile - 1) / kRowTile;
+    }
+    // blob layout (ints): product row, row_end, nz, nz_end, sys [NT each],
+    // group [NG+1], sysg [ns+1]; row tiles row, row_end, sys [NR each],
+    // group [NR+1], sysg [ns+1]; then the flag bytes (NT + NR)
+    const size_t o_row = 0, o_rend = o_row + NT, o_nz = o_rend + NT, o_nzend = o_nz + NT, o_sys = o_nzend + NT,
+                 o_grp = o_sys + NT, o_sysg = o_grp + NG + 1, o_rrow = o_sysg + ns + 1, o_rrend = o_rrow + NR,
+                 o_rsys = o_rrend + NR, o_rgrp = o_rsys + NR, o_rsysg = o_rgrp + NR + 1, o_flags = o_rsysg + ns + 1;
+    const size_t total = o_flags + (NT + NR + 3) / 4 + 1;
+    int st = S->h_tiles[par].ensure(total);
+    if (st != MTJG_OK) return st;
+    int *h = S->h_tiles[par].p;
+    unsigned char *hf = reinterpret_cast<unsigned char *>(h + o_flags);
+    int t = 0, g = 0, q = 0, vec_mask = 0;
+    h[o_sysg] = 0;
+    h[o_rsysg] = 0;
+    for (int s = 0; s < ns; ++s) {
+        const Req *r = S->slot_req[s];
         if (r) {
             const ResMat *m = r->mat;
-            const int t0 = (int)row.size(), T = (int)m->t_row.size();
-            row.insert(row.end(), m->t_row.begin(), m->t_row.end());
-            row_end.insert(row_end.end(), m->t_row_end.begin(), m->t_row_end.end());
-            nz.insert(nz.end(), m->t_nz.begin(), m->t_nz.end());
-            nz_end.insert(nz_end.end(), m->t_nz_end.begin(), m->t_nz_end.end());
-            flags.insert(flags.end(), m->t_flags.begin(), m->t_flags.end());
-            sys.insert(sys.end(), T, s);
-            for (unsigned char f : m->t_flags) vec_mask |= f >> 1;
-            const int gs = std::max(1, std::min(kGroupTiles, T / 4096));  // as for an uploaded CSR
-            for (int t = t0; t < t0 + T; t += gs) group.push_back(t);
-            for (int q = 0; q < m->n; q += kRowTile) {
-                rrow.push_back(r->voff + q);
-                rrow_end.push_back(r->voff + std::min(m->n, q + kRowTile));
-                rsys.push_back(s);
-                rflags.push_back(2);
-                rgroup.push_back((int)rgroup.size());
+            const int T = (int)m->t_row.size();
+            const int gs = std::max(1, std::min(kGroupTiles, T / 4096));
+            for (int k = 0; k < T; ++k) {
+                if (k % gs == 0) h[o_grp + g++] = t;
+                h[o_row + t] = m->t_row[k];
+                h[o_rend + t] = m->t_row_end[k];
+                h[o_nz + t] = m->t_nz[k];
+                h[o_nzend + t] = m->t_nz_end[k];
+                h[o_sys + t] = s;
+                hf[t] = m->t_flags[k];
+                vec_mask |= m->t_flags[k] >> 1;
+                ++t;
+            }
+            for (int row = 0; row < m->n; row += kRowTile) {
+                h[o_rrow + q] = r->voff + row;
+                h[o_rrend + q] = r->voff + std::min(m->n, row + kRowTile);
+                h[o_rsys + q] = s;
+                h[o_rgrp + q] = q;
+                hf[NT + q] = 2;
+                ++q;
             }
         }
-        sysg.push_back((int)group.size());
-        rsysg.push_back((int)rgroup.size());
+        h[o_sysg + s + 1] = g;
+        h[o_rsysg + s + 1] = q;
     }
-    const int NT = (int)row.size(), NG = (int)group.size(), NR = (int)rrow.size();
-    group.push_back(NT);
-    rgroup.push_back(NR);
-    auto up_i = [&](DevBuf<int> &d, const std::vector<int> &h) -> int {
-        int st = d.ensure(h.size());
-        if (st != MTJG_OK) return st;
-        if (!h.empty())
-            MTJG_CUDA(cudaMemcpyAsync(d.p, h.data(), sizeof(int) * h.size(), cudaMemcpyHostToDevice, S->ctx->stream));
-        return MTJG_OK;
-    };
-    auto up_u = [&](DevBuf<unsigned char> &d, const std::vector<unsigned char> &h) -> int {
-        int st = d.ensure(h.size());
-        if (st != MTJG_OK) return st;
-        if (!h.empty()) MTJG_CUDA(cudaMemcpyAsync(d.p, h.data(), h.size(), cudaMemcpyHostToDevice, S->ctx->stream));
-        return MTJG_OK;
-    };
-    int st = MTJG_OK;
-    if ((st = up_i(S->pt_row, row)) || (st = up_i(S->pt_row_end, row_end)) || (st = up_i(S->pt_nz, nz)) ||
-        (st = up_i(S->pt_nz_end, nz_end)) || (st = up_i(S->pt_sys, sys)) || (st = up_i(S->pt_group, group)) ||
-        (st = up_i(S->pt_sysg, sysg)) || (st = up_u(S->pt_flags, flags)) || (st = up_i(S->rt_row, rrow)) ||
-        (st = up_i(S->rt_row_end, rrow_end)) || (st = up_i(S->rt_sys, rsys)) || (st = up_i(S->rt_group, rgroup)) ||
-        (st = up_i(S->rt_sysg, rsysg)) || (st = up_u(S->rt_flags, rflags)))
-        return st;
-    st = S->part.ensure((size_t)std::max(NG, NR) * kParts + kParts);
-    if (st != MTJG_OK) return st;
+    h[o_grp + NG] = NT;
+    h[o_rgrp + NR] = NR;
+    if ((st = S->d_tiles.ensure(total)) != MTJG_OK) return st;
+    MTJG_CUDA(cudaMemcpyAsync(S->d_tiles.p, h, sizeof(int) * total, cudaMemcpyHostToDevice, S->ctx->stream));
+    if ((st = S->part.ensure((size_t)std::max(NG, NR) * kParts + kParts)) != MTJG_OK) return st;
+    int *d = S->d_tiles.p;
+    unsigned char *df = reinterpret_cast<unsigned char *>(d + o_flags);
     TileSet &P = S->ptiles;
     P.num_tiles = NT;
     P.num_groups = NG;
     P.num_sys = ns;
     P.vec = 1;
     P.vec_mask = vec_mask;
-    P.tile_row = S->pt_row.p;
-    P.tile_row_end = S->pt_row_end.p;
-    P.tile_nz = S->pt_nz.p;
-    P.tile_nz_end = S->pt_nz_end.p;
-    P.tile_sys = S->pt_sys.p;
-    P.tile_flags = S->pt_flags.p;
-    P.group_tile = S->pt_group.p;
-    P.sys_group = S->pt_sysg.p;
+    P.tile_row = d + o_row;
+    P.tile_row_end = d + o_rend;
+    P.tile_nz = d + o_nz;
+    P.tile_nz_end = d + o_nzend;
+    P.tile_sys = d + o_sys;
+    P.tile_flags = df;
+    P.group_tile = d + o_grp;
+    P.sys_group = d + o_sysg;
     P.sd = S->sd;
     TileSet &R = S->rtiles;
     R.num_tiles = NR;
@@ -233,14 +283,14 @@ int rebuild_tiles(mtjg_server *S)
     R.num_sys = ns;
     R.vec = 1;
     R.vec_mask = 1;
-    R.tile_row = S->rt_row.p;
-    R.tile_row_end = S->rt_row_end.p;
+    R.tile_row = d + o_rrow;
+    R.tile_row_end = d + o_rrend;
     R.tile_nz = nullptr;
     R.tile_nz_end = nullptr;
-    R.tile_sys = S->rt_sys.p;
-    R.tile_flags = S->rt_flags.p;
-    R.group_tile = S->rt_group.p;
-    R.sys_group = S->rt_sysg.p;
+    R.tile_sys = d + o_rsys;
+    R.tile_flags = df + NT;
+    R.group_tile = d + o_rgrp;
+    R.sys_group = d + o_rsysg;
     R.sd = S->sd;
     return MTJG_OK;
 }
@@ -261,7 +311,7 @@ int run_chunk(mtjg_server *S)
     mon.atol = S->cfg.atol;
     mon.dtol = S->cfg.dtol;
     const MonPtrs mp{S->st, mon, nullptr, nullptr, S->num_running};
-    const MixCfg mix{S->cfg.inner_rtol, S->cfg.inner_max_iter};
+    const MixCfg mix{S->cfg.inner_rtol, S->cfg.inner_max_iter, 0, S->cfg.rtol, S->cfg.atol};
     const int norm = MTJG_NORM_TWO;
     const CsrArgs none64{nullptr, nullptr, nullptr};
     const CsrArgsT<float> none32{nullptr, nullptr, nullptr};
@@ -290,6 +340,32 @@ void fail_all(mtjg_server *S, int code, const std::string &msg)
     std::lock_guard<std::mutex> lk(S->mu);
     S->error = code;
     S->error_msg = msg;
+    S->cv_done.notify_all();
+}
+
+double since(std::chrono::steady_clock::time_point a)
+{
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - a).count();
+}
+
+// Hands the finished systems staged by the previous status pass to the
+// caller (their x has reached the pinned area once ev_ret[par] is done).
+int deliver(mtjg_server *S, std::vector<Retired> &staged, int par)
+{
+    if (staged.empty()) return MTJG_OK;
+    MTJG_CUDA(cudaEventSynchronize(S->ev_ret[par]));
+    const double tn = S->now();
+    std::lock_guard<std::mutex> lk(S->mu);
+    for (Retired &f : staged) {
+        std::memcpy(f.r->x_out, S->h_x + f.r->voff, sizeof(double) * (size_t)f.r->mat->n);
+        f.out.latency_s = tn - f.r->t_submit;
+        S->done.push_back(f.out);
+        delete f.r;
+    }
+    S->inflight -= (int64_t)staged.size();
+    S->cv_done.notify_all();
+    staged.clear();
+    return MTJG_OK;
 }
 
 void scheduler(mtjg_server *S)
@@ -297,15 +373,87 @@ void scheduler(mtjg_server *S)
     cudaSetDevice(S->ctx->device);
     mtjg_ctx *ctx = S->ctx;
     const int ns = S->cfg.max_systems;
+    int64_t launched = 0, processed = 0;  // chunks queued / whose statuses were read
+    std::vector<Retired> staged;          // retired, x on its way to the pinned area
+    int staged_par = 0;
+    auto fatal = [&](int code) {
+        fail_all(S, code, mtjg_last_error());
+        cudaStreamSynchronize(ctx->stream);
+    };
     for (;;) {
+        // 1. wait for the oldest queued chunk when two are queued (or when
+        //    nothing else can be queued), then read its statuses
+        const bool idle = S->active == 0;
+        if (launched - processed == 2 || (launched > processed && idle)) {
+            const int par = (int)(processed % 2);
+            auto tw = std::chrono::steady_clock::now();
+            cudaError_t e = cudaEventSynchronize(S->ev_done[par]);
+            const double waited = since(tw);
+            if (e != cudaSuccess) return fatal(cuda_fail(e, "server chunk"));
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, S->ev_start[par], S->ev_done[par]) != cudaSuccess) ms = 0.f;
+            {
+                std::lock_guard<std::mutex> lk(S->mu);
+                S->gpu_s += 1e-3 * ms;
+                S->wait_s += waited;
+            }
+            if (S->h_flag[par][0]) return fatal(fail(MTJG_ERR_DEVICE_TIMEOUT, "a bounded wait in a device kernel gave up"));
+            auto th = std::chrono::steady_clock::now();
+            if (deliver(S, staged, staged_par) != MTJG_OK) return fatal(MTJG_ERR_CUDA);
+            const SysState *snap = S->h_snap[par];
+            for (int s = 0; s < ns; ++s) {
+                Req *r = S->slot_req[s];
+                if (!r || r->first_chunk > processed || snap[s].status == ST_RUNNING) continue;
+                const ResMat *m = r->mat;
+                cudaMemcpyAsync(S->h_x + r->voff, S->x64 + r->voff, sizeof(double) * (size_t)m->n,
+                                cudaMemcpyDeviceToHost, ctx->stream);
+                const SysState &q = snap[s];
+                Retired f;
+                f.r = r;
+                std::memset(&f.out, 0, sizeof(f.out));
+                f.out.ticket = r->ticket;
+                f.out.matrix = r->mid;
+                f.out.result.status = q.status == ST_DONE ? MTJG_OK : q.status;
+                f.out.result.iterations = q.iter;
+                f.out.result.residual = q.residual;
+                f.out.result.detail = q.detail;
+                f.out.result.history_len = q.hist_len;
+                f.out.result.inner_iterations = q.in_total;
+                f.out.queue_s = r->t_admit - r->t_submit;
+                staged.push_back(f);
+                // the segment's D2H is queued before any later upload into it
+                seg_free(S, r->voff, m->n);
+                S->slot_req[s] = nullptr;
+                S->h_sd[s] = SysDesc{nullptr, nullptr, nullptr, nullptr, 0, 0};
+                S->active--;
+                S->active_rows -= m->n;
+                S->retired++;
+                S->dirty = true;
+            }
+            staged_par = par;
+            cudaEventRecord(S->ev_ret[par], ctx->stream);
+            ++processed;
+            const double spent = since(th);
+            {
+                std::lock_guard<std::mutex> lk(S->mu);
+                S->host_s += spent;
+            }
+            continue;  // the next pass delivers, admits and queues
+        }
+        // 2. admission (FIFO while a slot and a workspace segment are free)
         std::vector<Req *> admit;
         {
             std::unique_lock<std::mutex> lk(S->mu);
-            S->cv.wait_for(lk, std::chrono::milliseconds(2),
-                           [&] { return S->stop || !S->pending.empty() || S->active > 0; });
+            if (launched == processed && staged.empty())
+                S->cv.wait_for(lk, std::chrono::milliseconds(2),
+                               [&] { return S->stop || !S->pending.empty() || S->active > 0; });
             // destroy abandons queued and running requests between chunks
-            if (S->stop || S->error != MTJG_OK) return;
-            // admission: FIFO while a slot and a workspace segment are free
+            if (S->stop || S->error != MTJG_OK) {
+                lk.unlock();
+                cudaStreamSynchronize(ctx->stream);
+                for (Retired &f : staged) delete f.r;
+                return;
+            }
             while (!S->pending.empty()) {
                 Req *r = S->pending.front();
                 const int n = r->mat->n;
@@ -322,97 +470,71 @@ void scheduler(mtjg_server *S)
                 r->slot = slot;
                 r->voff = voff;
                 r->t_admit = S->now();
+                r->first_chunk = launched;
                 S->slot_req[slot] = r;
                 S->active++;
+                S->active_rows += n;
                 S->admitted++;
                 admit.push_back(r);
             }
             S->max_active = std::max<int64_t>(S->max_active, S->active);
         }
+        auto th = std::chrono::steady_clock::now();
+        if (!staged.empty() && launched == processed) {
+            if (deliver(S, staged, staged_par) != MTJG_OK) return fatal(MTJG_ERR_CUDA);
+        }
+        const int par = (int)(launched % 2);  // this parity's staging was last read before chunk launched-2
         for (Req *r : admit) {
             const ResMat *m = r->mat;
             const size_t nb = sizeof(double) * (size_t)m->n;
-            cudaMemcpyAsync(S->b64 + r->voff, r->b.data(), nb, cudaMemcpyHostToDevice, ctx->stream);
-            cudaMemcpyAsync(S->x64 + r->voff, r->x0.data(), nb, cudaMemcpyHostToDevice, ctx->stream);
+            std::memcpy(S->h_b + r->voff, r->b.data(), nb);
+            cudaMemcpyAsync(S->b64 + r->voff, S->h_b + r->voff, nb, cudaMemcpyHostToDevice, ctx->stream);
+            if (r->x0.empty()) {
+                cudaMemsetAsync(S->x64 + r->voff, 0, nb, ctx->stream);
+            } else {
+                std::memcpy(S->h_x0 + r->voff, r->x0.data(), nb);
+                cudaMemcpyAsync(S->x64 + r->voff, S->h_x0 + r->voff, nb, cudaMemcpyHostToDevice, ctx->stream);
+            }
             cudaMemcpyAsync(S->inv32 + r->voff, m->invdiag32, sizeof(float) * (size_t)m->n, cudaMemcpyDeviceToDevice,
                             ctx->stream);
-            SysDesc d{m->A->rowptr, m->A->colind, m->A->val, m->A->val32, r->voff, 0};
-            S->h_sd[r->slot] = d;
-            SysState init;
+            S->h_sd[r->slot] = SysDesc{m->A->rowptr, m->A->colind, m->A->val, m->A->val32, r->voff, 0};
+            SysState &init = S->h_init[par][r->slot];
             std::memset(&init, 0, sizeof(init));
             init.status = ST_RUNNING;
             init.gate = ST_RUNNING;
             init.rho_1 = init.rho_2 = init.alpha = init.beta = init.omega = 1.0;
-            S->h_st[r->slot] = init;
-            cudaMemcpyAsync(S->st + r->slot, &S->h_st[r->slot], sizeof(SysState), cudaMemcpyHostToDevice,
-                            ctx->stream);
+            cudaMemcpyAsync(S->st + r->slot, &init, sizeof(SysState), cudaMemcpyHostToDevice, ctx->stream);
             S->dirty = true;
         }
-        if (S->active == 0) continue;
+        if (S->active == 0) {
+            const double spent = since(th);
+            std::lock_guard<std::mutex> lk(S->mu);
+            S->host_s += spent;
+            continue;
+        }
+        // 3. tile tables of a changed composition
         if (S->dirty) {
-            cudaMemcpyAsync(S->sd, S->h_sd.data(), sizeof(SysDesc) * (size_t)ns, cudaMemcpyHostToDevice, ctx->stream);
-            int st = rebuild_tiles(S);
-            if (st != MTJG_OK) {
-                fail_all(S, st, mtjg_last_error());
-                return;
-            }
+            std::memcpy(S->h_sdst[par], S->h_sd.data(), sizeof(SysDesc) * (size_t)ns);
+            cudaMemcpyAsync(S->sd, S->h_sdst[par], sizeof(SysDesc) * (size_t)ns, cudaMemcpyHostToDevice,
+                            ctx->stream);
+            int st = rebuild_tiles(S, par);
+            if (st != MTJG_OK) return fatal(st);
             S->dirty = false;
         }
+        // 4. queue the chunk and its status snapshot
+        cudaEventRecord(S->ev_start[par], ctx->stream);
         int st = run_chunk(S);
-        if (st != MTJG_OK) {
-            fail_all(S, st, mtjg_last_error());
-            return;
-        }
+        if (st != MTJG_OK) return fatal(st);
+        cudaMemcpyAsync(S->h_snap[par], S->st, sizeof(SysState) * (size_t)ns, cudaMemcpyDeviceToHost, ctx->stream);
+        cudaMemcpyAsync(S->h_flag[par], ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+        cudaEventRecord(S->ev_done[par], ctx->stream);
+        ++launched;
+        const double spent = since(th);
         {
             std::lock_guard<std::mutex> lk(S->mu);
             S->chunks++;
-        }
-        cudaMemcpyAsync(S->h_st.data(), S->st, sizeof(SysState) * (size_t)ns, cudaMemcpyDeviceToHost, ctx->stream);
-        cudaMemcpyAsync(ctx->h_pinned, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
-        cudaError_t e = cudaStreamSynchronize(ctx->stream);
-        if (e != cudaSuccess) {
-            fail_all(S, cuda_fail(e, "server chunk"), mtjg_last_error());
-            return;
-        }
-        if (ctx->h_pinned[0]) {
-            fail_all(S, MTJG_ERR_DEVICE_TIMEOUT, "a bounded wait in a device kernel gave up");
-            return;
-        }
-        // retire finished systems
-        std::vector<mtjg_server_result> fin;
-        for (int s = 0; s < ns; ++s) {
-            Req *r = S->slot_req[s];
-            if (!r || S->h_st[s].status == ST_RUNNING) continue;
-            const ResMat *m = r->mat;
-            cudaMemcpy(r->x_out, S->x64 + r->voff, sizeof(double) * (size_t)m->n, cudaMemcpyDeviceToHost);
-            const SysState &q = S->h_st[s];
-            mtjg_server_result out;
-            std::memset(&out, 0, sizeof(out));
-            out.ticket = r->ticket;
-            out.matrix = r->mid;
-            out.result.status = q.status == ST_DONE ? MTJG_OK : q.status;
-            out.result.iterations = q.iter;
-            out.result.residual = q.residual;
-            out.result.detail = q.detail;
-            out.result.history_len = q.hist_len;
-            out.result.inner_iterations = q.in_total;
-            const double tn = S->now();
-            out.latency_s = tn - r->t_submit;
-            out.queue_s = r->t_admit - r->t_submit;
-            fin.push_back(out);
-            seg_free(S, r->voff, m->n);
-            S->slot_req[s] = nullptr;
-            S->h_sd[s] = SysDesc{nullptr, nullptr, nullptr, nullptr, 0, 0};
-            S->active--;
-            S->retired++;
-            S->dirty = true;
-            delete r;
-        }
-        if (!fin.empty()) {
-            std::lock_guard<std::mutex> lk(S->mu);
-            for (auto &f : fin) S->done.push_back(f);
-            S->inflight -= (int64_t)fin.size();
-            S->cv_done.notify_all();
+            S->row_chunks += (double)S->active_rows;
+            S->host_s += spent;
         }
     }
 }
@@ -440,13 +562,19 @@ extern "C" int mtjg_server_create(mtjg_ctx *ctx, const mtjg_server_config *cfg, 
         !(cfg->inner_rtol > 0 && cfg->inner_rtol < 1) || cfg->inner_max_iter <= 0)
         return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "bad server configuration");
     MTJG_CUDA(cudaSetDevice(ctx->device));
-    // the scheduler thread works on a stream of its own, so the caller's
-    // context stays free for other work while requests run
-    mtjg_ctx *own = nullptr;
+    // the scheduler thread and matrix registration work on streams of their
+    // own, so the caller's context stays free for other work
+    mtjg_ctx *own = nullptr, *up = nullptr;
     int cst = mtjg_ctx_create(ctx->device, &own);
     if (cst != MTJG_OK) return cst;
+    cst = mtjg_ctx_create(ctx->device, &up);
+    if (cst != MTJG_OK) {
+        mtjg_ctx_destroy(own);
+        return cst;
+    }
     mtjg_server *S = new mtjg_server();
     S->ctx = own;
+    S->uctx = up;
     S->cfg = *cfg;
     S->t0 = std::chrono::steady_clock::now();
     const size_t P = (size_t)cfg->pool_rows, ns = (size_t)cfg->max_systems;
@@ -457,16 +585,28 @@ extern "C" int mtjg_server_create(mtjg_ctx *ctx, const mtjg_server_config *cfg, 
               cudaMalloc(&S->st, sizeof(SysState) * ns) == cudaSuccess &&
               cudaMalloc(&S->sd, sizeof(SysDesc) * ns) == cudaSuccess &&
               cudaMalloc(&S->num_running, sizeof(int) * 4) == cudaSuccess &&
-              cudaMalloc(&S->cnt, sizeof(unsigned) * ns) == cudaSuccess;
+              cudaMalloc(&S->cnt, sizeof(unsigned) * ns) == cudaSuccess &&
+              cudaHostAlloc((void **)&S->h_b, 8 * P, cudaHostAllocDefault) == cudaSuccess &&
+              cudaHostAlloc((void **)&S->h_x0, 8 * P, cudaHostAllocDefault) == cudaSuccess &&
+              cudaHostAlloc((void **)&S->h_x, 8 * P, cudaHostAllocDefault) == cudaSuccess;
+    for (int p = 0; p < 2 && ok; ++p) {
+        ok = cudaHostAlloc((void **)&S->h_snap[p], sizeof(SysState) * ns, cudaHostAllocDefault) == cudaSuccess &&
+             cudaHostAlloc((void **)&S->h_flag[p], sizeof(int) * 4, cudaHostAllocDefault) == cudaSuccess &&
+             cudaHostAlloc((void **)&S->h_init[p], sizeof(SysState) * ns, cudaHostAllocDefault) == cudaSuccess &&
+             cudaHostAlloc((void **)&S->h_sdst[p], sizeof(SysDesc) * ns, cudaHostAllocDefault) == cudaSuccess &&
+             cudaEventCreate(&S->ev_start[p]) == cudaSuccess && cudaEventCreate(&S->ev_done[p]) == cudaSuccess &&
+             cudaEventCreate(&S->ev_ret[p]) == cudaSuccess;
+    }
     if (!ok) {
         mtjg_server_destroy(S);
-        return fail(MTJG_ERR_OUT_OF_MEMORY, "server workspace does not fit in device memory");
+        return fail(MTJG_ERR_OUT_OF_MEMORY, "server workspace does not fit in device or pinned host memory");
     }
-    S->h_st.assign(ns, SysState{});
-    for (auto &q : S->h_st) q.status = ST_DONE;  // empty slots are not running
+    std::vector<SysState> empty(ns);
+    std::memset(empty.data(), 0, sizeof(SysState) * ns);
+    for (auto &q : empty) q.status = ST_DONE;  // empty slots are not running
     S->h_sd.assign(ns, SysDesc{nullptr, nullptr, nullptr, nullptr, 0, 0});
     S->slot_req.assign(ns, nullptr);
-    cudaMemcpy(S->st, S->h_st.data(), sizeof(SysState) * ns, cudaMemcpyHostToDevice);
+    cudaMemcpy(S->st, empty.data(), sizeof(SysState) * ns, cudaMemcpyHostToDevice);
     cudaMemset(S->num_running, 0, sizeof(int) * 4);
     S->free_seg[0] = (int)cfg->pool_rows;
     S->th = std::thread(scheduler, S);
@@ -480,10 +620,11 @@ extern "C" int mtjg_server_add_matrix(mtjg_server *S, int n, const int *rowptr, 
     if (!S || !matrix_id) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL argument");
     if (n <= 0 || n > S->cfg.pool_rows)
         return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "matrix larger than the server's vector pool");
+    mtjg_ctx *u = S->uctx;
     ResMat *m = new ResMat();
     m->n = n;
-    int st = mtjg_csr_upload(S->ctx, n, n, rowptr, colind, val, &m->A);
-    if (st == MTJG_OK) st = mtjg_precond_create(S->ctx, MTJG_PC_JACOBI, n, &m->J);
+    int st = mtjg_csr_upload(u, n, n, rowptr, colind, val, &m->A);
+    if (st == MTJG_OK) st = mtjg_precond_create(u, MTJG_PC_JACOBI, n, &m->J);
     if (st == MTJG_OK) st = mtjg_precond_set_matrix(m->J, m->A, nullptr);
     if (st != MTJG_OK) {
         mtjg_precond_destroy(m->J);
@@ -492,13 +633,13 @@ extern "C" int mtjg_server_add_matrix(mtjg_server *S, int n, const int *rowptr, 
         return st;
     }
     m->nnz = m->A->nnz;
-    const int grid = S->ctx->num_sms * 8;
+    const int grid = u->num_sms * 8;
     MTJG_CUDA(cudaMalloc(&m->A->val32, sizeof(float) * (size_t)(m->nnz + 4)));
-    MTJG_CUDA(cudaMemset(m->A->val32, 0, sizeof(float) * (size_t)(m->nnz + 4)));
+    MTJG_CUDA(cudaMemsetAsync(m->A->val32, 0, sizeof(float) * (size_t)(m->nnz + 4), u->stream));
     MTJG_CUDA(cudaMalloc(&m->invdiag32, sizeof(float) * (size_t)n));
-    k_to_f32<<<grid, kBlock, 0, S->ctx->stream>>>(m->nnz, m->A->val, m->A->val32);
-    k_to_f32<<<grid, kBlock, 0, S->ctx->stream>>>(n, m->J->invdiag, m->invdiag32);
-    MTJG_CUDA(cudaStreamSynchronize(S->ctx->stream));
+    k_to_f32<<<grid, kBlock, 0, u->stream>>>(m->nnz, m->A->val, m->A->val32);
+    k_to_f32<<<grid, kBlock, 0, u->stream>>>(n, m->J->invdiag, m->invdiag32);
+    MTJG_CUDA(cudaStreamSynchronize(u->stream));
     // the matrix's own product tiles (as mtjg_csr_upload plans them)
     const int vec = choose_vec(m->nnz, n);
     std::vector<int> tr;
@@ -537,7 +678,6 @@ extern "C" int mtjg_server_submit(mtjg_server *S, int matrix_id, const double *b
         const int n = r->mat->n;
         r->b.assign(b, b + n);
         if (x0) r->x0.assign(x0, x0 + n);
-        else r->x0.assign(n, 0.0);
         r->x_out = x_out;
         r->t_submit = S->now();
         r->ticket = S->next_ticket++;
@@ -586,6 +726,25 @@ extern "C" int mtjg_server_stats(mtjg_server *S, int64_t *chunks, int64_t *admit
     return MTJG_OK;
 }
 
+extern "C" int mtjg_server_timing(mtjg_server *S, double *gpu_s, double *host_s, double *wait_s,
+                                  double *mean_rows)
+{
+    if (!S) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL server");
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (gpu_s) *gpu_s = S->gpu_s;
+    if (host_s) *host_s = S->host_s;
+    if (wait_s) *wait_s = S->wait_s;
+    if (mean_rows) *mean_rows = S->chunks ? S->row_chunks / (double)S->chunks : 0.0;
+    return MTJG_OK;
+}
+
+extern "C" int mtjg_server_context(mtjg_server *S, mtjg_ctx **ctx)
+{
+    if (!S || !ctx) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL argument");
+    *ctx = S->ctx;
+    return MTJG_OK;
+}
+
 extern "C" int mtjg_server_destroy(mtjg_server *S)
 {
     if (!S) return MTJG_OK;
@@ -617,8 +776,21 @@ extern "C" int mtjg_server_destroy(mtjg_server *S)
     cudaFree(S->sd);
     cudaFree(S->num_running);
     cudaFree(S->cnt);
-    mtjg_ctx *ctx = S->ctx;
+    cudaFreeHost(S->h_b);
+    cudaFreeHost(S->h_x0);
+    cudaFreeHost(S->h_x);
+    for (int p = 0; p < 2; ++p) {
+        cudaFreeHost(S->h_snap[p]);
+        cudaFreeHost(S->h_flag[p]);
+        cudaFreeHost(S->h_init[p]);
+        cudaFreeHost(S->h_sdst[p]);
+        if (S->ev_start[p]) cudaEventDestroy(S->ev_start[p]);
+        if (S->ev_done[p]) cudaEventDestroy(S->ev_done[p]);
+        if (S->ev_ret[p]) cudaEventDestroy(S->ev_ret[p]);
+    }
+    mtjg_ctx *ctx = S->ctx, *u = S->uctx;
     delete S;
     mtjg_ctx_destroy(ctx);
+    mtjg_ctx_destroy(u);
     return MTJG_OK;
 }

@@ -65,10 +65,28 @@ struct CgP {  // p = z (first) or p = beta*p + z (p.scale(beta).add(z), :70-75)
     static constexpr bool kReduce = false;
     static constexpr bool kNeedsXr = false;
     __device__ bool active(int sys) const { return st[sys].status == ST_RUNNING; }
+    static constexpr bool kBatched = true;
     __device__ void row(int i, int sys, Acc &) const
     {
         const SysState &t = st[sys];
         p[i] = t.iter == 0 ? z[i] : fmac<S>(p[i], t.beta, z[i]);
+    }
+    __device__ void rows(int base, int end, int sys, Acc &) const
+    {
+        const bool first = st[sys].iter == 0;
+        const double beta = st[sys].beta;
+        double zv[kRowsPerThread], pv[kRowsPerThread];
+#pragma unroll
+        for (int u = 0; u < kRowsPerThread; ++u) {
+            const int i = base + u * kBlock;
+            zv[u] = i < end ? __ldg(z + i) : 0.0;
+            pv[u] = i < end && !first ? p[i] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < kRowsPerThread; ++u) {
+            const int i = base + u * kBlock;
+            if (i < end) p[i] = first ? zv[u] : fmac<S>(pv[u], beta, zv[u]);
+        }
     }
     __device__ void scalar(int, const Acc &) {}
 };
@@ -105,6 +123,7 @@ struct CgUpd {  // x += alpha p; r -= alpha q; next monitor test; fused z = M r,
     static constexpr bool kReduce = true;
     static constexpr bool kNeedsXr = false;
     static constexpr int kSlots = kSlotNorm | kSlotD2;
+    static constexpr bool kBatched = true;
     __device__ bool active(int sys) const { return m.st[sys].status == ST_RUNNING; }
     __device__ void row(int i, int sys, Acc &a) const
     {
@@ -122,6 +141,42 @@ struct CgUpd {  // x += alpha p; r -= alpha q; next monitor test; fused z = M r,
             a.v[2] = fmac<S>(rr, zz, a.v[2]);
         } else if (pc == kPcIdentity) {
             a.v[2] = fmac<S>(rr, rr, a.v[2]);
+        }
+    }
+    __device__ void rows(int base, int end, int sys, Acc &a) const
+    {
+        constexpr int U = kRowsPerThread;
+        const double al = m.st[sys].alpha;
+        const int nt = m.mon.norm;
+        double rv[U], xv[U], pv[U], qv[U], dv[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int i = base + u * kBlock;
+            const bool in = i < end;
+            rv[u] = in ? r[i] : 0.0;
+            xv[u] = in && al != 0 ? x[i] : 0.0;
+            pv[u] = in && al != 0 ? __ldg(p + i) : 0.0;
+            qv[u] = in && al != 0 ? __ldg(q + i) : 0.0;
+            dv[u] = in && pc == kPcJacobi ? __ldg(invdiag + i) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int i = base + u * kBlock;
+            if (i >= end) break;
+            double rr = rv[u];
+            if (al != 0) {
+                x[i] = fmac<S>(al, pv[u], xv[u]);
+                rr = fmac<S>(-al, qv[u], rr);
+                r[i] = rr;
+            }
+            norm_add<S>(a, rr, nt);
+            if (pc == kPcJacobi) {
+                const double zz = rr * dv[u];
+                z[i] = zz;
+                a.v[2] = fmac<S>(rr, zz, a.v[2]);
+            } else if (pc == kPcIdentity) {
+                a.v[2] = fmac<S>(rr, rr, a.v[2]);
+            }
         }
     }
     __device__ void scalar(int sys, const Acc &s)
@@ -585,7 +640,7 @@ struct mtjg_solver {
     std::vector<SysState> last_all;
     // mixed precision
     bool mixed = false;
-    MixCfg mix{1e-4, 1000};
+    MixCfg mix{1e-4, 1000, 0, 1e-10, 1e-50};
     std::vector<float *> v32;   // d, rin, z, p, q
     float *invdiag32 = nullptr;
     int64_t inv32_version = -1;
@@ -792,6 +847,9 @@ int mixed_body(mtjg_solver *S, mtjg_csr *A)
     const RedCtx rc = red_ctx(A, A->tiles);
     const MonPtrs mp{S->st, mon_dev(S), S->hist_r, S->hist_it, A->num_running};
     const int norm = S->mon.norm;
+    MixCfg mix = S->mix;
+    mix.rtol = S->mon.rtol;
+    mix.atol = S->mon.atol;
     cudaError_t e = launch_rows(ctx, A->rtiles, MxX{S->vecs[V_X], d, S->st}, rc, norm);
     if (e == cudaSuccess)
         e = launch_spmv(ctx, CsrArgs{A->rowptr, A->colind, A->val}, A->tiles, (const double *)S->vecs[V_X],
@@ -802,7 +860,7 @@ int mixed_body(mtjg_solver *S, mtjg_csr *A)
             e = launch_spmv(ctx, CsrArgsT<float>{A->rowptr, A->colind, A->val32}, A->tiles, (const float *)p,
                             MxQ{q, S->st}, rc, norm);
         if (e == cudaSuccess)
-            e = launch_rows(ctx, A->rtiles, MxUpd{d, rin, z, p, q, S->invdiag32, pcm, S->st, S->mix}, rc, norm);
+            e = launch_rows(ctx, A->rtiles, MxUpd{d, rin, z, p, q, S->invdiag32, pcm, S->st, mix}, rc, norm);
     }
     if (e != cudaSuccess) return cuda_fail(e, "mixed-precision phase");
     return MTJG_OK;
@@ -1158,7 +1216,7 @@ extern "C" int mtjg_solver_set_mixed(mtjg_solver *S, int enable, double inner_rt
                 return fail(MTJG_ERR_OUT_OF_MEMORY, "cudaMalloc failed for the FP32 work vectors");
     }
     S->mixed = enable != 0;
-    if (enable) S->mix = MixCfg{inner_rtol, inner_max_iter};
+    if (enable) S->mix = MixCfg{inner_rtol, inner_max_iter, 0, 0.0, 0.0};
     drop_graph(S);
     return MTJG_OK;
 }

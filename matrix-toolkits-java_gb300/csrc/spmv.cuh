@@ -4,8 +4,9 @@
 // kGroupTiles consecutive tiles of one system; CTA b takes groups b, b+G,
 // ...).  The row pointers, values and column indices of the next tile are
 // brought into shared memory by one thread with three cp.async.bulk copies
-// completing on an mbarrier, while the block computes the current tile (two
-// stages).  Each row is summed from shared memory in ascending entry order
+// completing on an mbarrier, while the block computes the current tile
+// (kSpmvStages stages; two measured best: occupancy hides the x gathers
+// better than a deeper pipeline).  Each row is summed from shared memory in ascending entry order
 // (vec == 1: one thread per row, the order of CompRowMatrix.mult,
 // S/CompRowMatrix.java:304-312) or by a group of `vec` lanes with a fixed
 // butterfly (vec > 1).  x is gathered through the read-only path (L1/L2).
@@ -32,8 +33,21 @@ constexpr int kValBytes = ((kValCap * 8 + 15) / 16) * 16;
 constexpr int kColBytes = ((kColCap * 4 + 15) / 16) * 16;
 constexpr int kRowBytes = ((kRowCap * 4 + 15) / 16) * 16;
 constexpr int kStageBytes = kValBytes + kColBytes + kRowBytes;
-constexpr int kSpmvSmem = 2 * kStageBytes;
-constexpr int kSpmvCtasPerSm = 4;
+#ifndef MTJG_SPMV_STAGES
+#define MTJG_SPMV_STAGES 2
+#endif
+#ifndef MTJG_SPMV_CTAS
+#define MTJG_SPMV_CTAS 6
+#endif
+#ifndef MTJG_SPMV_CTAS_REDUCE
+#define MTJG_SPMV_CTAS_REDUCE 5
+#endif
+constexpr int kSpmvStages = MTJG_SPMV_STAGES;  // tiles in shared memory per CTA (NST - 1 in flight ahead)
+constexpr int kSpmvSmem = kSpmvStages * kStageBytes;
+// resident CTAs per SM the register budget is set for: products without a
+// reduction, and products whose epilogue reduces (they hold more state)
+constexpr int kSpmvCtasPerSm = MTJG_SPMV_CTAS;
+constexpr int kSpmvCtasReduce = MTJG_SPMV_CTAS_REDUCE;
 constexpr long long kWaitLimit = 1LL << 22;
 // row pointer arrays handed to k_spmv carry this many padding entries
 constexpr int kRowptrPad = 4;
@@ -79,20 +93,21 @@ __device__ __forceinline__ int tile_system(const TileArgs &ta, int t)
 namespace {
 
 template <int VEC, bool S, class T, class Epi>
-__global__ void __launch_bounds__(kBlock, kSpmvCtasPerSm)
+__global__ void __launch_bounds__(kBlock, Epi::kReduce ? kSpmvCtasReduce : kSpmvCtasPerSm)
     k_spmv(CsrArgsT<T> A, TileArgs ta, const T *__restrict__ x, Epi epi, RedCtx rc, int normtype, int *err)
 {
     constexpr int kVA = 16 / (int)sizeof(T);  // values per 16 bytes
+    constexpr int NST = kSpmvStages;
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ __align__(8) uint64_t bar[NST];
     __shared__ double red_sm[kParts * kBlock];
     __shared__ T s_long[kBlock / 32];
 
     const int tid = threadIdx.x;
     const int G = gridDim.x, NG = ta.num_groups;
     if (tid == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
+#pragma unroll
+        for (int i = 0; i < NST; ++i) mbar_init(&bar[i], 1);
         mbar_fence_init();
     }
     __syncthreads();
@@ -145,22 +160,45 @@ __global__ void __launch_bounds__(kBlock, kSpmvCtasPerSm)
         bulk_g2s(srow(s), m.rowptr + p0, pb, &bar[s]);
     };
 
-    unsigned phase[2] = {0u, 0u};
+    // The k-th tile of the block's walk lives in stage k % NST; the copy of
+    // tile k + NST - 1 is issued while tile k is summed.  All decisions below
+    // are uniform over the block (the walk and staged() read global tables).
+    auto advance = [&](int &gg, int &tt) {
+        ++tt;
+        if (tt >= ta.group_tile[gg + 1]) {
+            gg = next_group(gg + G);
+            tt = gg < NG ? ta.group_tile[gg] : 0;
+        }
+    };
+    unsigned phase = 0u;    // bit i: parity of stage i's next completion
+    unsigned pending = 0u;  // bit i: a copy into stage i is in flight
     int s = 0;
-    // (g, t): the current group and tile; the walk is uniform over the block
+    // (g, t): the current group and tile; (pg, pt): the next tile to issue
     int g = next_group(blockIdx.x);
     int t = g < NG ? ta.group_tile[g] : 0;
-    if (tid == 0 && g < NG && staged(t)) issue(t, 0);
+    int pg = g, pt = t, si = 0;
+    for (int k = 0; k < NST - 1 && pg < NG; ++k) {
+        if (staged(pt)) {
+            if (tid == 0) issue(pt, si);
+            pending |= 1u << si;
+        }
+        si = si + 1 == NST ? 0 : si + 1;
+        advance(pg, pt);
+    }
     Acc acc;
     acc_zero(acc);
     while (g < NG) {
-        // the tile after t in this block's walk
-        int gn = g, tn = t + 1;
-        if (tn >= ta.group_tile[g + 1]) {
-            gn = next_group(g + G);
-            tn = gn < NG ? ta.group_tile[gn] : 0;
+        if (pg < NG) {  // into the stage freed at the end of the last turn
+            if (staged(pt)) {
+                if (tid == 0) issue(pt, si);
+                pending |= 1u << si;
+            }
+            si = si + 1 == NST ? 0 : si + 1;
+            advance(pg, pt);
         }
-        if (tid == 0 && gn < NG && staged(tn)) issue(tn, s ^ 1);
+        // the tile after t in this block's walk
+        int gn = g, tn = t;
+        advance(gn, tn);
         const int sys = tile_system(ta, t);
         const int r0 = ta.tile_row[t], r1 = ta.tile_row_end[t];
         // rows r are the matrix's own; vectors are indexed at vo + r
@@ -168,15 +206,17 @@ __global__ void __launch_bounds__(kBlock, kSpmvCtasPerSm)
         const T *xs = x + mv.voff;
         const int vgo = mv.voff;
         if (staged(t)) {
-            const bool ok = mbar_wait_bounded(&bar[s], phase[s], kWaitLimit);
+            const bool ok = mbar_wait_bounded(&bar[s], (phase >> s) & 1u, kWaitLimit);
             if (__syncthreads_or(!ok)) {
                 // a copy never completed: report, drain what is in flight, stop
                 if (tid == 0) atomicExch(err, 1);
-                mbar_wait_bounded(&bar[s], phase[s], kWaitLimit);
-                if (gn < NG && staged(tn)) mbar_wait_bounded(&bar[s ^ 1], phase[s ^ 1], kWaitLimit);
+#pragma unroll
+                for (int i = 0; i < NST; ++i)
+                    if (pending & (1u << i)) mbar_wait_bounded(&bar[i], (phase >> i) & 1u, kWaitLimit);
                 return;
             }
-            phase[s] ^= 1u;
+            phase ^= 1u << s;
+            pending &= ~(1u << s);
             const T *sv = sval(s);
             const int *sc = scol(s);
             const int *sr = srow(s);
@@ -248,11 +288,26 @@ __global__ void __launch_bounds__(kBlock, kSpmvCtasPerSm)
             }
         }
         __syncthreads();  // stage s is free for the copy issued next turn
-        s ^= 1;
+        s = s + 1 == NST ? 0 : s + 1;
         g = gn;
         t = tn;
     }
 }
+
+// An Op with kBatched = true also has rows(base, end, sys, acc): the rows
+// base, base + kBlock, ... (kRowsPerThread of them, those below end) with
+// every load of every row issued before the first store, so a thread keeps
+// all its rows' reads in flight at once (the compiler cannot hoist a later
+// row's loads above an earlier row's stores to other arrays by itself).
+// The arithmetic and the accumulation order are those of row() in row order.
+template <class Op, class = void>
+struct OpBatched {
+    static constexpr bool value = false;
+};
+template <class Op>
+struct OpBatched<Op, decltype((void)Op::kBatched)> {
+    static constexpr bool value = Op::kBatched;
+};
 
 // Row kernel: block b handles row tile b, kRowsPerThread rows per thread
 // (rows tid, tid + kBlock, ...), one partial per tile.
@@ -266,8 +321,12 @@ __global__ void __launch_bounds__(kBlock) k_rows(TileArgs ta, Op op, RedCtx rc, 
     Acc acc;
     acc_zero(acc);
     const int r0 = ta.tile_row[t], r1 = ta.tile_row_end[t];
+    if constexpr (OpBatched<Op>::value) {
+        for (int base = r0 + (int)threadIdx.x; base < r1; base += kRowTile) op.rows(base, r1, sys, acc);
+    } else {
 #pragma unroll 2
-    for (int r = r0 + (int)threadIdx.x; r < r1; r += kBlock) op.row(r, sys, acc);
+        for (int r = r0 + (int)threadIdx.x; r < r1; r += kBlock) op.row(r, sys, acc);
+    }
     if constexpr (Op::kReduce) group_partial<OpSlots<Op>::value>(acc, t, rc, normtype, red_sm);
 }
 
@@ -307,7 +366,7 @@ cudaError_t launch_spmv_t(mtjg_ctx *ctx, CsrArgsT<T> A, const TileSet &ts, const
         if (e != cudaSuccess) return e;
         attr_set.fetch_or(bit);
     }
-    const int cap = ctx->num_sms * kSpmvCtasPerSm;
+    const int cap = ctx->num_sms * (Epi::kReduce ? kSpmvCtasReduce : kSpmvCtasPerSm);
     const int grid = ts.num_groups < cap ? ts.num_groups : cap;
     k<<<grid, kBlock, kSpmvSmem, ctx->stream>>>(A, tile_args(ts), x, epi, rc, normtype, ctx->d_flag);
     ctx->launches++;

@@ -13,7 +13,9 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_DIR = os.path.join(os.path.dirname(_HERE), "lib")
-LIB_PATH = os.path.join(LIB_DIR, "libmtjg.so")
+# MTJG_LIB points at another build of the library (e.g. one built with other
+# tile settings); by default the in-tree build is loaded
+LIB_PATH = os.environ.get("MTJG_LIB") or os.path.join(LIB_DIR, "libmtjg.so")
 WORKLOADS_PATH = os.path.join(LIB_DIR, "libmtjg_workloads.so")
 
 # status codes (include/mtjg.h)
@@ -116,6 +118,8 @@ PROTOTYPES = {
     "mtjg_server_drain": (C.c_int, [_vp, C.c_double]),
     "mtjg_server_stats": (C.c_int, [_vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                     C.POINTER(C.c_double)]),
+    "mtjg_server_timing": (C.c_int, [_vp, _dp, _dp, _dp, _dp]),
+    "mtjg_server_context": (C.c_int, [_vp, C.POINTER(_vp)]),
     "mtjg_server_destroy": (C.c_int, [_vp]),
     "mtjg_solver_batch_results": (C.c_int, [_vp, C.POINTER(Result), C.c_int]),
     "mtjg_solver_batch_history": (C.c_int, [_vp, C.c_int, _dp, _ip, C.c_int, _ip]),

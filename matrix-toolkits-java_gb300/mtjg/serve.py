@@ -91,6 +91,29 @@ class Server:
         _raise(self._lib.mtjg_server_stats(self.h, C.byref(c), C.byref(a), C.byref(m), C.byref(t)), "stats")
         return {"chunks": c.value, "admitted": a.value, "max_active": m.value, "clock_s": t.value}
 
+    def timing(self):
+        g, h, w, r = C.c_double(), C.c_double(), C.c_double(), C.c_double()
+        _raise(self._lib.mtjg_server_timing(self.h, C.byref(g), C.byref(h), C.byref(w), C.byref(r)), "timing")
+        return {"gpu_s": g.value, "host_s": h.value, "wait_s": w.value, "mean_rows": r.value}
+
+    def event(self, slot: int):
+        """Records event `slot` on the server's stream."""
+        _raise(self._lib.mtjg_ctx_event_record(self._ctx(), slot), "event_record")
+
+    def elapsed_ms(self, a: int, b: int) -> float:
+        ms = C.c_float()
+        _raise(self._lib.mtjg_ctx_event_elapsed(self._ctx(), a, b, C.byref(ms)), "event_elapsed")
+        return ms.value
+
+    def launchCount(self) -> int:
+        """Kernels the server has launched so far."""
+        return int(self._lib.mtjg_ctx_launch_count(self._ctx()))
+
+    def _ctx(self):
+        h = C.c_void_p()
+        _raise(self._lib.mtjg_server_context(self.h, C.byref(h)), "server_context")
+        return h
+
     def close(self):
         if getattr(self, "h", None):
             self._lib.mtjg_server_destroy(self.h)
