@@ -484,7 +484,7 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=1500)
     ap.add_argument("--serve-max-systems", type=int, default=256)
     ap.add_argument("--serve-pool-rows", type=int, default=1 << 25)
-    ap.add_argument("--inner-rtol", type=float, default=1e-4)
+    ap.add_argument("--inner-rtol", type=float, default=1e-6)
     ap.add_argument("--plain-budget", type=float, default=8.0, help="seconds of plain FP64 one-at-a-time solves")
     ap.add_argument("--ref-seconds", type=float, default=6.0, help="reference arm: seconds of work per step")
     args = ap.parse_args()

@@ -123,6 +123,7 @@ struct TileSet {
     int *tile_nz_end = nullptr;   // device [num_tiles], served batches only (else tile_nz + 1)
     int *tile_sys = nullptr;   // device [num_tiles] (nullptr: all system 0)
     int *group_tile = nullptr; // device [num_groups + 1]: first tile of each reduction group
+    int *group_info = nullptr; // device [num_groups]: (system << 8) | lanes per row
     int *sys_group = nullptr;  // device [num_sys + 1]
     const struct SysDesc *sd = nullptr;  // device per-system matrices (served batches), else nullptr
     // device [num_tiles]: (lanes per row << 1) | 1 if the tile is a single long row

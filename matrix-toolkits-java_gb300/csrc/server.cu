@@ -33,15 +33,31 @@
 namespace mtjg {
 namespace {
 
+// Product tiles of one matrix (host copies).
+struct ProdTiles {
+    std::vector<int> row, row_end, nz, nz_end;
+    std::vector<unsigned char> flags;
+    void plan(const int *rowptr, int n, int vec, int nnz_cap, int rows_cap)
+    {
+        std::vector<int> tr;
+        plan_tiles(rowptr, 0, n, vec, tr, flags, nnz_cap, rows_cap);
+        tr.push_back(n);
+        for (size_t t = 0; t + 1 < tr.size(); ++t) {
+            row.push_back(tr[t]);
+            row_end.push_back(tr[t + 1]);
+            nz.push_back(rowptr[tr[t]]);
+            nz_end.push_back(rowptr[tr[t + 1]]);
+        }
+    }
+};
+
 struct ResMat {
     int n = 0;
     int64_t nnz = 0;
     mtjg_csr *A = nullptr;          // resident CSR (rows 0..n-1), FP32 values in A->val32
     mtjg_precond *J = nullptr;      // Jacobi (its invdiag)
     float *invdiag32 = nullptr;
-    // product tiles of this matrix (local rows and entries), host copies
-    std::vector<int> t_row, t_row_end, t_nz, t_nz_end;
-    std::vector<unsigned char> t_flags;
+    ProdTiles t64, t32;  // product tiles for FP64 and FP32 values (local rows and entries)
 };
 
 struct Req {
@@ -138,7 +154,7 @@ struct mtjg_server {
     // tiles of the current composition (one device blob)
     DevBuf<int> d_tiles;
     DevBuf<double> part;
-    TileSet ptiles, rtiles;
+    TileSet ptiles, ptiles32, rtiles;  // FP64 product tiles, FP32 product tiles, row tiles
     int *num_running = nullptr;
     unsigned *cnt = nullptr;
     bool dirty = true;
@@ -197,100 +213,122 @@ void seg_free(mtjg_server *S, int start, int n)
     }
 }
 
-// Rebuilds the product and row tiles of the admitted systems (slot order)
-// into the pinned blob of parity `par`, and queues its upload.
+// Host tables of one product tiling (tiles of admitted systems, slot order).
+struct ProdTables {
+    std::vector<int> row, rend, nz, nzend, sys, grp, ginfo, sysg{0};
+    std::vector<unsigned char> flags;
+    int vec_mask = 0;
+    void add(const ProdTiles &mt, int s)
+    {
+        const int T = (int)mt.row.size(), t0 = (int)row.size();
+        const int gs = std::max(1, std::min(kGroupTiles, T / 4096));  // as for an uploaded CSR
+        for (int k = 0; k < T; ++k) {
+            if (k % gs == 0) {
+                ginfo.push_back((s << 8) | (mt.flags[k] >> 1));
+                grp.push_back(t0 + k);
+            }
+            vec_mask |= mt.flags[k] >> 1;
+        }
+        row.insert(row.end(), mt.row.begin(), mt.row.end());
+        rend.insert(rend.end(), mt.row_end.begin(), mt.row_end.end());
+        nz.insert(nz.end(), mt.nz.begin(), mt.nz.end());
+        nzend.insert(nzend.end(), mt.nz_end.begin(), mt.nz_end.end());
+        sys.insert(sys.end(), T, s);
+        flags.insert(flags.end(), mt.flags.begin(), mt.flags.end());
+    }
+};
+
+// Rebuilds the product tiles (FP64 and FP32 tilings) and row tiles of the
+// admitted systems (slot order) into the pinned blob of parity `par`, and
+// queues its upload.
 int rebuild_tiles(mtjg_server *S, int par)
 {
     const int ns = S->cfg.max_systems;
-    int NT = 0, NG = 0, NR = 0;
-    for (int s = 0; s < ns; ++s) {
-        const Req *r = S->slot_req[s];
-        if (!r) continue;
-        const int T = (int)r->mat->t_row.size();
-        NT += T;
-        const int gs = std::max(1, std::min(kGroupTiles, T / 4096));  // as for an uploaded CSR
-        NG += (T + gs - 1) / gs;
-        NR += (r->mat->n + kRowTile - 1) / kRowTile;
-    }
-    // blob layout (ints): product row, row_end, nz, nz_end, sys [NT each],
-    // group [NG+1], sysg [ns+1]; row tiles row, row_end, sys [NR each],
-    // group [NR+1], sysg [ns+1]; then the flag bytes (NT + NR)
-    const size_t o_row = 0, o_rend = o_row + NT, o_nz = o_rend + NT, o_nzend = o_nz + NT, o_sys = o_nzend + NT,
-                 o_grp = o_sys + NT, o_sysg = o_grp + NG + 1, o_rrow = o_sysg + ns + 1, o_rrend = o_rrow + NR,
-                 o_rsys = o_rrend + NR, o_rgrp = o_rsys + NR, o_rsysg = o_rgrp + NR + 1, o_flags = o_rsysg + ns + 1;
-    const size_t total = o_flags + (NT + NR + 3) / 4 + 1;
-    int st = S->h_tiles[par].ensure(total);
-    if (st != MTJG_OK) return st;
-    int *h = S->h_tiles[par].p;
-    unsigned char *hf = reinterpret_cast<unsigned char *>(h + o_flags);
-    int t = 0, g = 0, q = 0, vec_mask = 0;
-    h[o_sysg] = 0;
-    h[o_rsysg] = 0;
+    ProdTables p64, p32;
+    std::vector<int> rrow, rrend, rsys, rgrp, rsysg{0};
     for (int s = 0; s < ns; ++s) {
         const Req *r = S->slot_req[s];
         if (r) {
             const ResMat *m = r->mat;
-            const int T = (int)m->t_row.size();
-            const int gs = std::max(1, std::min(kGroupTiles, T / 4096));
-            for (int k = 0; k < T; ++k) {
-                if (k % gs == 0) h[o_grp + g++] = t;
-                h[o_row + t] = m->t_row[k];
-                h[o_rend + t] = m->t_row_end[k];
-                h[o_nz + t] = m->t_nz[k];
-                h[o_nzend + t] = m->t_nz_end[k];
-                h[o_sys + t] = s;
-                hf[t] = m->t_flags[k];
-                vec_mask |= m->t_flags[k] >> 1;
-                ++t;
-            }
+            p64.add(m->t64, s);
+            p32.add(m->t32, s);
             for (int row = 0; row < m->n; row += kRowTile) {
-                h[o_rrow + q] = r->voff + row;
-                h[o_rrend + q] = r->voff + std::min(m->n, row + kRowTile);
-                h[o_rsys + q] = s;
-                h[o_rgrp + q] = q;
-                hf[NT + q] = 2;
-                ++q;
+                rgrp.push_back((int)rrow.size());
+                rrow.push_back(r->voff + row);
+                rrend.push_back(r->voff + std::min(m->n, row + kRowTile));
+                rsys.push_back(s);
             }
         }
-        h[o_sysg + s + 1] = g;
-        h[o_rsysg + s + 1] = q;
+        p64.sysg.push_back((int)p64.grp.size());
+        p32.sysg.push_back((int)p32.grp.size());
+        rsysg.push_back((int)rgrp.size());
     }
-    h[o_grp + NG] = NT;
-    h[o_rgrp + NR] = NR;
+    for (ProdTables *p : {&p64, &p32}) p->grp.push_back((int)p->row.size());
+    rgrp.push_back((int)rrow.size());
+    const int NR = (int)rrow.size();
+    // one blob: the int arrays back to back, then the flag bytes
+    std::vector<const std::vector<int> *> ints = {&p64.row, &p64.rend, &p64.nz,  &p64.nzend, &p64.sys,  &p64.grp,
+                                                  &p64.ginfo, &p64.sysg, &p32.row, &p32.rend, &p32.nz,   &p32.nzend,
+                                                  &p32.sys, &p32.grp,  &p32.ginfo, &p32.sysg, &rrow, &rrend,
+                                                  &rsys,    &rgrp,     &rsysg};
+    std::vector<size_t> off;
+    size_t total = 0;
+    for (auto *v : ints) {
+        off.push_back(total);
+        total += v->size();
+    }
+    const size_t o_flags = total;
+    const size_t nflags = p64.flags.size() + p32.flags.size() + (size_t)NR;
+    total += (nflags + 3) / 4 + 1;
+    int st = S->h_tiles[par].ensure(total);
+    if (st != MTJG_OK) return st;
+    int *h = S->h_tiles[par].p;
+    for (size_t i = 0; i < ints.size(); ++i)
+        if (!ints[i]->empty()) std::memcpy(h + off[i], ints[i]->data(), sizeof(int) * ints[i]->size());
+    unsigned char *hf = reinterpret_cast<unsigned char *>(h + o_flags);
+    if (!p64.flags.empty()) std::memcpy(hf, p64.flags.data(), p64.flags.size());
+    if (!p32.flags.empty()) std::memcpy(hf + p64.flags.size(), p32.flags.data(), p32.flags.size());
+    std::memset(hf + p64.flags.size() + p32.flags.size(), 2, (size_t)NR);
     if ((st = S->d_tiles.ensure(total)) != MTJG_OK) return st;
     MTJG_CUDA(cudaMemcpyAsync(S->d_tiles.p, h, sizeof(int) * total, cudaMemcpyHostToDevice, S->ctx->stream));
+    const int NG = std::max((int)p64.grp.size(), (int)p32.grp.size());
     if ((st = S->part.ensure((size_t)std::max(NG, NR) * kParts + kParts)) != MTJG_OK) return st;
     int *d = S->d_tiles.p;
     unsigned char *df = reinterpret_cast<unsigned char *>(d + o_flags);
-    TileSet &P = S->ptiles;
-    P.num_tiles = NT;
-    P.num_groups = NG;
-    P.num_sys = ns;
-    P.vec = 1;
-    P.vec_mask = vec_mask;
-    P.tile_row = d + o_row;
-    P.tile_row_end = d + o_rend;
-    P.tile_nz = d + o_nz;
-    P.tile_nz_end = d + o_nzend;
-    P.tile_sys = d + o_sys;
-    P.tile_flags = df;
-    P.group_tile = d + o_grp;
-    P.sys_group = d + o_sysg;
-    P.sd = S->sd;
+    auto set_prod = [&](TileSet &P, const ProdTables &p, size_t k0, unsigned char *flags) {
+        P.num_tiles = (int)p.row.size();
+        P.num_groups = (int)p.grp.size() - 1;
+        P.num_sys = ns;
+        P.vec = 1;
+        P.vec_mask = p.vec_mask;
+        P.tile_row = d + off[k0];
+        P.tile_row_end = d + off[k0 + 1];
+        P.tile_nz = d + off[k0 + 2];
+        P.tile_nz_end = d + off[k0 + 3];
+        P.tile_sys = d + off[k0 + 4];
+        P.group_tile = d + off[k0 + 5];
+        P.group_info = d + off[k0 + 6];
+        P.sys_group = d + off[k0 + 7];
+        P.tile_flags = flags;
+        P.sd = S->sd;
+    };
+    set_prod(S->ptiles, p64, 0, df);
+    set_prod(S->ptiles32, p32, 8, df + p64.flags.size());
     TileSet &R = S->rtiles;
     R.num_tiles = NR;
     R.num_groups = NR;
     R.num_sys = ns;
     R.vec = 1;
     R.vec_mask = 1;
-    R.tile_row = d + o_rrow;
-    R.tile_row_end = d + o_rrend;
+    R.tile_row = d + off[16];
+    R.tile_row_end = d + off[17];
     R.tile_nz = nullptr;
     R.tile_nz_end = nullptr;
-    R.tile_sys = d + o_rsys;
-    R.tile_flags = df + NT;
-    R.group_tile = d + o_rgrp;
-    R.sys_group = d + o_rsysg;
+    R.tile_sys = d + off[18];
+    R.group_tile = d + off[19];
+    R.group_info = nullptr;
+    R.sys_group = d + off[20];
+    R.tile_flags = df + p64.flags.size() + p32.flags.size();
     R.sd = S->sd;
     return MTJG_OK;
 }
@@ -324,7 +362,7 @@ int run_chunk(mtjg_server *S)
         for (int k = 0; k < kInnerPerBody && e == cudaSuccess; ++k) {
             e = launch_rows(ctx, S->rtiles, MxP{S->p32, S->z32, S->st}, rc, norm);
             if (e == cudaSuccess)
-                e = launch_spmv(ctx, none32, S->ptiles, (const float *)S->p32, MxQ{S->q32, S->st}, rc, norm);
+                e = launch_spmv(ctx, none32, S->ptiles32, (const float *)S->p32, MxQ{S->q32, S->st}, rc, norm);
             if (e == cudaSuccess)
                 e = launch_rows(ctx, S->rtiles,
                                 MxUpd{S->d32, S->rin, S->z32, S->p32, S->q32, S->inv32, kPcJacobi, S->st, mix}, rc,
@@ -550,7 +588,7 @@ extern "C" void mtjg_server_config_defaults(mtjg_server_config *cfg)
     cfg->rtol = 1e-10;
     cfg->atol = 1e-50;
     cfg->dtol = 1e+5;
-    cfg->inner_rtol = 1e-4;
+    cfg->inner_rtol = 1e-6;
     cfg->inner_max_iter = 2000;
 }
 
@@ -640,17 +678,11 @@ extern "C" int mtjg_server_add_matrix(mtjg_server *S, int n, const int *rowptr, 
     k_to_f32<<<grid, kBlock, 0, u->stream>>>(m->nnz, m->A->val, m->A->val32);
     k_to_f32<<<grid, kBlock, 0, u->stream>>>(n, m->J->invdiag, m->invdiag32);
     MTJG_CUDA(cudaStreamSynchronize(u->stream));
-    // the matrix's own product tiles (as mtjg_csr_upload plans them)
+    // the matrix's own product tiles: FP64 as mtjg_csr_upload plans them,
+    // and larger FP32 tiles for the inner products
     const int vec = choose_vec(m->nnz, n);
-    std::vector<int> tr;
-    plan_tiles(rowptr, 0, n, vec, tr, m->t_flags);
-    tr.push_back(n);
-    for (size_t t = 0; t + 1 < tr.size(); ++t) {
-        m->t_row.push_back(tr[t]);
-        m->t_row_end.push_back(tr[t + 1]);
-        m->t_nz.push_back(rowptr[tr[t]]);
-        m->t_nz_end.push_back(rowptr[tr[t + 1]]);
-    }
+    m->t64.plan(rowptr, n, vec, kTileNnz, kTileRows);
+    m->t32.plan(rowptr, n, vec, kTileNnz32, kTileRows32);
     std::lock_guard<std::mutex> lk(S->mats_mu);
     std::lock_guard<std::mutex> lk2(S->mu);
     *matrix_id = (int)S->mats.size();

@@ -17,14 +17,14 @@ int choose_vec(int64_t nnz, int64_t n)
 }
 
 void plan_tiles(const int *rowptr, int row_begin, int row_end, int vec, std::vector<int> &tile_row,
-                std::vector<unsigned char> &tile_flags)
+                std::vector<unsigned char> &tile_flags, int nnz_cap, int rows_cap_all)
 {
-    const int rows_cap = kTileRows / vec;
+    const int rows_cap = rows_cap_all / vec;
     int r = row_begin;
     while (r < row_end) {
         tile_row.push_back(r);
         int len0 = rowptr[r + 1] - rowptr[r];
-        if (len0 > kTileNnz) {
+        if (len0 > nnz_cap) {
             tile_flags.push_back((unsigned char)((vec << 1) | 1));
             r += 1;
             continue;
@@ -33,7 +33,7 @@ void plan_tiles(const int *rowptr, int row_begin, int row_end, int vec, std::vec
         r += 1;
         while (r < row_end && rows < rows_cap) {
             int len = rowptr[r + 1] - rowptr[r];
-            if (nz + len > kTileNnz) break;
+            if (nz + len > nnz_cap) break;
             nz += len;
             rows++;
             r++;
@@ -70,6 +70,11 @@ int upload_tiles(TileSet &ts, const std::vector<int> &tile_row, const std::vecto
         sys_group.push_back((int)group_tile.size());
     }
     ts.num_groups = (int)group_tile.size();
+    std::vector<int> group_info(std::max<size_t>(1, group_tile.size()));
+    for (int s = 0, g = 0; s < ts.num_sys; ++s)
+        for (; g < sys_group[s + 1]; ++g) group_info[g] = (s << 8) | (tile_flags[group_tile[g]] >> 1);
+    MTJG_CUDA(cudaMalloc(&ts.group_info, sizeof(int) * group_info.size()));
+    MTJG_CUDA(cudaMemcpy(ts.group_info, group_info.data(), sizeof(int) * group_info.size(), cudaMemcpyHostToDevice));
     group_tile.push_back(ts.num_tiles);
     MTJG_CUDA(cudaMalloc(&ts.group_tile, sizeof(int) * group_tile.size()));
     MTJG_CUDA(cudaMemcpy(ts.group_tile, group_tile.data(), sizeof(int) * group_tile.size(), cudaMemcpyHostToDevice));
@@ -105,9 +110,10 @@ void free_tiles(TileSet &ts)
     cudaFree(ts.tile_nz);
     cudaFree(ts.tile_sys);
     cudaFree(ts.group_tile);
+    cudaFree(ts.group_info);
     cudaFree(ts.sys_group);
     cudaFree(ts.tile_flags);
-    ts.tile_row = ts.tile_nz = ts.tile_sys = ts.group_tile = ts.sys_group = nullptr;
+    ts.tile_row = ts.tile_nz = ts.tile_sys = ts.group_tile = ts.group_info = ts.sys_group = nullptr;
     ts.tile_flags = nullptr;
     ts.num_tiles = 0;
     ts.num_groups = 0;

@@ -26,13 +26,22 @@
 
 namespace mtjg {
 
-constexpr int kValCap = kTileNnz + 2;     // doubles per stage (+2: 16-byte rounding)
-constexpr int kColCap = kTileNnz + 8;     // ints per stage (+8: 16-byte rounding at both ends)
-constexpr int kRowCap = kTileRows + 1 + 8;  // row pointers per stage
-constexpr int kValBytes = ((kValCap * 8 + 15) / 16) * 16;
-constexpr int kColBytes = ((kColCap * 4 + 15) / 16) * 16;
-constexpr int kRowBytes = ((kRowCap * 4 + 15) / 16) * 16;
-constexpr int kStageBytes = kValBytes + kColBytes + kRowBytes;
+// Shared-memory stage of one tile, per value type.  FP32 tiles may hold 1.5x
+// the entries and 2x the rows of FP64 tiles in about the same bytes (tiles
+// planned for FP64 always fit an FP32 stage).
+constexpr int kTileNnz32 = kTileNnz * 3 / 2;
+constexpr int kTileRows32 = 2 * kTileRows;
+constexpr int round16(int b) { return ((b + 15) / 16) * 16; }
+template <class T>
+struct Stage {
+    static constexpr int kNnz = sizeof(T) == 8 ? kTileNnz : kTileNnz32;
+    static constexpr int kRows = sizeof(T) == 8 ? kTileRows : kTileRows32;
+    // a tile's copies start and end on 16 bytes: up to 2 (16/sizeof(T) - 1) extra values
+    static constexpr int kValBytes = round16((kNnz + 2 * (16 / (int)sizeof(T) - 1)) * (int)sizeof(T));
+    static constexpr int kColBytes = round16((kNnz + 8) * 4);       // 16-byte rounding at both ends
+    static constexpr int kRowBytes = round16((kRows + 1 + 8) * 4);  // row pointers
+    static constexpr int kBytes = kValBytes + kColBytes + kRowBytes;
+};
 #ifndef MTJG_SPMV_STAGES
 #define MTJG_SPMV_STAGES 2
 #endif
@@ -43,7 +52,8 @@ constexpr int kStageBytes = kValBytes + kColBytes + kRowBytes;
 #define MTJG_SPMV_CTAS_REDUCE 5
 #endif
 constexpr int kSpmvStages = MTJG_SPMV_STAGES;  // tiles in shared memory per CTA (NST - 1 in flight ahead)
-constexpr int kSpmvSmem = kSpmvStages * kStageBytes;
+template <class T>
+constexpr int spmv_smem() { return kSpmvStages * Stage<T>::kBytes; }
 // resident CTAs per SM the register budget is set for: products without a
 // reduction, and products whose epilogue reduces (they hold more state)
 constexpr int kSpmvCtasPerSm = MTJG_SPMV_CTAS;
@@ -73,6 +83,7 @@ struct TileArgs {
     const int *tile_sys;
     const unsigned char *tile_flags;
     const int *group_tile;
+    const int *group_info;  // per group: (system << 8) | lanes per row of its tiles
     const SysDesc *sd;  // nullptr: one CSR (the kernel's argument), rows = vector indices
 };
 
@@ -112,13 +123,26 @@ __global__ void __launch_bounds__(kBlock, Epi::kReduce ? kSpmvCtasReduce : kSpmv
     }
     __syncthreads();
 
-    auto sval = [&](int s) { return reinterpret_cast<T *>(smem + s * kStageBytes); };
-    auto scol = [&](int s) { return reinterpret_cast<int *>(smem + s * kStageBytes + kValBytes); };
-    auto srow = [&](int s) { return reinterpret_cast<int *>(smem + s * kStageBytes + kValBytes + kColBytes); };
+    using St = Stage<T>;
+    auto sval = [&](int s) { return reinterpret_cast<T *>(smem + s * St::kBytes); };
+    auto scol = [&](int s) { return reinterpret_cast<int *>(smem + s * St::kBytes + St::kValBytes); };
+    auto srow = [&](int s) {
+        return reinterpret_cast<int *>(smem + s * St::kBytes + St::kValBytes + St::kColBytes);
+    };
     // a launch takes the groups of its lanes-per-row class (STRICT: all)
+    // whose system is active; one load per group, and a system's activity
+    // (fixed for the launch) is read once per run of its groups
+    int last_sys = -1;
+    bool last_active = false;
     auto group_active = [&](int g) {
-        const int t0 = ta.group_tile[g];
-        return (S || (ta.tile_flags[t0] >> 1) == VEC) && epi.active(tile_system(ta, t0));
+        const int info = ta.group_info[g];
+        if (!S && (info & 0xff) != VEC) return false;
+        const int sys = info >> 8;
+        if (sys != last_sys) {
+            last_sys = sys;
+            last_active = epi.active(sys);
+        }
+        return last_active;
     };
     auto next_group = [&](int g) {
         while (g < NG && !group_active(g)) g += G;
@@ -342,6 +366,7 @@ inline TileArgs tile_args(const TileSet &ts)
                     ts.tile_sys,
                     ts.tile_flags,
                     ts.group_tile,
+                    ts.group_info,
                     ts.sd};
 }
 
@@ -362,13 +387,13 @@ cudaError_t launch_spmv_t(mtjg_ctx *ctx, CsrArgsT<T> A, const TileSet &ts, const
     static std::atomic<unsigned long long> attr_set{0};
     const unsigned long long bit = 1ull << (ctx->device & 63);
     if (!(attr_set.load() & bit)) {
-        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kSpmvSmem);
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, spmv_smem<T>());
         if (e != cudaSuccess) return e;
         attr_set.fetch_or(bit);
     }
     const int cap = ctx->num_sms * (Epi::kReduce ? kSpmvCtasReduce : kSpmvCtasPerSm);
     const int grid = ts.num_groups < cap ? ts.num_groups : cap;
-    k<<<grid, kBlock, kSpmvSmem, ctx->stream>>>(A, tile_args(ts), x, epi, rc, normtype, ctx->d_flag);
+    k<<<grid, kBlock, spmv_smem<T>(), ctx->stream>>>(A, tile_args(ts), x, epi, rc, normtype, ctx->d_flag);
     ctx->launches++;
     return cudaGetLastError();
 }
@@ -421,7 +446,7 @@ inline RedCtx red_ctx(const mtjg_csr *A, const TileSet &ts)
 // Appends the product tiles of rows [row_begin, row_end) of a CSR (host row
 // pointers) to `tile_row` (first rows) / `tile_flags`.
 void plan_tiles(const int *rowptr, int row_begin, int row_end, int vec, std::vector<int> &tile_row,
-                std::vector<unsigned char> &tile_flags);
+                std::vector<unsigned char> &tile_flags, int nnz_cap = kTileNnz, int rows_cap = kTileRows);
 // Appends row-kernel tiles (kRowTile rows) of rows [row_begin, row_end).
 void plan_row_tiles(int row_begin, int row_end, std::vector<int> &tile_row, std::vector<unsigned char> &tile_flags);
 int choose_vec(int64_t nnz, int64_t n);

@@ -37,7 +37,7 @@ class Finished:
 
 class Server:
     def __init__(self, ctx: Context | None = None, max_systems=256, pool_rows=1 << 24, max_iter=100, rtol=1e-10,
-                 atol=1e-50, dtol=1e5, inner_rtol=1e-4, inner_max_iter=2000):
+                 atol=1e-50, dtol=1e5, inner_rtol=1e-6, inner_max_iter=2000):
         self.ctx = ctx or default_context()
         self._lib = self.ctx._lib
         cfg = L.ServerConfig()
