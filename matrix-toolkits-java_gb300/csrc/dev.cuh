@@ -41,14 +41,20 @@ __device__ __forceinline__ double jmax(double a, double b)
 // Acc slots: v[0], v[1] hold a vector norm (ONE/TWO: sum in v[0]; INFINITY:
 // max in v[0]; TWO_ROBUST: (scale, ssq) in v[0], v[1]); v[2], v[3] hold
 // plain sums (dot products).
+// Per-thread partial sums.  f[0] / f[1] are FP32 running sums that FP32
+// phases add into instead of slots 2 / 3: they reach the FP64 slots once per
+// thread and group (group_partial), so an FP32 dot product costs no FP64
+// conversion or add per row -- GB300's FP64 pipe is the narrow one.
 struct Acc {
     double v[kParts];
+    float f[2];
 };
 
 __device__ __forceinline__ void acc_zero(Acc &a)
 {
 #pragma unroll
     for (int i = 0; i < kParts; ++i) a.v[i] = 0.0;
+    a.f[0] = a.f[1] = 0.0f;
 }
 
 template <bool S>
@@ -191,6 +197,8 @@ __device__ __forceinline__ void block_reduce(Acc &a, int type, double *sm /* [kP
 template <int SLOTS>
 __device__ __forceinline__ void group_partial(Acc &a, int group, const RedCtx &rc, int type, double *sm)
 {
+    if constexpr ((SLOTS & kSlotD2) != 0) a.v[2] += (double)a.f[0];
+    if constexpr ((SLOTS & kSlotD3) != 0) a.v[3] += (double)a.f[1];
     block_reduce<SLOTS>(a, type, sm);
     if (threadIdx.x == 0) {
 #pragma unroll

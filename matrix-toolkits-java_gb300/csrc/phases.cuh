@@ -117,8 +117,8 @@ struct MxOuter {
             zf = rf * invdiag[i];
             z[i] = zf;
         }
-        a.v[2] += (double)(rf * zf);
-        a.v[3] += (double)(rf * rf);
+        a.f[0] = fmaf(rf, zf, a.f[0]);
+        a.f[1] = fmaf(rf, rf, a.f[1]);
     }
     __device__ void scalar(int sys, const Acc &s)
     {
@@ -180,7 +180,7 @@ struct MxQ {  // q = A32 p (FP32 row sums); alpha = rho / p.q
     __device__ void row(int i, int, float dd, float pi, Acc &a) const
     {
         q[i] = dd;
-        a.v[2] += (double)(pi * dd);
+        a.f[0] = fmaf(pi, dd, a.f[0]);
     }
     __device__ void scalar(int sys, const Acc &s)
     {
@@ -211,8 +211,8 @@ struct MxUpd {  // d += alpha p; rin -= alpha q; z = M rin; inner stopping test
             zf = rf * invdiag[i];
             z[i] = zf;
         }
-        a.v[2] += (double)(rf * zf);
-        a.v[3] += (double)(rf * rf);
+        a.f[0] = fmaf(rf, zf, a.f[0]);
+        a.f[1] = fmaf(rf, rf, a.f[1]);
     }
     __device__ void rows(int base, int end, int sys, Acc &a) const
     {
@@ -241,8 +241,8 @@ struct MxUpd {  // d += alpha p; rin -= alpha q; z = M rin; inner stopping test
                 zf = rf * iv[u];
                 z[i] = zf;
             }
-            a.v[2] += (double)(rf * zf);
-            a.v[3] += (double)(rf * rf);
+            a.f[0] = fmaf(rf, zf, a.f[0]);
+            a.f[1] = fmaf(rf, rf, a.f[1]);
         }
     }
     __device__ void scalar(int sys, const Acc &s)
