@@ -479,8 +479,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--only-spmv", action="store_true",
                     help="run only the CSR product loop (for profiling the product kernel)")
-    ap.add_argument("--workload", default="serve", choices=["serve", "poisson3d"],
-                    help="serve: the served request stream (headline); poisson3d: one CG + Jacobi system")
+    ap.add_argument("--workload", default="serve",
+                    choices=["serve", "poisson3d", "c4"] + sorted(CONFIGS),
+                    help="serve: the served request stream (headline); poisson3d: one CG + Jacobi system; "
+                         "c1/c2icc/c3gmres/c3bicg: the other single-system configurations; c4: the batch")
+    ap.add_argument("--batch-systems", type=int, default=4096)
     ap.add_argument("--serve-requests", type=int, default=1500)
     ap.add_argument("--serve-max-systems", type=int, default=256)
     ap.add_argument("--serve-pool-rows", type=int, default=1 << 25)
@@ -493,8 +496,12 @@ def main():
         return
     if args.workload == "serve":
         main_serve(args)
-    else:
+    elif args.workload == "poisson3d":
         main_poisson3d(args)
+    elif args.workload == "c4":
+        run_batch(args)
+    else:
+        run_config(args)
 
 
 def main_poisson3d(args):
@@ -734,6 +741,131 @@ def main_serve(args):
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
+    print(json.dumps(line))
+
+
+CONFIGS = {
+    # name: (matrix, seed, solver, preconditioner, max iterations)
+    "c1": (("poisson2d", 128), 1, "cg", "jacobi", 2000),
+    "c2icc": (("poisson3d", 128), 2, "cg", "icc", MAX_ITER),
+    "c3gmres": (("convdiff3d", 96), 3, "gmres", "ilu", MAX_ITER),
+    "c3bicg": (("convdiff3d", 96), 3, "bicgstab", "ilu", MAX_ITER),
+}
+
+
+def run_config(args):
+    """One of the other configurations: plain FP64 solves/s of one system,
+    device-resident (CUDA events on the library's stream), plus the
+    preconditioner's set-up time (setMatrix, host clock)."""
+    from mtjg import _lib as L
+    from mtjg import sparse, workloads
+
+    (kind, N), seed, sname, pname, max_iter = CONFIGS[args.workload]
+    lib = L.load()
+    ctx = sparse.Context(int(os.environ.get("LOCAL_RANK", "0")))
+    n, rp, ci, v = getattr(workloads, kind)(N)
+    A = sparse.CompRowMatrix(n, n, rp, ci, v, ctx)
+    b = A.mult(workloads.uniform(n, seed))
+    solver = {"cg": sparse.CG, "bicgstab": sparse.BiCGstab}[sname](n, ctx=ctx) if sname != "gmres" else \
+        sparse.GMRES(n, restart=30, ctx=ctx)
+    M = {"jacobi": lambda: sparse.DiagonalPreconditioner(n, ctx), "ilu": lambda: sparse.ILU(A),
+         "icc": lambda: sparse.ICC(A)}[pname]()
+    t0 = time.perf_counter()
+    M.setMatrix(A)
+    ctx.synchronize()
+    setup_s = time.perf_counter() - t0
+    solver.setPreconditioner(M)
+    solver.setIterationMonitor(sparse.DefaultIterationMonitor(max_iter, RTOL, 1e-50, 1e5))
+    solver._sync_monitor()
+    db, dx = C.c_void_p(), C.c_void_p()
+    lib.mtjg_dev_alloc(ctx.h, 8 * n, C.byref(db))
+    lib.mtjg_dev_alloc(ctx.h, 8 * n, C.byref(dx))
+    lib.mtjg_memcpy_h2d(ctx.h, db, b.ctypes.data_as(C.c_void_p), 8 * n)
+    zeros = np.zeros(n)
+    res = L.Result()
+    times = []
+    for i in range(args.warmup + args.steps):
+        lib.mtjg_memcpy_h2d(ctx.h, dx, zeros.ctypes.data_as(C.c_void_p), 8 * n)
+        lib.mtjg_ctx_event_record(ctx.h, 0)
+        code = lib.mtjg_solver_solve_dev(solver.h, A.h, db, dx, C.byref(res))
+        lib.mtjg_ctx_event_record(ctx.h, 1)
+        ms = C.c_float()
+        lib.mtjg_ctx_event_elapsed(ctx.h, 0, 1, C.byref(ms))
+        if code != 0:
+            raise RuntimeError(f"solve failed: {code} {L.last_error()}")
+        if i >= args.warmup:
+            times.append(ms.value)
+    xh = np.empty(n)
+    lib.mtjg_memcpy_d2h(ctx.h, xh.ctypes.data_as(C.c_void_p), dx, 8 * n)
+    ms = statistics.mean(times)
+    line = {"metric": "solves/s", "value": 1e3 / ms, "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"{sname} + {pname}, {kind} {N}, rtol 1e-10, x0 = 0", "n": n, "nnz": len(ci),
+                       "seed": seed},
+            "iterations": res.iterations, "final_rel_residual": float(np.linalg.norm(b - A.mult(xh)) / np.linalg.norm(b)),
+            "precond_setup_s": setup_s}
+    print(json.dumps(line))
+
+
+def run_batch(args):
+    """The batched configuration: 4096 random SPD Laplacians (n log-uniform
+    in [500, 50000]) in one block-diagonal batch, CG + Jacobi per system to
+    rtol 1e-10, FP64 and mixed precision; device-resident, CUDA events."""
+    from concurrent.futures import ThreadPoolExecutor
+    from mtjg import _lib as L
+    from mtjg import sparse, workloads
+
+    count = args.batch_systems
+    sizes = workloads.batch_sizes(count, 4)
+    with ThreadPoolExecutor(16) as ex:
+        systems = list(ex.map(lambda k: workloads.laplacian(int(sizes[k]), 4 + k), range(count)))
+    lib = L.load()
+    ctx = sparse.Context(int(os.environ.get("LOCAL_RANK", "0")))
+    A = sparse.BatchCompRowMatrix(systems, ctx)
+    nt = A.numRows()
+    b = np.concatenate([workloads.uniform(s[0], 100 + k) for k, s in enumerate(systems)])
+    db, dx = C.c_void_p(), C.c_void_p()
+    lib.mtjg_dev_alloc(ctx.h, 8 * nt, C.byref(db))
+    lib.mtjg_dev_alloc(ctx.h, 8 * nt, C.byref(dx))
+    lib.mtjg_memcpy_h2d(ctx.h, db, b.ctypes.data_as(C.c_void_p), 8 * nt)
+    zeros = np.zeros(nt)
+    out = {}
+    for mode in ("fp64", "mixed"):
+        solver = sparse.CG(nt, ctx=ctx)
+        M = sparse.DiagonalPreconditioner(nt, ctx)
+        M.setMatrix(A)
+        solver.setPreconditioner(M)
+        solver.setIterationMonitor(sparse.DefaultIterationMonitor(MAX_ITER if mode == "fp64" else 100, RTOL,
+                                                                  1e-50, 1e5))
+        if mode == "mixed":
+            solver.setMixedPrecision(True, args.inner_rtol, 2000)
+        solver._sync_monitor()
+        res = L.Result()
+        times = []
+        for i in range(args.warmup + args.steps):
+            lib.mtjg_memcpy_h2d(ctx.h, dx, zeros.ctypes.data_as(C.c_void_p), 8 * nt)
+            lib.mtjg_ctx_event_record(ctx.h, 0)
+            code = lib.mtjg_solver_solve_dev(solver.h, A.h, db, dx, C.byref(res))
+            lib.mtjg_ctx_event_record(ctx.h, 1)
+            ms = C.c_float()
+            lib.mtjg_ctx_event_elapsed(ctx.h, 0, 1, C.byref(ms))
+            if code not in (0, 1, 2, 3):
+                raise RuntimeError(f"batch solve failed: {code} {L.last_error()}")
+            if i >= args.warmup:
+                times.append(ms.value)
+        per = (L.Result * count)()
+        lib.mtjg_solver_batch_results(solver.h, per, count)
+        its = [per[k].iterations for k in range(count)]
+        out[mode] = {"ms": statistics.mean(times), "solves_s": count * 1e3 / statistics.mean(times),
+                     "converged": sum(1 for k in range(count) if per[k].status == 0),
+                     "max_iterations": max(its), "mean_iterations": float(np.mean(its))}
+    line = {"metric": "batched solves/s", "value": out["mixed"]["solves_s"], "unit": "solves/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": out["mixed"]["ms"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": f"batched: {count} random SPD Laplacians, n log-uniform [500, 50000], CG + Jacobi, "
+                                   "rtol 1e-10", "rows": nt, "nnz": int(A.rowptr[-1]), "seed": 4},
+            "fp64": out["fp64"], "mixed": out["mixed"], "mixed_vs_fp64": out["fp64"]["ms"] / out["mixed"]["ms"]}
     print(json.dumps(line))
 
 
