@@ -63,6 +63,44 @@ def _traffic(grid):
     return SPMV_TRAFFIC_128 if grid == N_GRID else None
 
 
+class Ranks:
+    """The replicas of a --gpus N run (one process per GPU, launched by
+    torch.distributed.run): a gloo group on the host for the barrier around
+    the timed region and for gathering each rank's numbers.  The data path
+    has no collective: every rank serves its own copy of the workload."""
+
+    def __init__(self):
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.dist = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def gather(self, obj):
+        if not self.dist:
+            return [obj]
+        objs = [None] * self.world
+        self.dist.all_gather_object(objs, obj)
+        return objs
+
+    def close(self):
+        if self.dist:
+            self.dist.destroy_process_group()
+            self.dist = None
+
+
+def replica_rate(objs, units, key="sec"):
+    """Whole-job rate of N replicas: all ranks' units over the slowest rank's time."""
+    return len(objs) * units / max(o[key] for o in objs)
+
+
 def _peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -533,15 +571,12 @@ def main_poisson3d(args):
         print(json.dumps(line))
         return
 
+    ranks = Ranks()
+    ranks.barrier()
     out = run_gpu(args)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("gloo")
-        objs = [None] * world
-        dist.all_gather_object(objs, out)
-        dist.destroy_process_group()
-    else:
-        objs = [out]
+    ranks.barrier()
+    objs = ranks.gather(out)
+    ranks.close()
     if rank != 0:
         return
     ms = max(o["ms_solve"] for o in objs)
@@ -658,8 +693,11 @@ def main_serve(args):
     # the single large system: plain FP64 CG + Jacobi and the CSR product roofline
     c2 = run_gpu(args)
     knobs = (args.serve_max_systems, args.serve_pool_rows, args.inner_rtol)
+    ranks = Ranks()
+    ranks.barrier()
     with ClockSampler(local) as clk:
         times, results, rhs, stats, launches = serve_backlog(ctx, mats, reqs, args.steps, args.warmup, *knobs)
+    ranks.barrier()
     # every served result: status and the FP64 true residual b - A x
     import scipy.sparse as sp
     worst, failed = 0.0, 0
@@ -682,18 +720,12 @@ def main_serve(args):
     value_rank = len(reqs) / sec
     plain_rate = len(plain) / sum(t for _, t, _ in plain)
     out = {"value": value_rank, "sec": sec, "e2e": open_loop["solves_s"], "plain": plain_rate, "c2": c2}
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("gloo")
-        objs = [None] * world
-        dist.all_gather_object(objs, out)
-        dist.destroy_process_group()
-    else:
-        objs = [out]
+    objs = ranks.gather(out)
+    ranks.close()
     if rank != 0:
         return
     sec_max = max(o["sec"] for o in objs)
-    value = world * len(reqs) / sec_max
+    value = replica_rate(objs, len(reqs))
     e2e = sum(o["e2e"] for o in objs)
     cpu = None
     if not args.no_cpu:
