@@ -29,6 +29,15 @@ __device__ __forceinline__ float fmac(float a, float b, float c)
         return fmaf(a, b, c);
 }
 
+// MTJ assigns a row sum only when it is nonzero (CompRowMatrix.mult,
+// S/CompRowMatrix.java:309-311), so a -0.0 sum leaves +0.0 behind.  Done on
+// the bits: an FP64 compare would take an issue slot of the narrow FP64 pipe
+// for every row.
+__device__ __forceinline__ double mtj_assign(double d)
+{
+    return __double_as_longlong(d) == (long long)0x8000000000000000ULL ? 0.0 : d;
+}
+
 // java.lang.Math.max: NaN propagates.
 __device__ __forceinline__ double jmax(double a, double b)
 {

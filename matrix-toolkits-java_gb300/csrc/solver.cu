@@ -103,7 +103,7 @@ struct CgQ {  // q = A p; alpha = rho / p.q (:77-78)
     __device__ double init(int, int) const { return 0.0; }
     __device__ void row(int i, int, double d, double pi, Acc &a) const
     {
-        const double qq = d != 0.0 ? d : 0.0;
+        const double qq = mtj_assign(d);
         q[i] = qq;
         a.v[2] = fmac<S>(pi, qq, a.v[2]);
     }
@@ -289,7 +289,7 @@ struct BiV {  // v = A phat; alpha = rho_1 / rtilde.v (:98-99)
     __device__ double init(int, int) const { return 0.0; }
     __device__ void row(int i, int, double d, double, Acc &a) const
     {
-        const double vv = d != 0.0 ? d : 0.0;
+        const double vv = mtj_assign(d);
         v[i] = vv;
         a.v[2] = fmac<S>(rt[i], vv, a.v[2]);
     }
@@ -339,7 +339,7 @@ struct BiT {  // t = A shat; omega = t.s / t.t (:107-108)
     __device__ double init(int, int) const { return 0.0; }
     __device__ void row(int i, int, double d, double, Acc &a) const
     {
-        const double tt = d != 0.0 ? d : 0.0;
+        const double tt = mtj_assign(d);
         t[i] = tt;
         a.v[2] = fmac<S>(tt, s[i], a.v[2]);
         a.v[3] = fmac<S>(tt, tt, a.v[3]);
@@ -445,7 +445,7 @@ struct GmAv {
     static constexpr bool kNeedsXr = false;
     __device__ bool active(int sys) const { return st[sys].gate == ST_RUNNING; }
     __device__ double init(int, int) const { return 0.0; }
-    __device__ void row(int i, int, double d, double, Acc &) const { u[i] = d != 0.0 ? d : 0.0; }
+    __device__ void row(int i, int, double d, double, Acc &) const { u[i] = mtj_assign(d); }
     __device__ void scalar(int, const Acc &) {}
 };
 

@@ -310,7 +310,7 @@ struct EpiMult {
     static constexpr bool kNeedsXr = false;
     __device__ bool active(int) const { return true; }
     __device__ double init(int, int) const { return 0.0; }
-    __device__ void row(int r, int, double d, double, Acc &) const { y[r] = d != 0.0 ? d : 0.0; }
+    __device__ void row(int r, int, double d, double, Acc &) const { y[r] = mtj_assign(d); }
     __device__ void scalar(int, const Acc &) {}
 };
 

@@ -29,8 +29,15 @@ namespace mtjg {
 // Shared-memory stage of one tile, per value type.  FP32 tiles may hold 1.5x
 // the entries and 2x the rows of FP64 tiles in about the same bytes (tiles
 // planned for FP64 always fit an FP32 stage).
-constexpr int kTileNnz32 = kTileNnz * 3 / 2;
-constexpr int kTileRows32 = 2 * kTileRows;
+#ifndef MTJG_TILE_NNZ32
+#define MTJG_TILE_NNZ32 (MTJG_TILE_NNZ * 3 / 2)
+#endif
+#ifndef MTJG_TILE_ROWS32
+#define MTJG_TILE_ROWS32 (2 * MTJG_TILE_ROWS)
+#endif
+constexpr int kTileNnz32 = MTJG_TILE_NNZ32;
+constexpr int kTileRows32 = MTJG_TILE_ROWS32;
+static_assert(kTileNnz32 >= kTileNnz && kTileRows32 >= kTileRows, "FP64 tiles must fit an FP32 stage");
 constexpr int round16(int b) { return ((b + 15) / 16) * 16; }
 template <class T>
 struct Stage {
