@@ -218,10 +218,11 @@ struct ProdTables {
     std::vector<int> row, rend, nz, nzend, sys, grp, ginfo, sysg{0};
     std::vector<unsigned char> flags;
     int vec_mask = 0;
+    int group_div = 4096;  // a system of T tiles forms groups of clamp(T / group_div, 1, kGroupTiles) tiles
     void add(const ProdTiles &mt, int s)
     {
         const int T = (int)mt.row.size(), t0 = (int)row.size();
-        const int gs = std::max(1, std::min(kGroupTiles, T / 4096));  // as for an uploaded CSR
+        const int gs = std::max(1, std::min(kGroupTiles, T / group_div));
         for (int k = 0; k < T; ++k) {
             if (k % gs == 0) {
                 ginfo.push_back((s << 8) | (mt.flags[k] >> 1));
@@ -245,6 +246,9 @@ int rebuild_tiles(mtjg_server *S, int par)
 {
     const int ns = S->cfg.max_systems;
     ProdTables p64, p32;
+    // the served batch spreads over its many systems, so the FP32 tiling (the
+    // inner iterations) takes larger groups: fewer block-wide reductions
+    p32.group_div = 64;
     std::vector<int> rrow, rrend, rsys, rgrp, rsysg{0};
     for (int s = 0; s < ns; ++s) {
         const Req *r = S->slot_req[s];

@@ -120,8 +120,11 @@ __global__ void __launch_bounds__(kBlock, Epi::kReduce ? kSpmvCtasReduce : kSpmv
     __shared__ __align__(8) uint64_t bar[NST];
     __shared__ double red_sm[kParts * kBlock];
     __shared__ T s_long[kBlock / 32];
+    __shared__ unsigned s_done[NST];    // warps done with the tile in stage i
+    __shared__ unsigned s_issued[NST];  // copies issued into stage i
+    __shared__ int s_abort;
 
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31;
     const int G = gridDim.x, NG = ta.num_groups;
     if (tid == 0) {
 #pragma unroll
@@ -191,9 +194,13 @@ __global__ void __launch_bounds__(kBlock, Epi::kReduce ? kSpmvCtasReduce : kSpmv
         bulk_g2s(srow(s), m.rowptr + p0, pb, &bar[s]);
     };
 
-    // The k-th tile of the block's walk lives in stage k % NST; the copy of
-    // tile k + NST - 1 is issued while tile k is summed.  All decisions below
-    // are uniform over the block (the walk and staged() read global tables).
+    // The k-th tile of the block's walk lives in stage k % NST.  The first
+    // NST tiles are issued up front; after that the last warp to finish the
+    // tile in stage s issues the tile NST further on into s, so warps never
+    // wait for each other between tiles (only at group ends, for the block
+    // reduction).  The walk and staged() read global tables and are uniform
+    // over the block.
+    constexpr int NW = kBlock / 32;
     auto advance = [&](int &gg, int &tt) {
         ++tt;
         if (tt >= ta.group_tile[gg + 1]) {
@@ -201,32 +208,34 @@ __global__ void __launch_bounds__(kBlock, Epi::kReduce ? kSpmvCtasReduce : kSpmv
             tt = gg < NG ? ta.group_tile[gg] : 0;
         }
     };
-    unsigned phase = 0u;    // bit i: parity of stage i's next completion
-    unsigned pending = 0u;  // bit i: a copy into stage i is in flight
-    int s = 0;
+    if (tid == 0) {
+#pragma unroll
+        for (int i = 0; i < NST; ++i) s_done[i] = s_issued[i] = 0u;
+        s_abort = 0;
+    }
     // (g, t): the current group and tile; (pg, pt): the next tile to issue
     int g = next_group(blockIdx.x);
     int t = g < NG ? ta.group_tile[g] : 0;
-    int pg = g, pt = t, si = 0;
-    for (int k = 0; k < NST - 1 && pg < NG; ++k) {
-        if (staged(pt)) {
-            if (tid == 0) issue(pt, si);
-            pending |= 1u << si;
+    int pg = g, pt = t;
+    __syncthreads();
+    for (int k = 0; k < NST && pg < NG; ++k) {
+        if (tid == 0 && staged(pt)) {
+            s_issued[k] += 1u;
+            issue(pt, k);
         }
-        si = si + 1 == NST ? 0 : si + 1;
         advance(pg, pt);
     }
+    // bit i: parity of the copies of stage i this thread has waited for (and
+    // so of stage i's next completion).  A copy into a stage is issued only
+    // after every warp is done with the stage's previous tile, so a thread is
+    // at most one copy behind s_issued[i]; the parities tell which.
+    unsigned phase = 0u;
+    bool skip = false;  // a copy never completed: walk on without work, drain, stop
+    int s = 0;
+    __syncthreads();
     Acc acc;
     acc_zero(acc);
     while (g < NG) {
-        if (pg < NG) {  // into the stage freed at the end of the last turn
-            if (staged(pt)) {
-                if (tid == 0) issue(pt, si);
-                pending |= 1u << si;
-            }
-            si = si + 1 == NST ? 0 : si + 1;
-            advance(pg, pt);
-        }
         // the tile after t in this block's walk
         int gn = g, tn = t;
         advance(gn, tn);
@@ -236,18 +245,24 @@ __global__ void __launch_bounds__(kBlock, Epi::kReduce ? kSpmvCtasReduce : kSpmv
         const MatView mv = view(t);
         const T *xs = x + mv.voff;
         const int vgo = mv.voff;
-        if (staged(t)) {
-            const bool ok = mbar_wait_bounded(&bar[s], (phase >> s) & 1u, kWaitLimit);
-            if (__syncthreads_or(!ok)) {
-                // a copy never completed: report, drain what is in flight, stop
-                if (tid == 0) atomicExch(err, 1);
-#pragma unroll
-                for (int i = 0; i < NST; ++i)
-                    if (pending & (1u << i)) mbar_wait_bounded(&bar[i], (phase >> i) & 1u, kWaitLimit);
-                return;
+        if (!skip && staged(t)) {
+            bool ok = false;
+            for (long long i = 0; i < kWaitLimit; ++i) {
+                if (mbar_try_wait(&bar[s], (phase >> s) & 1u)) {
+                    ok = true;
+                    break;
+                }
+                if ((i & 1023) == 1023 && *(volatile int *)&s_abort) break;
             }
-            phase ^= 1u << s;
-            pending &= ~(1u << s);
+            if (ok) phase ^= 1u << s;
+            // the warp skips together (the lane shuffles below need all lanes)
+            if (!__all_sync(0xffffffffu, ok)) {
+                *(volatile int *)&s_abort = 1;
+                if (lane == 0) atomicExch(err, 1);
+                skip = true;
+            }
+        }
+        if (!skip && staged(t)) {
             const T *sv = sval(s);
             const int *sc = scol(s);
             const int *sr = srow(s);
@@ -289,7 +304,7 @@ __global__ void __launch_bounds__(kBlock, Epi::kReduce ? kSpmvCtasReduce : kSpmv
                     if (r < r1 && l == 0) epi.row(vgo + r, sys, sum, Epi::kNeedsXr ? __ldg(xs + r) : T(0), acc);
                 }
             }
-        } else {
+        } else if (!staged(t)) {
             // a single row longer than a stage: straight from global memory
             const int r = r0;
             const int b = mv.rowptr[r], e = mv.rowptr[r + 1];
@@ -311,6 +326,21 @@ __global__ void __launch_bounds__(kBlock, Epi::kReduce ? kSpmvCtasReduce : kSpmv
             }
             if (tid == 0) epi.row(vgo + r, sys, sum, Epi::kNeedsXr ? __ldg(xs + r) : T(0), acc);
         }
+        // release stage s: the last warp done with it issues the tile NST on
+        __syncwarp();
+        if (lane == 0) {
+            __threadfence_block();
+            const unsigned c = atomicAdd(&s_done[s], 1u);
+            if (c == NW - 1) {
+                s_done[s] = 0u;
+                __threadfence_block();
+                if (pg < NG && staged(pt) && !*(volatile int *)&s_abort) {
+                    s_issued[s] += 1u;
+                    issue(pt, s);
+                }
+            }
+        }
+        if (pg < NG) advance(pg, pt);
         if (gn != g) {
             // the group is complete
             if constexpr (Epi::kReduce) {
@@ -318,10 +348,18 @@ __global__ void __launch_bounds__(kBlock, Epi::kReduce ? kSpmvCtasReduce : kSpmv
                 acc_zero(acc);
             }
         }
-        __syncthreads();  // stage s is free for the copy issued next turn
         s = s + 1 == NST ? 0 : s + 1;
         g = gn;
         t = tn;
+    }
+    __syncthreads();  // every thread has left the walk: s_abort and s_issued are final
+    if (*(volatile int *)&s_abort) {
+        // wait (bounded) for every copy this thread has not waited for, so
+        // none lands in shared memory after the block has left (no copy is
+        // issued once s_abort is set)
+#pragma unroll
+        for (int i = 0; i < NST; ++i)
+            if ((s_issued[i] & 1u) != ((phase >> i) & 1u)) mbar_wait_bounded(&bar[i], (phase >> i) & 1u, kWaitLimit);
     }
 }
 
