@@ -147,7 +147,9 @@ MTJG_API int mtjg_csr_upload(mtjg_ctx *ctx, int num_rows, int num_cols,
  * range (checked).  Solving it with a CG or BiCGstab solver of size
  * sys_rows[num_systems] runs every system in the same launches, each with
  * its own scalars and DefaultIterationMonitor; a system's results do not
- * depend on the other systems of the batch.  No reference counterpart: MTJ
+ * depend on the other systems of the batch (they equal a batch of that one
+ * system; a batch groups its dot products in larger blocks than a lone
+ * mtjg_csr_upload, so results differ from that by rounding).  No reference counterpart: MTJ
  * solves one system per call (IterativeSolver.solve, S/IterativeSolver.java:30-44). */
 MTJG_API int mtjg_batch_upload(mtjg_ctx *ctx, int num_systems, const int *sys_rows, const int *rowptr,
                                const int *colind, const double *val, mtjg_csr **out);

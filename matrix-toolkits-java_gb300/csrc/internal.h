@@ -58,7 +58,19 @@ constexpr int kParts = 4;             // partial-sum slots per group
 // of kRowsPerThread * kBlock rows.  Few block-wide reductions matter on
 // GB300, whose FP64 pipe is narrow: a tree over 256 threads costs more FP64
 // issue slots than the vector work of 256 rows.
-constexpr int kGroupTiles = 8;        // at most; see group_size_for
+constexpr int kGroupTiles = 8;        // at most
+#ifndef MTJG_GROUP_DIV
+#define MTJG_GROUP_DIV 4096
+#endif
+// A system of T product tiles forms groups of clamp(T / kGroupDiv, 1,
+// kGroupTiles) tiles: a function of the system alone, so its sums are the
+// same alone and in any batch.
+constexpr int kGroupDiv = MTJG_GROUP_DIV;
+// Systems of a batch (mtjg_batch_upload) and of the server's FP32 tiling
+// divide by this instead: a batch fills the GPU with many systems, so fewer,
+// larger groups (fewer block-wide reductions) cost it no parallelism.  A
+// system's sums are then the same in any batch, and in a batch of one.
+constexpr int kBatchGroupDiv = 64;
 constexpr int kRowsPerThread = 4;
 constexpr int kRowTile = kBlock * kRowsPerThread;
 

@@ -248,7 +248,7 @@ int rebuild_tiles(mtjg_server *S, int par)
     ProdTables p64, p32;
     // the served batch spreads over its many systems, so the FP32 tiling (the
     // inner iterations) takes larger groups: fewer block-wide reductions
-    p32.group_div = 64;
+    p32.group_div = kBatchGroupDiv;
     std::vector<int> rrow, rrend, rsys, rgrp, rsysg{0};
     for (int s = 0; s < ns; ++s) {
         const Req *r = S->slot_req[s];

@@ -52,20 +52,20 @@ void plan_row_tiles(int row_begin, int row_end, std::vector<int> &tile_row, std:
 
 int upload_tiles(TileSet &ts, const std::vector<int> &tile_row, const std::vector<unsigned char> &tile_flags,
                  const std::vector<int> *tile_sys, const std::vector<int> &sys_tile, int vec, const int *rowptr,
-                 int group_size)
+                 int group_size, int group_div)
 {
     free_tiles(ts);
     ts.num_tiles = (int)tile_flags.size();
     ts.num_sys = (int)sys_tile.size() - 1;
     // reduction groups: runs of consecutive tiles inside each system.  A
-    // system of T tiles uses groups of min(group_size, T / 4096) tiles (at
+    // system of T tiles uses groups of min(group_size, T / kGroupDiv) tiles (at
     // least 1): large systems amortise the block reduction over several
     // tiles while keeping thousands of groups for the CTAs to share evenly;
     // the size depends on the system alone, never on the rest of a batch.
     std::vector<int> group_tile, sys_group = {0};
     for (int s = 0; s < ts.num_sys; ++s) {
         const int t0 = sys_tile[s], t1 = sys_tile[s + 1];
-        const int gs = std::max(1, std::min(group_size, (t1 - t0) / 4096));
+        const int gs = std::max(1, std::min(group_size, (t1 - t0) / group_div));
         for (int t = t0; t < t1; t += gs) group_tile.push_back(t);
         sys_group.push_back((int)group_tile.size());
     }
@@ -449,8 +449,11 @@ static int csr_upload_impl(mtjg_ctx *ctx, int n, int m, const int *rowptr, const
     }
     tile_row.push_back(n);
     rtile_row.push_back(n);
+    // a batch (mtjg_batch_upload, any number of systems) spreads over its
+    // systems, so its systems take larger reduction groups than a lone
+    // uploaded CSR, which needs many groups to fill the GPU by itself
     st = upload_tiles(A->tiles, tile_row, tile_flags, sys_rows ? &tile_sys : nullptr, sys_tile, vec, rowptr,
-                      kGroupTiles);
+                      kGroupTiles, sys_rows ? kBatchGroupDiv : kGroupDiv);
     if (st != MTJG_OK) return bail(st);
     st = upload_tiles(A->rtiles, rtile_row, rtile_flags, sys_rows ? &rtile_sys : nullptr, rsys_tile, 1, nullptr, 1);
     if (st != MTJG_OK) return bail(st);

@@ -501,7 +501,7 @@ int choose_vec(int64_t nnz, int64_t n);
 // tiles).
 int upload_tiles(TileSet &ts, const std::vector<int> &tile_row, const std::vector<unsigned char> &tile_flags,
                  const std::vector<int> *tile_sys, const std::vector<int> &sys_tile, int vec, const int *rowptr,
-                 int group_size);
+                 int group_size, int group_div = kGroupDiv);
 void free_tiles(TileSet &ts);
 // Device exclusive scan of n ints into out[0..n] (out[n] = total).
 int exclusive_scan(mtjg_ctx *ctx, const int *in, int *out, int n);

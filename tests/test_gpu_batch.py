@@ -1,7 +1,8 @@
 """Batched solves: many independent systems in the same launches.
 
 Each system's iterate, iteration count and residual history must be
-bit-identical to solving that system alone, and independent of the batch's
+bit-identical to solving that system alone (as a batch of one), and
+independent of the batch's
 composition and order; and each must match the oracle (iterations +-2,
 relative residual history within 1e-10 of r_0).
 """
@@ -35,7 +36,9 @@ def _rhs(systems):
 
 
 def _solo(ctx, n, rp, ci, v, b, pc, max_iter):
-    A = sparse.CompRowMatrix(n, n, rp, ci, v, ctx)
+    # alone = a batch of one (a batch's systems take the batch grouping of
+    # their reductions, which depends on the system only)
+    A = sparse.BatchCompRowMatrix([(n, rp, ci, v)], ctx)
     s = sparse.CG(n, ctx=ctx)
     if pc:
         M = sparse.DiagonalPreconditioner(n, ctx)

@@ -65,7 +65,7 @@ def test_mixed_batch_equals_solo(ctx):
     x = np.zeros(nt)
     res = s.solveBatch(A, np.concatenate(bs), x)
     for k, (n, rp, ci, v) in enumerate(systems):
-        As = sparse.CompRowMatrix(n, n, rp, ci, v, ctx)
+        As = sparse.BatchCompRowMatrix([(n, rp, ci, v)], ctx)  # alone: a batch of one
         ss = _mixed_solver(ctx, As, n, True)
         xs = np.zeros(n)
         ss.solve(As, bs[k], xs)
