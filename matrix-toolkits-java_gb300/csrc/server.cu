@@ -58,7 +58,17 @@ struct ResMat {
     mtjg_precond *J = nullptr;      // Jacobi (its invdiag)
     float *invdiag32 = nullptr;
     ProdTiles t64, t32;  // product tiles for FP64 and FP32 values (local rows and entries)
+    int uses = 0;          // requests submitted and not yet delivered (under the server lock)
+    bool removed = false;  // mtjg_server_remove_matrix: freed once uses reaches 0
 };
+
+void free_matrix(ResMat *m)
+{
+    mtjg_precond_destroy(m->J);
+    mtjg_csr_destroy(m->A);
+    cudaFree(m->invdiag32);
+    delete m;
+}
 
 struct Req {
     int64_t ticket = 0;
@@ -402,6 +412,12 @@ int deliver(mtjg_server *S, std::vector<Retired> &staged, int par)
         std::memcpy(f.r->x_out, S->h_x + f.r->voff, sizeof(double) * (size_t)f.r->mat->n);
         f.out.latency_s = tn - f.r->t_submit;
         S->done.push_back(f.out);
+        ResMat *m = S->mats[f.r->mid];
+        if (--m->uses == 0 && m->removed) {
+            // its last request is out; no queued chunk reads a retired system's matrix
+            free_matrix(m);
+            S->mats[f.r->mid] = nullptr;
+        }
         delete f.r;
     }
     S->inflight -= (int64_t)staged.size();
@@ -705,12 +721,14 @@ extern "C" int mtjg_server_submit(mtjg_server *S, int matrix_id, const double *b
             delete r;
             return fail(S->error, S->error_msg);
         }
-        if (matrix_id < 0 || matrix_id >= (int)S->mats.size()) {
+        if (matrix_id < 0 || matrix_id >= (int)S->mats.size() || !S->mats[matrix_id] ||
+            S->mats[matrix_id]->removed) {
             delete r;
-            return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "unknown matrix id");
+            return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "unknown or removed matrix id");
         }
         r->mid = matrix_id;
         r->mat = S->mats[matrix_id];
+        S->mats[matrix_id]->uses++;
         const int n = r->mat->n;
         r->b.assign(b, b + n);
         if (x0) r->x0.assign(x0, x0 + n);
@@ -722,6 +740,21 @@ extern "C" int mtjg_server_submit(mtjg_server *S, int matrix_id, const double *b
         S->inflight++;
     }
     S->cv.notify_one();
+    return MTJG_OK;
+}
+
+extern "C" int mtjg_server_remove_matrix(mtjg_server *S, int matrix_id)
+{
+    if (!S) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL server");
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (matrix_id < 0 || matrix_id >= (int)S->mats.size() || !S->mats[matrix_id] || S->mats[matrix_id]->removed)
+        return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "unknown or removed matrix id");
+    ResMat *m = S->mats[matrix_id];
+    m->removed = true;
+    if (m->uses == 0) {
+        free_matrix(m);
+        S->mats[matrix_id] = nullptr;
+    }
     return MTJG_OK;
 }
 
@@ -794,12 +827,8 @@ extern "C" int mtjg_server_destroy(mtjg_server *S)
     cudaStreamSynchronize(S->ctx->stream);
     for (Req *r : S->pending) delete r;
     for (Req *r : S->slot_req) delete r;
-    for (ResMat *m : S->mats) {
-        mtjg_precond_destroy(m->J);
-        mtjg_csr_destroy(m->A);
-        cudaFree(m->invdiag32);
-        delete m;
-    }
+    for (ResMat *m : S->mats)
+        if (m) free_matrix(m);
     cudaFree(S->b64);
     cudaFree(S->x64);
     cudaFree(S->d32);

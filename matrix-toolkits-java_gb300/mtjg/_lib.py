@@ -113,6 +113,7 @@ PROTOTYPES = {
     "mtjg_server_config_defaults": (None, [C.POINTER(ServerConfig)]),
     "mtjg_server_create": (C.c_int, [_vp, C.POINTER(ServerConfig), C.POINTER(_vp)]),
     "mtjg_server_add_matrix": (C.c_int, [_vp, C.c_int, _ip, _ip, _dp, _ip]),
+    "mtjg_server_remove_matrix": (C.c_int, [_vp, C.c_int]),
     "mtjg_server_submit": (C.c_int, [_vp, C.c_int, _dp, _dp, _dp, C.POINTER(C.c_int64)]),
     "mtjg_server_poll": (C.c_int, [_vp, C.POINTER(ServerResult), C.c_int, _ip]),
     "mtjg_server_drain": (C.c_int, [_vp, C.c_double]),

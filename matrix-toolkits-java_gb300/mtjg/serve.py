@@ -59,6 +59,11 @@ class Server:
         self.sizes[mid.value] = int(n)
         return mid.value
 
+    def removeMatrix(self, mid: int):
+        """Releases a registered matrix (freed once its requests are reported)."""
+        _raise(self._lib.mtjg_server_remove_matrix(self.h, int(mid)), "remove_matrix")
+        self.sizes.pop(mid, None)
+
     def submit(self, mid: int, b, x0=None) -> int:
         n = self.sizes[mid]
         b = L.f64(b)

@@ -109,3 +109,21 @@ def test_unknown_matrix_is_rejected(servers):
     srv = servers(max_systems=4, pool_rows=1000)
     with pytest.raises(KeyError):
         srv.submit(5, np.zeros(3))
+
+
+def test_remove_matrix_while_its_requests_run(servers):
+    from mtjg import sparse
+    mats = [workloads.poisson2d(150), workloads.laplacian(2000, 6)]
+    srv = servers(max_systems=8, pool_rows=1 << 18)
+    mids = [srv.addMatrix(*m) for m in mats]
+    t = [srv.submit(mids[0], workloads.uniform(22500, 70 + k)) for k in range(3)]
+    srv.removeMatrix(mids[0])  # its three requests still finish
+    with pytest.raises(KeyError):
+        srv.submit(mids[0], workloads.uniform(22500, 1))
+    with pytest.raises(sparse.IllegalArgumentException):  # removed twice
+        srv.removeMatrix(mids[0])
+    u = srv.submit(mids[1], workloads.uniform(2000, 5))
+    srv.drain(120.0)
+    res = {r.ticket: r for r in srv.poll()}
+    assert all(res[k].status == 0 for k in t + [u])
+    srv.removeMatrix(mids[1])  # nothing outstanding: freed at once
