@@ -56,7 +56,7 @@ MAX_ITER = 5000
 # DRAM bytes (read + write) of one k_spmv launch of CompRowMatrix.mult on the
 # 3D Poisson 128^3 matrix, from one ncu capture (dram__bytes_read.sum +
 # dram__bytes_write.sum); the algorithmic bytes of that launch are 216.92 MB
-SPMV_TRAFFIC_128 = 212.05e6
+SPMV_TRAFFIC_128 = 212.32e6
 
 
 def _traffic(grid):
@@ -523,8 +523,8 @@ def main():
                          "c1/c2icc/c3gmres/c3bicg: the other single-system configurations; c4: the batch")
     ap.add_argument("--batch-systems", type=int, default=4096)
     ap.add_argument("--serve-requests", type=int, default=1500)
-    ap.add_argument("--serve-max-systems", type=int, default=256)
-    ap.add_argument("--serve-pool-rows", type=int, default=1 << 25)
+    ap.add_argument("--serve-max-systems", type=int, default=512)
+    ap.add_argument("--serve-pool-rows", type=int, default=1 << 26)
     ap.add_argument("--inner-rtol", type=float, default=1e-6)
     ap.add_argument("--plain-budget", type=float, default=8.0, help="seconds of plain FP64 one-at-a-time solves")
     ap.add_argument("--ref-seconds", type=float, default=6.0, help="reference arm: seconds of work per step")

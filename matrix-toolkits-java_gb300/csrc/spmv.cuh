@@ -107,6 +107,21 @@ __device__ __forceinline__ int tile_system(const TileArgs &ta, int t)
     return ta.tile_sys ? ta.tile_sys[t] : 0;
 }
 
+// A staged tile as its copies and its rows need it: the CSR it reads (its
+// system's own, for a served batch), its rows and entries, and where its
+// rows sit in the vectors.
+template <class T>
+struct TileDesc {
+    const T *val;
+    const int *colind;
+    const int *rowptr;
+    int r0, r1;    // rows [r0, r1) of the matrix
+    int nz0, nz1;  // entries [nz0, nz1)
+    int voff;      // vector index of row 0
+    int sys;
+    int staged;
+};
+
 // Kernels and launchers are private to each translation unit (see k_finalize).
 namespace {
 
@@ -123,6 +138,13 @@ __global__ void __launch_bounds__(kBlock, Epi::kReduce ? kSpmvCtasReduce : kSpmv
     __shared__ unsigned s_done[NST];    // warps done with the tile in stage i
     __shared__ unsigned s_issued[NST];  // copies issued into stage i
     __shared__ int s_abort;
+    // s_hdr[i]: the tile whose copies were issued into stage i, written
+    // before the copies (the mbarrier's completion publishes it with them);
+    // s_next: the next tile to issue, prepared one issue ahead so that the
+    // dependent table loads behind it (tile -> system -> its CSR) stay off
+    // the path from a freed stage to its next copy
+    __shared__ TileDesc<T> s_hdr[NST];
+    __shared__ TileDesc<T> s_next;
 
     const int tid = threadIdx.x, lane = tid & 31;
     const int G = gridDim.x, NG = ta.num_groups;
@@ -176,30 +198,50 @@ __global__ void __launch_bounds__(kBlock, Epi::kReduce ? kSpmvCtasReduce : kSpmv
         }
         return MatView{A.rowptr, A.colind, A.val, 0};
     };
-    // tile t's row pointers, values and columns, rounded out to 16 bytes
-    // (the arrays carry the padding this reads past their ends)
-    auto issue = [&](int t, int s) {
+    // tile t from the global tables
+    auto prepare = [&](int t) {
         const MatView m = view(t);
-        const int nz0 = ta.tile_nz[t], nz1 = ta.tile_nz_end[t];
-        const int r0 = ta.tile_row[t], r1 = ta.tile_row_end[t];
-        const int v0 = nz0 & ~(kVA - 1), v1 = (nz1 + kVA - 1) & ~(kVA - 1);
-        const int c0 = nz0 & ~3, c1 = (nz1 + 3) & ~3;
-        const int p0 = r0 & ~3, p1 = (r1 + 1 + 3) & ~3;
+        TileDesc<T> d;
+        d.val = m.val;
+        d.colind = m.colind;
+        d.rowptr = m.rowptr;
+        d.r0 = ta.tile_row[t];
+        d.r1 = ta.tile_row_end[t];
+        d.nz0 = ta.tile_nz[t];
+        d.nz1 = ta.tile_nz_end[t];
+        d.voff = m.voff;
+        d.sys = tile_system(ta, t);
+        d.staged = staged(t) ? 1 : 0;
+        return d;
+    };
+    // the staged tile d's row pointers, values and columns into stage s,
+    // rounded out to 16 bytes (the arrays carry the padding this reads past
+    // their ends), after its header
+    auto issue = [&](const TileDesc<T> &d, int s) {
+        s_hdr[s] = d;
+        const int v0 = d.nz0 & ~(kVA - 1), v1 = (d.nz1 + kVA - 1) & ~(kVA - 1);
+        const int c0 = d.nz0 & ~3, c1 = (d.nz1 + 3) & ~3;
+        const int p0 = d.r0 & ~3, p1 = (d.r1 + 1 + 3) & ~3;
         const unsigned vb = (unsigned)(v1 - v0) * (unsigned)sizeof(T), cb = (unsigned)(c1 - c0) * 4u,
                        pb = (unsigned)(p1 - p0) * 4u;
         fence_proxy_async();
         mbar_arrive_expect_tx(&bar[s], vb + cb + pb);
-        if (vb) bulk_g2s(sval(s), m.val + v0, vb, &bar[s]);
-        if (cb) bulk_g2s(scol(s), m.colind + c0, cb, &bar[s]);
-        bulk_g2s(srow(s), m.rowptr + p0, pb, &bar[s]);
+        if (vb) bulk_g2s(sval(s), d.val + v0, vb, &bar[s]);
+        if (cb) bulk_g2s(scol(s), d.colind + c0, cb, &bar[s]);
+        bulk_g2s(srow(s), d.rowptr + p0, pb, &bar[s]);
     };
 
     // The k-th tile of the block's walk lives in stage k % NST.  The first
     // NST tiles are issued up front; after that the last warp to finish the
-    // tile in stage s issues the tile NST further on into s, so warps never
-    // wait for each other between tiles (only at group ends, for the block
-    // reduction).  The walk and staged() read global tables and are uniform
-    // over the block.
+    // tile in stage s issues the tile NST further on into s (from s_next),
+    // so warps never wait for each other between tiles (only at group ends,
+    // for the block reduction).  The walk and staged() read global tables
+    // and are uniform over the block; a staged tile's rows come from its
+    // stage header.
+    //
+    // s_next is handed from issuer to issuer: the issuer of the tile for
+    // stage s writes it before its release of the stage after s, and the
+    // next issuer is the last warp to release that stage, so it sees it.
     constexpr int NW = kBlock / 32;
     auto advance = [&](int &gg, int &tt) {
         ++tt;
@@ -221,10 +263,11 @@ __global__ void __launch_bounds__(kBlock, Epi::kReduce ? kSpmvCtasReduce : kSpmv
     for (int k = 0; k < NST && pg < NG; ++k) {
         if (tid == 0 && staged(pt)) {
             s_issued[k] += 1u;
-            issue(pt, k);
+            issue(prepare(pt), k);
         }
         advance(pg, pt);
     }
+    if (tid == 0 && pg < NG) s_next = prepare(pt);
     // bit i: parity of the copies of stage i this thread has waited for (and
     // so of stage i's next completion).  A copy into a stage is issued only
     // after every warp is done with the stage's previous tile, so a thread is
@@ -239,13 +282,8 @@ __global__ void __launch_bounds__(kBlock, Epi::kReduce ? kSpmvCtasReduce : kSpmv
         // the tile after t in this block's walk
         int gn = g, tn = t;
         advance(gn, tn);
-        const int sys = tile_system(ta, t);
-        const int r0 = ta.tile_row[t], r1 = ta.tile_row_end[t];
-        // rows r are the matrix's own; vectors are indexed at vo + r
-        const MatView mv = view(t);
-        const T *xs = x + mv.voff;
-        const int vgo = mv.voff;
-        if (!skip && staged(t)) {
+        const bool st = staged(t);
+        if (!skip && st) {
             bool ok = false;
             for (long long i = 0; i < kWaitLimit; ++i) {
                 if (mbar_try_wait(&bar[s], (phase >> s) & 1u)) {
@@ -262,11 +300,14 @@ __global__ void __launch_bounds__(kBlock, Epi::kReduce ? kSpmvCtasReduce : kSpmv
                 skip = true;
             }
         }
-        if (!skip && staged(t)) {
+        if (!skip && st) {
+            // rows r are the matrix's own; vectors are indexed at vgo + r
+            const TileDesc<T> &h = s_hdr[s];
+            const int r0 = h.r0, r1 = h.r1, sys = h.sys, vgo = h.voff, nzb = h.nz0;
+            const T *xs = x + vgo;
             const T *sv = sval(s);
             const int *sc = scol(s);
             const int *sr = srow(s);
-            const int nzb = ta.tile_nz[t];
             const int vo = nzb & ~(kVA - 1), co = nzb & ~3, po = r0 & ~3;
             if constexpr (VEC == 1) {
                 for (int r = r0 + tid; r < r1; r += kBlock) {
@@ -304,9 +345,13 @@ __global__ void __launch_bounds__(kBlock, Epi::kReduce ? kSpmvCtasReduce : kSpmv
                     if (r < r1 && l == 0) epi.row(vgo + r, sys, sum, Epi::kNeedsXr ? __ldg(xs + r) : T(0), acc);
                 }
             }
-        } else if (!staged(t)) {
+        } else if (!st) {
             // a single row longer than a stage: straight from global memory
-            const int r = r0;
+            const int sys = tile_system(ta, t);
+            const int r = ta.tile_row[t];
+            const MatView mv = view(t);
+            const T *xs = x + mv.voff;
+            const int vgo = mv.voff;
             const int b = mv.rowptr[r], e = mv.rowptr[r + 1];
             T sum = tid == 0 ? epi.init(vgo + r, sys) : T(0);
             if constexpr (S) {
@@ -334,9 +379,14 @@ __global__ void __launch_bounds__(kBlock, Epi::kReduce ? kSpmvCtasReduce : kSpmv
             if (c == NW - 1) {
                 s_done[s] = 0u;
                 __threadfence_block();
-                if (pg < NG && staged(pt) && !*(volatile int *)&s_abort) {
-                    s_issued[s] += 1u;
-                    issue(pt, s);
+                if (pg < NG && !*(volatile int *)&s_abort) {
+                    if (s_next.staged) {
+                        s_issued[s] += 1u;
+                        issue(s_next, s);
+                    }
+                    int qg = pg, qt = pt;
+                    advance(qg, qt);
+                    if (qg < NG) s_next = prepare(qt);
                 }
             }
         }
