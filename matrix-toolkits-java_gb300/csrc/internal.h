@@ -58,7 +58,10 @@ constexpr int kParts = 4;             // partial-sum slots per group
 // of kRowsPerThread * kBlock rows.  Few block-wide reductions matter on
 // GB300, whose FP64 pipe is narrow: a tree over 256 threads costs more FP64
 // issue slots than the vector work of 256 rows.
-constexpr int kGroupTiles = 8;        // at most
+#ifndef MTJG_GROUP_TILES
+#define MTJG_GROUP_TILES 8
+#endif
+constexpr int kGroupTiles = MTJG_GROUP_TILES;  // at most
 #ifndef MTJG_GROUP_DIV
 #define MTJG_GROUP_DIV 4096
 #endif
@@ -73,6 +76,14 @@ constexpr int kGroupDiv = MTJG_GROUP_DIV;
 constexpr int kBatchGroupDiv = 64;
 constexpr int kRowsPerThread = 4;
 constexpr int kRowTile = kBlock * kRowsPerThread;
+// A row tile of the vector phases (one block, one partial) is kRowPasses
+// passes of kRowTile rows: more passes spread one block-wide reduction over
+// more rows.
+#ifndef MTJG_ROW_PASSES
+#define MTJG_ROW_PASSES 2
+#endif
+constexpr int kRowPasses = MTJG_ROW_PASSES;
+constexpr int kRowTileRows = kRowTile * kRowPasses;
 
 // device status of a system (SysState::status)
 enum : int {

@@ -5,6 +5,11 @@
 
 #include "spmv.cuh"
 
+// resident blocks per SM the FP32 update of the inner solve is compiled for
+#ifndef MTJG_MXUPD_MINB
+#define MTJG_MXUPD_MINB 0
+#endif
+
 namespace mtjg {
 
 constexpr int kPcIdentity = 0, kPcJacobi = 1, kPcExternal = 2;
@@ -200,6 +205,7 @@ struct MxUpd {  // d += alpha p; rin -= alpha q; z = M rin; inner stopping test
     static constexpr int kSlots = kSlotD2 | kSlotD3;
     __device__ bool active(int sys) const { return st[sys].status == ST_RUNNING && st[sys].phase == 1; }
     static constexpr bool kBatched = true;
+    static constexpr int kMinBlocks = MTJG_MXUPD_MINB;
     __device__ void row(int i, int sys, Acc &a) const
     {
         const float al = (float)st[sys].in_alpha;

@@ -266,10 +266,10 @@ int rebuild_tiles(mtjg_server *S, int par)
             const ResMat *m = r->mat;
             p64.add(m->t64, s);
             p32.add(m->t32, s);
-            for (int row = 0; row < m->n; row += kRowTile) {
+            for (int row = 0; row < m->n; row += kRowTileRows) {
                 rgrp.push_back((int)rrow.size());
                 rrow.push_back(r->voff + row);
-                rrend.push_back(r->voff + std::min(m->n, row + kRowTile));
+                rrend.push_back(r->voff + std::min(m->n, row + kRowTileRows));
                 rsys.push_back(s);
             }
         }

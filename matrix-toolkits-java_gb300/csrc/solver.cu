@@ -14,6 +14,12 @@
 
 #include "phases.cuh"
 
+// resident blocks per SM the CG update is compiled for (it keeps four rows of
+// five FP64 vectors in flight per thread)
+#ifndef MTJG_CGUPD_MINB
+#define MTJG_CGUPD_MINB 4
+#endif
+
 namespace mtjg {
 
 int precond_apply_dev(mtjg_precond *M, const double *b, double *x, const int *status);
@@ -124,6 +130,7 @@ struct CgUpd {  // x += alpha p; r -= alpha q; next monitor test; fused z = M r,
     static constexpr bool kNeedsXr = false;
     static constexpr int kSlots = kSlotNorm | kSlotD2;
     static constexpr bool kBatched = true;
+    static constexpr int kMinBlocks = MTJG_CGUPD_MINB;
     __device__ bool active(int sys) const { return m.st[sys].status == ST_RUNNING; }
     __device__ void row(int i, int sys, Acc &a) const
     {

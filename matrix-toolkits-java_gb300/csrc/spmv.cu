@@ -44,7 +44,7 @@ void plan_tiles(const int *rowptr, int row_begin, int row_end, int vec, std::vec
 
 void plan_row_tiles(int row_begin, int row_end, std::vector<int> &tile_row, std::vector<unsigned char> &tile_flags)
 {
-    for (int r = row_begin; r < row_end; r += kRowTile) {
+    for (int r = row_begin; r < row_end; r += kRowTileRows) {
         tile_row.push_back(r);
         tile_flags.push_back((unsigned char)(1 << 1));
     }

@@ -14,8 +14,8 @@
 // decides what a finished row sum becomes (y = Ax, y += alpha*Ax,
 // r = b - Ax, fused dot products, ...).
 //
-// k_rows: one block per row tile (kRowTile rows, kRowsPerThread rows per
-// thread, strided for coalescing).
+// k_rows: one block per row tile (kRowTileRows rows: kRowPasses passes of
+// kRowsPerThread rows per thread, strided for coalescing).
 //
 // A phase with a reduction accumulates per thread over a whole group, then
 // stores one block-reduced partial per group; k_finalize (dev.cuh) reduces
@@ -427,11 +427,21 @@ template <class Op>
 struct OpBatched<Op, decltype((void)Op::kBatched)> {
     static constexpr bool value = Op::kBatched;
 };
+// Resident blocks per SM a row phase asks the register allocator for
+// (Op::kMinBlocks; 0: no bound).
+template <class Op, class = void>
+struct OpMinBlocks {
+    static constexpr int value = 0;
+};
+template <class Op>
+struct OpMinBlocks<Op, decltype((void)Op::kMinBlocks)> {
+    static constexpr int value = Op::kMinBlocks;
+};
 
 // Row kernel: block b handles row tile b, kRowsPerThread rows per thread
 // (rows tid, tid + kBlock, ...), one partial per tile.
 template <class Op>
-__global__ void __launch_bounds__(kBlock) k_rows(TileArgs ta, Op op, RedCtx rc, int normtype)
+__global__ void __launch_bounds__(kBlock, OpMinBlocks<Op>::value) k_rows(TileArgs ta, Op op, RedCtx rc, int normtype)
 {
     __shared__ double red_sm[kParts * kBlock];
     const int t = blockIdx.x;
@@ -542,7 +552,7 @@ inline RedCtx red_ctx(const mtjg_csr *A, const TileSet &ts)
 // pointers) to `tile_row` (first rows) / `tile_flags`.
 void plan_tiles(const int *rowptr, int row_begin, int row_end, int vec, std::vector<int> &tile_row,
                 std::vector<unsigned char> &tile_flags, int nnz_cap = kTileNnz, int rows_cap = kTileRows);
-// Appends row-kernel tiles (kRowTile rows) of rows [row_begin, row_end).
+// Appends row-kernel tiles (kRowTileRows rows) of rows [row_begin, row_end).
 void plan_row_tiles(int row_begin, int row_end, std::vector<int> &tile_row, std::vector<unsigned char> &tile_flags);
 int choose_vec(int64_t nnz, int64_t n);
 // Uploads a host tiling (tile_row has num_tiles+1 entries, sys_tile has
