@@ -76,14 +76,17 @@ constexpr int kGroupDiv = MTJG_GROUP_DIV;
 constexpr int kBatchGroupDiv = 64;
 constexpr int kRowsPerThread = 4;
 constexpr int kRowTile = kBlock * kRowsPerThread;
-// A row tile of the vector phases (one block, one partial) is kRowPasses
-// passes of kRowTile rows: more passes spread one block-wide reduction over
-// more rows.
+// A row tile of the vector phases (one block, one partial) of a batched or
+// served system is kRowPasses passes of kRowTile rows: more passes spread one
+// block-wide reduction over more rows.  A lone uploaded CSR takes them from
+// kRowTileLoneMin rows on; below that it keeps one pass, so a small system
+// still spreads over many blocks.
 #ifndef MTJG_ROW_PASSES
 #define MTJG_ROW_PASSES 2
 #endif
 constexpr int kRowPasses = MTJG_ROW_PASSES;
 constexpr int kRowTileRows = kRowTile * kRowPasses;
+constexpr int kRowTileLoneMin = 1 << 20;
 
 // device status of a system (SysState::status)
 enum : int {

@@ -42,9 +42,10 @@ void plan_tiles(const int *rowptr, int row_begin, int row_end, int vec, std::vec
     }
 }
 
-void plan_row_tiles(int row_begin, int row_end, std::vector<int> &tile_row, std::vector<unsigned char> &tile_flags)
+void plan_row_tiles(int row_begin, int row_end, int rows, std::vector<int> &tile_row,
+                    std::vector<unsigned char> &tile_flags)
 {
-    for (int r = row_begin; r < row_end; r += kRowTileRows) {
+    for (int r = row_begin; r < row_end; r += rows) {
         tile_row.push_back(r);
         tile_flags.push_back((unsigned char)(1 << 1));
     }
@@ -441,7 +442,7 @@ static int csr_upload_impl(mtjg_ctx *ctx, int n, int m, const int *rowptr, const
         const int r0 = sys_rows ? sys_rows[s] : 0, r1 = sys_rows ? sys_rows[s + 1] : n;
         const int vs = choose_vec((int64_t)rowptr[r1] - rowptr[r0], r1 - r0);
         plan_tiles(rowptr, r0, r1, vs, tile_row, tile_flags);
-        plan_row_tiles(r0, r1, rtile_row, rtile_flags);
+        plan_row_tiles(r0, r1, sys_rows || n >= kRowTileLoneMin ? kRowTileRows : kRowTile, rtile_row, rtile_flags);
         tile_sys.resize(tile_flags.size(), s);
         rtile_sys.resize(rtile_flags.size(), s);
         sys_tile.push_back((int)tile_flags.size());
@@ -450,8 +451,9 @@ static int csr_upload_impl(mtjg_ctx *ctx, int n, int m, const int *rowptr, const
     tile_row.push_back(n);
     rtile_row.push_back(n);
     // a batch (mtjg_batch_upload, any number of systems) spreads over its
-    // systems, so its systems take larger reduction groups than a lone
-    // uploaded CSR, which needs many groups to fill the GPU by itself
+    // systems, so its systems take larger reduction groups (product and row
+    // tiles) than a lone uploaded CSR, which needs many groups to fill the
+    // GPU by itself
     st = upload_tiles(A->tiles, tile_row, tile_flags, sys_rows ? &tile_sys : nullptr, sys_tile, vec, rowptr,
                       kGroupTiles, sys_rows ? kBatchGroupDiv : kGroupDiv);
     if (st != MTJG_OK) return bail(st);

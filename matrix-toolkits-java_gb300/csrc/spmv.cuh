@@ -14,8 +14,8 @@
 // decides what a finished row sum becomes (y = Ax, y += alpha*Ax,
 // r = b - Ax, fused dot products, ...).
 //
-// k_rows: one block per row tile (kRowTileRows rows: kRowPasses passes of
-// kRowsPerThread rows per thread, strided for coalescing).
+// k_rows: one block per row tile (passes of kRowTile rows, kRowsPerThread
+// rows per thread and pass, strided for coalescing).
 //
 // A phase with a reduction accumulates per thread over a whole group, then
 // stores one block-reduced partial per group; k_finalize (dev.cuh) reduces
@@ -309,7 +309,49 @@ __global__ void __launch_bounds__(kBlock, Epi::kReduce ? kSpmvCtasReduce : kSpmv
             const int *sc = scol(s);
             const int *sr = srow(s);
             const int vo = nzb & ~(kVA - 1), co = nzb & ~3, po = r0 & ~3;
-            if constexpr (VEC == 1) {
+            if constexpr (VEC == 1 && Stage<T>::kRows > kBlock) {
+                // a tile may hold up to 2 kBlock rows: a thread's two rows
+                // gather together (one latency round, not two); each row's
+                // sum keeps its order and the rows finish in row order
+                static_assert(Stage<T>::kRows <= 2 * kBlock, "at most two rows per thread");
+                const int ra = r0 + tid, rb = ra + kBlock;
+                if (ra < r1) {
+                    const bool hb = rb < r1;
+                    const int ba = sr[ra - po], la = sr[ra + 1 - po] - ba;
+                    const int bb = hb ? sr[rb - po] : 0, lb = hb ? sr[rb + 1 - po] - bb : 0;
+                    T suma = epi.init(vgo + ra, sys), sumb = hb ? epi.init(vgo + rb, sys) : T(0);
+                    T xra = T(0), xrb = T(0);
+                    bool da = false, db = false;
+                    const int lm = la > lb ? la : lb;
+#pragma unroll 4
+                    for (int k = 0; k < lm; ++k) {
+                        if (k < la) {
+                            const int c = sc[ba + k - co];
+                            const T xv = __ldg(xs + c);
+                            if (c == ra) {
+                                xra = xv;
+                                da = true;
+                            }
+                            suma = fmac<S>(sv[ba + k - vo], xv, suma);
+                        }
+                        if (k < lb) {
+                            const int c = sc[bb + k - co];
+                            const T xv = __ldg(xs + c);
+                            if (c == rb) {
+                                xrb = xv;
+                                db = true;
+                            }
+                            sumb = fmac<S>(sv[bb + k - vo], xv, sumb);
+                        }
+                    }
+                    if constexpr (Epi::kNeedsXr) {
+                        if (!da) xra = __ldg(xs + ra);
+                        if (hb && !db) xrb = __ldg(xs + rb);
+                    }
+                    epi.row(vgo + ra, sys, suma, xra, acc);
+                    if (hb) epi.row(vgo + rb, sys, sumb, xrb, acc);
+                }
+            } else if constexpr (VEC == 1) {
                 for (int r = r0 + tid; r < r1; r += kBlock) {
                     const int b = sr[r - po], e = sr[r + 1 - po];
                     T sum = epi.init(vgo + r, sys);
@@ -552,8 +594,10 @@ inline RedCtx red_ctx(const mtjg_csr *A, const TileSet &ts)
 // pointers) to `tile_row` (first rows) / `tile_flags`.
 void plan_tiles(const int *rowptr, int row_begin, int row_end, int vec, std::vector<int> &tile_row,
                 std::vector<unsigned char> &tile_flags, int nnz_cap = kTileNnz, int rows_cap = kTileRows);
-// Appends row-kernel tiles (kRowTileRows rows) of rows [row_begin, row_end).
-void plan_row_tiles(int row_begin, int row_end, std::vector<int> &tile_row, std::vector<unsigned char> &tile_flags);
+// Appends row-kernel tiles of `rows` rows (a multiple of kRowTile) of rows
+// [row_begin, row_end).
+void plan_row_tiles(int row_begin, int row_end, int rows, std::vector<int> &tile_row,
+                    std::vector<unsigned char> &tile_flags);
 int choose_vec(int64_t nnz, int64_t n);
 // Uploads a host tiling (tile_row has num_tiles+1 entries, sys_tile has
 // num_sys+1 tile offsets) and groups each system's tiles by group_size
