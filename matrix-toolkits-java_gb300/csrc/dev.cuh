@@ -131,6 +131,14 @@ struct OpSlots<Op, decltype((void)Op::kSlots)> {
     static constexpr int value = Op::kSlots;
 };
 
+// Shared-memory rows (kBlock doubles each) a block reduction of SLOTS uses:
+// two for a norm (the robust norm's scale and sum), one per plain sum.
+template <int SLOTS>
+constexpr int red_rows()
+{
+    return ((SLOTS & kSlotNorm) ? 2 : 0) + ((SLOTS & kSlotD2) ? 1 : 0) + ((SLOTS & kSlotD3) ? 1 : 0);
+}
+
 template <int SLOTS>
 __device__ __forceinline__ void acc_merge_m(Acc &a, const Acc &b, int type)
 {
@@ -166,17 +174,19 @@ __device__ __forceinline__ void acc_shfl_down(Acc &a, int off, int type)
 // finishes with a 5-level butterfly.  That costs about a quarter of the
 // FP64 instructions of a shuffle tree run in every warp.
 template <int SLOTS>
-__device__ __forceinline__ void block_reduce(Acc &a, int type, double *sm /* [kParts * kBlock] */)
+__device__ __forceinline__ void block_reduce(Acc &a, int type, double *sm /* [red_rows<SLOTS>() * kBlock] */)
 {
     constexpr bool kN = (SLOTS & kSlotNorm) != 0, k2 = (SLOTS & kSlotD2) != 0, k3 = (SLOTS & kSlotD3) != 0;
+    // rows: norm scale, norm sum (with a norm), then slot 2, then slot 3
+    constexpr int o2 = kN ? 2 * kBlock : 0, o3 = o2 + (k2 ? kBlock : 0);
     const int tid = threadIdx.x, lane = tid & 31, nt = blockDim.x;
     const bool robust = type == MTJG_NORM_TWO_ROBUST;
     if constexpr (kN) {
         sm[tid] = a.v[0];
         if (robust) sm[kBlock + tid] = a.v[1];
     }
-    if constexpr (k2) sm[2 * kBlock + tid] = a.v[2];
-    if constexpr (k3) sm[3 * kBlock + tid] = a.v[3];
+    if constexpr (k2) sm[o2 + tid] = a.v[2];
+    if constexpr (k3) sm[o3 + tid] = a.v[3];
     __syncthreads();
     if (tid < 32 && SLOTS != 0) {
         Acc o;
@@ -184,15 +194,15 @@ __device__ __forceinline__ void block_reduce(Acc &a, int type, double *sm /* [kP
             a.v[0] = sm[lane];
             a.v[1] = robust ? sm[kBlock + lane] : 0.0;
         }
-        if constexpr (k2) a.v[2] = sm[2 * kBlock + lane];
-        if constexpr (k3) a.v[3] = sm[3 * kBlock + lane];
+        if constexpr (k2) a.v[2] = sm[o2 + lane];
+        if constexpr (k3) a.v[3] = sm[o3 + lane];
         for (int i = lane + 32; i < nt; i += 32) {
             if constexpr (kN) {
                 o.v[0] = sm[i];
                 o.v[1] = robust ? sm[kBlock + i] : 0.0;
             }
-            if constexpr (k2) o.v[2] = sm[2 * kBlock + i];
-            if constexpr (k3) o.v[3] = sm[3 * kBlock + i];
+            if constexpr (k2) o.v[2] = sm[o2 + i];
+            if constexpr (k3) o.v[3] = sm[o3 + i];
             acc_merge_m<SLOTS>(a, o, type);
         }
 #pragma unroll

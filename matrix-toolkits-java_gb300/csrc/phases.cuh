@@ -9,6 +9,12 @@
 #ifndef MTJG_MXUPD_MINB
 #define MTJG_MXUPD_MINB 0
 #endif
+// resident CTAs per SM of the FP32 product of the inner solve: 6 fit (40
+// registers, a one-slot reduction), but 5 leave L1 room for the gathers of
+// the served mix and measured 8 % faster there
+#ifndef MTJG_MXQ_CTAS
+#define MTJG_MXQ_CTAS 5
+#endif
 
 namespace mtjg {
 
@@ -180,6 +186,7 @@ struct MxQ {  // q = A32 p (FP32 row sums); alpha = rho / p.q
     static constexpr bool kReduce = true;
     static constexpr bool kNeedsXr = true;
     static constexpr int kSlots = kSlotD2;
+    static constexpr int kCtas = MTJG_MXQ_CTAS;
     __device__ bool active(int sys) const { return st[sys].status == ST_RUNNING && st[sys].phase == 1; }
     __device__ float init(int, int) const { return 0.0f; }
     __device__ void row(int i, int, float dd, float pi, Acc &a) const

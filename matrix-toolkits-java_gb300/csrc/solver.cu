@@ -19,6 +19,11 @@
 #ifndef MTJG_CGUPD_MINB
 #define MTJG_CGUPD_MINB 4
 #endif
+// resident CTAs per SM of the CG product (40 registers without spills in
+// FAST numerics; its one-slot reduction leaves room in shared memory)
+#ifndef MTJG_CGQ_CTAS
+#define MTJG_CGQ_CTAS 6
+#endif
 
 namespace mtjg {
 
@@ -105,6 +110,7 @@ struct CgQ {  // q = A p; alpha = rho / p.q (:77-78)
     static constexpr bool kReduce = true;
     static constexpr bool kNeedsXr = true;  // p_i arrives with the row's diagonal gather
     static constexpr int kSlots = kSlotD2;
+    static constexpr int kCtas = MTJG_CGQ_CTAS;
     __device__ bool active(int sys) const { return st[sys].status == ST_RUNNING; }
     __device__ double init(int, int) const { return 0.0; }
     __device__ void row(int i, int, double d, double pi, Acc &a) const

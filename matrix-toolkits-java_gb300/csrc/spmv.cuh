@@ -122,18 +122,32 @@ struct TileDesc {
     int staged;
 };
 
+// Resident CTAs per SM a product kernel is compiled and launched for:
+// Epi::kCtas when the epilogue declares it (it fits that many CTAs' registers
+// without spilling), else kSpmvCtasPerSm, or kSpmvCtasReduce when it reduces.
+template <class Epi, class = void>
+struct EpiCtas {
+    static constexpr int value = Epi::kReduce ? kSpmvCtasReduce : kSpmvCtasPerSm;
+};
+template <class Epi>
+struct EpiCtas<Epi, decltype((void)Epi::kCtas)> {
+    static constexpr int value = Epi::kCtas;
+};
+
 // Kernels and launchers are private to each translation unit (see k_finalize).
 namespace {
 
 template <int VEC, bool S, class T, class Epi>
-__global__ void __launch_bounds__(kBlock, Epi::kReduce ? kSpmvCtasReduce : kSpmvCtasPerSm)
+__global__ void __launch_bounds__(kBlock, EpiCtas<Epi>::value)
     k_spmv(CsrArgsT<T> A, TileArgs ta, const T *__restrict__ x, Epi epi, RedCtx rc, int normtype, int *err)
 {
     constexpr int kVA = 16 / (int)sizeof(T);  // values per 16 bytes
     constexpr int NST = kSpmvStages;
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t bar[NST];
-    __shared__ double red_sm[kParts * kBlock];
+    // block reductions use only the epilogue's slots (and so fit more CTAs)
+    constexpr int kRedRows = Epi::kReduce ? red_rows<OpSlots<Epi>::value>() : 0;
+    __shared__ double red_sm[(kRedRows > 0 ? kRedRows : 1) * kBlock];
     __shared__ T s_long[kBlock / 32];
     __shared__ unsigned s_done[NST];    // warps done with the tile in stage i
     __shared__ unsigned s_issued[NST];  // copies issued into stage i
@@ -538,7 +552,7 @@ cudaError_t launch_spmv_t(mtjg_ctx *ctx, CsrArgsT<T> A, const TileSet &ts, const
         if (e != cudaSuccess) return e;
         attr_set.fetch_or(bit);
     }
-    const int cap = ctx->num_sms * (Epi::kReduce ? kSpmvCtasReduce : kSpmvCtasPerSm);
+    const int cap = ctx->num_sms * EpiCtas<Epi>::value;
     const int grid = ts.num_groups < cap ? ts.num_groups : cap;
     k<<<grid, kBlock, spmv_smem<T>(), ctx->stream>>>(A, tile_args(ts), x, epi, rc, normtype, ctx->d_flag);
     ctx->launches++;
