@@ -290,9 +290,10 @@ MTJG_API int mtjg_server_create(mtjg_ctx *ctx, const mtjg_server_config *cfg, mt
  * nonzero diagonal); *matrix_id identifies it in submissions. */
 MTJG_API int mtjg_server_add_matrix(mtjg_server *S, int n, const int *rowptr, const int *colind,
                                     const double *val, int *matrix_id);
-/* Releases a registered matrix: new submissions naming it fail at once, and
- * its device memory is freed when its last submitted request has been
- * reported (at once when none is outstanding). */
+/* Releases a registered matrix: new submissions naming it fail at once;
+ * requests already submitted still finish, and its device memory is freed
+ * when the last of them has completed (its x written to x_out), at once when
+ * none is outstanding. */
 MTJG_API int mtjg_server_remove_matrix(mtjg_server *S, int matrix_id);
 /* Queues a solve of A x = b (x0 may be NULL for zeros).  b and x0 are copied;
  * x_out receives the solution and must stay valid until the request is
