@@ -386,6 +386,30 @@ __global__ void __launch_bounds__(kBlock, EpiCtas<Epi>::value)
                     }
                     epi.row(vgo + r, sys, sum, xr, acc);
                 }
+            } else if constexpr (Stage<T>::kRows > kBlock) {
+                // up to two passes of kBlock / VEC rows: a lane group's two
+                // rows gather together; each keeps its entry order and its
+                // butterfly, and the rows finish in row order
+                const int gg = tid / VEC, l = tid % VEC;
+                const int ra = r0 + gg, rb = ra + kBlock / VEC;
+                const bool ha = ra < r1, hb = rb < r1;
+                T suma = T(0), sumb = T(0);
+                if (ha && l == 0) suma = epi.init(vgo + ra, sys);
+                if (hb && l == 0) sumb = epi.init(vgo + rb, sys);
+                const int ba = ha ? sr[ra - po] : 0, la = ha ? sr[ra + 1 - po] - ba : 0;
+                const int bb = hb ? sr[rb - po] : 0, lb = hb ? sr[rb + 1 - po] - bb : 0;
+                const int lm = la > lb ? la : lb;
+                for (int k = l; k < lm; k += VEC) {
+                    if (k < la) suma = fmac<S>(sv[ba + k - vo], __ldg(xs + sc[ba + k - co]), suma);
+                    if (k < lb) sumb = fmac<S>(sv[bb + k - vo], __ldg(xs + sc[bb + k - co]), sumb);
+                }
+#pragma unroll
+                for (int off = VEC / 2; off > 0; off >>= 1) {
+                    suma += __shfl_xor_sync(0xffffffffu, suma, off, VEC);
+                    sumb += __shfl_xor_sync(0xffffffffu, sumb, off, VEC);
+                }
+                if (ha && l == 0) epi.row(vgo + ra, sys, suma, Epi::kNeedsXr ? __ldg(xs + ra) : T(0), acc);
+                if (hb && l == 0) epi.row(vgo + rb, sys, sumb, Epi::kNeedsXr ? __ldg(xs + rb) : T(0), acc);
             } else {
                 const int gg = tid / VEC, l = tid % VEC;
                 for (int base = r0; base < r1; base += kBlock / VEC) {
