@@ -84,6 +84,33 @@ def _py_system(seed, spd):
     return n, list(map(int, rp)), list(map(int, ci)), list(map(float, v)), A, rng
 
 
+def _seq_dot(x, y):
+    s = 0.0
+    for a, b in zip(x.tolist(), y.tolist()):
+        s += a * b
+    return s
+
+
+@pytest.mark.parametrize("n", [0, 1, 7, 255, 256, 1000])
+def test_dot_sequential_and_blocked(n):
+    """DenseVector.dot (M/DenseVector.java:267-279) sums x_i y_i in index
+    order; under sum_order(B) the oracle sums blocks of B entries and combines
+    the block sums pairwise (stride 1, 2, 4, ...).  Bit for bit both ways."""
+    rng = np.random.default_rng(100 + n)
+    x, y = rng.uniform(-1, 1, n), rng.uniform(-1, 1, n)
+    assert O.dot(x, y) == _seq_dot(x, y)
+    B = 64
+    parts = [_seq_dot(x[k:k + B], y[k:k + B]) for k in range(0, n, B)]
+    w = 1
+    while w < len(parts):
+        for k in range(0, len(parts) - w, 2 * w):
+            parts[k] += parts[k + w]
+        w *= 2
+    with O.sum_order(B):
+        assert O.dot(x, y) == (parts[0] if parts else 0.0)
+    assert O.dot(x, y) == _seq_dot(x, y)  # the sequential order is back
+
+
 @pytest.mark.parametrize("seed", range(20))
 def test_products_bitwise(seed):
     n, rp, ci, v, A, rng = _py_system(seed, False)
