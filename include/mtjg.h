@@ -244,7 +244,9 @@ MTJG_API int mtjg_solver_solve_dev(mtjg_solver *S, mtjg_csr *A, const double *db
  * enable = 0 restores the FP64 solver.  No counterpart in the reference. */
 MTJG_API int mtjg_solver_set_mixed(mtjg_solver *S, int enable, double inner_rtol, int inner_max_iter);
 /* Residual history of the last solve: the (residual, iteration) pairs passed
- * to IterationReporter.monitor, oldest first (up to history_cap). */
+ * to IterationReporter.monitor, oldest first (up to history_cap); for a
+ * batch, that of the system the result describes (the first that did not
+ * converge, else system 0). */
 MTJG_API int mtjg_solver_history(mtjg_solver *S, double *resid, int *iters, int cap, int *len);
 /* Per-system outcome and residual history of the last batched solve (the
  * aggregate mtjg_result reports the first system that did not converge). */

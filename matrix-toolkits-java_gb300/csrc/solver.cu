@@ -672,6 +672,9 @@ struct mtjg_solver {
     cudaEvent_t ev[2] = {nullptr, nullptr};
     SysState last{};
     int last_valid = 0;
+    int last_sys = 0;          // the system of the last solve that S->last describes
+    bool last_empty = false;   // the last solve had n == 0: its history is empty_it (residuals 0)
+    std::vector<int> empty_it;
 };
 
 namespace {
@@ -948,6 +951,49 @@ int capture(mtjg_solver *S, mtjg_csr *A)
 
 int map_status(int st) { return st == ST_DONE ? MTJG_OK : st; }
 
+// Copies the first m entries of the residual history of system `sys` of the
+// last solve.
+int copy_history(mtjg_solver *S, int sys, double *resid, int *iters, int m)
+{
+    if (m <= 0) return MTJG_OK;
+    if (S->last_empty) {
+        for (int k = 0; k < m; ++k) {
+            if (resid) resid[k] = 0.0;
+            if (iters) iters[k] = S->empty_it[(size_t)k];
+        }
+        return MTJG_OK;
+    }
+    const size_t off = (size_t)sys * (size_t)S->mon.history_cap;
+    MTJG_CUDA(cudaSetDevice(S->ctx->device));
+    if (resid) MTJG_CUDA(cudaMemcpy(resid, S->hist_r + off, sizeof(double) * (size_t)m, cudaMemcpyDeviceToHost));
+    if (iters) MTJG_CUDA(cudaMemcpy(iters, S->hist_it + off, sizeof(int) * (size_t)m, cudaMemcpyDeviceToHost));
+    return MTJG_OK;
+}
+
+// The caller's view of S->last: its result and, for a solve that did not
+// converge, the message of the exception MTJ would throw.
+int report(mtjg_solver *S, mtjg_result *res)
+{
+    const int code = map_status(S->last.status);
+    if (res) {
+        res->status = code;
+        res->iterations = S->last.iter;
+        res->residual = S->last.residual;
+        res->detail = S->last.detail;
+        res->history_len = S->last.hist_len;
+        res->inner_iterations = S->last.in_total;
+    }
+    if (code == MTJG_NOT_CONVERGED_BREAKDOWN)
+        set_error(S->last.detail == 1 ? "Breakdown: rho" : "Breakdown: omega");
+    else if (code == MTJG_NOT_CONVERGED_ITERATIONS)
+        set_error("Iterations");
+    else if (code == MTJG_NOT_CONVERGED_DIVERGENCE)
+        set_error("Divergence");
+    else if (code == MTJG_ERR_SINGULAR)
+        set_error("MatrixSingularException in the GMRES triangular solve");
+    return code;
+}
+
 // Device state for `ns` systems: scalars and monitor histories.
 int ensure_state(mtjg_solver *S, int ns)
 {
@@ -1040,62 +1086,65 @@ int run(mtjg_solver *S, mtjg_csr *A, mtjg_result *res)
     MTJG_CUDA(cudaStreamSynchronize(ctx->stream));
     S->last = S->last_all[0];
     S->last_valid = 1;
+    S->last_empty = false;
     if (flag) {
         cudaMemset(ctx->d_flag, 0, sizeof(int));
         return fail(MTJG_ERR_DEVICE_TIMEOUT, "a bounded wait in a device kernel gave up during the solve");
     }
     // a batch reports its first system that did not converge (else system 0)
-    for (const SysState &q : S->last_all)
-        if (q.status != ST_DONE) {
-            S->last = q;
+    S->last_sys = 0;
+    for (size_t i = 0; i < S->last_all.size(); ++i)
+        if (S->last_all[i].status != ST_DONE) {
+            S->last = S->last_all[i];
+            S->last_sys = (int)i;
             break;
         }
-    const int code = map_status(S->last.status);
-    if (res) {
-        res->status = code;
-        res->iterations = S->last.iter;
-        res->residual = S->last.residual;
-        res->detail = S->last.detail;
-        res->history_len = S->last.hist_len;
-        res->inner_iterations = S->last.in_total;
-    }
-    if (code == MTJG_NOT_CONVERGED_BREAKDOWN)
-        set_error(S->last.detail == 1 ? "Breakdown: rho" : "Breakdown: omega");
-    else if (code == MTJG_NOT_CONVERGED_ITERATIONS)
-        set_error("Iterations");
-    else if (code == MTJG_NOT_CONVERGED_DIVERGENCE)
-        set_error("Divergence");
-    else if (code == MTJG_ERR_SINGULAR)
-        set_error("MatrixSingularException in the GMRES triangular solve");
-    return code;
+    return report(S, res);
 }
 
-// n == 0: every vector is empty, every norm is 0.  The first test converges
-// when atol > 0; otherwise MTJ loops without effect until maxIter.
+// n == 0: every vector is empty and every norm 0, so the monitor sees r = 0
+// at every test (DefaultIterationMonitor.convergedI,
+// S/DefaultIterationMonitor.java:133-155): it converges at the first test iff
+// 0 < max(rtol * 0, atol), i.e. atol > 0, and otherwise stops at maxIter.
+// Short of that the solvers run on zero vectors as MTJ's do: CG tests every
+// iteration up to maxIter (S/CG.java:66-86); BiCGstab breaks down on rho = 0
+// at once (S/BiCGstab.java:75-79); GMRES tests the cycle's first residual
+// once more inside the cycle, then every step, and a full cycle ends in a
+// singular (all-zero) Hessenberg matrix (S/GMRES.java:137-166).  The
+// history (all residuals 0) stays on the host.
 int run_empty(mtjg_solver *S, mtjg_result *res)
 {
     std::memset(&S->last, 0, sizeof(S->last));
+    std::vector<int> &it = S->empty_it;
+    it.assign(1, 0);
+    const int mi = std::max(0, S->mon.max_iter);
     const bool conv = 0.0 < std::max(S->mon.rtol * 0.0, S->mon.atol);
-    S->last.status = conv ? ST_DONE : (S->mon.max_iter <= 0 ? MTJG_NOT_CONVERGED_ITERATIONS
-                                                            : MTJG_NOT_CONVERGED_ITERATIONS);
-    S->last.iter = conv ? 0 : std::max(0, S->mon.max_iter);
-    S->last.hist_len = 1;
+    if (conv) {
+        S->last.status = ST_DONE;
+    } else if (mi == 0) {
+        S->last.status = MTJG_NOT_CONVERGED_ITERATIONS;
+    } else if (S->kind == MTJG_BICGSTAB) {
+        S->last.status = MTJG_NOT_CONVERGED_BREAKDOWN;
+        S->last.detail = 1;  // rho
+    } else if (S->kind == MTJG_CG) {
+        S->last.status = MTJG_NOT_CONVERGED_ITERATIONS;
+        S->last.iter = mi;
+        for (int k = 1; k <= mi; ++k) it.push_back(k);
+    } else if (mi < S->restart) {
+        S->last.status = MTJG_NOT_CONVERGED_ITERATIONS;
+        S->last.iter = mi;
+        for (int k = 0; k <= mi; ++k) it.push_back(k);
+    } else {
+        S->last.status = MTJG_ERR_SINGULAR;
+        S->last.iter = S->restart;
+        for (int k = 0; k < S->restart; ++k) it.push_back(k);
+    }
+    S->last.hist_len = (int)it.size();
+    S->last_all.assign(1, S->last);
+    S->last_sys = 0;
     S->last_valid = 1;
-    if (S->hist_r && S->mon.history_cap > 0) {
-        const double z = 0.0;
-        const int it = 0;
-        cudaMemcpy(S->hist_r, &z, sizeof(double), cudaMemcpyHostToDevice);
-        cudaMemcpy(S->hist_it, &it, sizeof(int), cudaMemcpyHostToDevice);
-    }
-    if (res) {
-        res->status = map_status(S->last.status);
-        res->iterations = S->last.iter;
-        res->residual = 0.0;
-        res->detail = 0;
-        res->history_len = 1;
-        res->inner_iterations = 0;
-    }
-    return map_status(S->last.status);
+    S->last_empty = true;
+    return report(S, res);
 }
 
 int check_sizes(mtjg_solver *S, mtjg_csr *A)
@@ -1257,14 +1306,7 @@ extern "C" int mtjg_solver_batch_history(mtjg_solver *S, int sys, double *resid,
     if (sys < 0 || sys >= (int)S->last_all.size()) return fail(MTJG_ERR_INDEX_OUT_OF_BOUNDS, "system index");
     const int have = std::min(S->last_all[sys].hist_len, S->mon.history_cap);
     if (len) *len = have;
-    const int m = std::min(have, cap);
-    if (m > 0) {
-        const size_t off = (size_t)sys * (size_t)S->mon.history_cap;
-        MTJG_CUDA(cudaSetDevice(S->ctx->device));
-        if (resid) MTJG_CUDA(cudaMemcpy(resid, S->hist_r + off, sizeof(double) * (size_t)m, cudaMemcpyDeviceToHost));
-        if (iters) MTJG_CUDA(cudaMemcpy(iters, S->hist_it + off, sizeof(int) * (size_t)m, cudaMemcpyDeviceToHost));
-    }
-    return MTJG_OK;
+    return copy_history(S, sys, resid, iters, std::min(have, cap));
 }
 
 extern "C" int mtjg_solver_solve(mtjg_solver *S, mtjg_csr *A, const double *b, double *x, mtjg_result *res)
@@ -1310,11 +1352,5 @@ extern "C" int mtjg_solver_history(mtjg_solver *S, double *resid, int *iters, in
     if (!S) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL solver");
     const int have = S->last_valid ? std::min(S->last.hist_len, S->mon.history_cap) : 0;
     if (len) *len = have;
-    const int m = std::min(have, cap);
-    if (m > 0) {
-        MTJG_CUDA(cudaSetDevice(S->ctx->device));
-        if (resid) MTJG_CUDA(cudaMemcpy(resid, S->hist_r, sizeof(double) * (size_t)m, cudaMemcpyDeviceToHost));
-        if (iters) MTJG_CUDA(cudaMemcpy(iters, S->hist_it, sizeof(int) * (size_t)m, cudaMemcpyDeviceToHost));
-    }
-    return MTJG_OK;
+    return copy_history(S, S->last_sys, resid, iters, std::min(have, cap));
 }

@@ -416,6 +416,41 @@ def test_gmres_singular_hessenberg(ctx):
         solver.solve(A, b, np.zeros(n))
 
 
+@pytest.mark.parametrize("sname", ["cg", "bicgstab", "gmres"])
+@pytest.mark.parametrize("max_iter,atol", [(7, 1e-50), (7, 0.0), (2, 0.0), (0, 0.0)])
+def test_empty_system_matches_oracle(ctx, sname, max_iter, atol):
+    """A 0x0 system: every norm is 0, so the outcome is MTJ's monitor and loop
+    logic alone -- converged at the first test when atol > 0; otherwise CG
+    runs to maxIter, BiCGstab breaks down on rho = 0, and GMRES runs to
+    maxIter or, after a full restart cycle, meets a singular Hessenberg
+    matrix.  Status, iteration count and reported history as the oracle's."""
+    restart = 3
+    rp = np.zeros(1, dtype=np.int32)
+    ci = np.zeros(0, dtype=np.int32)
+    v = np.zeros(0)
+    A = sparse.CompRowMatrix(0, 0, rp, ci, v, ctx)
+    assert A.mult(np.zeros(0)).shape == (0,)
+    cls, okind = SOLVERS[sname]
+    solver = cls(0, restart=restart, ctx=ctx) if sname == "gmres" else cls(0, ctx=ctx)
+    mon = sparse.DefaultIterationMonitor(max_iter, 1e-10, atol, 1e5)
+    mon.setIterationReporter(sparse.IterationReporter(), history_cap=64)
+    solver.setIterationMonitor(mon)
+    status = 0
+    try:
+        solver.solve(A, np.zeros(0), np.zeros(0))
+    except sparse.IterativeSolverNotConvergedException as e:
+        status = e.getReason().value
+    except sparse.MatrixSingularException:
+        status = O.ERR_SINGULAR
+    _, res, hr, hi = O.solve(okind, O.Csr(0, 0, rp, ci, v), np.zeros(0), np.zeros(0), None, max_iter=max_iter,
+                             rtol=1e-10, atol=atol, restart=restart)
+    assert status == res.status
+    assert mon.iterations() == res.iterations
+    gr, gi = solver.history
+    assert np.array_equal(gi, hi)
+    assert np.array_equal(gr, hr)
+
+
 @pytest.mark.parametrize("norm", [0, 2, 3])
 def test_other_norms(ctx, norm):
     n, rp, ci, v = workloads.poisson2d(16)
