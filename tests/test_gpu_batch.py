@@ -86,6 +86,37 @@ def test_batch_equals_solo_bitwise(ctx, pc):
             assert np.array_equal(hb[0], hist[0]) and np.array_equal(hb[1], hist[1]), i
 
 
+@pytest.mark.parametrize("pc", [False, True], ids=["identity", "jacobi"])
+def test_batch_with_an_empty_system(ctx, pc):
+    """A system of zero rows inside a batch converges at its first test, as it
+    does alone, and leaves the other systems' results as they are alone."""
+    empty = (0, np.zeros(1, dtype=np.int32), np.zeros(0, dtype=np.int32), np.zeros(0))
+    systems = [workloads.poisson2d(9), empty, workloads.laplacian(700, 41), empty]
+    bs = _rhs(systems)
+    max_iter = 400
+    A = sparse.BatchCompRowMatrix(systems, ctx)
+    ntot = A.numRows()
+    solver = sparse.CG(ntot, ctx=ctx)
+    if pc:
+        M = sparse.DiagonalPreconditioner(ntot, ctx)
+        M.setMatrix(A)
+        solver.setPreconditioner(M)
+    mon = sparse.DefaultIterationMonitor(max_iter, 1e-10, 1e-50, 1e5)
+    mon.setIterationReporter(None, history_cap=max_iter + 8)
+    solver.setIterationMonitor(mon)
+    x = np.zeros(ntot)
+    res = solver.solveBatch(A, np.concatenate(bs), x)
+    for pos, (n, rp, ci, v) in enumerate(systems):
+        r0, r1 = A.systemRows(pos)
+        xs, st, it, hist = _solo(ctx, n, rp, ci, v, bs[pos], pc, max_iter)
+        assert res[pos][0] == st == 0 and res[pos][1] == it, (pos, res[pos], st, it)
+        if n == 0:
+            assert it == 0 and r0 == r1
+        assert np.array_equal(x[r0:r1], xs), pos
+        hb = solver.batchHistory(pos)
+        assert np.array_equal(hb[0], hist[0]) and np.array_equal(hb[1], hist[1]), pos
+
+
 def test_batch_matches_oracle(ctx):
     systems = _systems()[:-1]
     bs = _rhs(systems)
