@@ -127,3 +127,26 @@ def test_remove_matrix_while_its_requests_run(servers):
     res = {r.ticket: r for r in srv.poll()}
     assert all(res[k].status == 0 for k in t + [u])
     srv.removeMatrix(mids[1])  # nothing outstanding: freed at once
+
+
+def test_zero_rhs_and_iteration_limit(servers):
+    """b = 0 converges at the first test with x = 0; a server whose refinement
+    budget cannot reach rtol reports the iteration limit; a normal request
+    beside either is unaffected."""
+    mats = [workloads.poisson2d(60), workloads.poisson2d(200)]
+    srv = servers(max_systems=8, pool_rows=1 << 18)
+    mids = [srv.addMatrix(*m) for m in mats]
+    zero = srv.submit(mids[0], np.zeros(3600))
+    ok = srv.submit(mids[1], workloads.uniform(40000, 3))
+    srv.drain(120.0)
+    res = {r.ticket: r for r in srv.poll()}
+    assert res[zero].status == 0 and res[zero].iterations == 0
+    assert not np.any(res[zero].x)
+    assert res[ok].status == 0
+    tight = servers(max_systems=8, pool_rows=1 << 18, max_iter=2, inner_max_iter=5)
+    tids = [tight.addMatrix(*m) for m in mats]
+    lim = tight.submit(tids[1], workloads.uniform(40000, 3))
+    tight.drain(120.0)
+    res = {r.ticket: r for r in tight.poll()}
+    assert res[lim].status == 1  # IterativeSolverNotConvergedException, Reason.Iterations
+    assert res[lim].iterations <= 2
