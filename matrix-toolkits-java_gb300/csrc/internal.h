@@ -34,12 +34,15 @@ void ctx_release(mtjg_ctx *ctx);
 // ------------------------------------------------------------ tiling
 // For CSR products, rows are cut into tiles of at most kTileRows/vec rows
 // and kTileNnz entries (one long row may exceed kTileNnz; it forms a tile of
-// its own).  Row kernels use tiles of kBlock rows.  Tiles never straddle two
+// its own).  Row kernels use row tiles of kRowTile or kRowTileRows rows
+// (below).  Tiles never straddle two
 // systems of a batch, and reductions are sums of per-tile partials in tile
 // order, so no result depends on the grid size or on the other systems of a
 // batch.
 // Tile shape and pipeline depth can be set at build time (-DMTJG_TILE_ROWS=...)
-// to tune them.  The defaults were measured on GB300: 1152-entry tiles with
+// to tune them, as can the row-tile passes and group sizes below and, beside
+// their kernels, the resident blocks of the CG and FP32 inner-solve phases
+// (MTJG_CGQ_CTAS, MTJG_CGUPD_MINB, MTJG_MXQ_CTAS, MTJG_MXUPD_MINB).  The defaults were measured on GB300: 1152-entry tiles with
 // 6 (plain) / 5 (reducing) resident product CTAs per SM served the mixed
 // request stream 11% faster than 1792-entry tiles with 4, at 4% more time
 // per 3D Poisson 128^3 CG solve.
@@ -54,8 +57,8 @@ constexpr int kTileRows = MTJG_TILE_ROWS;
 constexpr int kTileNnz = MTJG_TILE_NNZ;
 constexpr int kParts = 4;             // partial-sum slots per group
 // A reduction group is what one block sums before a block-wide reduction:
-// up to kGroupTiles consecutive product tiles of one system, or one row tile
-// of kRowsPerThread * kBlock rows.  Few block-wide reductions matter on
+// up to kGroupTiles consecutive product tiles of one system, or one row
+// tile.  Few block-wide reductions matter on
 // GB300, whose FP64 pipe is narrow: a tree over 256 threads costs more FP64
 // issue slots than the vector work of 256 rows.
 #ifndef MTJG_GROUP_TILES
