@@ -12,7 +12,7 @@
  *  - Every function returns an int status: MTJG_OK (0) or a code below.
  *    Nothing throws.  mtjg_last_error() gives the message of the calling
  *    thread's last failure.  The codes map one to one onto the exceptions
- *    the reference throws (see INTEGRATION.md for the Java mapping).
+ *    the reference throws.
  *  - CSR is MTJ's: 0-based int32 row pointers and column indices, column
  *    indices ascending inside each row, float64 values.
  *  - Host pointers are borrowed for the duration of the call only.  "_dev"
@@ -48,6 +48,9 @@ enum {
     MTJG_ERR_ILLEGAL_ARGUMENT = 10,
     /* IndexOutOfBoundsException (M/AbstractMatrix.java:170-177) */
     MTJG_ERR_INDEX_OUT_OF_BOUNDS = 11,
+    /* java.io.IOException / EOFException / NumberFormatException while reading
+     * Matrix Market text (M/io/MatrixVectorReader.java) */
+    MTJG_ERR_IO = 12,
     /* RuntimeException("Zero pivot encountered on row ..."), S/ILU.java:105-107, S/ICC.java:112-114 */
     MTJG_ERR_ZERO_PIVOT = 20,
     /* "Zero diagonal entry encountered on row ..." S/ICC.java:128-131,
@@ -153,6 +156,33 @@ MTJG_API int mtjg_csr_upload(mtjg_ctx *ctx, int num_rows, int num_cols,
  * solves one system per call (IterativeSolver.solve, S/IterativeSolver.java:30-44). */
 MTJG_API int mtjg_batch_upload(mtjg_ctx *ctx, int num_systems, const int *sys_rows, const int *rowptr,
                                const int *colind, const double *val, mtjg_csr **out);
+/* new CompRowMatrix(new MatrixVectorReader(reader)), S/CompRowMatrix.java:86-166:
+ * reads a Matrix Market file (or text of `len` bytes) and uploads it as a
+ * device CSR.  Coordinate real or integer, general / symmetric /
+ * skew-symmetric (mirrored entries added after the file's own; the last
+ * value assigned to a position wins, as CompRowMatrix.set overwrites).
+ * Pattern, array (dense) and complex files are MTJG_ERR_UNSUPPORTED, as in
+ * MTJ; malformed text MTJG_ERR_IO; an entry on a row outside the matrix
+ * MTJG_ERR_INDEX_OUT_OF_BOUNDS, on a column outside it
+ * MTJG_ERR_ILLEGAL_ARGUMENT.  Without a "%%MatrixMarket" first line the text
+ * is coordinate real general (M/io/MatrixVectorReader.java:122-240). */
+MTJG_API int mtjg_csr_read_matrix_market(mtjg_ctx *ctx, const char *path, mtjg_csr **out);
+MTJG_API int mtjg_csr_parse_matrix_market(mtjg_ctx *ctx, const char *text, int64_t len, mtjg_csr **out);
+/* The same parse into host arrays, without a device: call with NULL arrays
+ * to learn the sizes, then with rowptr[num_rows + 1] and colind / val of
+ * `cap` >= nnz entries. */
+MTJG_API int mtjg_csr_parse_matrix_market_host(const char *text, int64_t len, int *num_rows, int *num_cols,
+                                               int64_t *nnz, int *rowptr, int *colind, double *val, int64_t cap);
+/* new DenseVector(new MatrixVectorReader(reader)), M/DenseVector.java:52-96:
+ * coordinate or array, real or integer; *size receives the vector's size and
+ * the first min(cap, size) entries go to out. */
+MTJG_API int mtjg_vector_read_matrix_market(const char *path, double *out, int64_t cap, int64_t *size);
+MTJG_API int mtjg_vector_parse_matrix_market(const char *text, int64_t len, double *out, int64_t cap,
+                                             int64_t *size);
+/* CompRowMatrix.getRowPointers / getColumnIndices / getData
+ * (S/CompRowMatrix.java:255-271): the device CSR copied to host arrays of
+ * num_rows + 1 and nnz entries (any of them may be NULL). */
+MTJG_API int mtjg_csr_to_host(const mtjg_csr *A, int *rowptr, int *colind, double *val);
 /* New values, same pattern (CompRowMatrix.set on the data array). */
 MTJG_API int mtjg_csr_update_values(mtjg_csr *A, const double *val);
 MTJG_API int mtjg_csr_destroy(mtjg_csr *A);
@@ -184,9 +214,11 @@ MTJG_API int mtjg_csr_trans_mult_dev(mtjg_csr *A, const double *dx, double *dy);
  * handed out at start-up (a JVM off-heap pool, a serving process with a
  * memory budget), and loops that cannot afford cudaMalloc/cudaFree, which may
  * synchronise the device.
- *   - Limit: A's product tiling may have at most 16384 reduction groups (one
- *     system up to about 33 million rows at 7 entries per row, or a batch of
- *     at most 16384 systems); larger A gives MTJG_ERR_ILLEGAL_ARGUMENT.
+ *   - Limit: A's product tiling may have at most 16384 reduction groups.  A
+ *     group is at most 8 product tiles of at most 1152 entries, so one system
+ *     fits up to about 16384 * 8 * 1152 = 151 million entries (about 21
+ *     million rows at 7 entries per row); a batch fits at most 16384
+ *     systems.  Larger A gives MTJG_ERR_ILLEGAL_ARGUMENT.
  *   - Nothing has to start at zero: partials are written before they are read
  *     within the call, and each norm is stored, not accumulated.
  *   - The scratch is one array per device, shared by all contexts and threads:
@@ -194,7 +226,10 @@ MTJG_API int mtjg_csr_trans_mult_dev(mtjg_csr *A, const double *dx, double *dy);
  *     race and return wrong norms.  Calls in order on one stream are safe.
  *   - The first call on each device looks the scratch's address up once
  *     (with that device current).  A caller that captures streams makes one
- *     call before capture begins, so this set-up is not inside a capture. */
+ *     call before capture begins, so this set-up is not inside a capture.
+ *   - cudaDeviceReset by the host ends every handle of this library on that
+ *     device, this entry's saved scratch address included: make new handles
+ *     (and so a new first call) after a reset. */
 MTJG_API int mtjg_csr_mult_add_norm_noalloc(mtjg_csr *A, double alpha, const double *dx, double *dy,
                                             double *dnorm);
 

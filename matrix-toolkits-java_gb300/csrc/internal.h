@@ -161,11 +161,16 @@ struct TileSet {
     std::vector<int> h_tile_row;
 };
 
-// A row-ordered triangular operator solved level by level.
+// A row-ordered triangular operator and its dependency levels.  A sweep
+// (one launch) hands out chunks of at most 32 rows of one level, in level
+// order, from a ticket counter.
 struct LevelSchedule {
     int n = 0;
     int num_levels = 0;
-    int *perm = nullptr;               // device: rows ordered by level
+    int num_chunks = 0;
+    int *perm = nullptr;               // device: rows ordered by level (stable in row index)
+    int *chunk = nullptr;              // device [num_chunks + 1]: first perm position of each chunk
+    unsigned *ticket = nullptr;        // device: next chunk of the running sweep
     std::vector<int> level_ptr;        // host: [num_levels + 1]
 };
 

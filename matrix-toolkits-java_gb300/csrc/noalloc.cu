@@ -8,10 +8,12 @@
 // image (g_noalloc_part below), so the call itself allocates nothing.
 //
 // Scratch rules:
-//   * size: kNoAllocMaxGroups groups of kParts doubles (512 KB).  A matrix
-//     whose product tiling has more groups (a single system of more than
-//     about 33 million rows at 7 entries per row, or a batch of more than
-//     16384 systems) is rejected with MTJG_ERR_ILLEGAL_ARGUMENT.
+//   * size: kNoAllocMaxGroups groups of kParts doubles (512 KB).  A group is
+//     at most kGroupTiles (8) product tiles of at most kTileNnz (1152)
+//     entries, so one system fits up to 16384 * 8 * 1152 = 151 million
+//     entries (about 21 million rows at 7 entries per row), and a batch up to
+//     16384 systems.  A matrix whose product tiling has more groups is
+//     rejected with MTJG_ERR_ILLEGAL_ARGUMENT.
 //   * nothing has to start at zero: every group partial is written by the
 //     product kernel before k_finalize reads it within the same call, and
 //     each norm is stored, not accumulated.
@@ -23,7 +25,9 @@
 //   * set-up: the first call on each device looks the array's device address
 //     up once (cudaGetSymbolAddress, with that device current) and keeps it.
 //     A caller that captures streams makes one call before capture begins,
-//     so that this first-call set-up does not fall inside the capture.
+//     so that this first-call set-up does not fall inside the capture.  A
+//     cudaDeviceReset ends every handle of the library on that device, the
+//     saved address included; callers make new handles after a reset.
 #include <mutex>
 
 #include "spmv.cuh"

@@ -5,8 +5,21 @@
 // take rows in dependency order from a ticket counter and each row waits
 // (bounded) for the levels of the rows it reads, so one launch finds all
 // levels in O(nnz).  The rows are then grouped by level on the host (a
-// counting sort, stable in row index) and every level is one launch of a
-// row-per-thread kernel that sums in MTJ's entry order.
+// counting sort, stable in row index) and cut into chunks of at most 32 rows
+// of one level.
+//
+// A triangular solve is one launch (k_trsv_sweep).  Its output vector is
+// first filled with kPending, a signalling NaN that no arithmetic produces
+// (an operation on a signalling NaN returns a quiet one).  Warps take chunks
+// in level order from a ticket counter, one row per lane; a row reads the
+// entries x_c it depends on with relaxed loads, polling (bounded) while one
+// still holds kPending, and stores its own x_i with a single 64-bit store.
+// The value is its own ready flag: no fence, no counter, no level barrier,
+// and a row starts as soon as the rows it reads are done, so the sweep runs
+// at the depth of the dependency graph times one L2 round trip.  A row waits
+// only on rows of lower levels, whose tickets were all handed to running
+// warps before its own, so the sweep cannot deadlock.  Each row sums in
+// MTJ's entry order, so results are those of the row-by-row Java loop.
 #include <algorithm>
 #include <cstring>
 
@@ -161,7 +174,67 @@ __global__ void k_ilu_level(const int *perm, int beg, int cnt, const int *rp, co
     }
 }
 
-// Triangular solve of one level, one row per thread.
+// ---------------------------------------------------- triangular sweeps
+// x entries not yet solved hold this signalling NaN.
+constexpr unsigned long long kPending = 0x7FF40000DEADBEEFull;
+constexpr unsigned long long kQuietNaN = 0x7FF8000000000000ull;
+constexpr long long kSweepSpinLimit = 1LL << 21;
+constexpr int kSweepBlock = 128;
+constexpr int kSweepBlocksPerSm = 8;
+
+__device__ __forceinline__ double ld_relaxed(const double *p)
+{
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return __longlong_as_double((long long)v);
+}
+
+__device__ __forceinline__ void st_relaxed(double *p, double v)
+{
+    asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"((unsigned long long)__double_as_longlong(v))
+                 : "memory");
+}
+
+__device__ __forceinline__ bool pending(double v) { return (unsigned long long)__double_as_longlong(v) == kPending; }
+
+// Fills the outputs of the coming sweeps with kPending and resets their
+// ticket counters.  x2 may be null.
+__global__ void k_sweep_prep(int n, double *x1, double *x2, unsigned *t1, unsigned *t2, const int *status)
+{
+    if (status && *status != ST_RUNNING) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (t1) *t1 = 0u;
+        if (t2) *t2 = 0u;
+    }
+    const double p = __longlong_as_double((long long)kPending);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        x1[i] = p;
+        if (x2) x2[i] = p;
+    }
+}
+
+// x_c for a row of the sweep: a relaxed load, polled while it is pending.
+// Gives up (bad) after kSweepSpinLimit polls or when another wait has given
+// up (the context's error flag is set).
+__device__ __forceinline__ double wait_x(const double *x, int c, const int *err, bool &bad)
+{
+    double v = ld_relaxed(x + c);
+    if (!pending(v)) return v;
+    unsigned ns = 32;
+    for (long long polls = 1;; ++polls) {
+        __nanosleep(ns);
+        ns = ns < 256 ? 2 * ns : ns;
+        v = ld_relaxed(x + c);
+        if (!pending(v)) return v;
+        if (polls > kSweepSpinLimit || ((polls & 31) == 0 && *(volatile const int *)err)) {
+            bad = true;
+            return 0.0;
+        }
+    }
+}
+
+// One triangular solve, one launch.  Rows (one per lane) and their entries,
+// in MTJ's order:
 //  MODE 0: UnitLowerCompRowMatrix.solve   x_i = b_i - sum_{k<diag} v_k x_ck  (S/UnitLowerCompRowMatrix.java:56-64)
 //  MODE 1: UpperCompRowMatrix.solve       x_i = (b_i - sum_{k>diag} v_k x_ck) / v_diag (S/UpperCompRowMatrix.java:56-64)
 //  MODE 2: UpperCompRowMatrix.transSolve in gather form on the transpose of
@@ -170,36 +243,76 @@ __global__ void k_ilu_level(const int *perm, int beg, int cnt, const int *rp, co
 //  MODE 3: UnitLowerCompRowMatrix.transSolve in gather form on the
 //          transpose of the strict lower part, source rows descending
 //          (S/UnitLowerCompRowMatrix.java:78-83)
+// A row's entries are read in groups of kGrp, whose x loads are all in
+// flight before the first wait.
 template <bool S, int MODE>
-__global__ void __launch_bounds__(kBlock) k_trsv(const int *__restrict__ perm, int beg, int cnt,
-                                                 const int *__restrict__ rp, const int *__restrict__ ci,
-                                                 const double *__restrict__ v, const int *__restrict__ diag,
-                                                 const double *__restrict__ diagv, const double *b, double *x,
-                                                 const int *status)
+__global__ void __launch_bounds__(kSweepBlock) k_trsv_sweep(const int *__restrict__ perm,
+                                                          const int *__restrict__ chunk, int num_chunks,
+                                                          const int *__restrict__ rp, const int *__restrict__ ci,
+                                                          const double *__restrict__ v,
+                                                          const int *__restrict__ diag,
+                                                          const double *__restrict__ diagv, const double *b,
+                                                          double *x, unsigned *ticket, const int *status, int *err)
 {
+    constexpr int kGrp = 4;
     if (status && *status != ST_RUNNING) return;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= cnt) return;
-    const int i = perm[beg + t];
-    if constexpr (MODE == 0) {
-        double sum = 0.0;
-        const int e = diag[i];
-        for (int k = rp[i]; k < e; ++k) sum = fmac<S>(v[k], x[ci[k]], sum);
-        x[i] = b[i] - sum;
-    } else if constexpr (MODE == 1) {
-        double sum = 0.0;
-        const int d = diag[i], e = rp[i + 1];
-        for (int k = d + 1; k < e; ++k) sum = fmac<S>(v[k], x[ci[k]], sum);
-        x[i] = (b[i] - sum) / v[d];
-    } else if constexpr (MODE == 2) {
-        double xc = b[i];
-        const int e = rp[i + 1];
-        for (int k = rp[i]; k < e; ++k) xc = fmac<S>(-v[k], x[ci[k]], xc);
-        x[i] = xc / diagv[i];
-    } else {
-        double xc = b[i];
-        for (int k = rp[i + 1] - 1; k >= rp[i]; --k) xc = fmac<S>(-v[k], x[ci[k]], xc);
-        x[i] = xc;
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        unsigned c = 0;
+        if (lane == 0) c = atomicAdd(ticket, 1u);
+        c = __shfl_sync(0xffffffffu, c, 0);
+        if (c >= (unsigned)num_chunks) return;
+        const int beg = chunk[c], cnt = chunk[c + 1] - beg;
+        bool bad = false;
+        if (lane < cnt) {
+            const int i = perm[beg + lane];
+            const double bi = b[i];
+            // entry range, walked upwards from kb (MODE 3: downwards from ke - 1)
+            int kb, ke;
+            if constexpr (MODE == 0) {
+                kb = rp[i];
+                ke = diag[i];
+            } else if constexpr (MODE == 1) {
+                kb = diag[i] + 1;
+                ke = rp[i + 1];
+            } else {
+                kb = rp[i];
+                ke = rp[i + 1];
+            }
+            double acc = (MODE >= 2) ? bi : 0.0;
+            for (int k0 = 0; k0 < ke - kb && !bad; k0 += kGrp) {
+                int cc[kGrp];
+                double vv[kGrp], xv[kGrp];
+#pragma unroll
+                for (int u = 0; u < kGrp; ++u) {
+                    const int k = MODE == 3 ? ke - 1 - (k0 + u) : kb + k0 + u;
+                    const bool in = k0 + u < ke - kb;
+                    cc[u] = in ? ci[k] : -1;
+                    vv[u] = in ? v[k] : 0.0;
+                }
+#pragma unroll
+                for (int u = 0; u < kGrp; ++u) xv[u] = cc[u] >= 0 ? ld_relaxed(x + cc[u]) : 0.0;
+#pragma unroll
+                for (int u = 0; u < kGrp; ++u) {
+                    if (cc[u] < 0 || bad) continue;
+                    if (pending(xv[u])) xv[u] = wait_x(x, cc[u], err, bad);
+                    if constexpr (MODE <= 1) acc = fmac<S>(vv[u], xv[u], acc);
+                    else acc = fmac<S>(-vv[u], xv[u], acc);
+                }
+            }
+            double xi;
+            if constexpr (MODE == 0) xi = bi - acc;
+            else if constexpr (MODE == 1) xi = (bi - acc) / v[diag[i]];
+            else if constexpr (MODE == 2) xi = acc / diagv[i];
+            else xi = acc;
+            // a stored pending pattern would read as "not solved": store a quiet NaN
+            if ((unsigned long long)__double_as_longlong(xi) == kPending) xi = __longlong_as_double((long long)kQuietNaN);
+            if (!bad) st_relaxed(x + i, xi);
+        }
+        if (__any_sync(0xffffffffu, bad)) {
+            if (lane == 0) atomicExch(err, 1);
+            return;
+        }
     }
 }
 
@@ -217,9 +330,13 @@ static int grid_for(mtjg_ctx *ctx, int n)
 static void free_sched(LevelSchedule &s)
 {
     cudaFree(s.perm);
-    s.perm = nullptr;
+    cudaFree(s.chunk);
+    cudaFree(s.ticket);
+    s.perm = s.chunk = nullptr;
+    s.ticket = nullptr;
     s.level_ptr.clear();
     s.num_levels = 0;
+    s.num_chunks = 0;
 }
 
 // Finds the levels on the device, then groups rows by level.
@@ -262,41 +379,80 @@ static int build_levels(mtjg_ctx *ctx, int n, int desc, int range, const int *rp
     for (int l = 0; l < nl; ++l) out.level_ptr[l + 1] += out.level_ptr[l];
     std::vector<int> pos(out.level_ptr.begin(), out.level_ptr.end() - 1), perm(n);
     for (int i = 0; i < n; ++i) perm[pos[h[i]]++] = i;
+    // chunks of at most 32 rows, never straddling two levels
+    std::vector<int> chunk;
+    for (int l = 0; l < nl; ++l)
+        for (int p = out.level_ptr[l]; p < out.level_ptr[l + 1]; p += 32) chunk.push_back(p);
+    out.num_chunks = (int)chunk.size();
+    chunk.push_back(n);
     MTJG_CUDA(cudaMalloc(&out.perm, sizeof(int) * (size_t)n));
     MTJG_CUDA(cudaMemcpy(out.perm, perm.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice));
+    MTJG_CUDA(cudaMalloc(&out.chunk, sizeof(int) * chunk.size()));
+    MTJG_CUDA(cudaMemcpy(out.chunk, chunk.data(), sizeof(int) * chunk.size(), cudaMemcpyHostToDevice));
+    MTJG_CUDA(cudaMalloc(&out.ticket, sizeof(unsigned)));
+    MTJG_CUDA(cudaMemset(out.ticket, 0, sizeof(unsigned)));
     return MTJG_OK;
 }
 
-template <int MODE>
-static cudaError_t run_levels_t(mtjg_ctx *ctx, bool strict, const LevelSchedule &s, const int *rp, const int *ci,
-                                const double *v, const int *diag, const double *diagv, const double *b, double *x,
-                                const int *status)
+// Fills the outputs of the next sweeps (x2 may be null) with kPending and
+// resets their tickets.
+static cudaError_t sweep_prep(mtjg_ctx *ctx, int n, double *x1, double *x2, LevelSchedule *s1, LevelSchedule *s2,
+                              const int *status)
 {
-    for (int l = 0; l < s.num_levels; ++l) {
-        const int beg = s.level_ptr[l], cnt = s.level_ptr[l + 1] - beg;
-        const int grid = (cnt + kBlock - 1) / kBlock;
-        if (strict)
-            k_trsv<true, MODE><<<grid, kBlock, 0, ctx->stream>>>(s.perm, beg, cnt, rp, ci, v, diag, diagv, b, x,
-                                                                  status);
-        else
-            k_trsv<false, MODE><<<grid, kBlock, 0, ctx->stream>>>(s.perm, beg, cnt, rp, ci, v, diag, diagv, b, x,
-                                                                   status);
-        ctx->launches++;
-    }
+    k_sweep_prep<<<grid_for(ctx, n), kBlock, 0, ctx->stream>>>(n, x1, x2, s1 ? s1->ticket : nullptr,
+                                                               s2 ? s2->ticket : nullptr, status);
+    ctx->launches++;
     return cudaGetLastError();
 }
 
-static cudaError_t run_levels(mtjg_ctx *ctx, int mode, const LevelSchedule &s, const int *rp, const int *ci,
-                              const double *v, const int *diag, const double *diagv, const double *b, double *x,
-                              const int *status)
+template <int MODE>
+static cudaError_t sweep_t(mtjg_ctx *ctx, bool strict, const LevelSchedule &s, const int *rp, const int *ci,
+                           const double *v, const int *diag, const double *diagv, const double *b, double *x,
+                           const int *status)
+{
+    if (s.num_chunks == 0) return cudaSuccess;
+    const int warps = ctx->num_sms * kSweepBlocksPerSm * (kSweepBlock / 32);
+    const int grid = (std::min(warps, s.num_chunks) + kSweepBlock / 32 - 1) / (kSweepBlock / 32);
+    if (strict)
+        k_trsv_sweep<true, MODE><<<grid, kSweepBlock, 0, ctx->stream>>>(s.perm, s.chunk, s.num_chunks, rp, ci, v, diag,
+                                                                      diagv, b, x, s.ticket, status, ctx->d_flag);
+    else
+        k_trsv_sweep<false, MODE><<<grid, kSweepBlock, 0, ctx->stream>>>(s.perm, s.chunk, s.num_chunks, rp, ci, v,
+                                                                       diag, diagv, b, x, s.ticket, status,
+                                                                       ctx->d_flag);
+    ctx->launches++;
+    return cudaGetLastError();
+}
+
+// One triangular solve x = T \ b.  x must have been filled with kPending and
+// s's ticket reset (sweep_prep) since its last sweep, and x must not alias b.
+static cudaError_t sweep(mtjg_ctx *ctx, int mode, const LevelSchedule &s, const int *rp, const int *ci,
+                         const double *v, const int *diag, const double *diagv, const double *b, double *x,
+                         const int *status)
 {
     const bool strict = ctx->numerics == MTJG_NUMERICS_STRICT;
     switch (mode) {
-    case 0: return run_levels_t<0>(ctx, strict, s, rp, ci, v, diag, diagv, b, x, status);
-    case 1: return run_levels_t<1>(ctx, strict, s, rp, ci, v, diag, diagv, b, x, status);
-    case 2: return run_levels_t<2>(ctx, strict, s, rp, ci, v, diag, diagv, b, x, status);
-    default: return run_levels_t<3>(ctx, strict, s, rp, ci, v, diag, diagv, b, x, status);
+    case 0: return sweep_t<0>(ctx, strict, s, rp, ci, v, diag, diagv, b, x, status);
+    case 1: return sweep_t<1>(ctx, strict, s, rp, ci, v, diag, diagv, b, x, status);
+    case 2: return sweep_t<2>(ctx, strict, s, rp, ci, v, diag, diagv, b, x, status);
+    default: return sweep_t<3>(ctx, strict, s, rp, ci, v, diag, diagv, b, x, status);
     }
+}
+
+// Two sweeps, b -> y (first operator) -> x (second): y and (when it does not
+// alias b) x are filled in one pass before the first; an x that aliases b is
+// filled between the two.
+static cudaError_t sweep_pair(mtjg_ctx *ctx, int n, int mode1, LevelSchedule &s1, const int *rp1, const int *ci1,
+                              const double *v1, const int *diag1, const double *diagv1, int mode2, LevelSchedule &s2,
+                              const int *rp2, const int *ci2, const double *v2, const int *diag2,
+                              const double *diagv2, const double *b, double *y, double *x, const int *status)
+{
+    const bool alias = x == b;
+    cudaError_t e = sweep_prep(ctx, n, y, alias ? nullptr : x, &s1, &s2, status);
+    if (e == cudaSuccess) e = sweep(ctx, mode1, s1, rp1, ci1, v1, diag1, diagv1, b, y, status);
+    if (e == cudaSuccess && alias) e = sweep_prep(ctx, n, x, nullptr, nullptr, nullptr, status);
+    if (e == cudaSuccess) e = sweep(ctx, mode2, s2, rp2, ci2, v2, diag2, diagv2, y, x, status);
+    return e;
 }
 
 static int read_err_min(mtjg_ctx *ctx, int *err_min_dev, int *out)
@@ -327,15 +483,13 @@ int precond_apply_dev(mtjg_precond *M, const double *b, double *x, const int *st
         ctx->launches++;
         e = cudaGetLastError();
         break;
-    case MTJG_PC_ILU:
-        e = run_levels(ctx, 0, M->lo, M->rowptr, M->colind, M->data, M->diag, nullptr, b, M->y, status);
-        if (e == cudaSuccess)
-            e = run_levels(ctx, 1, M->up, M->rowptr, M->colind, M->data, M->diag, nullptr, M->y, x, status);
+    case MTJG_PC_ILU:  // L y = b, then U x = y (S/ILU.java:64-70)
+        e = sweep_pair(ctx, n, 0, M->lo, M->rowptr, M->colind, M->data, M->diag, nullptr, 1, M->up, M->rowptr,
+                       M->colind, M->data, M->diag, nullptr, b, M->y, x, status);
         break;
     default:  // ICC: R' y = b, then R x = y (S/ICC.java:67-73)
-        e = run_levels(ctx, 2, M->lo, M->rt_rowptr, M->rt_colind, M->rt_val, nullptr, M->diagv, b, M->y, status);
-        if (e == cudaSuccess)
-            e = run_levels(ctx, 1, M->up, M->rowptr, M->colind, M->data, M->diag, nullptr, M->y, x, status);
+        e = sweep_pair(ctx, n, 2, M->lo, M->rt_rowptr, M->rt_colind, M->rt_val, nullptr, M->diagv, 1, M->up,
+                       M->rowptr, M->colind, M->data, M->diag, nullptr, b, M->y, x, status);
         break;
     }
     if (e != cudaSuccess) return cuda_fail(e, "preconditioner apply");
@@ -611,8 +765,8 @@ static int precond_trans_apply_dev(mtjg_precond *M, const double *b, double *x)
     int st = ilu_trans_setup(M);
     if (st != MTJG_OK) return st;
     IluTrans *t = static_cast<IluTrans *>(M->trans);
-    cudaError_t e = run_levels(M->ctx, 2, t->ut, t->ut_rp, t->ut_ci, t->ut_v, nullptr, M->diagv, b, M->y, nullptr);
-    if (e == cudaSuccess) e = run_levels(M->ctx, 3, t->lt, t->lt_rp, t->lt_ci, t->lt_v, nullptr, nullptr, M->y, x, nullptr);
+    cudaError_t e = sweep_pair(M->ctx, M->n, 2, t->ut, t->ut_rp, t->ut_ci, t->ut_v, nullptr, M->diagv, 3, t->lt,
+                               t->lt_rp, t->lt_ci, t->lt_v, nullptr, nullptr, b, M->y, x, nullptr);
     if (e != cudaSuccess) return cuda_fail(e, "ILU transApply");
     return MTJG_OK;
 }

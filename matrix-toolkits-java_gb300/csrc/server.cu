@@ -407,22 +407,29 @@ int deliver(mtjg_server *S, std::vector<Retired> &staged, int par)
     if (staged.empty()) return MTJG_OK;
     MTJG_CUDA(cudaEventSynchronize(S->ev_ret[par]));
     const double tn = S->now();
-    std::lock_guard<std::mutex> lk(S->mu);
-    for (Retired &f : staged) {
-        std::memcpy(f.r->x_out, S->h_x + f.r->voff, sizeof(double) * (size_t)f.r->mat->n);
-        f.out.latency_s = tn - f.r->t_submit;
-        S->done.push_back(f.out);
-        ResMat *m = S->mats[f.r->mid];
-        if (--m->uses == 0 && m->removed) {
-            // its last request is out; no queued chunk reads a retired system's matrix
-            free_matrix(m);
-            S->mats[f.r->mid] = nullptr;
+    // matrices whose last request this delivers are unlinked under the lock
+    // and freed after it (cudaFree waits for the device; submit and poll
+    // must not wait with it)
+    std::vector<ResMat *> release;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        for (Retired &f : staged) {
+            std::memcpy(f.r->x_out, S->h_x + f.r->voff, sizeof(double) * (size_t)f.r->mat->n);
+            f.out.latency_s = tn - f.r->t_submit;
+            S->done.push_back(f.out);
+            ResMat *m = S->mats[f.r->mid];
+            if (--m->uses == 0 && m->removed) {
+                // its last request is out; no queued chunk reads a retired system's matrix
+                release.push_back(m);
+                S->mats[f.r->mid] = nullptr;
+            }
+            delete f.r;
         }
-        delete f.r;
+        S->inflight -= (int64_t)staged.size();
+        S->cv_done.notify_all();
     }
-    S->inflight -= (int64_t)staged.size();
-    S->cv_done.notify_all();
     staged.clear();
+    for (ResMat *m : release) free_matrix(m);
     return MTJG_OK;
 }
 
@@ -685,19 +692,27 @@ extern "C" int mtjg_server_add_matrix(mtjg_server *S, int n, const int *rowptr, 
     if (st == MTJG_OK) st = mtjg_precond_create(u, MTJG_PC_JACOBI, n, &m->J);
     if (st == MTJG_OK) st = mtjg_precond_set_matrix(m->J, m->A, nullptr);
     if (st != MTJG_OK) {
-        mtjg_precond_destroy(m->J);
-        mtjg_csr_destroy(m->A);
-        delete m;
+        free_matrix(m);
         return st;
     }
     m->nnz = m->A->nnz;
     const int grid = u->num_sms * 8;
-    MTJG_CUDA(cudaMalloc(&m->A->val32, sizeof(float) * (size_t)(m->nnz + 4)));
-    MTJG_CUDA(cudaMemsetAsync(m->A->val32, 0, sizeof(float) * (size_t)(m->nnz + 4), u->stream));
-    MTJG_CUDA(cudaMalloc(&m->invdiag32, sizeof(float) * (size_t)n));
-    k_to_f32<<<grid, kBlock, 0, u->stream>>>(m->nnz, m->A->val, m->A->val32);
-    k_to_f32<<<grid, kBlock, 0, u->stream>>>(n, m->J->invdiag, m->invdiag32);
-    MTJG_CUDA(cudaStreamSynchronize(u->stream));
+    // every failure from here on releases what the matrix holds so far
+    cudaError_t e = cudaMalloc(&m->A->val32, sizeof(float) * (size_t)(m->nnz + 4));
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(m->A->val32, 0, sizeof(float) * (size_t)(m->nnz + 4), u->stream);
+    if (e == cudaSuccess) e = cudaMalloc(&m->invdiag32, sizeof(float) * (size_t)n);
+    if (e == cudaSuccess) {
+        k_to_f32<<<grid, kBlock, 0, u->stream>>>(m->nnz, m->A->val, m->A->val32);
+        k_to_f32<<<grid, kBlock, 0, u->stream>>>(n, m->J->invdiag, m->invdiag32);
+        u->launches += 2;
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(u->stream);
+    if (e != cudaSuccess) {
+        free_matrix(m);
+        return cuda_fail(e, "registering a server matrix");
+    }
     // the matrix's own product tiles: FP64 as mtjg_csr_upload plans them,
     // and larger FP32 tiles for the inner products
     const int vec = choose_vec(m->nnz, n);
@@ -746,15 +761,21 @@ extern "C" int mtjg_server_submit(mtjg_server *S, int matrix_id, const double *b
 extern "C" int mtjg_server_remove_matrix(mtjg_server *S, int matrix_id)
 {
     if (!S) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL server");
-    std::lock_guard<std::mutex> lk(S->mu);
-    if (matrix_id < 0 || matrix_id >= (int)S->mats.size() || !S->mats[matrix_id] || S->mats[matrix_id]->removed)
-        return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "unknown or removed matrix id");
-    ResMat *m = S->mats[matrix_id];
-    m->removed = true;
-    if (m->uses == 0) {
-        free_matrix(m);
-        S->mats[matrix_id] = nullptr;
+    ResMat *release = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        if (matrix_id < 0 || matrix_id >= (int)S->mats.size() || !S->mats[matrix_id] ||
+            S->mats[matrix_id]->removed)
+            return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "unknown or removed matrix id");
+        ResMat *m = S->mats[matrix_id];
+        m->removed = true;
+        if (m->uses == 0) {
+            release = m;
+            S->mats[matrix_id] = nullptr;
+        }
     }
+    // freed outside the lock: cudaFree waits for the device
+    if (release) free_matrix(release);
     return MTJG_OK;
 }
 

@@ -538,6 +538,17 @@ extern "C" int mtjg_csr_dims(const mtjg_csr *A, int *n, int *m, int64_t *nnz)
     return MTJG_OK;
 }
 
+extern "C" int mtjg_csr_to_host(const mtjg_csr *A, int *rowptr, int *colind, double *val)
+{
+    if (!A) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL matrix");
+    MTJG_CUDA(cudaSetDevice(A->ctx->device));
+    MTJG_CUDA(cudaStreamSynchronize(A->ctx->stream));
+    if (rowptr) std::memcpy(rowptr, A->h_rowptr.data(), sizeof(int) * (size_t)(A->n + 1));
+    if (colind && A->nnz) MTJG_CUDA(cudaMemcpy(colind, A->colind, sizeof(int) * (size_t)A->nnz, cudaMemcpyDeviceToHost));
+    if (val && A->nnz) MTJG_CUDA(cudaMemcpy(val, A->val, sizeof(double) * (size_t)A->nnz, cudaMemcpyDeviceToHost));
+    return MTJG_OK;
+}
+
 static int ensure_transpose(mtjg_csr *A)
 {
     if (A->t_rowptr) return MTJG_OK;

@@ -25,6 +25,7 @@ NOT_CONVERGED_DIVERGENCE = 2
 NOT_CONVERGED_BREAKDOWN = 3
 ERR_ILLEGAL_ARGUMENT = 10
 ERR_INDEX_OUT_OF_BOUNDS = 11
+ERR_IO = 12
 ERR_ZERO_PIVOT = 20
 ERR_ZERO_DIAGONAL = 21
 ERR_MISSING_DIAGONAL = 22
@@ -84,6 +85,13 @@ PROTOTYPES = {
     "mtjg_memcpy_d2h": (C.c_int, [_vp, _vp, _vp, _i64]),
     "mtjg_csr_upload": (C.c_int, [_vp, C.c_int, C.c_int, _ip, _ip, _dp, C.POINTER(_vp)]),
     "mtjg_csr_update_values": (C.c_int, [_vp, _dp]),
+    "mtjg_csr_read_matrix_market": (C.c_int, [_vp, C.c_char_p, C.POINTER(_vp)]),
+    "mtjg_csr_parse_matrix_market": (C.c_int, [_vp, C.c_char_p, _i64, C.POINTER(_vp)]),
+    "mtjg_csr_parse_matrix_market_host": (C.c_int, [C.c_char_p, _i64, _ip, _ip, C.POINTER(_i64), _ip, _ip, _dp,
+                                                    _i64]),
+    "mtjg_vector_read_matrix_market": (C.c_int, [C.c_char_p, _dp, _i64, C.POINTER(_i64)]),
+    "mtjg_vector_parse_matrix_market": (C.c_int, [C.c_char_p, _i64, _dp, _i64, C.POINTER(_i64)]),
+    "mtjg_csr_to_host": (C.c_int, [_vp, _ip, _ip, _dp]),
     "mtjg_csr_destroy": (C.c_int, [_vp]),
     "mtjg_csr_dims": (C.c_int, [_vp, _ip, _ip, C.POINTER(_i64)]),
     "mtjg_csr_mult": (C.c_int, [_vp, _dp, _dp]),

@@ -43,6 +43,10 @@ class CudaError(RuntimeError):
     pass
 
 
+class UnsupportedOperationException(RuntimeError):
+    pass
+
+
 class NotConvergedException(Exception):
     class Reason(enum.Enum):  # M/NotConvergedException.java:33-49
         Iterations = 1
@@ -81,6 +85,10 @@ def _raise(code: int, what: str = ""):
         raise IndexOutOfBoundsException(msg)
     if code in (L.ERR_ZERO_PIVOT, L.ERR_ZERO_DIAGONAL, L.ERR_MISSING_DIAGONAL):
         raise RuntimeError(msg)
+    if code == L.ERR_IO:
+        raise IOError(msg)
+    if code == L.ERR_UNSUPPORTED:
+        raise UnsupportedOperationException(msg)
     if code == L.ERR_SINGULAR:
         raise MatrixSingularException(msg)
     raise CudaError(f"{what}: code {code}: {msg}")
@@ -172,6 +180,35 @@ class CompRowMatrix:
             rp.append(len(cols))
         return cls(n, m, np.array(rp), np.array(cols, dtype=np.int32), np.array(vals), ctx)
 
+    @classmethod
+    def fromMatrixMarket(cls, source, ctx=None):
+        """new CompRowMatrix(new MatrixVectorReader(...)) (S/CompRowMatrix.java:86-166).
+
+        ``source`` is a path, or the file's text as bytes.  The library reads
+        and parses it and uploads the CSR (mtjg_csr_read_matrix_market /
+        mtjg_csr_parse_matrix_market); the host arrays behind the getters
+        are copied back from the device."""
+        self = cls.__new__(cls)
+        self.ctx = ctx or default_context()
+        self._lib = self.ctx._lib
+        h = C.c_void_p()
+        if isinstance(source, (bytes, bytearray)):
+            buf = bytes(source)
+            _raise(self._lib.mtjg_csr_parse_matrix_market(self.ctx.h, buf, len(buf), C.byref(h)), "matrix market")
+        else:
+            _raise(self._lib.mtjg_csr_read_matrix_market(self.ctx.h, str(source).encode(), C.byref(h)),
+                   "matrix market")
+        self.h = h
+        n, m, nnz = C.c_int(), C.c_int(), C.c_int64()
+        _raise(self._lib.mtjg_csr_dims(h, C.byref(n), C.byref(m), C.byref(nnz)), "dims")
+        self.n, self.m = n.value, m.value
+        self.rowptr = np.empty(self.n + 1, dtype=np.int32)
+        self.colind = np.empty(max(nnz.value, 1), dtype=np.int32)
+        self.data = np.empty(max(nnz.value, 1))
+        _raise(self._lib.mtjg_csr_to_host(h, L.iptr(self.rowptr), L.iptr(self.colind), L.dptr(self.data)), "to_host")
+        self.colind, self.data = self.colind[:nnz.value], self.data[:nnz.value]
+        return self
+
     def numRows(self):
         return self.n
 
@@ -244,6 +281,41 @@ class CompRowMatrix:
             self.close()
         except Exception:
             pass
+
+
+def parseMatrixMarket(text: bytes):
+    """The CSR that CompRowMatrix(MatrixVectorReader) builds from Matrix
+    Market text, parsed by the library on the host (no device needed):
+    returns (numRows, numColumns, rowptr, colind, data)."""
+    lib = L.load()
+    text = bytes(text)
+    n, m, nnz = C.c_int(), C.c_int(), C.c_int64()
+    _raise(lib.mtjg_csr_parse_matrix_market_host(text, len(text), C.byref(n), C.byref(m), C.byref(nnz), None, None,
+                                                 None, 0), "matrix market")
+    rp = np.empty(n.value + 1, dtype=np.int32)
+    ci = np.empty(max(nnz.value, 1), dtype=np.int32)
+    v = np.empty(max(nnz.value, 1))
+    _raise(lib.mtjg_csr_parse_matrix_market_host(text, len(text), C.byref(n), C.byref(m), C.byref(nnz), L.iptr(rp),
+                                                 L.iptr(ci), L.dptr(v), nnz.value), "matrix market")
+    return n.value, m.value, rp, ci[:nnz.value], v[:nnz.value]
+
+
+def readVector(source):
+    """new DenseVector(new MatrixVectorReader(...)) (M/DenseVector.java:52-96):
+    a path or the text as bytes; returns a float64 numpy vector."""
+    lib = L.load()
+    size = C.c_int64()
+    if isinstance(source, (bytes, bytearray)):
+        buf = bytes(source)
+        _raise(lib.mtjg_vector_parse_matrix_market(buf, len(buf), None, 0, C.byref(size)), "vector")
+        out = np.empty(max(size.value, 1))
+        _raise(lib.mtjg_vector_parse_matrix_market(buf, len(buf), L.dptr(out), size.value, C.byref(size)), "vector")
+    else:
+        path = str(source).encode()
+        _raise(lib.mtjg_vector_read_matrix_market(path, None, 0, C.byref(size)), "vector")
+        out = np.empty(max(size.value, 1))
+        _raise(lib.mtjg_vector_read_matrix_market(path, L.dptr(out), size.value, C.byref(size)), "vector")
+    return out[:size.value]
 
 
 def block_diagonal(systems):

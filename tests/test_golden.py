@@ -151,3 +151,35 @@ def test_gpu_solves_meet_parity_bar_on_fixture(ctx, numerics, sysname, rname, ki
     assert rel <= bar, (rel, bar)
     xo = GOLD[key + "/x"]
     assert np.max(np.abs(x - xo)) <= 1e-8 * max(1.0, np.max(np.abs(xo)))
+
+
+# ------------------------------------------------- full-size configurations
+CONF_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "mtj_configs.npz")
+
+
+def test_config_fixture_inputs_and_c1_reproduce():
+    """The full-size fixture (tests/golden/make_configs.py): the generators
+    give the same 2D Poisson 128^2 system here, and the oracle reproduces its
+    CG + Jacobi history and x bit for bit (the larger runs take minutes on
+    one core and are checked by the GPU tests through the fixture)."""
+    import hashlib
+
+    from mtjg import workloads
+
+    conf = np.load(CONF_PATH)
+    n, rp, ci, v = workloads.poisson2d(128)
+    A = O.Csr(n, n, rp, ci, v)
+    b = O.mult(A, workloads.uniform(n, 1))
+    h = hashlib.sha256()
+    for a in (rp, ci, v, b):
+        h.update(np.ascontiguousarray(a).tobytes())
+    assert h.hexdigest() == str(conf["c1/input_sha256"])
+    pc = O.Precond(O.PC_JACOBI, n)
+    assert pc.set_matrix(A) == O.OK
+    x, res, hr, hi = O.solve(O.CG, A, b, np.zeros(n), pc, max_iter=2000, rtol=1e-10)
+    assert res.status == int(conf["c1/status"][0]) and res.iterations == int(conf["c1/iterations"][0])
+    assert np.array_equal(hr, conf["c1/hist_r"]) and np.array_equal(hi, conf["c1/hist_it"])
+    assert np.array_equal(x[conf["c1/x_index"]], conf["c1/x_sample"])
+    for name in ("c2jac", "c2icc", "c3gmres", "c3bicg"):
+        assert int(conf[name + "/status"][0]) == 0
+        assert len(conf[name + "/hist_r"]) == len(conf[name + "/hist_it"]) > 1

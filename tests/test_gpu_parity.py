@@ -7,6 +7,8 @@ must match the oracle's iteration count within +-2 and its relative residual
 history r_k / r_0 within 1e-10 over the common prefix, the bar MTJ's drop-in
 states.
 """
+import zlib
+
 import numpy as np
 import pytest
 
@@ -346,7 +348,8 @@ def _order_envelope(sname, pname, n, rp, ci, v, b):
 def test_reference_style_random_systems(ctx, seed, sname, pname):
     # TS/IterativeSolverTestAbstract.java:140-168 (solve and repeat 5 times,
     # x recovered within 1e-4), with the preconditioner actually installed
-    rng = np.random.default_rng(1000 * seed + hash(sname + pname) % 997)
+    # a fixed per-case seed (zlib.crc32 does not change between processes, unlike hash())
+    rng = np.random.default_rng(1000 * seed + zlib.crc32((sname + pname).encode()) % 997)
     n = int(rng.integers(1, 51))
     bw = int(rng.integers(1, min(10, n) + 1))
     Ad = spd_system(n, bw, rng) if sname == "cg" else nonsingular_system(n, bw, rng)
