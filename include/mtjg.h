@@ -74,8 +74,12 @@ enum { MTJG_NORM_ONE = 0, MTJG_NORM_TWO = 1, MTJG_NORM_TWO_ROBUST = 2, MTJG_NORM
  * DiagonalPreconditioner, ILU, ICC */
 enum { MTJG_PC_IDENTITY = 0, MTJG_PC_JACOBI = 1, MTJG_PC_ILU = 2, MTJG_PC_ICC = 3 };
 
-/* IterativeSolver implementations: S/CG.java, S/BiCGstab.java, S/GMRES.java */
-enum { MTJG_CG = 0, MTJG_BICGSTAB = 1, MTJG_GMRES = 2 };
+/* IterativeSolver implementations: S/CG.java, S/BiCGstab.java, S/GMRES.java,
+ * S/BiCG.java, S/CGS.java, S/QMR.java, S/Chebyshev.java, S/IR.java */
+enum {
+    MTJG_CG = 0, MTJG_BICGSTAB = 1, MTJG_GMRES = 2, MTJG_BICG = 3, MTJG_CGS = 4, MTJG_QMR = 5,
+    MTJG_CHEBYSHEV = 6, MTJG_IR = 7
+};
 
 /* Arithmetic of the products and vector updates.  FAST uses fused
  * multiply-add.  STRICT rounds every product and sum separately, as Java
@@ -97,8 +101,9 @@ typedef struct mtjg_monitor {
 } mtjg_monitor;
 
 /* Outcome of a solve: IterationMonitor.iterations()/residual() at exit and
- * the exception reason, if any.  detail: 1 = breakdown on "rho",
- * 2 = breakdown on "omega" (S/BiCGstab.java:77-83). */
+ * the exception reason, if any.  detail names the quantity of a breakdown:
+ * 1 "rho", 2 "omega" (S/BiCGstab.java:77-83), 3 "xi", 4 "delta", 5 "ep",
+ * 6 "beta", 7 "gamma" (S/QMR.java:134-195). */
 typedef struct mtjg_result {
     int status;
     int iterations;
@@ -251,12 +256,20 @@ MTJG_API int mtjg_precond_values(mtjg_precond *M, double *out, int64_t cap, int6
 MTJG_API int mtjg_precond_destroy(mtjg_precond *M);
 
 /* ---- IterativeSolver ---------------------------------------------------- */
-/* new CG(template) / new BiCGstab(template) / new GMRES(template, restart):
- * scratch vectors of size n live on the device with the solver
- * (S/CG.java:51-56, S/BiCGstab.java:53-63, S/GMRES.java:99-125).
- * restart <= 0 for GMRES is MTJG_ERR_ILLEGAL_ARGUMENT (S/GMRES.java:114-116). */
+/* new CG(template) / new BiCGstab(template) / new GMRES(template, restart) /
+ * new BiCG / CGS / QMR / IR(template) / new Chebyshev(template, eigmin,
+ * eigmax): scratch vectors of size n live on the device with the solver
+ * (S/CG.java:51-56, S/BiCGstab.java:53-63, S/GMRES.java:99-125,
+ * S/BiCG.java:52-61, S/CGS.java:52-63, S/QMR.java:65-80, S/IR.java:52-55,
+ * S/Chebyshev.java:62-68).  restart <= 0 for GMRES is
+ * MTJG_ERR_ILLEGAL_ARGUMENT (S/GMRES.java:114-116).  A Chebyshev solver
+ * needs mtjg_solver_set_eigenvalues before it solves. */
 MTJG_API int mtjg_solver_create(mtjg_ctx *ctx, int kind, int n, int restart,
                                 mtjg_solver **out);
+/* Chebyshev.setEigenvalues(eigmin, eigmax), S/Chebyshev.java:78-88: bounds of
+ * the spectrum of M^-1 A; eigmin <= 0, eigmax <= 0 or eigmin > eigmax is
+ * MTJG_ERR_ILLEGAL_ARGUMENT. */
+MTJG_API int mtjg_solver_set_eigenvalues(mtjg_solver *S, double eigmin, double eigmax);
 /* setPreconditioner(M) (NULL = identity), S/AbstractIterativeSolver.java:50-52 */
 MTJG_API int mtjg_solver_set_precond(mtjg_solver *S, mtjg_precond *M);
 /* setIterationMonitor(new DefaultIterationMonitor(...)), S/AbstractIterativeSolver.java:62-64 */

@@ -122,6 +122,11 @@ struct SysState {
     int in_fresh;   // 1: the next inner direction is p = z
     int pad2;
     double in_rho, in_rho_1, in_alpha, in_beta, in_r0;
+    // QMR (S/QMR.java:120-121): xi, gamma, theta, eta, delta, ep, the
+    // previous gamma / theta, and coef: the direction scale factors
+    // (coef[0], coef[1]) or the d / s scale factor (coef[0])
+    double xi, gamma, gamma_1, theta, theta_1, eta, delta, ep;
+    double coef[2];
 };
 
 struct MonCfgDev {
@@ -205,6 +210,8 @@ struct mtjg_csr {
     int *t_rowptr = nullptr, *t_colind = nullptr;
     double *t_val = nullptr;
     mtjg::TileSet t_tiles;
+    double *t_part = nullptr;  // reduction scratch of the transposed tiling
+    int64_t version = 0;       // changes whenever the values (and so the transpose) change
     // FP32 copy of the values (mixed precision), built on first use
     float *val32 = nullptr;
     // reduction scratch sized for this matrix's tiles

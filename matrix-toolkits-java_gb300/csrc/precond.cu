@@ -496,6 +496,12 @@ int precond_apply_dev(mtjg_precond *M, const double *b, double *x, const int *st
     return MTJG_OK;
 }
 
+// Preconditioner.transApply on device vectors, gated like
+// precond_apply_dev; and the set-up it needs (ILU's transposed factors),
+// which allocates and so must run before any stream capture.
+int precond_trans_apply_dev(mtjg_precond *M, const double *b, double *x, const int *status);
+int precond_prepare_trans(mtjg_precond *M);
+
 // ILU.transApply (S/ILU.java:72-78): U'y = b, then L'x = y.  Built on first use.
 struct IluTrans {
     int *ut_rp = nullptr, *ut_ci = nullptr;
@@ -759,14 +765,21 @@ static int ilu_trans_setup(mtjg_precond *M)
     return build_levels(ctx, M->n, 1, 0, t->lt_rp, t->lt_ci, nullptr, nullptr, t->lt);
 }
 
-static int precond_trans_apply_dev(mtjg_precond *M, const double *b, double *x)
+int mtjg::precond_prepare_trans(mtjg_precond *M)
 {
-    if (M->kind != MTJG_PC_ILU) return precond_apply_dev(M, b, x, nullptr);
+    return M->kind == MTJG_PC_ILU ? ilu_trans_setup(M) : MTJG_OK;
+}
+
+// DiagonalPreconditioner and ICC are their own transposes here
+// (S/DiagonalPreconditioner.java:60-62, S/ICC.java:75-77); ILU sweeps U' then L'.
+int mtjg::precond_trans_apply_dev(mtjg_precond *M, const double *b, double *x, const int *status)
+{
+    if (M->kind != MTJG_PC_ILU) return precond_apply_dev(M, b, x, status);
     int st = ilu_trans_setup(M);
     if (st != MTJG_OK) return st;
     IluTrans *t = static_cast<IluTrans *>(M->trans);
     cudaError_t e = sweep_pair(M->ctx, M->n, 2, t->ut, t->ut_rp, t->ut_ci, t->ut_v, nullptr, M->diagv, 3, t->lt,
-                               t->lt_rp, t->lt_ci, t->lt_v, nullptr, nullptr, b, M->y, x, nullptr);
+                               t->lt_rp, t->lt_ci, t->lt_v, nullptr, nullptr, b, M->y, x, status);
     if (e != cudaSuccess) return cuda_fail(e, "ILU transApply");
     return MTJG_OK;
 }
@@ -780,7 +793,7 @@ static int precond_host_call(mtjg_precond *M, const double *b, double *x, bool t
     const size_t nb = sizeof(double) * (size_t)M->n;
     if (M->n == 0) return MTJG_OK;
     MTJG_CUDA(cudaMemcpyAsync(M->d_b, b, nb, cudaMemcpyHostToDevice, ctx->stream));
-    int st = trans ? precond_trans_apply_dev(M, M->d_b, M->d_x) : precond_apply_dev(M, M->d_b, M->d_x, nullptr);
+    int st = trans ? precond_trans_apply_dev(M, M->d_b, M->d_x, nullptr) : precond_apply_dev(M, M->d_b, M->d_x, nullptr);
     if (st != MTJG_OK) return st;
     MTJG_CUDA(cudaMemcpyAsync(x, M->d_x, nb, cudaMemcpyDeviceToHost, ctx->stream));
     MTJG_CUDA(cudaStreamSynchronize(ctx->stream));

@@ -12,7 +12,7 @@
 #include <algorithm>
 #include <cstring>
 
-#include "phases.cuh"
+#include "krylov_ext.cuh"
 
 // resident blocks per SM the CG update is compiled for (it keeps four rows of
 // five FP64 vectors in flight per thread)
@@ -28,6 +28,9 @@
 namespace mtjg {
 
 int precond_apply_dev(mtjg_precond *M, const double *b, double *x, const int *status);
+int precond_trans_apply_dev(mtjg_precond *M, const double *b, double *x, const int *status);
+int precond_prepare_trans(mtjg_precond *M);
+int csr_ensure_transpose(mtjg_csr *A);
 
 
 // ================================================================== CG
@@ -667,6 +670,10 @@ struct mtjg_solver {
     int g_numerics = -1;
     int g_norm = -1;
     int64_t g_version = 0;
+    int64_t g_aversion = -1;
+    // Chebyshev's eigenvalue bounds (Chebyshev.setEigenvalues)
+    double eigmin = 0, eigmax = 0;
+    bool eig_set = false;
     int g_kernels = 0;
     int chunk = 16;
     cudaEvent_t ev[2] = {nullptr, nullptr};
@@ -679,7 +686,15 @@ struct mtjg_solver {
 
 namespace {
 
-enum { V_B = 0, V_X, V_R, V_Z, V_P, V_Q, V_RT, V_PH, V_S, V_SH, V_T, V_V, V_U, V_W, V_COUNT };
+enum {
+    V_B = 0, V_X, V_R, V_Z, V_P, V_Q, V_RT, V_PH, V_S, V_SH, V_T, V_V, V_U, V_W,
+    // BiCG, CGS, QMR
+    V_ZT, V_PT, V_QT, V_VH, V_UH, V_SUM, V_Y, V_D, V_VT, V_WT, V_YT, V_ZTL, V_PTL,
+    V_COUNT
+};
+
+// transposed products (A.transMult / transMultAdd) and M.transApply
+bool needs_transpose(int kind) { return kind == MTJG_BICG || kind == MTJG_QMR; }
 
 MonCfgDev mon_dev(const mtjg_solver *S)
 {
@@ -789,6 +804,171 @@ struct Phases {
         PH_CHECK(launch_spmv(S->ctx, csr(), A->tiles, shat, BiT<STRICT>{v(V_T), v(V_S), S->st}, rc(), norm()));
         PH_CHECK(launch_rows(S->ctx, A->rtiles,
                              BiR<STRICT>{v(V_X), v(V_R), v(V_S), shat, v(V_T), v(V_RT), mp()}, rc(), norm()));
+        return MTJG_OK;
+    }
+
+    // M.transApply (b -> x) with a gate word
+    int pct(const double *b, double *x, const int *gate)
+    {
+        if (!S->M || S->M->kind == MTJG_PC_IDENTITY) return pc(b, x, gate);
+        return precond_trans_apply_dev(S->M, b, x, gate);
+    }
+    CsrArgs tcsr() const { return CsrArgs{A->t_rowptr, A->t_colind, A->t_val}; }
+    RedCtx trc() const { return RedCtx{A->t_part, A->cnt, A->t_tiles.sys_group, A->num_running}; }
+    const int *gate() const { return &S->st->status; }
+
+    // ---- IR (S/IR.java:57-70)
+    int ir_init()
+    {
+        PH_CHECK(launch_spmv(S->ctx, csr(), A->tiles, v(V_X), IrRes<STRICT>{v(V_B), v(V_R), mp(), true}, rc(),
+                             norm()));
+        return MTJG_OK;
+    }
+    int ir_body()
+    {
+        const int pcm = pc_mode(S);
+        if (pcm == kPcExternal) {
+            int st = pc(v(V_R), v(V_Z), gate());
+            if (st != MTJG_OK) return st;
+        }
+        PH_CHECK(launch_rows(S->ctx, A->rtiles, IrX<STRICT>{v(V_X), v(V_R), v(V_Z), invdiag(), pcm, S->st}, rc(),
+                             norm()));
+        PH_CHECK(launch_spmv(S->ctx, csr(), A->tiles, v(V_X), IrRes<STRICT>{v(V_B), v(V_R), mp(), false}, rc(),
+                             norm()));
+        return MTJG_OK;
+    }
+
+    // ---- Chebyshev (S/Chebyshev.java:90-120)
+    ChCfg cheb() const { return ChCfg{(S->eigmax - S->eigmin) / 2.0, (S->eigmax + S->eigmin) / 2.0}; }
+    int cheb_init()
+    {
+        const int pcm = pc_mode(S);
+        double *z = pcm == kPcIdentity ? v(V_R) : v(V_Z);
+        PH_CHECK(launch_spmv(S->ctx, csr(), A->tiles, v(V_X),
+                             ChInit<STRICT>{v(V_B), v(V_R), z, invdiag(), pcm, mp(), cheb()}, rc(), norm()));
+        return MTJG_OK;
+    }
+    int cheb_body()
+    {
+        const int pcm = pc_mode(S);
+        double *z = pcm == kPcIdentity ? v(V_R) : v(V_Z);
+        if (pcm == kPcExternal) {
+            int st = pc(v(V_R), z, gate());
+            if (st != MTJG_OK) return st;
+        }
+        PH_CHECK(launch_rows(S->ctx, A->rtiles, CgP<STRICT>{v(V_P), z, S->st}, rc(), norm()));
+        PH_CHECK(launch_spmv(S->ctx, csr(), A->tiles, v(V_P), ChQ{v(V_Q), S->st}, rc(), norm()));
+        PH_CHECK(launch_rows(S->ctx, A->rtiles,
+                             ChUpd<STRICT>{v(V_X), v(V_R), z, v(V_P), v(V_Q), invdiag(), pcm, mp(), cheb()}, rc(),
+                             norm()));
+        return MTJG_OK;
+    }
+
+    // ---- BiCG (S/BiCG.java:63-102)
+    int bicg_init()
+    {
+        const int pcm = pc_mode(S);
+        double *z = pcm == kPcIdentity ? v(V_R) : v(V_Z), *zt = pcm == kPcIdentity ? v(V_RT) : v(V_ZT);
+        PH_CHECK(launch_spmv(S->ctx, csr(), A->tiles, v(V_X),
+                             BgInit<STRICT>{v(V_B), v(V_R), v(V_RT), z, zt, invdiag(), pcm, mp()}, rc(), norm()));
+        return MTJG_OK;
+    }
+    int bicg_body()
+    {
+        const int pcm = pc_mode(S);
+        double *z = pcm == kPcIdentity ? v(V_R) : v(V_Z), *zt = pcm == kPcIdentity ? v(V_RT) : v(V_ZT);
+        if (pcm == kPcExternal) {
+            int st = pc(v(V_R), z, gate());
+            if (st == MTJG_OK) st = pct(v(V_RT), zt, gate());
+            if (st != MTJG_OK) return st;
+            PH_CHECK(launch_rows(S->ctx, A->rtiles, BgRho<STRICT>{z, v(V_RT), mp()}, rc(), norm()));
+        }
+        PH_CHECK(launch_rows(S->ctx, A->rtiles, BgP<STRICT>{v(V_P), v(V_PT), z, zt, S->st}, rc(), norm()));
+        PH_CHECK(launch_spmv(S->ctx, csr(), A->tiles, v(V_P), ChQ{v(V_Q), S->st}, rc(), norm()));
+        PH_CHECK(launch_spmv(S->ctx, tcsr(), A->t_tiles, v(V_PT), BgQt<STRICT>{v(V_QT), v(V_Q), S->st}, trc(),
+                             norm()));
+        PH_CHECK(launch_rows(S->ctx, A->rtiles,
+                             BgUpd<STRICT>{v(V_X), v(V_R), v(V_RT), z, zt, v(V_P), v(V_Q), v(V_QT), invdiag(), pcm,
+                                           mp()},
+                             rc(), norm()));
+        return MTJG_OK;
+    }
+
+    // ---- CGS (S/CGS.java:65-105)
+    int cgs_init()
+    {
+        PH_CHECK(launch_spmv(S->ctx, csr(), A->tiles, v(V_X), CsInit<STRICT>{v(V_B), v(V_R), v(V_RT), mp()}, rc(),
+                             norm()));
+        return MTJG_OK;
+    }
+    int cgs_body()
+    {
+        const int pcm = pc_mode(S);
+        double *phat = pcm == kPcIdentity ? v(V_P) : v(V_PH);
+        PH_CHECK(launch_rows(S->ctx, A->rtiles,
+                             CsP<STRICT>{v(V_U), v(V_P), phat, v(V_R), v(V_Q), invdiag(), pcm, S->st}, rc(), norm()));
+        if (pcm == kPcExternal) {
+            int st = pc(v(V_P), phat, gate());
+            if (st != MTJG_OK) return st;
+        }
+        PH_CHECK(launch_spmv(S->ctx, csr(), A->tiles, phat, CsV<STRICT>{v(V_VH), v(V_RT), S->st}, rc(), norm()));
+        PH_CHECK(launch_rows(S->ctx, A->rtiles,
+                             CsQ<STRICT>{v(V_Q), v(V_SUM), v(V_UH), v(V_X), v(V_VH), v(V_U), invdiag(), pcm, S->st},
+                             rc(), norm()));
+        if (pcm == kPcExternal) {
+            int st = pc(v(V_SUM), v(V_UH), gate());
+            if (st != MTJG_OK) return st;
+            PH_CHECK(launch_rows(S->ctx, A->rtiles, CsX<STRICT>{v(V_X), v(V_UH), S->st}, rc(), norm()));
+        }
+        PH_CHECK(launch_spmv(S->ctx, csr(), A->tiles, v(V_UH), CsQh<STRICT>{v(V_R), v(V_RT), mp()}, rc(), norm()));
+        return MTJG_OK;
+    }
+
+    // ---- QMR (S/QMR.java:117-213)
+    int qmr_init()
+    {
+        const int pcm = pc_mode(S);
+        PH_CHECK(launch_spmv(S->ctx, csr(), A->tiles, v(V_X),
+                             QmInit<STRICT>{v(V_B), v(V_R), v(V_VT), v(V_WT), v(V_Y), v(V_Z), invdiag(), pcm, mp()},
+                             rc(), norm()));
+        if (pcm == kPcExternal) {
+            int st = pc(v(V_VT), v(V_Y), gate());
+            if (st == MTJG_OK) st = pct(v(V_WT), v(V_Z), gate());
+            if (st != MTJG_OK) return st;
+            PH_CHECK(launch_rows(S->ctx, A->rtiles, QmNorms<STRICT>{v(V_Y), v(V_Z), mp()}, rc(), norm()));
+        }
+        return MTJG_OK;
+    }
+    int qmr_body()
+    {
+        const int pcm = pc_mode(S);
+        PH_CHECK(launch_rows(S->ctx, A->rtiles,
+                             QmA<STRICT>{v(V_V), v(V_Y), v(V_W), v(V_Z), v(V_YT), v(V_ZTL), v(V_VT), v(V_WT),
+                                         invdiag(), pcm, mp()},
+                             rc(), norm()));
+        if (pcm == kPcExternal) {
+            int st = pc(v(V_Y), v(V_YT), gate());
+            if (st == MTJG_OK) st = pct(v(V_Z), v(V_ZTL), gate());
+            if (st != MTJG_OK) return st;
+        }
+        PH_CHECK(launch_rows(S->ctx, A->rtiles, QmP<STRICT>{v(V_P), v(V_Q), v(V_YT), v(V_ZTL), S->st}, rc(), norm()));
+        PH_CHECK(launch_spmv(S->ctx, csr(), A->tiles, v(V_P), QmPt<STRICT>{v(V_PTL), v(V_Q), mp()}, rc(), norm()));
+        PH_CHECK(launch_rows(S->ctx, A->rtiles,
+                             QmV<STRICT>{v(V_VT), v(V_Y), v(V_V), v(V_PTL), invdiag(), pcm, S->st}, rc(), norm()));
+        if (pcm == kPcExternal) {
+            int st = pc(v(V_VT), v(V_Y), gate());
+            if (st != MTJG_OK) return st;
+            PH_CHECK(launch_rows(S->ctx, A->rtiles, QmRho<STRICT>{v(V_Y), S->st}, rc(), norm()));
+        }
+        PH_CHECK(launch_spmv(S->ctx, tcsr(), A->t_tiles, v(V_Q),
+                             QmW<STRICT>{v(V_WT), v(V_Z), v(V_W), invdiag(), pcm, mp()}, trc(), norm()));
+        if (pcm == kPcExternal) {
+            int st = pct(v(V_WT), v(V_Z), gate());
+            if (st != MTJG_OK) return st;
+            PH_CHECK(launch_rows(S->ctx, A->rtiles, QmXi<STRICT>{v(V_Z), mp()}, rc(), norm()));
+        }
+        PH_CHECK(launch_rows(S->ctx, A->rtiles,
+                             QmUpd<STRICT>{v(V_D), v(V_S), v(V_X), v(V_R), v(V_P), v(V_PTL), mp()}, rc(), norm()));
         return MTJG_OK;
     }
 
@@ -909,9 +1089,16 @@ int run_phase(mtjg_solver *S, mtjg_csr *A, bool init)
 {
     if (S->mixed) return init ? MTJG_OK : mixed_body(S, A);
     Phases<STRICT> ph{S, A};
-    if (S->kind == MTJG_CG) return init ? ph.cg_init() : ph.cg_body();
-    if (S->kind == MTJG_BICGSTAB) return init ? ph.bi_init() : ph.bi_body();
-    return init ? ph.gm_init() : ph.gm_body();
+    switch (S->kind) {
+    case MTJG_CG: return init ? ph.cg_init() : ph.cg_body();
+    case MTJG_BICGSTAB: return init ? ph.bi_init() : ph.bi_body();
+    case MTJG_BICG: return init ? ph.bicg_init() : ph.bicg_body();
+    case MTJG_CGS: return init ? ph.cgs_init() : ph.cgs_body();
+    case MTJG_QMR: return init ? ph.qmr_init() : ph.qmr_body();
+    case MTJG_CHEBYSHEV: return init ? ph.cheb_init() : ph.cheb_body();
+    case MTJG_IR: return init ? ph.ir_init() : ph.ir_body();
+    default: return init ? ph.gm_init() : ph.gm_body();
+    }
 }
 
 int phase(mtjg_solver *S, mtjg_csr *A, bool init)
@@ -946,6 +1133,7 @@ int capture(mtjg_solver *S, mtjg_csr *A)
     S->g_numerics = ctx->numerics;
     S->g_norm = S->mon.norm;
     S->g_version = S->M ? S->M->version : 0;
+    S->g_aversion = A->version;
     return MTJG_OK;
 }
 
@@ -983,8 +1171,11 @@ int report(mtjg_solver *S, mtjg_result *res)
         res->history_len = S->last.hist_len;
         res->inner_iterations = S->last.in_total;
     }
-    if (code == MTJG_NOT_CONVERGED_BREAKDOWN)
-        set_error(S->last.detail == 1 ? "Breakdown: rho" : "Breakdown: omega");
+    if (code == MTJG_NOT_CONVERGED_BREAKDOWN) {
+        static const char *what[] = {"", "rho", "omega", "xi", "delta", "ep", "beta", "gamma"};
+        const int d = S->last.detail;
+        set_error(std::string("Breakdown: ") + (d >= 1 && d <= 7 ? what[d] : "?"));
+    }
     else if (code == MTJG_NOT_CONVERGED_ITERATIONS)
         set_error("Iterations");
     else if (code == MTJG_NOT_CONVERGED_DIVERGENCE)
@@ -1043,10 +1234,17 @@ int run(mtjg_solver *S, mtjg_csr *A, mtjg_result *res)
     MTJG_CUDA(cudaMemcpyAsync(A->num_running, &S->num_sys, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
     MTJG_CUDA(cudaMemsetAsync(A->cnt, 0, sizeof(unsigned) * (size_t)ns, ctx->stream));
     MTJG_CUDA(cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream));
+    // what the loop body needs that allocates: before any capture
+    if (needs_transpose(S->kind)) {
+        st = csr_ensure_transpose(A);
+        if (st == MTJG_OK && S->M) st = precond_prepare_trans(S->M);
+        if (st != MTJG_OK) return st;
+    }
     st = phase(S, A, true);
     if (st != MTJG_OK) return st;
     const bool stale = !S->gexec || S->g_A != A || S->g_M != S->M || S->g_numerics != ctx->numerics ||
-                       S->g_norm != S->mon.norm || S->g_version != (S->M ? S->M->version : 0);
+                       S->g_norm != S->mon.norm || S->g_version != (S->M ? S->M->version : 0) ||
+                       S->g_aversion != A->version;
     if (stale) {
         st = capture(S, A);
         if (st != MTJG_OK) return st;
@@ -1123,10 +1321,12 @@ int run_empty(mtjg_solver *S, mtjg_result *res)
         S->last.status = ST_DONE;
     } else if (mi == 0) {
         S->last.status = MTJG_NOT_CONVERGED_ITERATIONS;
-    } else if (S->kind == MTJG_BICGSTAB) {
+    } else if (S->kind == MTJG_BICGSTAB || S->kind == MTJG_BICG || S->kind == MTJG_CGS || S->kind == MTJG_QMR) {
+        // rho = 0: BiCGstab, BiCG and CGS form it as a dot product of zero
+        // vectors, QMR as a norm (S/BiCG.java:75-79, S/CGS.java:75-79, S/QMR.java:134-137)
         S->last.status = MTJG_NOT_CONVERGED_BREAKDOWN;
         S->last.detail = 1;  // rho
-    } else if (S->kind == MTJG_CG) {
+    } else if (S->kind == MTJG_CG || S->kind == MTJG_CHEBYSHEV || S->kind == MTJG_IR) {
         S->last.status = MTJG_NOT_CONVERGED_ITERATIONS;
         S->last.iter = mi;
         for (int k = 1; k <= mi; ++k) it.push_back(k);
@@ -1156,6 +1356,8 @@ int check_sizes(mtjg_solver *S, mtjg_csr *A)
     if (S->n != A->n) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "b.size() != A.numRows()");
     if (S->M && S->M->n != A->n) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "preconditioner size differs from A");
     if (S->M && !S->M->ready) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "preconditioner setMatrix has not been called");
+    if (S->kind == MTJG_CHEBYSHEV && !S->eig_set)
+        return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "Chebyshev needs its eigenvalue bounds (mtjg_solver_set_eigenvalues)");
     if (S->mixed && (S->kind != MTJG_CG ||
                      (S->M && S->M->kind != MTJG_PC_IDENTITY && S->M->kind != MTJG_PC_JACOBI)))
         return fail(MTJG_ERR_UNSUPPORTED, "mixed precision supports CG with the identity or Jacobi preconditioner");
@@ -1174,7 +1376,7 @@ extern "C" int mtjg_solver_create(mtjg_ctx *ctx, int kind, int n, int restart, m
 {
     if (!ctx || !out) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL argument");
     *out = nullptr;
-    if (kind < MTJG_CG || kind > MTJG_GMRES) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "unknown solver kind");
+    if (kind < MTJG_CG || kind > MTJG_IR) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "unknown solver kind");
     if (n < 0) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "negative size");
     if (kind == MTJG_GMRES && restart <= 0) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "restart must be a positive integer");
     MTJG_CUDA(cudaSetDevice(ctx->device));
@@ -1187,8 +1389,13 @@ extern "C" int mtjg_solver_create(mtjg_ctx *ctx, int kind, int n, int restart, m
     mtjg_monitor_defaults(&S->mon);
     S->vecs.assign(V_COUNT, nullptr);
     std::vector<int> need;
-    if (kind == MTJG_CG) need = {V_B, V_X, V_R, V_Z, V_P, V_Q};
+    if (kind == MTJG_CG || kind == MTJG_CHEBYSHEV) need = {V_B, V_X, V_R, V_Z, V_P, V_Q};
     else if (kind == MTJG_BICGSTAB) need = {V_B, V_X, V_R, V_RT, V_P, V_PH, V_S, V_SH, V_T, V_V};
+    else if (kind == MTJG_BICG) need = {V_B, V_X, V_R, V_Z, V_P, V_Q, V_RT, V_ZT, V_PT, V_QT};
+    else if (kind == MTJG_CGS) need = {V_B, V_X, V_R, V_RT, V_P, V_Q, V_U, V_PH, V_VH, V_UH, V_SUM};
+    else if (kind == MTJG_QMR)
+        need = {V_B, V_X, V_R, V_Y, V_Z, V_V, V_W, V_P, V_Q, V_D, V_S, V_VT, V_WT, V_YT, V_ZTL, V_PTL};
+    else if (kind == MTJG_IR) need = {V_B, V_X, V_R, V_Z};
     else need = {V_B, V_X, V_R, V_U, V_W};
     const size_t nb = sizeof(double) * (size_t)std::max(1, n);
     bool ok = ensure_state(S, 1) == MTJG_OK;
@@ -1261,6 +1468,23 @@ extern "C" int mtjg_solver_set_monitor(mtjg_solver *S, const mtjg_monitor *mon)
     S->mon = *mon;
     drop_graph(S);
     return ensure_state(S, std::max(1, S->num_sys));
+}
+
+extern "C" int mtjg_solver_set_eigenvalues(mtjg_solver *S, double eigmin, double eigmax)
+{
+    if (!S) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL solver");
+    if (S->kind != MTJG_CHEBYSHEV) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "eigenvalue bounds are Chebyshev's");
+    // Chebyshev.setEigenvalues, S/Chebyshev.java:78-88
+    if (eigmin <= 0) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "eigmin <= 0");
+    if (eigmax <= 0) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "eigmax <= 0");
+    if (eigmin > eigmax) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "eigmin > eigmax");
+    MTJG_CUDA(cudaSetDevice(S->ctx->device));
+    MTJG_CUDA(cudaStreamSynchronize(S->ctx->stream));
+    S->eigmin = eigmin;
+    S->eigmax = eigmax;
+    S->eig_set = true;
+    drop_graph(S);
+    return MTJG_OK;
 }
 
 extern "C" int mtjg_solver_set_mixed(mtjg_solver *S, int enable, double inner_rtol, int inner_max_iter)

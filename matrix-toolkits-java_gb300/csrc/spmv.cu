@@ -495,8 +495,11 @@ extern "C" int mtjg_csr_update_values(mtjg_csr *A, const double *val)
     cudaFree(A->t_rowptr);
     cudaFree(A->t_colind);
     cudaFree(A->t_val);
+    cudaFree(A->t_part);
     A->t_rowptr = A->t_colind = nullptr;
-    A->t_val = nullptr;
+    A->t_val = A->t_part = nullptr;
+    static std::atomic<int64_t> s_version{0};
+    A->version = ++s_version;
     free_tiles(A->t_tiles);
     cudaFree(A->val32);  // the FP32 copy too
     A->val32 = nullptr;
@@ -514,6 +517,7 @@ extern "C" int mtjg_csr_destroy(mtjg_csr *A)
     cudaFree(A->t_rowptr);
     cudaFree(A->t_colind);
     cudaFree(A->t_val);
+    cudaFree(A->t_part);
     cudaFree(A->val32);
     cudaFree(A->part);
     cudaFree(A->cnt);
@@ -549,7 +553,15 @@ extern "C" int mtjg_csr_to_host(const mtjg_csr *A, int *rowptr, int *colind, dou
     return MTJG_OK;
 }
 
-static int ensure_transpose(mtjg_csr *A)
+namespace mtjg {
+// The transpose of A (for transMult and the transposed products of BiCG and
+// QMR), its tiles and its reduction scratch, built on first use.
+int csr_ensure_transpose(mtjg_csr *A);
+}  // namespace mtjg
+
+static int ensure_transpose(mtjg_csr *A) { return mtjg::csr_ensure_transpose(A); }
+
+int mtjg::csr_ensure_transpose(mtjg_csr *A)
 {
     if (A->t_rowptr) return MTJG_OK;
     mtjg_ctx *ctx = A->ctx;
@@ -565,7 +577,10 @@ static int ensure_transpose(mtjg_csr *A)
     plan_tiles(trp.data(), 0, A->m, vec, tile_row, tile_flags);
     tile_row.push_back(A->m);
     std::vector<int> sys_tile = {0, (int)tile_flags.size()};
-    return upload_tiles(A->t_tiles, tile_row, tile_flags, nullptr, sys_tile, vec, trp.data(), kGroupTiles);
+    st = upload_tiles(A->t_tiles, tile_row, tile_flags, nullptr, sys_tile, vec, trp.data(), kGroupTiles);
+    if (st != MTJG_OK) return st;
+    MTJG_CUDA(cudaMalloc(&A->t_part, sizeof(double) * (size_t)std::max(1, A->t_tiles.num_groups) * kParts));
+    return MTJG_OK;
 }
 
 static int check_err_flag(mtjg_ctx *ctx)

@@ -37,7 +37,7 @@ ERR_DEVICE_TIMEOUT = 42
 
 NORM_ONE, NORM_TWO, NORM_TWO_ROBUST, NORM_INFINITY = 0, 1, 2, 3
 PC_IDENTITY, PC_JACOBI, PC_ILU, PC_ICC = 0, 1, 2, 3
-CG, BICGSTAB, GMRES = 0, 1, 2
+CG, BICGSTAB, GMRES, BICG, CGS, QMR, CHEBYSHEV, IR = 0, 1, 2, 3, 4, 5, 6, 7
 NUMERICS_FAST, NUMERICS_STRICT = 0, 1
 
 
@@ -118,6 +118,7 @@ PROTOTYPES = {
     "mtjg_solver_destroy": (C.c_int, [_vp]),
     "mtjg_batch_upload": (C.c_int, [_vp, C.c_int, _ip, _ip, _ip, _dp, C.POINTER(_vp)]),
     "mtjg_solver_set_mixed": (C.c_int, [_vp, C.c_int, C.c_double, C.c_int]),
+    "mtjg_solver_set_eigenvalues": (C.c_int, [_vp, C.c_double, C.c_double]),
     "mtjg_server_config_defaults": (None, [C.POINTER(ServerConfig)]),
     "mtjg_server_create": (C.c_int, [_vp, C.POINTER(ServerConfig), C.POINTER(_vp)]),
     "mtjg_server_add_matrix": (C.c_int, [_vp, C.c_int, _ip, _ip, _dp, _ip]),

@@ -8,6 +8,7 @@ src/main/java/no/uib/cipr/matrix/sparse/, M/ = src/main/java/no/uib/cipr/matrix/
   DiagonalPreconditioner      S/DiagonalPreconditioner.java
   ILU, ICC                    S/ILU.java, S/ICC.java
   CG, BiCGstab, GMRES         S/CG.java, S/BiCGstab.java, S/GMRES.java
+  BiCG, CGS, QMR, Chebyshev, IR  S/BiCG.java, S/CGS.java, S/QMR.java, S/Chebyshev.java, S/IR.java
   DefaultIterationMonitor     S/DefaultIterationMonitor.java
   IterativeSolverNotConvergedException, NotConvergedException.Reason
 
@@ -73,6 +74,10 @@ class IterativeSolverNotConvergedException(NotConvergedException):
 
     def getIterations(self):
         return self._it
+
+
+# mtjg_result.detail of a breakdown -> the name MTJ's exception message carries
+BREAKDOWN = {1: "rho", 2: "omega", 3: "xi", 4: "delta", 5: "ep", 6: "beta", 7: "gamma"}
 
 
 def _raise(code: int, what: str = ""):
@@ -593,7 +598,7 @@ class AbstractIterativeSolver:
         self._replay()
         if code in (L.NOT_CONVERGED_ITERATIONS, L.NOT_CONVERGED_DIVERGENCE, L.NOT_CONVERGED_BREAKDOWN):
             reason = NotConvergedException.Reason(code)
-            msg = {1: "rho", 2: "omega"}.get(res.detail, "") if code == L.NOT_CONVERGED_BREAKDOWN else ""
+            msg = BREAKDOWN.get(res.detail, "") if code == L.NOT_CONVERGED_BREAKDOWN else ""
             raise IterativeSolverNotConvergedException(reason, res.residual, res.iterations, msg)
         _raise(code, "solve")
         return x
@@ -662,6 +667,46 @@ class BiCGstab(AbstractIterativeSolver):
     """S/BiCGstab.java"""
 
     kind = L.BICGSTAB
+
+
+class BiCG(AbstractIterativeSolver):
+    """S/BiCG.java (uses M.transApply and A.transMult)."""
+
+    kind = L.BICG
+
+
+class CGS(AbstractIterativeSolver):
+    """S/CGS.java"""
+
+    kind = L.CGS
+
+
+class QMR(AbstractIterativeSolver):
+    """S/QMR.java with M1 = M2 = the solver's preconditioner (QMR(Vector),
+    :65-80; setPreconditioner, :216-220)."""
+
+    kind = L.QMR
+
+
+class IR(AbstractIterativeSolver):
+    """S/IR.java (Richardson iteration with the preconditioner)."""
+
+    kind = L.IR
+
+
+class Chebyshev(AbstractIterativeSolver):
+    """S/Chebyshev.java: new Chebyshev(template, eigmin, eigmax)."""
+
+    kind = L.CHEBYSHEV
+
+    def __init__(self, template, eigmin, eigmax, ctx=None):
+        super().__init__(template, 0, ctx)
+        self.setEigenvalues(eigmin, eigmax)
+
+    def setEigenvalues(self, eigmin, eigmax):
+        """Chebyshev.setEigenvalues, S/Chebyshev.java:78-88."""
+        _raise(self._lib.mtjg_solver_set_eigenvalues(self.h, float(eigmin), float(eigmax)), "setEigenvalues")
+        self.eigmin, self.eigmax = float(eigmin), float(eigmax)
 
 
 class GMRES(AbstractIterativeSolver):

@@ -592,8 +592,8 @@ static int bicgstab_solve(int n, const int *rp, const int *ci, const double *v, 
     int st;
     for (m->iter = 0; (st = mon_check_vec(m, n, r)) < 0; m->iter++) {
         rho_1 = or_dot(n, rtilde, r);
-        if (rho_1 == 0) { st = OR_NC_BREAKDOWN; *detail = 1; break; }
-        if (omega == 0) { st = OR_NC_BREAKDOWN; *detail = 2; break; }
+        if (rho_1 == 0) { st = OR_NC_BREAKDOWN; *detail = OR_BD_RHO; break; }
+        if (omega == 0) { st = OR_NC_BREAKDOWN; *detail = OR_BD_OMEGA; break; }
         if (m->iter == 0)
             memcpy(p, r, sizeof(double) * (size_t)n);
         else {
@@ -726,10 +726,241 @@ done:
     return st;
 }
 
+static void pc_trans_apply_or_identity(or_pc *pc, int n, const double *b, double *x)
+{
+    if (pc) or_pc_trans_apply(pc, b, x);
+    else if (x != b) memcpy(x, b, sizeof(double) * (size_t)n);
+}
+
+static void vcopy(int n, double *d, const double *s) { memcpy(d, s, sizeof(double) * (size_t)n); }
+
+/* BiCG.solve, S/BiCG.java:63-102 */
+static int bicg_solve(int n, const int *rp, const int *ci, const double *v, or_pc *pc,
+                      const double *b, double *x, mon_state *m, int *detail)
+{
+    double rho_1 = 1, rho_2 = 1, alpha = 1, beta = 1;
+    size_t sz = (size_t)n + 1;
+    double *z = calloc(sz, 8), *p = calloc(sz, 8), *q = calloc(sz, 8), *r = calloc(sz, 8);
+    double *zt = calloc(sz, 8), *pt = calloc(sz, 8), *qt = calloc(sz, 8), *rt = calloc(sz, 8);
+    vcopy(n, r, b);
+    or_mult_add(n, rp, ci, v, -1, x, r);
+    vcopy(n, rt, r);
+    int st;
+    for (m->iter = 0; (st = mon_check_vec(m, n, r)) < 0; m->iter++) {
+        pc_apply_or_identity(pc, n, r, z);
+        pc_trans_apply_or_identity(pc, n, rt, zt);
+        rho_1 = or_dot(n, z, rt);
+        if (rho_1 == 0.) { st = OR_NC_BREAKDOWN; *detail = OR_BD_RHO; break; }
+        if (m->iter == 0) {
+            vcopy(n, p, z);
+            vcopy(n, pt, zt);
+        } else {
+            beta = rho_1 / rho_2;
+            vscale(n, p, beta);
+            vadd(n, p, z);
+            vscale(n, pt, beta);
+            vadd(n, pt, zt);
+        }
+        or_mult(n, rp, ci, v, p, q);
+        or_trans_mult(n, n, rp, ci, v, pt, qt);
+        alpha = rho_1 / or_dot(n, pt, q);
+        vadd_a(n, x, alpha, p);
+        vadd_a(n, r, -alpha, q);
+        vadd_a(n, rt, -alpha, qt);
+        rho_2 = rho_1;
+    }
+    free(z); free(p); free(q); free(r); free(zt); free(pt); free(qt); free(rt);
+    return st;
+}
+
+/* CGS.solve, S/CGS.java:65-105 */
+static int cgs_solve(int n, const int *rp, const int *ci, const double *v, or_pc *pc,
+                     const double *b, double *x, mon_state *m, int *detail)
+{
+    double rho_1 = 0, rho_2 = 0, alpha = 0, beta = 0;
+    size_t sz = (size_t)n + 1;
+    double *p = calloc(sz, 8), *q = calloc(sz, 8), *u = calloc(sz, 8), *phat = calloc(sz, 8);
+    double *qhat = calloc(sz, 8), *vhat = calloc(sz, 8), *uhat = calloc(sz, 8), *sum = calloc(sz, 8);
+    double *r = calloc(sz, 8), *rt = calloc(sz, 8);
+    vcopy(n, r, b);
+    or_mult_add(n, rp, ci, v, -1, x, r);
+    vcopy(n, rt, r);
+    int st;
+    for (m->iter = 0; (st = mon_check_vec(m, n, r)) < 0; m->iter++) {
+        rho_1 = or_dot(n, rt, r);
+        if (rho_1 == 0) { st = OR_NC_BREAKDOWN; *detail = OR_BD_RHO; break; }
+        if (m->iter == 0) {
+            vcopy(n, u, r);
+            vcopy(n, p, u);
+        } else {
+            beta = rho_1 / rho_2;
+            vcopy(n, u, r);
+            vadd_a(n, u, beta, q);
+            vcopy(n, sum, q);
+            vadd_a(n, sum, beta, p);
+            vcopy(n, p, u);
+            vadd_a(n, p, beta, sum);
+        }
+        pc_apply_or_identity(pc, n, p, phat);
+        or_mult(n, rp, ci, v, phat, vhat);
+        alpha = rho_1 / or_dot(n, rt, vhat);
+        vset_a(n, q, -alpha, vhat);
+        vadd(n, q, u);
+        vcopy(n, sum, u);
+        vadd(n, sum, q);
+        pc_apply_or_identity(pc, n, sum, uhat);
+        vadd_a(n, x, alpha, uhat);
+        or_mult(n, rp, ci, v, uhat, qhat);
+        vadd_a(n, r, -alpha, qhat);
+        rho_2 = rho_1;
+    }
+    free(p); free(q); free(u); free(phat); free(qhat); free(vhat); free(uhat); free(sum); free(r); free(rt);
+    return st;
+}
+
+/* QMR.solve, S/QMR.java:117-213, with M1 = M2 = the solver's preconditioner
+ * (QMR(Vector), :65-80, and setPreconditioner, :216-220) */
+static int qmr_solve(int n, const int *rp, const int *ci, const double *vals, or_pc *pc,
+                     const double *b, double *x, mon_state *m, int *detail)
+{
+    double rho = 0, rho_1 = 0, xi = 0, gamma = 1., gamma_1 = 0, theta = 0, theta_1 = 0,
+           eta = -1., delta = 0, ep = 0, beta = 0;
+    size_t sz = (size_t)n + 1;
+    double *r = calloc(sz, 8), *y = calloc(sz, 8), *z = calloc(sz, 8), *v = calloc(sz, 8);
+    double *w = calloc(sz, 8), *p = calloc(sz, 8), *q = calloc(sz, 8), *d = calloc(sz, 8);
+    double *s = calloc(sz, 8), *v_tld = calloc(sz, 8), *w_tld = calloc(sz, 8), *y_tld = calloc(sz, 8);
+    double *z_tld = calloc(sz, 8), *p_tld = calloc(sz, 8);
+    vcopy(n, r, b);
+    or_mult_add(n, rp, ci, vals, -1, x, r);
+    vcopy(n, v_tld, r);
+    pc_apply_or_identity(pc, n, v_tld, y);
+    rho = or_norm(n, y, OR_NORM_TWO);
+    vcopy(n, w_tld, r);
+    pc_trans_apply_or_identity(pc, n, w_tld, z);
+    xi = or_norm(n, z, OR_NORM_TWO);
+    int st;
+    for (m->iter = 0; (st = mon_check_vec(m, n, r)) < 0; m->iter++) {
+        if (rho == 0) { st = OR_NC_BREAKDOWN; *detail = OR_BD_RHO; break; }
+        if (xi == 0) { st = OR_NC_BREAKDOWN; *detail = OR_BD_XI; break; }
+        vset_a(n, v, 1 / rho, v_tld);
+        vscale(n, y, 1 / rho);
+        vset_a(n, w, 1 / xi, w_tld);
+        vscale(n, z, 1 / xi);
+        delta = or_dot(n, z, y);
+        if (delta == 0) { st = OR_NC_BREAKDOWN; *detail = OR_BD_DELTA; break; }
+        pc_apply_or_identity(pc, n, y, y_tld);
+        pc_trans_apply_or_identity(pc, n, z, z_tld);
+        if (m->iter == 0) {
+            vcopy(n, p, y_tld);
+            vcopy(n, q, z_tld);
+        } else {
+            vscale(n, p, -xi * delta / ep);
+            vadd(n, p, y_tld);
+            vscale(n, q, -rho * delta / ep);
+            vadd(n, q, z_tld);
+        }
+        or_mult(n, rp, ci, vals, p, p_tld);
+        ep = or_dot(n, q, p_tld);
+        if (ep == 0) { st = OR_NC_BREAKDOWN; *detail = OR_BD_EP; break; }
+        beta = ep / delta;
+        if (beta == 0) { st = OR_NC_BREAKDOWN; *detail = OR_BD_BETA; break; }
+        vset_a(n, v_tld, -beta, v);
+        vadd(n, v_tld, p_tld);
+        pc_apply_or_identity(pc, n, v_tld, y);
+        rho_1 = rho;
+        rho = or_norm(n, y, OR_NORM_TWO);
+        /* A.transMultAdd(q, w_tld.set(-beta, w)): transMultAdd(1, q, w_tld) */
+        vset_a(n, w_tld, -beta, w);
+        or_trans_mult_add(n, n, rp, ci, vals, 1, q, w_tld);
+        pc_trans_apply_or_identity(pc, n, w_tld, z);
+        xi = or_norm(n, z, OR_NORM_TWO);
+        gamma_1 = gamma;
+        theta_1 = theta;
+        theta = rho / (gamma_1 * beta);
+        gamma = 1 / sqrt(1 + theta * theta);
+        if (gamma == 0) { st = OR_NC_BREAKDOWN; *detail = OR_BD_GAMMA; break; }
+        eta = -eta * rho_1 * gamma * gamma / (beta * gamma_1 * gamma_1);
+        if (m->iter == 0) {
+            vset_a(n, d, eta, p);
+            vset_a(n, s, eta, p_tld);
+        } else {
+            double val = theta_1 * theta_1 * gamma * gamma;
+            vscale(n, d, val);
+            vadd_a(n, d, eta, p);
+            vscale(n, s, val);
+            vadd_a(n, s, eta, p_tld);
+        }
+        vadd(n, x, d);
+        vadd_a(n, r, -1, s);
+    }
+    free(r); free(y); free(z); free(v); free(w); free(p); free(q); free(d); free(s);
+    free(v_tld); free(w_tld); free(y_tld); free(z_tld); free(p_tld);
+    return st;
+}
+
+/* Chebyshev.solve, S/Chebyshev.java:90-120 */
+static int chebyshev_solve(double eigmin, double eigmax, int n, const int *rp, const int *ci, const double *v,
+                           or_pc *pc, const double *b, double *x, mon_state *m)
+{
+    double alpha = 0, beta = 0, c = 0, d = 0;
+    size_t sz = (size_t)n + 1;
+    double *p = calloc(sz, 8), *z = calloc(sz, 8), *r = calloc(sz, 8), *q = calloc(sz, 8);
+    vcopy(n, r, b);
+    or_mult_add(n, rp, ci, v, -1, x, r);
+    c = (eigmax - eigmin) / 2.0;
+    d = (eigmax + eigmin) / 2.0;
+    int st;
+    for (m->iter = 0; (st = mon_check_vec(m, n, r)) < 0; m->iter++) {
+        pc_apply_or_identity(pc, n, r, z);
+        if (m->iter == 0) {
+            vcopy(n, p, z);
+            alpha = 2.0 / d;
+        } else {
+            beta = (alpha * c) / 2.0;
+            beta *= beta;
+            alpha = 1.0 / (d - beta);
+            vscale(n, p, beta);
+            vadd(n, p, z);
+        }
+        or_mult(n, rp, ci, v, p, q);
+        vadd_a(n, x, alpha, p);
+        vadd_a(n, r, -alpha, q);
+    }
+    free(p); free(z); free(r); free(q);
+    return st;
+}
+
+/* IR.solve, S/IR.java:57-70 */
+static int ir_solve(int n, const int *rp, const int *ci, const double *v, or_pc *pc, const double *b,
+                    double *x, mon_state *m)
+{
+    size_t sz = (size_t)n + 1;
+    double *z = calloc(sz, 8), *r = calloc(sz, 8);
+    vcopy(n, r, b);
+    or_mult_add(n, rp, ci, v, -1, x, r);
+    int st;
+    for (m->iter = 0; (st = mon_check_vec(m, n, r)) < 0; m->iter++) {
+        pc_apply_or_identity(pc, n, r, z);
+        vadd(n, x, z);
+        vcopy(n, r, b);
+        or_mult_add(n, rp, ci, v, -1, x, r);
+    }
+    free(z); free(r);
+    return st;
+}
+
 int or_solve(int kind, int restart, int n, const int *rowptr, const int *colind,
              const double *val, or_pc *pc, const double *b, double *x,
              const or_monitor *mon, or_result *res,
              double *hist_r, int *hist_it, int hist_cap)
+{
+    return or_solve_ex(kind, restart, 0.0, 0.0, n, rowptr, colind, val, pc, b, x, mon, res, hist_r, hist_it,
+                       hist_cap);
+}
+
+int or_solve_ex(int kind, int restart, double eigmin, double eigmax, int n, const int *rowptr,
+                const int *colind, const double *val, or_pc *pc, const double *b, double *x,
+                const or_monitor *mon, or_result *res, double *hist_r, int *hist_it, int hist_cap)
 {
     mon_state m;
     memset(&m, 0, sizeof(m));
@@ -741,6 +972,14 @@ int or_solve(int kind, int restart, int n, const int *rowptr, const int *colind,
     if (pc && pc->n != n) return OR_ERR_ILLEGAL_ARGUMENT;
     if (kind == OR_CG) st = cg_solve(n, rowptr, colind, val, pc, b, x, &m, &detail);
     else if (kind == OR_BICGSTAB) st = bicgstab_solve(n, rowptr, colind, val, pc, b, x, &m, &detail);
+    else if (kind == OR_BICG) st = bicg_solve(n, rowptr, colind, val, pc, b, x, &m, &detail);
+    else if (kind == OR_CGS) st = cgs_solve(n, rowptr, colind, val, pc, b, x, &m, &detail);
+    else if (kind == OR_QMR) st = qmr_solve(n, rowptr, colind, val, pc, b, x, &m, &detail);
+    else if (kind == OR_CHEBYSHEV) {
+        /* Chebyshev.setEigenvalues, S/Chebyshev.java:78-88 */
+        if (eigmin <= 0 || eigmax <= 0 || eigmin > eigmax) return OR_ERR_ILLEGAL_ARGUMENT;
+        st = chebyshev_solve(eigmin, eigmax, n, rowptr, colind, val, pc, b, x, &m);
+    } else if (kind == OR_IR) st = ir_solve(n, rowptr, colind, val, pc, b, x, &m);
     else {
         if (restart <= 0) return OR_ERR_ILLEGAL_ARGUMENT;
         st = gmres_solve(restart, n, rowptr, colind, val, pc, b, x, &m, &detail);

@@ -42,7 +42,9 @@ enum {
 
 enum { OR_NORM_ONE = 0, OR_NORM_TWO = 1, OR_NORM_TWO_ROBUST = 2, OR_NORM_INFINITY = 3 };
 enum { OR_PC_IDENTITY = 0, OR_PC_JACOBI = 1, OR_PC_ILU = 2, OR_PC_ICC = 3, OR_PC_ICC_LITERAL = 4 };
-enum { OR_CG = 0, OR_BICGSTAB = 1, OR_GMRES = 2 };
+enum { OR_CG = 0, OR_BICGSTAB = 1, OR_GMRES = 2, OR_BICG = 3, OR_CGS = 4, OR_QMR = 5, OR_CHEBYSHEV = 6, OR_IR = 7 };
+/* or_result.detail of a breakdown: which quantity became zero */
+enum { OR_BD_RHO = 1, OR_BD_OMEGA = 2, OR_BD_XI = 3, OR_BD_DELTA = 4, OR_BD_EP = 5, OR_BD_BETA = 6, OR_BD_GAMMA = 7 };
 
 typedef struct or_monitor {
     int max_iter;
@@ -54,7 +56,7 @@ typedef struct or_result {
     int status;
     int iterations;
     double residual;
-    int detail;        /* breakdown: 1 = "rho", 2 = "omega" */
+    int detail;        /* breakdown: OR_BD_* ("rho", "omega", "xi", "delta", "ep", "beta", "gamma") */
     int history_len;   /* monitor calls made (may exceed the history capacity) */
 } or_result;
 
@@ -88,11 +90,16 @@ void or_pc_trans_apply(or_pc *pc, const double *b, double *x);
 /* factor values (ILU/ICC: the in-place data array; Jacobi: invdiag) */
 int or_pc_values(const or_pc *pc, double *out, int cap);
 
-/* IterativeSolver.solve (S/CG.java, S/BiCGstab.java, S/GMRES.java) */
+/* IterativeSolver.solve (S/CG.java, S/BiCGstab.java, S/GMRES.java, S/BiCG.java,
+ * S/CGS.java, S/QMR.java, S/Chebyshev.java, S/IR.java); pc NULL = identity */
 int or_solve(int kind, int restart, int n, const int *rowptr, const int *colind,
              const double *val, or_pc *pc, const double *b, double *x,
              const or_monitor *mon, or_result *res,
              double *hist_r, int *hist_it, int hist_cap);
+/* the same with Chebyshev's eigenvalue bounds (ignored by the other kinds) */
+int or_solve_ex(int kind, int restart, double eigmin, double eigmax, int n, const int *rowptr,
+                const int *colind, const double *val, or_pc *pc, const double *b, double *x,
+                const or_monitor *mon, or_result *res, double *hist_r, int *hist_it, int hist_cap);
 
 #ifdef __cplusplus
 }

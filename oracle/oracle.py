@@ -29,7 +29,9 @@ OK, NC_ITERATIONS, NC_DIVERGENCE, NC_BREAKDOWN = 0, 1, 2, 3
 ERR_ILLEGAL_ARGUMENT, ERR_ZERO_PIVOT, ERR_ZERO_DIAGONAL, ERR_MISSING_DIAGONAL, ERR_SINGULAR = 10, 20, 21, 22, 23
 NORM_ONE, NORM_TWO, NORM_TWO_ROBUST, NORM_INFINITY = 0, 1, 2, 3
 PC_IDENTITY, PC_JACOBI, PC_ILU, PC_ICC, PC_ICC_LITERAL = 0, 1, 2, 3, 4
-CG, BICGSTAB, GMRES = 0, 1, 2
+CG, BICGSTAB, GMRES, BICG, CGS, QMR, CHEBYSHEV, IR = 0, 1, 2, 3, 4, 5, 6, 7
+# breakdown detail: which quantity became zero
+BD_RHO, BD_OMEGA, BD_XI, BD_DELTA, BD_EP, BD_BETA, BD_GAMMA = 1, 2, 3, 4, 5, 6, 7
 
 
 def build() -> str:
@@ -77,8 +79,12 @@ def lib():
         l.or_pc_apply.argtypes = [C.c_void_p, _dp, _dp]
         l.or_pc_trans_apply.argtypes = [C.c_void_p, _dp, _dp]
         l.or_pc_values.argtypes = [C.c_void_p, _dp, C.c_int]
+        l.or_solve.restype = C.c_int
         l.or_solve.argtypes = [C.c_int, C.c_int, C.c_int, _ip, _ip, _dp, C.c_void_p, _dp, _dp,
                                C.POINTER(Monitor), C.POINTER(Result), _dp, _ip, C.c_int]
+        l.or_solve_ex.restype = C.c_int
+        l.or_solve_ex.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, _ip, _ip, _dp, C.c_void_p,
+                                  _dp, _dp, C.POINTER(Monitor), C.POINTER(Result), _dp, _ip, C.c_int]
         l.or_set_sum_order.argtypes = [C.c_int]
         _lib = l
     return _lib
@@ -197,8 +203,9 @@ class Precond:
 
 
 def solve(kind, A: Csr, b, x0, pc: Precond | None = None, max_iter=100000, rtol=1e-5, atol=1e-50, dtol=1e5,
-          norm_type=NORM_TWO, restart=30, hist_cap=None):
-    """Runs the restated solver; returns (x, Result, hist_r, hist_it)."""
+          norm_type=NORM_TWO, restart=30, hist_cap=None, eigmin=0.0, eigmax=0.0):
+    """Runs the restated solver; returns (x, Result, hist_r, hist_it).
+    eigmin / eigmax are Chebyshev's eigenvalue bounds."""
     b = np.ascontiguousarray(b, dtype=np.float64)
     x = np.array(x0, dtype=np.float64, copy=True)
     if hist_cap is None:
@@ -207,7 +214,8 @@ def solve(kind, A: Csr, b, x0, pc: Precond | None = None, max_iter=100000, rtol=
     hi = np.empty(max(hist_cap, 1), dtype=np.int32)
     mon = Monitor(max_iter, rtol, atol, dtol, norm_type)
     res = Result()
-    lib().or_solve(kind, restart, A.n, _i(A.rp), _i(A.ci), _d(A.v), pc.h if pc else None, _d(b),
-                   _d(x) if len(x) else _d(np.zeros(1)), C.byref(mon), C.byref(res), _d(hr), _i(hi), hist_cap)
+    res.status = lib().or_solve_ex(kind, restart, eigmin, eigmax, A.n, _i(A.rp), _i(A.ci), _d(A.v),
+                                   pc.h if pc else None, _d(b), _d(x) if len(x) else _d(np.zeros(1)), C.byref(mon),
+                                   C.byref(res), _d(hr), _i(hi), hist_cap)
     k = min(res.history_len, hist_cap)
     return x, res, hr[:k].copy(), hi[:k].copy()

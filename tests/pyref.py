@@ -339,3 +339,226 @@ def gmres(rp, ci, v, b, x, M, mon, restart=30):
         normr = norm2(r)
         mon.iter += 1
     return x
+
+
+# --------------------------------------------- BiCG, CGS, QMR, Chebyshev, IR
+def trans_mult(rp, ci, v, x, m):
+    """CompRowMatrix.transMult, S/CompRowMatrix.java:350-366 (scatter)."""
+    y = [0.0] * m
+    for i in range(len(rp) - 1):
+        for k in range(rp[i], rp[i + 1]):
+            y[ci[k]] = y[ci[k]] + v[k] * x[i]
+    return y
+
+
+def trans_mult_add(rp, ci, v, alpha, x, y):
+    """CompRowMatrix.transMultAdd, S/CompRowMatrix.java:369-388."""
+    y = [yi * (1 / alpha) for yi in y]
+    for i in range(len(rp) - 1):
+        for k in range(rp[i], rp[i + 1]):
+            y[ci[k]] = y[ci[k]] + v[k] * x[i]
+    return [yi * alpha for yi in y]
+
+
+def ilu_trans_apply(rp, ci, data, dg, b):
+    """ILU.transApply (S/ILU.java:72-78): U' then L' scatter solves
+    (S/UpperCompRowMatrix.java:70-90, S/UnitLowerCompRowMatrix.java:70-86)."""
+    n = len(rp) - 1
+    y = list(b)
+    for i in range(n):
+        y[i] = y[i] / data[dg[i]]
+        for k in range(dg[i] + 1, rp[i + 1]):
+            y[ci[k]] = y[ci[k]] - data[k] * y[i]
+    x = list(y)
+    for i in range(n - 1, -1, -1):
+        for k in range(rp[i], dg[i]):
+            x[ci[k]] = x[ci[k]] - data[k] * x[i]
+    return x
+
+
+def _set(alpha, y):  # DenseVector.set(alpha, y), M/DenseVector.java:216-231
+    return [0.0] * len(y) if alpha == 0 else [alpha * t for t in y]
+
+
+def _add(d, alpha, y):  # DenseVector.add(alpha, y), M/DenseVector.java:249-264
+    return list(d) if alpha == 0 else [d[i] + alpha * y[i] for i in range(len(d))]
+
+
+def bicg(rp, ci, v, b, x, M, Mt, mon):
+    """BiCG.solve, S/BiCG.java:63-102."""
+    n = len(b)
+    x = list(x)
+    rho_1 = rho_2 = 1.0
+    r = mult_add(rp, ci, v, -1.0, x, b)
+    rt = list(r)
+    p = pt = [0.0] * n
+    mon.iter = 0
+    while not mon.converged(norm2(r)):
+        z = M(r)
+        zt = Mt(rt)
+        rho_1 = dot(z, rt)
+        if rho_1 == 0:
+            raise NotConverged(3, mon.iter, mon.residual, 1)
+        if mon.iter == 0:
+            p, pt = list(z), list(zt)
+        else:
+            beta = rho_1 / rho_2
+            p = [p[i] * beta + z[i] for i in range(n)]
+            pt = [pt[i] * beta + zt[i] for i in range(n)]
+        q = mult(rp, ci, v, p)
+        qt = trans_mult(rp, ci, v, pt, n)
+        alpha = rho_1 / dot(pt, q)
+        x = _add(x, alpha, p)
+        r = _add(r, -alpha, q)
+        rt = _add(rt, -alpha, qt)
+        rho_2 = rho_1
+        mon.iter += 1
+    return x
+
+
+def cgs(rp, ci, v, b, x, M, mon):
+    """CGS.solve, S/CGS.java:65-105."""
+    n = len(b)
+    x = list(x)
+    rho_2 = 0.0
+    r = mult_add(rp, ci, v, -1.0, x, b)
+    rt = list(r)
+    p = q = [0.0] * n
+    mon.iter = 0
+    while not mon.converged(norm2(r)):
+        rho_1 = dot(rt, r)
+        if rho_1 == 0:
+            raise NotConverged(3, mon.iter, mon.residual, 1)
+        if mon.iter == 0:
+            u = list(r)
+            p = list(u)
+        else:
+            beta = rho_1 / rho_2
+            u = _add(r, beta, q)
+            s = _add(q, beta, p)
+            p = _add(u, beta, s)
+        phat = M(p)
+        vhat = mult(rp, ci, v, phat)
+        alpha = rho_1 / dot(rt, vhat)
+        q = _set(-alpha, vhat)
+        q = [q[i] + u[i] for i in range(n)]
+        s = [u[i] + q[i] for i in range(n)]
+        uhat = M(s)
+        x = _add(x, alpha, uhat)
+        qhat = mult(rp, ci, v, uhat)
+        r = _add(r, -alpha, qhat)
+        rho_2 = rho_1
+        mon.iter += 1
+    return x
+
+
+def qmr(rp, ci, v, b, x, M, Mt, mon):
+    """QMR.solve, S/QMR.java:117-213 with M1 = M2 = M."""
+    n = len(b)
+    x = list(x)
+    rho_1 = xi = gamma_1 = theta = theta_1 = delta = ep = beta = 0.0
+    gamma, eta = 1.0, -1.0
+    r = mult_add(rp, ci, v, -1.0, x, b)
+    v_tld = list(r)
+    y = M(v_tld)
+    rho = norm2(y)
+    w_tld = list(r)
+    z = Mt(w_tld)
+    xi = norm2(z)
+    p = q = d = s = [0.0] * n
+    mon.iter = 0
+    while not mon.converged(norm2(r)):
+        if rho == 0:
+            raise NotConverged(3, mon.iter, mon.residual, 1)
+        if xi == 0:
+            raise NotConverged(3, mon.iter, mon.residual, 3)
+        vv = _set(1 / rho, v_tld)
+        y = [t * (1 / rho) for t in y]
+        w = _set(1 / xi, w_tld)
+        z = [t * (1 / xi) for t in z]
+        delta = dot(z, y)
+        if delta == 0:
+            raise NotConverged(3, mon.iter, mon.residual, 4)
+        y_tld = M(y)
+        z_tld = Mt(z)
+        if mon.iter == 0:
+            p, q = list(y_tld), list(z_tld)
+        else:
+            cp = -xi * delta / ep
+            cq = -rho * delta / ep
+            p = [p[i] * cp + y_tld[i] for i in range(n)]
+            q = [q[i] * cq + z_tld[i] for i in range(n)]
+        p_tld = mult(rp, ci, v, p)
+        ep = dot(q, p_tld)
+        if ep == 0:
+            raise NotConverged(3, mon.iter, mon.residual, 5)
+        beta = ep / delta
+        if beta == 0:
+            raise NotConverged(3, mon.iter, mon.residual, 6)
+        v_tld = _set(-beta, vv)
+        v_tld = [v_tld[i] + p_tld[i] for i in range(n)]
+        y = M(v_tld)
+        rho_1 = rho
+        rho = norm2(y)
+        w_tld = trans_mult_add(rp, ci, v, 1.0, q, _set(-beta, w))
+        z = Mt(w_tld)
+        xi = norm2(z)
+        gamma_1 = gamma
+        theta_1 = theta
+        theta = rho / (gamma_1 * beta)
+        gamma = 1 / math.sqrt(1 + theta * theta)
+        if gamma == 0:
+            raise NotConverged(3, mon.iter, mon.residual, 7)
+        eta = -eta * rho_1 * gamma * gamma / (beta * gamma_1 * gamma_1)
+        if mon.iter == 0:
+            d = _set(eta, p)
+            s = _set(eta, p_tld)
+        else:
+            val = theta_1 * theta_1 * gamma * gamma
+            d = _add([t * val for t in d], eta, p)
+            s = _add([t * val for t in s], eta, p_tld)
+        x = [x[i] + d[i] for i in range(n)]
+        r = _add(r, -1.0, s)
+        mon.iter += 1
+    return x
+
+
+def chebyshev(rp, ci, v, b, x, M, mon, eigmin, eigmax):
+    """Chebyshev.solve, S/Chebyshev.java:90-120."""
+    n = len(b)
+    x = list(x)
+    alpha = 0.0
+    r = mult_add(rp, ci, v, -1.0, x, b)
+    c = (eigmax - eigmin) / 2.0
+    d = (eigmax + eigmin) / 2.0
+    p = [0.0] * n
+    mon.iter = 0
+    while not mon.converged(norm2(r)):
+        z = M(r)
+        if mon.iter == 0:
+            p = list(z)
+            alpha = 2.0 / d
+        else:
+            beta = (alpha * c) / 2.0
+            beta *= beta
+            alpha = 1.0 / (d - beta)
+            p = [p[i] * beta + z[i] for i in range(n)]
+        q = mult(rp, ci, v, p)
+        x = _add(x, alpha, p)
+        r = _add(r, -alpha, q)
+        mon.iter += 1
+    return x
+
+
+def ir(rp, ci, v, b, x, M, mon):
+    """IR.solve, S/IR.java:57-70."""
+    n = len(b)
+    x = list(x)
+    r = mult_add(rp, ci, v, -1.0, x, b)
+    mon.iter = 0
+    while not mon.converged(norm2(r)):
+        z = M(r)
+        x = [x[i] + z[i] for i in range(n)]
+        r = mult_add(rp, ci, v, -1.0, x, b)
+        mon.iter += 1
+    return x

@@ -1,0 +1,194 @@
+"""BiCG, CGS, QMR, Chebyshev and IR on the GPU against the oracle.
+
+Same bars as the CG / BiCGstab / GMRES parity tests: the oracle's status
+and breakdown reason, its iteration count within 2, the relative residual
+history r_k / r_0 within 1e-10 over the common prefix (the same iteration
+numbers passed to the reporter), x within 1e-8; and the reference's own
+solver tests (TS/BiCGTest, CGSTest, QMRTest, ChebyshevTest and their
+Diagonal / ILU variants): x recovered within 1e-4 on seeded random systems
+of the reference's shapes."""
+import zlib
+
+import numpy as np
+import pytest
+
+import oracle as O
+from helpers import dense_to_csr, nonsingular_system, spd_system
+from mtjg import sparse, workloads
+
+pytestmark = pytest.mark.gpu
+
+KIND = {"bicg": O.BICG, "cgs": O.CGS, "qmr": O.QMR, "chebyshev": O.CHEBYSHEV, "ir": O.IR}
+PCS = {"identity": (None, None), "jacobi": (sparse.DiagonalPreconditioner, O.PC_JACOBI),
+       "ilu": (sparse.ILU, O.PC_ILU), "icc": (sparse.ICC, O.PC_ICC)}
+
+
+@pytest.fixture(params=[0, 1], ids=["fast", "strict"])
+def numerics(request, ctx):
+    ctx.setNumerics(request.param)
+    yield request.param
+    ctx.setNumerics(0)
+
+
+def _dense(n, rp, ci, v):
+    A = np.zeros((n, n))
+    for i in range(n):
+        A[i, ci[rp[i]:rp[i + 1]]] = v[rp[i]:rp[i + 1]]
+    return A
+
+
+def _solver(name, n, ctx, eig):
+    if name == "chebyshev":
+        return sparse.Chebyshev(n, eig[0], eig[1], ctx=ctx)
+    return {"bicg": sparse.BiCG, "cgs": sparse.CGS, "qmr": sparse.QMR, "ir": sparse.IR}[name](n, ctx=ctx)
+
+
+def _both(ctx, name, pname, n, rp, ci, v, b, x0, max_iter=3000, rtol=1e-10, eig=(0.0, 0.0)):
+    A = sparse.CompRowMatrix(n, n, rp, ci, v, ctx)
+    Ao = O.Csr(n, n, rp, ci, v)
+    solver = _solver(name, n, ctx, eig)
+    pcls, pk = PCS[pname]
+    pco = None
+    if pcls is not None:
+        M = pcls(n, ctx) if pcls is sparse.DiagonalPreconditioner else pcls(A)
+        M.setMatrix(A)
+        solver.setPreconditioner(M)
+        pco = O.Precond(pk, n)
+        assert pco.set_matrix(Ao) == 0
+    mon = sparse.DefaultIterationMonitor(max_iter, rtol, 1e-50, 1e5)
+    mon.setIterationReporter(sparse.IterationReporter(), history_cap=2 * max_iter + 64)
+    solver.setIterationMonitor(mon)
+    x = np.array(x0, dtype=np.float64, copy=True)
+    exc = None
+    try:
+        solver.solve(A, b, x)
+    except sparse.IterativeSolverNotConvergedException as e:
+        exc = e
+    xo, res, hr, hi = O.solve(KIND[name], Ao, b, x0, pco, max_iter=max_iter, rtol=rtol, eigmin=eig[0],
+                              eigmax=eig[1])
+    return x, exc, solver, mon, xo, res, hr, hi
+
+
+def _gap(solver, hr, hi):
+    gr, gi = solver.history
+    k = min(len(gr), len(hr))
+    assert k > 0
+    assert np.array_equal(gi[:k], hi[:k])
+    return float(np.max(np.abs(gr[:k] - hr[:k])) / max(abs(hr[0]), 1e-300))
+
+
+CASES = [(s, p, "convdiff3d", 10) for s in ("bicg", "cgs", "qmr") for p in ("identity", "jacobi", "ilu")]
+CASES += [("ir", p, "convdiff3d", 10) for p in ("jacobi", "ilu")]
+CASES += [("chebyshev", p, "poisson2d", 16) for p in ("identity", "jacobi", "icc")]
+CASES += [(s, "icc", "poisson2d", 16) for s in ("bicg", "cgs", "qmr", "ir")]
+
+
+@pytest.mark.parametrize("case", CASES, ids=["-".join(map(str, c)) for c in CASES])
+def test_matches_oracle(ctx, numerics, case):
+    name, pname, mat, N = case
+    n, rp, ci, v = getattr(workloads, mat)(N)
+    b = O.mult(O.Csr(n, n, rp, ci, v), workloads.uniform(n, 1))
+    eig = (0.0, 0.0)
+    if name == "chebyshev":
+        # the spectrum of M^-1 A (ChebyshevTest uses A's; with M it is M^-1 A's)
+        Ad = _dense(n, rp, ci, v)
+        if pname == "identity":
+            ev = np.linalg.eigvalsh(Ad)
+        else:
+            pco = O.Precond(PCS[pname][1], n)
+            pco.set_matrix(O.Csr(n, n, rp, ci, v))
+            Minv = np.column_stack([pco.apply(e) for e in np.eye(n)])
+            ev = np.sort(np.linalg.eigvals(Minv @ Ad).real)
+        eig = (float(ev[0]), float(ev[-1]))
+    x, exc, solver, mon, xo, res, hr, hi = _both(ctx, name, pname, n, rp, ci, v, b, np.zeros(n), eig=eig)
+    assert res.status == 0 and exc is None, (res.status, exc)
+    assert abs(mon.iterations() - res.iterations) <= 2, (mon.iterations(), res.iterations)
+    assert _gap(solver, hr, hi) <= 1e-10
+    assert np.max(np.abs(x - xo)) <= 1e-8 * max(1.0, np.max(np.abs(xo)))
+
+
+BREAKDOWNS = [
+    ("bicg", [[1.0, 0.0], [-1.0, -1.0]], [1.0, 0.0], "rho"),
+    ("cgs", [[1.0, 0.0], [-1.0, -1.0]], [1.0, 0.0], "rho"),
+    ("qmr", [[1.0, 0.0], [-1.0, -1.0]], [1.0, 0.0], "xi"),
+    ("qmr", [[2.0, -2.0, 0.0], [2.0, 1.0, 0.0], [2.0, 2.0, -2.0]], [-1.0, -1.0, 0.0], "delta"),
+    ("qmr", [[0.0, 1.0], [2.0, -2.0]], [1.0, 0.0], "ep"),
+    ("qmr", [[0.0, 0.0, 0.0], [1.0, 2.0, -1.0], [-1.0, -2.0, 0.0]], [1.0, -1.0, 1.0], "gamma"),
+]
+
+
+@pytest.mark.parametrize("case", BREAKDOWNS, ids=[f"{c[0]}-{c[3]}" for c in BREAKDOWNS])
+def test_breakdowns_match_oracle(ctx, numerics, case):
+    name, Ad, b, what = case
+    n, _, rp, ci, v = dense_to_csr(np.array(Ad))
+    x, exc, solver, mon, xo, res, hr, hi = _both(ctx, name, "identity", n, rp, ci, v, np.array(b), np.zeros(n),
+                                                 max_iter=50)
+    assert res.status == O.NC_BREAKDOWN and sparse.BREAKDOWN[res.detail] == what
+    assert exc is not None and exc.getReason() == sparse.NotConvergedException.Reason.Breakdown
+    assert exc.message == what
+    assert exc.getIterations() == res.iterations
+
+
+def test_chebyshev_rejects_bad_bounds(ctx):
+    for lo, hi in ((0.0, 1.0), (1.0, -1.0), (2.0, 1.0)):
+        with pytest.raises(sparse.IllegalArgumentException):
+            sparse.Chebyshev(10, lo, hi, ctx=ctx)
+
+
+@pytest.mark.parametrize("name", ["bicg", "cgs", "qmr", "chebyshev", "ir"])
+@pytest.mark.parametrize("max_iter,atol", [(7, 1e-50), (7, 0.0), (0, 0.0)])
+def test_empty_system_matches_oracle(ctx, name, max_iter, atol):
+    rp = np.zeros(1, dtype=np.int32)
+    A = sparse.CompRowMatrix(0, 0, rp, np.zeros(0, np.int32), np.zeros(0), ctx)
+    solver = _solver(name, 0, ctx, (1.0, 2.0))
+    mon = sparse.DefaultIterationMonitor(max_iter, 1e-10, atol, 1e5)
+    mon.setIterationReporter(sparse.IterationReporter(), history_cap=64)
+    solver.setIterationMonitor(mon)
+    status = 0
+    try:
+        solver.solve(A, np.zeros(0), np.zeros(0))
+    except sparse.IterativeSolverNotConvergedException as e:
+        status = e.getReason().value
+    _, res, hr, hi = O.solve(KIND[name], O.Csr(0, 0, rp, np.zeros(0, np.int32), np.zeros(0)), np.zeros(0),
+                             np.zeros(0), None, max_iter=max_iter, rtol=1e-10, atol=atol, eigmin=1.0, eigmax=2.0)
+    assert status == res.status
+    assert mon.iterations() == res.iterations
+    gr, gi = solver.history
+    assert np.array_equal(gi, hi) and np.array_equal(gr, hr)
+
+
+@pytest.mark.parametrize("seed", range(4))
+@pytest.mark.parametrize("name", ["bicg", "cgs", "qmr", "chebyshev", "ir"])
+@pytest.mark.parametrize("pname", ["identity", "jacobi", "ilu"])
+def test_reference_style_random_systems(ctx, seed, name, pname):
+    # TS/IterativeSolverTestAbstract.java:140-168: solve five right-hand sides
+    # with one solver, x within 1e-4; the preconditioner actually installed
+    if name == "ir" and pname == "identity":
+        pytest.skip("Richardson without a preconditioner diverges on these systems")
+    rng = np.random.default_rng(1000 * seed + zlib.crc32((name + pname).encode()) % 997)
+    n = int(rng.integers(2, 51))
+    bw = int(rng.integers(1, min(10, n) + 1))
+    Ad = spd_system(n, bw, rng) if name == "chebyshev" else nonsingular_system(n, bw, rng)
+    n, _, rp, ci, v = dense_to_csr(Ad)
+    A = sparse.CompRowMatrix(n, n, rp, ci, v, ctx)
+    eig = (1.0, 1.0)
+    if name == "chebyshev":
+        if pname == "identity":
+            ev = np.linalg.eigvalsh(Ad)
+        else:
+            pco = O.Precond(PCS[pname][1], n)
+            pco.set_matrix(O.Csr(n, n, rp, ci, v))
+            ev = np.sort(np.linalg.eigvals(np.column_stack([pco.apply(e) for e in np.eye(n)]) @ Ad).real)
+        eig = (float(ev[0]), float(ev[-1]))
+    solver = _solver(name, n, ctx, eig)
+    pcls = PCS[pname][0]
+    if pcls is not None:
+        M = pcls(n, ctx) if pcls is sparse.DiagonalPreconditioner else pcls(A)
+        M.setMatrix(A)
+        solver.setPreconditioner(M)
+    for _ in range(5):
+        xt = rng.random(n)
+        b = Ad @ xt
+        x = rng.random(n)
+        solver.solve(A, b, x)
+        assert np.max(np.abs(x - xt)) <= 1e-4

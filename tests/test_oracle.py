@@ -235,3 +235,100 @@ def test_icc_negative_pivot_propagates_like_literal():
     va, vb = a.values(), b.values()
     assert np.array_equal(np.isnan(va), np.isnan(vb))
     assert np.array_equal(va[~np.isnan(va)], vb[~np.isnan(vb)])
+
+
+# ---------------------------------------- BiCG, CGS, QMR, Chebyshev, IR (rank-2 solvers)
+def _pc_pair(pk, rp, ci, v, A, n):
+    """(oracle preconditioner, pyref apply, pyref transApply)."""
+    if pk == O.PC_IDENTITY:
+        ident = lambda r: list(r)  # noqa: E731
+        return None, ident, ident
+    pc = O.Precond(pk, n)
+    assert pc.set_matrix(A) == O.OK
+    if pk == O.PC_JACOBI:
+        M = pyref.jacobi(rp, ci, v)
+        return pc, M, M
+    if pk == O.PC_ILU:
+        data, dg = pyref.ilu_factor(rp, ci, v)
+        return pc, (lambda r: pyref.ilu_apply(rp, ci, data, dg, r)), \
+            (lambda r: pyref.ilu_trans_apply(rp, ci, data, dg, r))
+    data, dg = pyref.icc_factor(rp, ci, v)
+    M = lambda r: pyref.icc_apply(rp, ci, data, dg, r)  # noqa: E731
+    return pc, M, M
+
+
+def _run_py(fn, *a):
+    try:
+        return fn(*a), 0, 0
+    except pyref.NotConverged as e:
+        return None, e.code, e.detail
+
+
+@pytest.mark.parametrize("seed", range(8))
+@pytest.mark.parametrize("name", ["bicg", "cgs", "qmr", "ir", "chebyshev"])
+@pytest.mark.parametrize("pk", [O.PC_IDENTITY, O.PC_JACOBI, O.PC_ILU, O.PC_ICC])
+@pytest.mark.parametrize("max_iter", [3, 400])
+def test_rank2_solver_histories_bitwise(seed, name, pk, max_iter):
+    spd = name == "chebyshev" or pk == O.PC_ICC
+    n, rp, ci, v, A, rng = _py_system(seed + 300, spd)
+    b = list(rng.standard_normal(n))
+    x0 = list(rng.standard_normal(n))
+    pc, M, Mt = _pc_pair(pk, rp, ci, v, A, n)
+    mon = pyref.Monitor(max_iter, 1e-10)
+    kind = {"bicg": O.BICG, "cgs": O.CGS, "qmr": O.QMR, "ir": O.IR, "chebyshev": O.CHEBYSHEV}[name]
+    eig = (0.0, 0.0)
+    if name == "bicg":
+        xp, code, detail = _run_py(pyref.bicg, rp, ci, v, b, x0, M, Mt, mon)
+    elif name == "cgs":
+        xp, code, detail = _run_py(pyref.cgs, rp, ci, v, b, x0, M, mon)
+    elif name == "qmr":
+        xp, code, detail = _run_py(pyref.qmr, rp, ci, v, b, x0, M, Mt, mon)
+    elif name == "ir":
+        xp, code, detail = _run_py(pyref.ir, rp, ci, v, b, x0, M, mon)
+    else:
+        # ChebyshevTest.createSolver: the extremal eigenvalues of A (TS/ChebyshevTest.java)
+        Ad = np.zeros((n, n))
+        for i in range(n):
+            Ad[i, ci[rp[i]:rp[i + 1]]] = v[rp[i]:rp[i + 1]]
+        ev = np.linalg.eigvalsh(Ad)
+        eig = (float(ev[0]), float(ev[-1]))
+        xp, code, detail = _run_py(pyref.chebyshev, rp, ci, v, b, x0, M, mon, *eig)
+    xo, res, hr, hi = O.solve(kind, A, np.array(b), np.array(x0), pc, max_iter=max_iter, rtol=1e-10,
+                              eigmin=eig[0], eigmax=eig[1])
+    assert res.status == code and res.detail == detail, (res.status, code, res.detail, detail)
+    assert res.iterations == mon.iter
+    assert np.array_equal(hr, np.array([h[0] for h in mon.hist]))
+    assert np.array_equal(hi, np.array([h[1] for h in mon.hist]))
+    if code == 0:
+        assert np.array_equal(xo, np.array(xp))
+
+
+@pytest.mark.parametrize("seed", range(6))
+@pytest.mark.parametrize("name", ["bicg", "cgs", "qmr", "chebyshev", "ir"])
+@pytest.mark.parametrize("pk", [O.PC_IDENTITY, O.PC_JACOBI, O.PC_ILU])
+def test_rank2_solvers_recover_x(seed, name, pk):
+    # TS/BiCGTest, CGSTest, QMRTest, ChebyshevTest (+Diagonal/ILU variants):
+    # x recovered within 1e-4 on the shifted random systems of
+    # TS/IterativeSolverTestAbstract.java:110-168; IR needs a preconditioner
+    # that contracts (Jacobi on these diagonally dominant systems does)
+    if name == "ir" and pk == O.PC_IDENTITY:
+        pytest.skip("Richardson without a preconditioner diverges on these systems")
+    rng = np.random.default_rng(4000 + seed)
+    n = int(rng.integers(2, 51))
+    bw = int(rng.integers(1, min(10, n) + 1))
+    spd = name == "chebyshev"
+    Ad = spd_system(n, bw, rng) if spd else nonsingular_system(n, bw, rng)
+    n, _, rp, ci, v = dense_to_csr(Ad)
+    A = O.Csr(n, n, rp, ci, v)
+    pc = None
+    if pk != O.PC_IDENTITY:
+        pc = O.Precond(pk, n)
+        assert pc.set_matrix(A) == O.OK
+    ev = np.linalg.eigvalsh(Ad) if spd else np.array([0.0, 0.0])
+    kind = {"bicg": O.BICG, "cgs": O.CGS, "qmr": O.QMR, "ir": O.IR, "chebyshev": O.CHEBYSHEV}[name]
+    xt = rng.random(n)
+    b = Ad @ xt
+    x, res, _, _ = O.solve(kind, A, b, rng.random(n), pc, max_iter=100000, rtol=1e-10,
+                           eigmin=float(ev[0]), eigmax=float(ev[-1]))
+    assert res.status == 0
+    assert np.max(np.abs(x - xt)) <= 1e-4
