@@ -71,8 +71,8 @@ enum {
 enum { MTJG_NORM_ONE = 0, MTJG_NORM_TWO = 1, MTJG_NORM_TWO_ROBUST = 2, MTJG_NORM_INFINITY = 3 };
 
 /* Preconditioner kinds: identity (S/AbstractIterativeSolver.java:82-96),
- * DiagonalPreconditioner, ILU, ICC */
-enum { MTJG_PC_IDENTITY = 0, MTJG_PC_JACOBI = 1, MTJG_PC_ILU = 2, MTJG_PC_ICC = 3 };
+ * DiagonalPreconditioner, ILU, ICC, SSOR, ILUT */
+enum { MTJG_PC_IDENTITY = 0, MTJG_PC_JACOBI = 1, MTJG_PC_ILU = 2, MTJG_PC_ICC = 3, MTJG_PC_SSOR = 4, MTJG_PC_ILUT = 5 };
 
 /* IterativeSolver implementations: S/CG.java, S/BiCGstab.java, S/GMRES.java,
  * S/BiCG.java, S/CGS.java, S/QMR.java, S/Chebyshev.java, S/IR.java */
@@ -239,9 +239,21 @@ MTJG_API int mtjg_csr_mult_add_norm_noalloc(mtjg_csr *A, double alpha, const dou
                                             double *dnorm);
 
 /* ---- Preconditioner ---------------------------------------------------- */
-/* new DiagonalPreconditioner(n) / new ILU(CompRowMatrix) / new ICC(CompRowMatrix),
- * S/DiagonalPreconditioner.java:43-45, S/ILU.java:54-62, S/ICC.java:57-65 */
+/* new DiagonalPreconditioner(n) / new ILU(CompRowMatrix) / new ICC(CompRowMatrix) /
+ * new SSOR(CompRowMatrix) / new ILUT(FlexCompRowMatrix),
+ * S/DiagonalPreconditioner.java:43-45, S/ILU.java:54-62, S/ICC.java:57-65,
+ * S/SSOR.java:75-77, S/ILUT.java:95-97 (SSOR: reverse, omegaF = omegaR = 1;
+ * ILUT: tau = 1e-6, p = 25) */
 MTJG_API int mtjg_precond_create(mtjg_ctx *ctx, int kind, int n, mtjg_precond **out);
+/* SSOR(F, reverse, omegaF, omegaR) / SSOR.setOmega, S/SSOR.java:62-96: omegas
+ * outside [0, 2] are MTJG_ERR_ILLEGAL_ARGUMENT.  SSOR's apply(b, x) is one
+ * symmetric SOR sweep starting from x's content (S/SSOR.java:148-192), so x
+ * is read as well as written. */
+MTJG_API int mtjg_precond_set_ssor(mtjg_precond *M, int reverse, double omega_f, double omega_r);
+/* ILUT(LU, tau, p), S/ILUT.java:68-85: drop tolerance and fill per row; takes
+ * effect at the next setMatrix.  The factor runs on the host (it is a chain
+ * over the rows), its solves on the device. */
+MTJG_API int mtjg_precond_set_ilut(mtjg_precond *M, double tau, int p);
 /* Preconditioner.setMatrix(A), S/Preconditioner.java:56-63: Jacobi extracts
  * the inverse diagonal, ILU and ICC copy A and factor it.  On a setup error
  * *err_row receives the number MTJ's message prints. */
@@ -253,6 +265,11 @@ MTJG_API int mtjg_precond_apply_dev(mtjg_precond *M, const double *db, double *d
 /* The factored values (ILU/ICC: the in-place CSR data array of MTJ's copy,
  * Jacobi: the inverse diagonal), copied to host; returns the count in *len. */
 MTJG_API int mtjg_precond_values(mtjg_precond *M, double *out, int64_t cap, int64_t *len);
+/* The factor's pattern (ILU, ICC, SSOR: A's; ILUT: its rows after the factor,
+ * positions [0, max(stored, diagonal + 1)) of each), with each row's
+ * diagonal position within the row, in the layout of mtjg_precond_values. */
+MTJG_API int mtjg_precond_pattern(mtjg_precond *M, int *rowptr, int *colind, int *diag, int64_t cap,
+                                  int64_t *nnz);
 MTJG_API int mtjg_precond_destroy(mtjg_precond *M);
 
 /* ---- IterativeSolver ---------------------------------------------------- */

@@ -24,7 +24,7 @@ INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["spmv.cu", "precond.cu", "solver.cu", "server.cu", "noalloc.cu"]
-CPP_SOURCES = ["abi.cpp", "icc_host.cpp", "mmio.cpp"]
+CPP_SOURCES = ["abi.cpp", "icc_host.cpp", "ilut_host.cpp", "mmio.cpp"]
 
 
 def _cuda_home() -> str:

@@ -241,7 +241,13 @@ struct mtjg_precond {
     mtjg::LevelSchedule up;             // U / R solve (rows descending)
     double *y = nullptr;                // temporary of apply
     double *d_b = nullptr, *d_x = nullptr;  // host-call staging
-    void *trans = nullptr;              // ILU transApply operators, built on first use
+    void *trans = nullptr;              // ILU / ILUT transApply operators, built on first use
+    // SSOR(F, reverse, omegaF, omegaR) (S/SSOR.java:62-73) and ILUT(LU, tau, p)
+    // (S/ILUT.java:68-85), with MTJ's defaults
+    bool reverse = true;
+    double omega_f = 1, omega_r = 1;
+    double tau = 1e-6;
+    int p = 25;
 };
 
 struct mtjg_solver;

@@ -21,6 +21,7 @@
 // warps before its own, so the sweep cannot deadlock.  Each row sums in
 // MTJ's entry order, so results are those of the row-by-row Java loop.
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 
 #include "spmv.cuh"
@@ -28,6 +29,9 @@
 namespace mtjg {
 
 int icc_factor_host(int n, const int *rowptr, const int *colind, const int *diag, double *data, int *err_row);
+int ilut_factor_host(int n, const int *rowptr, const int *colind, const double *val, double tau, int p,
+                     std::vector<int> &out_rp, std::vector<int> &out_ci, std::vector<double> &out_v,
+                     std::vector<int> &out_diag, int *err_row);
 
 constexpr long long kSpinLimit = 1LL << 24;
 
@@ -180,7 +184,23 @@ constexpr unsigned long long kPending = 0x7FF40000DEADBEEFull;
 constexpr unsigned long long kQuietNaN = 0x7FF8000000000000ull;
 constexpr long long kSweepSpinLimit = 1LL << 21;
 constexpr int kSweepBlock = 128;
-constexpr int kSweepBlocksPerSm = 8;
+// warps per SM a sweep launches, and polls of a pending entry before the
+// poller starts to sleep between polls; both can be set in the environment
+// (MTJG_SWEEP_WARPS, MTJG_SWEEP_SPIN) to tune them
+// (measured on GB300, 3D Poisson 128^3 ICC and 96^3 convection-diffusion
+// ILU applies: sleeping between polls costs more than the polls -- 2.6 vs
+// 1.7 ms per ICC apply at 4 warps per SM -- and fewer pollers win: 32 warps
+// per SM 2.2 ms against 1.7 ms at 4 or 8)
+constexpr int kSweepWarpsPerSm = 8;
+constexpr int kSweepSpin = 4096;
+
+static int env_int(const char *name, int dflt, int lo, int hi)
+{
+    const char *v = getenv(name);
+    if (!v || !*v) return dflt;
+    const int x = atoi(v);
+    return x < lo ? lo : (x > hi ? hi : x);
+}
 
 __device__ __forceinline__ double ld_relaxed(const double *p)
 {
@@ -216,14 +236,16 @@ __global__ void k_sweep_prep(int n, double *x1, double *x2, unsigned *t1, unsign
 // x_c for a row of the sweep: a relaxed load, polled while it is pending.
 // Gives up (bad) after kSweepSpinLimit polls or when another wait has given
 // up (the context's error flag is set).
-__device__ __forceinline__ double wait_x(const double *x, int c, const int *err, bool &bad)
+__device__ __forceinline__ double wait_x(const double *x, int c, const int *err, int spin, bool &bad)
 {
     double v = ld_relaxed(x + c);
     if (!pending(v)) return v;
     unsigned ns = 32;
     for (long long polls = 1;; ++polls) {
-        __nanosleep(ns);
-        ns = ns < 256 ? 2 * ns : ns;
+        if (polls > spin) {
+            __nanosleep(ns);
+            ns = ns < 256 ? 2 * ns : ns;
+        }
         v = ld_relaxed(x + c);
         if (!pending(v)) return v;
         if (polls > kSweepSpinLimit || ((polls & 31) == 0 && *(volatile const int *)err)) {
@@ -243,6 +265,12 @@ __device__ __forceinline__ double wait_x(const double *x, int c, const int *err,
 //  MODE 3: UnitLowerCompRowMatrix.transSolve in gather form on the
 //          transpose of the strict lower part, source rows descending
 //          (S/UnitLowerCompRowMatrix.java:78-83)
+//  MODE 4: SSOR's forward sweep (S/SSOR.java:163-172): sigma over the row in
+//          entry order, lower entries from the new iterate x (waited for),
+//          upper entries from aux (the old x); x_i = aux_i + omega (sigma' - aux_i)
+//  MODE 5: SSOR's backward sweep (S/SSOR.java:180-189): lower entries from
+//          aux (the forward iterate), upper entries from the new x (waited
+//          for); x_i = aux_i + omega (sigma' - aux_i)
 // A row's entries are read in groups of kGrp, whose x loads are all in
 // flight before the first wait.
 template <bool S, int MODE>
@@ -252,7 +280,8 @@ __global__ void __launch_bounds__(kSweepBlock) k_trsv_sweep(const int *__restric
                                                           const double *__restrict__ v,
                                                           const int *__restrict__ diag,
                                                           const double *__restrict__ diagv, const double *b,
-                                                          double *x, unsigned *ticket, const int *status, int *err)
+                                                          double *x, unsigned *ticket, const int *status, int *err,
+                                                          int spin, const double *__restrict__ aux, double omega)
 {
     constexpr int kGrp = 4;
     if (status && *status != ST_RUNNING) return;
@@ -268,7 +297,7 @@ __global__ void __launch_bounds__(kSweepBlock) k_trsv_sweep(const int *__restric
             const int i = perm[beg + lane];
             const double bi = b[i];
             // entry range, walked upwards from kb (MODE 3: downwards from ke - 1)
-            int kb, ke;
+            int kb, ke, dk = -1;
             if constexpr (MODE == 0) {
                 kb = rp[i];
                 ke = diag[i];
@@ -279,24 +308,28 @@ __global__ void __launch_bounds__(kSweepBlock) k_trsv_sweep(const int *__restric
                 kb = rp[i];
                 ke = rp[i + 1];
             }
-            double acc = (MODE >= 2) ? bi : 0.0;
+            if constexpr (MODE >= 4) dk = diag[i];
+            double acc = (MODE == 2 || MODE == 3) ? bi : 0.0;
             for (int k0 = 0; k0 < ke - kb && !bad; k0 += kGrp) {
                 int cc[kGrp];
                 double vv[kGrp], xv[kGrp];
+                bool wt[kGrp];  // the entry is read from the sweep's own output
 #pragma unroll
                 for (int u = 0; u < kGrp; ++u) {
                     const int k = MODE == 3 ? ke - 1 - (k0 + u) : kb + k0 + u;
-                    const bool in = k0 + u < ke - kb;
+                    const bool in = k0 + u < ke - kb && k != dk;
                     cc[u] = in ? ci[k] : -1;
                     vv[u] = in ? v[k] : 0.0;
+                    wt[u] = MODE == 4 ? k < dk : (MODE == 5 ? k > dk : true);
                 }
 #pragma unroll
-                for (int u = 0; u < kGrp; ++u) xv[u] = cc[u] >= 0 ? ld_relaxed(x + cc[u]) : 0.0;
+                for (int u = 0; u < kGrp; ++u)
+                    xv[u] = cc[u] < 0 ? 0.0 : (wt[u] ? ld_relaxed(x + cc[u]) : aux[cc[u]]);
 #pragma unroll
                 for (int u = 0; u < kGrp; ++u) {
                     if (cc[u] < 0 || bad) continue;
-                    if (pending(xv[u])) xv[u] = wait_x(x, cc[u], err, bad);
-                    if constexpr (MODE <= 1) acc = fmac<S>(vv[u], xv[u], acc);
+                    if (wt[u] && pending(xv[u])) xv[u] = wait_x(x, cc[u], err, spin, bad);
+                    if constexpr (MODE <= 1 || MODE >= 4) acc = fmac<S>(vv[u], xv[u], acc);
                     else acc = fmac<S>(-vv[u], xv[u], acc);
                 }
             }
@@ -304,7 +337,13 @@ __global__ void __launch_bounds__(kSweepBlock) k_trsv_sweep(const int *__restric
             if constexpr (MODE == 0) xi = bi - acc;
             else if constexpr (MODE == 1) xi = (bi - acc) / v[diag[i]];
             else if constexpr (MODE == 2) xi = acc / diagv[i];
-            else xi = acc;
+            else if constexpr (MODE == 3) xi = acc;
+            else {
+                // sigma = (b_i - sigma) / a_ii; x_i = old_i + omega (sigma - old_i)
+                const double sig = (bi - acc) / v[dk], old = aux[i];
+                if constexpr (S) xi = __dadd_rn(old, __dmul_rn(omega, __dsub_rn(sig, old)));
+                else xi = fma(omega, sig - old, old);
+            }
             // a stored pending pattern would read as "not solved": store a quiet NaN
             if ((unsigned long long)__double_as_longlong(xi) == kPending) xi = __longlong_as_double((long long)kQuietNaN);
             if (!bad) st_relaxed(x + i, xi);
@@ -408,18 +447,20 @@ static cudaError_t sweep_prep(mtjg_ctx *ctx, int n, double *x1, double *x2, Leve
 template <int MODE>
 static cudaError_t sweep_t(mtjg_ctx *ctx, bool strict, const LevelSchedule &s, const int *rp, const int *ci,
                            const double *v, const int *diag, const double *diagv, const double *b, double *x,
-                           const int *status)
+                           const int *status, const double *aux = nullptr, double omega = 0.0)
 {
     if (s.num_chunks == 0) return cudaSuccess;
-    const int warps = ctx->num_sms * kSweepBlocksPerSm * (kSweepBlock / 32);
+    const int warps = ctx->num_sms * env_int("MTJG_SWEEP_WARPS", kSweepWarpsPerSm, 1, 40);
+    const int spin = env_int("MTJG_SWEEP_SPIN", kSweepSpin, 0, 1 << 20);
     const int grid = (std::min(warps, s.num_chunks) + kSweepBlock / 32 - 1) / (kSweepBlock / 32);
     if (strict)
         k_trsv_sweep<true, MODE><<<grid, kSweepBlock, 0, ctx->stream>>>(s.perm, s.chunk, s.num_chunks, rp, ci, v, diag,
-                                                                      diagv, b, x, s.ticket, status, ctx->d_flag);
+                                                                      diagv, b, x, s.ticket, status, ctx->d_flag,
+                                                                      spin, aux, omega);
     else
         k_trsv_sweep<false, MODE><<<grid, kSweepBlock, 0, ctx->stream>>>(s.perm, s.chunk, s.num_chunks, rp, ci, v,
                                                                        diag, diagv, b, x, s.ticket, status,
-                                                                       ctx->d_flag);
+                                                                       ctx->d_flag, spin, aux, omega);
     ctx->launches++;
     return cudaGetLastError();
 }
@@ -483,7 +524,27 @@ int precond_apply_dev(mtjg_precond *M, const double *b, double *x, const int *st
         ctx->launches++;
         e = cudaGetLastError();
         break;
-    case MTJG_PC_ILU:  // L y = b, then U x = y (S/ILU.java:64-70)
+    case MTJG_PC_SSOR: {  // S/SSOR.java:148-192: forward sweep into y, then backward into x
+        if (x == b) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "SSOR apply needs distinct b and x");
+        const bool strict = ctx->numerics == MTJG_NUMERICS_STRICT;
+        e = sweep_prep(ctx, n, M->y, nullptr, &M->lo, &M->up, status);
+        if (e == cudaSuccess)
+            e = sweep_t<4>(ctx, strict, M->lo, M->rowptr, M->colind, M->data, M->diag, nullptr, b, M->y, status, x,
+                           M->omega_f);
+        if (e == cudaSuccess && M->reverse) {
+            e = sweep_prep(ctx, n, x, nullptr, nullptr, nullptr, status);
+            if (e == cudaSuccess)
+                e = sweep_t<5>(ctx, strict, M->up, M->rowptr, M->colind, M->data, M->diag, nullptr, b, x, status,
+                               M->y, M->omega_r);
+        } else if (e == cudaSuccess) {
+            k_copy<<<grid_for(ctx, n), kBlock, 0, ctx->stream>>>(n, M->y, x, status);
+            ctx->launches++;
+            e = cudaGetLastError();
+        }
+        break;
+    }
+    case MTJG_PC_ILU:   // L y = b, then U x = y (S/ILU.java:64-70)
+    case MTJG_PC_ILUT:  // the same solves on the ILUT factor (S/ILUT.java:111-113)
         e = sweep_pair(ctx, n, 0, M->lo, M->rowptr, M->colind, M->data, M->diag, nullptr, 1, M->up, M->rowptr,
                        M->colind, M->data, M->diag, nullptr, b, M->y, x, status);
         break;
@@ -550,7 +611,7 @@ extern "C" int mtjg_precond_create(mtjg_ctx *ctx, int kind, int n, mtjg_precond 
 {
     if (!ctx || !out) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL argument");
     *out = nullptr;
-    if (kind < MTJG_PC_IDENTITY || kind > MTJG_PC_ICC) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "unknown preconditioner");
+    if (kind < MTJG_PC_IDENTITY || kind > MTJG_PC_ILUT) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "unknown preconditioner");
     if (n < 0) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "negative size");
     MTJG_CUDA(cudaSetDevice(ctx->device));
     mtjg_precond *M = new mtjg_precond();
@@ -693,6 +754,96 @@ static int icc_setup(mtjg_precond *M, mtjg_csr *A, int *err_row)
     return build_levels(ctx, n, 1, 2, M->rowptr, M->colind, M->diag, nullptr, M->up);
 }
 
+// SSOR.setMatrix (S/SSOR.java:98-113): F.set(A), the diagonal positions;
+// the sweeps' dependency levels (forward: the lower part, backward: the upper)
+static int ssor_setup(mtjg_precond *M, int *err_row)
+{
+    int st = find_diagonal(M, err_row);
+    if (st == MTJG_ERR_MISSING_DIAGONAL) return fail(st, "Missing diagonal on row " + std::to_string(*err_row));
+    if (st != MTJG_OK) return st;
+    st = build_levels(M->ctx, M->n, 0, 1, M->rowptr, M->colind, M->diag, nullptr, M->lo);
+    if (st != MTJG_OK) return st;
+    return build_levels(M->ctx, M->n, 1, 2, M->rowptr, M->colind, M->diag, nullptr, M->up);
+}
+
+// ILUT.setMatrix (S/ILUT.java:119-123): the factor on the host
+// (ilut_host.cpp), its rows uploaded as a CSR, then ILU's solve levels.
+static int ilut_setup(mtjg_precond *M, mtjg_csr *A, int *err_row)
+{
+    mtjg_ctx *ctx = M->ctx;
+    const int n = M->n;
+    std::vector<int> ci((size_t)A->nnz);
+    std::vector<double> val((size_t)A->nnz);
+    if (A->nnz) {
+        MTJG_CUDA(cudaMemcpy(ci.data(), A->colind, sizeof(int) * (size_t)A->nnz, cudaMemcpyDeviceToHost));
+        MTJG_CUDA(cudaMemcpy(val.data(), A->val, sizeof(double) * (size_t)A->nnz, cudaMemcpyDeviceToHost));
+    }
+    std::vector<int> frp, fci, fdiag;
+    std::vector<double> fv;
+    int st = ilut_factor_host(n, A->h_rowptr.data(), ci.data(), val.data(), M->tau, M->p, frp, fci, fv, fdiag,
+                              err_row);
+    if (st != MTJG_OK) return st;
+    const int64_t nnz = frp[(size_t)n];
+    M->nnz = nnz;
+    MTJG_CUDA(cudaMalloc(&M->rowptr, sizeof(int) * (size_t)(n + 1 + kRowptrPad)));
+    MTJG_CUDA(cudaMalloc(&M->colind, sizeof(int) * (size_t)(nnz + 4)));
+    MTJG_CUDA(cudaMalloc(&M->data, sizeof(double) * (size_t)(nnz + 2)));
+    MTJG_CUDA(cudaMalloc(&M->diag, sizeof(int) * (size_t)std::max(1, n)));
+    MTJG_CUDA(cudaMemcpy(M->rowptr, frp.data(), sizeof(int) * (size_t)(n + 1), cudaMemcpyHostToDevice));
+    if (nnz) {
+        MTJG_CUDA(cudaMemcpy(M->colind, fci.data(), sizeof(int) * (size_t)nnz, cudaMemcpyHostToDevice));
+        MTJG_CUDA(cudaMemcpy(M->data, fv.data(), sizeof(double) * (size_t)nnz, cudaMemcpyHostToDevice));
+    }
+    if (n) MTJG_CUDA(cudaMemcpy(M->diag, fdiag.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice));
+    st = build_levels(ctx, n, 0, 1, M->rowptr, M->colind, M->diag, nullptr, M->lo);
+    if (st != MTJG_OK) return st;
+    return build_levels(ctx, n, 1, 2, M->rowptr, M->colind, M->diag, nullptr, M->up);
+}
+
+extern "C" int mtjg_precond_set_ssor(mtjg_precond *M, int reverse, double omega_f, double omega_r)
+{
+    if (!M) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL preconditioner");
+    if (M->kind != MTJG_PC_SSOR) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "not an SSOR preconditioner");
+    // SSOR.setOmega, S/SSOR.java:87-96
+    if (omega_f < 0 || omega_f > 2) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "omegaF must be between 0 and 2");
+    if (omega_r < 0 || omega_r > 2) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "omegaR must be between 0 and 2");
+    M->reverse = reverse != 0;
+    M->omega_f = omega_f;
+    M->omega_r = omega_r;
+    M->version++;
+    return MTJG_OK;
+}
+
+extern "C" int mtjg_precond_set_ilut(mtjg_precond *M, double tau, int p)
+{
+    if (!M) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL preconditioner");
+    if (M->kind != MTJG_PC_ILUT) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "not an ILUT preconditioner");
+    M->tau = tau;
+    M->p = p;
+    return MTJG_OK;
+}
+
+extern "C" int mtjg_precond_pattern(mtjg_precond *M, int *rowptr, int *colind, int *diag, int64_t cap,
+                                    int64_t *nnz)
+{
+    if (!M) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL preconditioner");
+    MTJG_CUDA(cudaSetDevice(M->ctx->device));
+    MTJG_CUDA(cudaStreamSynchronize(M->ctx->stream));
+    const bool has = M->rowptr && M->kind != MTJG_PC_JACOBI;
+    if (nnz) *nnz = has ? M->nnz : 0;
+    if (!has) return MTJG_OK;
+    if (rowptr) MTJG_CUDA(cudaMemcpy(rowptr, M->rowptr, sizeof(int) * (size_t)(M->n + 1), cudaMemcpyDeviceToHost));
+    const int64_t m = std::min(cap, M->nnz);
+    if (colind && m > 0) MTJG_CUDA(cudaMemcpy(colind, M->colind, sizeof(int) * (size_t)m, cudaMemcpyDeviceToHost));
+    if (diag && M->n) {
+        std::vector<int> d((size_t)M->n), rp((size_t)M->n + 1);
+        MTJG_CUDA(cudaMemcpy(d.data(), M->diag, sizeof(int) * (size_t)M->n, cudaMemcpyDeviceToHost));
+        MTJG_CUDA(cudaMemcpy(rp.data(), M->rowptr, sizeof(int) * (size_t)(M->n + 1), cudaMemcpyDeviceToHost));
+        for (int i = 0; i < M->n; ++i) diag[i] = d[(size_t)i] - rp[(size_t)i];  // position within the row
+    }
+    return MTJG_OK;
+}
+
 extern "C" int mtjg_precond_set_matrix(mtjg_precond *M, mtjg_csr *A, int *err_row)
 {
     int dummy = 0;
@@ -703,9 +854,10 @@ extern "C" int mtjg_precond_set_matrix(mtjg_precond *M, mtjg_csr *A, int *err_ro
     if (M->kind == MTJG_PC_IDENTITY) return MTJG_OK;
     if (A->n != M->n)
         return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "Matrix size differs from preconditioner size");
-    if ((M->kind == MTJG_PC_ILU || M->kind == MTJG_PC_ICC) && A->n != A->m)
-        return fail(MTJG_ERR_ILLEGAL_ARGUMENT, M->kind == MTJG_PC_ILU ? "ILU only applies to square matrices"
-                                                                       : "ICC only applies to square matrices");
+    if (M->kind != MTJG_PC_JACOBI && A->n != A->m)
+        return fail(MTJG_ERR_ILLEGAL_ARGUMENT, M->kind == MTJG_PC_ICC    ? "ICC only applies to square matrices"
+                                               : M->kind == MTJG_PC_SSOR ? "SSOR only applies to square matrices"
+                                                                         : "ILU only applies to square matrices");
     mtjg_ctx *ctx = M->ctx;
     MTJG_CUDA(cudaSetDevice(ctx->device));
     MTJG_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -733,9 +885,11 @@ extern "C" int mtjg_precond_set_matrix(mtjg_precond *M, mtjg_csr *A, int *err_ro
         M->ready = true;
         return MTJG_OK;
     }
-    int st = copy_pattern(M, A);
+    int st = M->kind == MTJG_PC_ILUT ? ilut_setup(M, A, err_row) : copy_pattern(M, A);
     if (st != MTJG_OK) return st;
-    st = M->kind == MTJG_PC_ILU ? ilu_setup(M, err_row) : icc_setup(M, A, err_row);
+    if (M->kind == MTJG_PC_ILU) st = ilu_setup(M, err_row);
+    else if (M->kind == MTJG_PC_ICC) st = icc_setup(M, A, err_row);
+    else if (M->kind == MTJG_PC_SSOR) st = ssor_setup(M, err_row);
     if (st != MTJG_OK) return st;
     MTJG_CUDA(cudaStreamSynchronize(ctx->stream));
     M->ready = true;
@@ -765,16 +919,19 @@ static int ilu_trans_setup(mtjg_precond *M)
     return build_levels(ctx, M->n, 1, 0, t->lt_rp, t->lt_ci, nullptr, nullptr, t->lt);
 }
 
+static bool lu_kind(const mtjg_precond *M) { return M->kind == MTJG_PC_ILU || M->kind == MTJG_PC_ILUT; }
+
 int mtjg::precond_prepare_trans(mtjg_precond *M)
 {
-    return M->kind == MTJG_PC_ILU ? ilu_trans_setup(M) : MTJG_OK;
+    return lu_kind(M) ? ilu_trans_setup(M) : MTJG_OK;
 }
 
-// DiagonalPreconditioner and ICC are their own transposes here
-// (S/DiagonalPreconditioner.java:60-62, S/ICC.java:75-77); ILU sweeps U' then L'.
+// DiagonalPreconditioner, ICC and SSOR are their own transposes here
+// (S/DiagonalPreconditioner.java:60-62, S/ICC.java:75-77, S/SSOR.java:194-197);
+// ILU and ILUT sweep U' then L' (S/ILU.java:72-78, S/ILUT.java:115-117).
 int mtjg::precond_trans_apply_dev(mtjg_precond *M, const double *b, double *x, const int *status)
 {
-    if (M->kind != MTJG_PC_ILU) return precond_apply_dev(M, b, x, status);
+    if (!lu_kind(M)) return precond_apply_dev(M, b, x, status);
     int st = ilu_trans_setup(M);
     if (st != MTJG_OK) return st;
     IluTrans *t = static_cast<IluTrans *>(M->trans);
@@ -793,6 +950,8 @@ static int precond_host_call(mtjg_precond *M, const double *b, double *x, bool t
     const size_t nb = sizeof(double) * (size_t)M->n;
     if (M->n == 0) return MTJG_OK;
     MTJG_CUDA(cudaMemcpyAsync(M->d_b, b, nb, cudaMemcpyHostToDevice, ctx->stream));
+    // SSOR's sweep starts from x's content (S/SSOR.java:160)
+    if (M->kind == MTJG_PC_SSOR) MTJG_CUDA(cudaMemcpyAsync(M->d_x, x, nb, cudaMemcpyHostToDevice, ctx->stream));
     int st = trans ? precond_trans_apply_dev(M, M->d_b, M->d_x, nullptr) : precond_apply_dev(M, M->d_b, M->d_x, nullptr);
     if (st != MTJG_OK) return st;
     MTJG_CUDA(cudaMemcpyAsync(x, M->d_x, nb, cudaMemcpyDeviceToHost, ctx->stream));
@@ -828,7 +987,7 @@ extern "C" int mtjg_precond_values(mtjg_precond *M, double *out, int64_t cap, in
     if (M->kind == MTJG_PC_JACOBI) {
         total = M->invdiag ? M->n : 0;
         src = M->invdiag;
-    } else if (M->kind == MTJG_PC_ILU || M->kind == MTJG_PC_ICC) {
+    } else if (M->kind != MTJG_PC_IDENTITY) {
         total = M->data ? M->nnz : 0;
         src = M->data;
     }

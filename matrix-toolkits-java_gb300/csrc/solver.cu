@@ -1399,7 +1399,9 @@ extern "C" int mtjg_solver_create(mtjg_ctx *ctx, int kind, int n, int restart, m
     else need = {V_B, V_X, V_R, V_U, V_W};
     const size_t nb = sizeof(double) * (size_t)std::max(1, n);
     bool ok = ensure_state(S, 1) == MTJG_OK;
-    for (int k : need) ok = ok && cudaMalloc(&S->vecs[k], nb) == cudaSuccess;
+    // scratch vectors start at zero: SSOR's apply reads its output vector
+    // (MTJ's start as copies of the solver's template vector)
+    for (int k : need) ok = ok && cudaMalloc(&S->vecs[k], nb) == cudaSuccess && cudaMemset(S->vecs[k], 0, nb) == cudaSuccess;
     if (kind == MTJG_GMRES) {
         const size_t ld = (size_t)restart + 1;
         ok = ok && cudaMalloc(&S->V, nb * ld) == cudaSuccess;

@@ -36,7 +36,7 @@ ERR_OUT_OF_MEMORY = 41
 ERR_DEVICE_TIMEOUT = 42
 
 NORM_ONE, NORM_TWO, NORM_TWO_ROBUST, NORM_INFINITY = 0, 1, 2, 3
-PC_IDENTITY, PC_JACOBI, PC_ILU, PC_ICC = 0, 1, 2, 3
+PC_IDENTITY, PC_JACOBI, PC_ILU, PC_ICC, PC_SSOR, PC_ILUT = 0, 1, 2, 3, 4, 5
 CG, BICGSTAB, GMRES, BICG, CGS, QMR, CHEBYSHEV, IR = 0, 1, 2, 3, 4, 5, 6, 7
 NUMERICS_FAST, NUMERICS_STRICT = 0, 1
 
@@ -108,6 +108,9 @@ PROTOTYPES = {
     "mtjg_precond_trans_apply": (C.c_int, [_vp, _dp, _dp]),
     "mtjg_precond_apply_dev": (C.c_int, [_vp, _vp, _vp]),
     "mtjg_precond_values": (C.c_int, [_vp, _dp, _i64, C.POINTER(_i64)]),
+    "mtjg_precond_set_ssor": (C.c_int, [_vp, C.c_int, C.c_double, C.c_double]),
+    "mtjg_precond_set_ilut": (C.c_int, [_vp, C.c_double, C.c_int]),
+    "mtjg_precond_pattern": (C.c_int, [_vp, _ip, _ip, _ip, _i64, C.POINTER(_i64)]),
     "mtjg_precond_destroy": (C.c_int, [_vp]),
     "mtjg_solver_create": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.POINTER(_vp)]),
     "mtjg_solver_set_precond": (C.c_int, [_vp, _vp]),

@@ -412,6 +412,18 @@ class Preconditioner:
             _raise(self._lib.mtjg_precond_values(self.h, L.dptr(out), ln.value, C.byref(ln)), "values")
         return out
 
+    def pattern(self):
+        """(rowptr, colind, diag) of the factor, in the layout of values();
+        diag holds each row's diagonal position within the row."""
+        nnz = C.c_int64(0)
+        _raise(self._lib.mtjg_precond_pattern(self.h, None, None, None, 0, C.byref(nnz)), "pattern")
+        rp = np.empty(self.n + 1, dtype=np.int32)
+        ci = np.empty(max(nnz.value, 1), dtype=np.int32)
+        dg = np.empty(max(self.n, 1), dtype=np.int32)
+        _raise(self._lib.mtjg_precond_pattern(self.h, L.iptr(rp), L.iptr(ci), L.iptr(dg), nnz.value, C.byref(nnz)),
+               "pattern")
+        return rp, ci[:nnz.value], dg[:self.n]
+
     def close(self):
         if getattr(self, "h", None):
             self._lib.mtjg_precond_destroy(self.h)
@@ -447,6 +459,51 @@ class ILU(Preconditioner):
         if hasattr(LU, "isSquare") and not LU.isSquare():
             raise IllegalArgumentException("ILU only applies to square matrices")
         super().__init__(n, ctx or getattr(LU, "ctx", None))
+
+
+class SSOR(Preconditioner):
+    """new SSOR(CompRowMatrix F, reverse, omegaF, omegaR) (S/SSOR.java:62-77).
+    apply(b, x) is one symmetric SOR sweep starting from x's content, as in
+    MTJ (S/SSOR.java:148-192): pass the x to start from (zeros when None)."""
+
+    kind = L.PC_SSOR
+
+    def __init__(self, F, reverse=True, omegaF=1.0, omegaR=1.0, ctx=None):
+        n = F.numRows() if hasattr(F, "numRows") else int(F)
+        if hasattr(F, "isSquare") and not F.isSquare():
+            raise IllegalArgumentException("SSOR only applies to square matrices")
+        super().__init__(n, ctx or getattr(F, "ctx", None))
+        self.reverse = bool(reverse)
+        self.setOmega(omegaF, omegaR)
+
+    def setOmega(self, omegaF, omegaR):
+        """SSOR.setOmega, S/SSOR.java:87-96."""
+        _raise(self._lib.mtjg_precond_set_ssor(self.h, 1 if self.reverse else 0, float(omegaF), float(omegaR)),
+               "setOmega")
+        self.omegaF, self.omegaR = float(omegaF), float(omegaR)
+
+    def apply(self, b, x=None):
+        out = np.zeros(self.n) if x is None else x
+        return super().apply(b, out)
+
+    def transApply(self, b, x=None):
+        out = np.zeros(self.n) if x is None else x
+        return super().transApply(b, out)
+
+
+class ILUT(Preconditioner):
+    """new ILUT(FlexCompRowMatrix LU, tau, p) (S/ILUT.java:68-97); LU gives the
+    size (a CompRowMatrix or the row count)."""
+
+    kind = L.PC_ILUT
+
+    def __init__(self, LU, tau=1e-6, p=25, ctx=None):
+        n = LU.numRows() if hasattr(LU, "numRows") else int(LU)
+        if hasattr(LU, "isSquare") and not LU.isSquare():
+            raise IllegalArgumentException("ILU only applies to square matrices")
+        super().__init__(n, ctx or getattr(LU, "ctx", None))
+        _raise(self._lib.mtjg_precond_set_ilut(self.h, float(tau), int(p)), "ILUT")
+        self.tau, self.p = float(tau), int(p)
 
 
 class ICC(Preconditioner):

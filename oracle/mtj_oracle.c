@@ -223,9 +223,22 @@ static int mon_check_vec(mon_state *m, int n, const double *r)
 
 /* ------------------------------------------------------- preconditioners */
 
+/* SparseVector storage (S/SparseVector.java): sorted indices in
+ * index[0, used), capacity cap; slots past used keep whatever they held. */
+typedef struct svec {
+    int *index;
+    double *data;
+    int cap, used;
+} svec;
+
 struct or_pc {
     int kind;
     int n;
+    /* SSOR (S/SSOR.java:37-52) and ILUT (S/ILUT.java:68-85) parameters */
+    int reverse, p;
+    double omega_f, omega_r, tau;
+    svec *rows;          /* ILUT factor rows */
+    double *xx;          /* SSOR half iterate */
     /* Jacobi */
     double *invdiag;
     /* ILU / ICC: private CSR copy factored in place + diagonal positions */
@@ -241,14 +254,34 @@ or_pc *or_pc_new(int kind, int n)
     pc->kind = kind;
     pc->n = n;
     pc->y = (double *)calloc((size_t)(n > 0 ? n : 1), sizeof(double));
+    pc->xx = (double *)calloc((size_t)(n > 0 ? n : 1), sizeof(double));
+    /* new SSOR(F) = SSOR(F, true, 1, 1) (S/SSOR.java:75-77); new ILUT(LU) =
+     * ILUT(LU, 1e-6, 25) (S/ILUT.java:95-97) */
+    pc->reverse = 1;
+    pc->omega_f = pc->omega_r = 1;
+    pc->tau = 1e-6;
+    pc->p = 25;
     if (kind == OR_PC_JACOBI)
         pc->invdiag = (double *)calloc((size_t)(n > 0 ? n : 1), sizeof(double));
     return pc;
 }
 
+static void free_rows(or_pc *pc)
+{
+    if (!pc->rows) return;
+    for (int i = 0; i < pc->n; ++i) {
+        free(pc->rows[i].index);
+        free(pc->rows[i].data);
+    }
+    free(pc->rows);
+    pc->rows = NULL;
+}
+
 void or_pc_free(or_pc *pc)
 {
     if (!pc) return;
+    free_rows(pc);
+    free(pc->xx);
     free(pc->invdiag);
     free(pc->rowptr);
     free(pc->colind);
@@ -412,6 +445,307 @@ static int icc_factor_reach(or_pc *pc, int *detail)
     return st;
 }
 
+/* ------------------------------------------------------------------ ILUT */
+
+/* Arrays.binarySearchGreater(index, key, 0, used) (S/Arrays.java:51-54,
+ * :123-156): the first position whose index is >= key, else used. */
+static int sv_greater(const svec *v, int key)
+{
+    int begin = 0, end = v->used;
+    if (begin == end) return end;
+    end--;
+    int mid = (end + begin) >> 1;
+    while (begin <= end) {
+        mid = (end + begin) >> 1;
+        if (v->index[mid] < key) begin = mid + 1;
+        else if (v->index[mid] > key) end = mid - 1;
+        else return mid;
+    }
+    return v->index[mid] >= key ? mid : mid + 1;
+}
+
+/* SparseVector.getIndex (S/SparseVector.java:188-231): position of ind,
+ * inserted (value 0) when absent; the storage doubles (at most `size`) when
+ * full, into fresh zero-filled arrays. */
+static int sv_get_index(svec *v, int ind, int size)
+{
+    int i = sv_greater(v, ind);
+    if (i < v->used && v->index[i] == ind) return i;
+    int *ni = v->index;
+    double *nd = v->data;
+    int grew = 0;
+    if (++v->used > v->cap) {
+        int len = v->cap != 0 ? v->cap << 1 : 1;
+        if (len > size) len = size;
+        ni = (int *)calloc((size_t)(len > 0 ? len : 1), sizeof(int));
+        nd = (double *)calloc((size_t)(len > 0 ? len : 1), sizeof(double));
+        if (i) {
+            memcpy(ni, v->index, sizeof(int) * (size_t)i);
+            memcpy(nd, v->data, sizeof(double) * (size_t)i);
+        }
+        v->cap = len;
+        grew = 1;
+    }
+    int tail = v->used - i - 1;
+    if (tail > 0) {
+        memmove(ni + i + 1, v->index + i, sizeof(int) * (size_t)tail);
+        memmove(nd + i + 1, v->data + i, sizeof(double) * (size_t)tail);
+    }
+    ni[i] = ind;
+    nd[i] = 0.;
+    if (grew) {
+        free(v->index);
+        free(v->data);
+    }
+    v->index = ni;
+    v->data = nd;
+    return i;
+}
+
+/* SparseVector.set (S/SparseVector.java:157-164): the position first (it may
+ * reallocate the storage), then the value */
+static void sv_set(svec *v, int ind, double value, int size)
+{
+    int i = sv_get_index(v, ind, size);
+    v->data[i] = value;
+}
+
+/* SparseVector.zero (S/SparseVector.java:238-242): values cleared, used = 0,
+ * the index array keeps its contents */
+static void sv_zero(svec *v)
+{
+    for (int i = 0; i < v->cap; ++i) v->data[i] = 0;
+    v->used = 0;
+}
+
+/* SparseVector.norm2 (S/SparseVector.java:282-287) */
+static double sv_norm2(const svec *v)
+{
+    double norm = 0;
+    for (int i = 0; i < v->used; ++i) norm += v->data[i] * v->data[i];
+    return sqrt(norm);
+}
+
+typedef struct {
+    int index;
+    double value;
+} ide;
+
+/* Collections.sort of ILUT.IntDoubleEntry (S/ILUT.java:282-302): by
+ * decreasing magnitude, stable (a merge sort keeps equal magnitudes in the
+ * order they were added, i.e. by increasing index) */
+static void ide_sort(ide *a, ide *tmp, int n)
+{
+    if (n < 2) return;
+    int h = n / 2;
+    ide_sort(a, tmp, h);
+    ide_sort(a + h, tmp, n - h);
+    int i = 0, j = h, k = 0;
+    while (i < h && j < n) {
+        if (fabs(a[j].value) > fabs(a[i].value)) tmp[k++] = a[j++];
+        else tmp[k++] = a[i++];
+    }
+    while (i < h) tmp[k++] = a[i++];
+    while (j < n) tmp[k++] = a[j++];
+    memcpy(a, tmp, sizeof(ide) * (size_t)n);
+}
+
+/* ILUT.gather (S/ILUT.java:225-272) of the dense row z into row v (row d) */
+static void ilut_gather(or_pc *pc, const double *z, svec *v, double taui, int d, ide *lo, ide *up, ide *tmp)
+{
+    int n = pc->n, nl = 0, nu = 0, nlo = 0, nup = 0;
+    for (int i = 0; i < v->used; ++i) {
+        if (v->index[i] < d) nl++;
+        else if (v->index[i] > d) nu++;
+    }
+    sv_zero(v);
+    for (int i = 0; i < d; ++i)
+        if (fabs(z[i]) > taui) { lo[nlo].index = i; lo[nlo].value = z[i]; nlo++; }
+    for (int i = d + 1; i < n; ++i)
+        if (fabs(z[i]) > taui) { up[nup].index = i; up[nup].value = z[i]; nup++; }
+    ide_sort(lo, tmp, nlo);
+    ide_sort(up, tmp, nup);
+    sv_set(v, d, z[d], n);
+    int ml = nl + pc->p < nlo ? nl + pc->p : nlo, mu = nu + pc->p < nup ? nu + pc->p : nup;
+    for (int i = 0; i < ml; ++i) sv_set(v, lo[i].index, lo[i].value, n);
+    for (int i = 0; i < mu; ++i) sv_set(v, up[i].index, up[i].value, n);
+}
+
+/* ILUT.setMatrix + factor (S/ILUT.java:119-208), literally: the dense work
+ * row LUi, every earlier row k visited (O(n^2)).  LU.set(A); LU.compact()
+ * leaves each row holding A's nonzero entries, storage exactly full. */
+static int ilut_factor(or_pc *pc, const int *rowptr, const int *colind, const double *val, int *detail)
+{
+    int n = pc->n, st = OR_OK;
+    free_rows(pc);
+    pc->rows = (svec *)calloc((size_t)(n > 0 ? n : 1), sizeof(svec));
+    pc->diagind = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    for (int k = 0; k < n; ++k) {
+        int nz = 0;
+        for (int j = rowptr[k]; j < rowptr[k + 1]; ++j) nz += val[j] != 0.;
+        svec *v = &pc->rows[k];
+        v->cap = v->used = nz;
+        v->index = (int *)calloc((size_t)(nz > 0 ? nz : 1), sizeof(int));
+        v->data = (double *)calloc((size_t)(nz > 0 ? nz : 1), sizeof(double));
+        for (int j = rowptr[k], q = 0; j < rowptr[k + 1]; ++j)
+            if (val[j] != 0.) { v->index[q] = colind[j]; v->data[q] = val[j]; q++; }
+    }
+    for (int k = 0; k < n; ++k) {
+        pc->diagind[k] = jbinsearch(pc->rows[k].index, 0, pc->rows[k].used, k);
+        if (pc->diagind[k] < 0) { *detail = k + 1; return OR_ERR_MISSING_DIAGONAL; }
+    }
+    double *LUi = (double *)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
+    ide *lo = (ide *)malloc(sizeof(ide) * (size_t)(n > 0 ? n : 1));
+    ide *up = (ide *)malloc(sizeof(ide) * (size_t)(n > 0 ? n : 1));
+    ide *tmp = (ide *)malloc(sizeof(ide) * (size_t)(n > 0 ? n : 1));
+    for (int i = 1; i < n && st == OR_OK; ++i) {
+        svec *rowi = &pc->rows[i];
+        double taui = sv_norm2(rowi) * pc->tau;
+        for (int c = 0; c < n; ++c) LUi[c] = 0;
+        for (int j = 0; j < rowi->used; ++j) LUi[rowi->index[j]] = rowi->data[j];
+        for (int k = 0; k < i; ++k) {
+            const svec *rk = &pc->rows[k];
+            double dk = rk->data[pc->diagind[k]];
+            if (dk == 0) { *detail = k + 1; st = OR_ERR_ZERO_DIAGONAL; break; }
+            double LUik = LUi[k] / dk;
+            if (fabs(LUik) <= taui) continue;
+            for (int j = pc->diagind[k] + 1; j < rk->used; ++j) LUi[rk->index[j]] -= LUik * rk->data[j];
+            LUi[k] = LUik;
+        }
+        if (st != OR_OK) break;
+        ilut_gather(pc, LUi, rowi, taui, i, lo, up, tmp);
+        int di = pc->diagind[i];
+        if (di >= rowi->cap || rowi->index[di] != i) {
+            pc->diagind[i] = jbinsearch(rowi->index, 0, rowi->used, i);
+            if (pc->diagind[i] < 0) { *detail = i + 1; st = OR_ERR_MISSING_DIAGONAL; }
+        }
+    }
+    free(LUi); free(lo); free(up); free(tmp);
+    return st;
+}
+
+/* positions of row i the factor's triangular solves read: [0, diagind] and
+ * the stored entries */
+static int ilut_row_len(const or_pc *pc, int i)
+{
+    int u = pc->rows[i].used, d = pc->diagind[i] + 1;
+    return u > d ? u : d;
+}
+
+/* ILUT.apply (S/ILUT.java:111-113): UnitLowerFlexCompRowMatrix.solve (:321-336)
+ * into y, then UpperFlexCompRowMatrix.solve (:375-391) */
+static void ilut_apply(or_pc *pc, const double *b, double *x)
+{
+    int n = pc->n;
+    double *y = pc->y;
+    for (int i = 0; i < n; ++i) {
+        const svec *r = &pc->rows[i];
+        double sum = 0;
+        for (int j = 0; j < pc->diagind[i]; ++j) sum += r->data[j] * y[r->index[j]];
+        y[i] = b[i] - sum;
+    }
+    for (int i = n - 1; i >= 0; --i) {
+        const svec *r = &pc->rows[i];
+        double sum = 0;
+        for (int j = pc->diagind[i] + 1; j < r->used; ++j) sum += r->data[j] * x[r->index[j]];
+        x[i] = (y[i] - sum) / r->data[pc->diagind[i]];
+    }
+}
+
+/* ILUT.transApply (S/ILUT.java:115-117): UpperFlexCompRowMatrix.transSolve
+ * (:393-410) into y, then UnitLowerFlexCompRowMatrix.transSolve (:338-353) */
+static void ilut_trans_apply(or_pc *pc, const double *b, double *x)
+{
+    int n = pc->n;
+    double *y = pc->y;
+    if (y != b) memcpy(y, b, sizeof(double) * (size_t)n);
+    for (int i = 0; i < n; ++i) {
+        const svec *r = &pc->rows[i];
+        y[i] /= r->data[pc->diagind[i]];
+        for (int j = pc->diagind[i] + 1; j < r->used; ++j) y[r->index[j]] -= r->data[j] * y[i];
+    }
+    if (x != y) memcpy(x, y, sizeof(double) * (size_t)n);
+    for (int i = n - 1; i >= 0; --i) {
+        const svec *r = &pc->rows[i];
+        for (int j = 0; j < pc->diagind[i]; ++j) x[r->index[j]] -= r->data[j] * x[i];
+    }
+}
+
+/* ------------------------------------------------------------------ SSOR */
+
+/* SSOR.apply (S/SSOR.java:148-192): one symmetric SOR sweep from the current
+ * content of x (forward into xx, then backward into x when reverse) */
+static void ssor_apply(or_pc *pc, const double *b, double *x)
+{
+    int n = pc->n;
+    const int *rp = pc->rowptr, *ci = pc->colind, *dg = pc->diagind;
+    const double *d = pc->data;
+    double *xx = pc->xx;
+    memcpy(xx, x, sizeof(double) * (size_t)n);
+    for (int i = 0; i < n; ++i) {
+        double sigma = 0;
+        for (int j = rp[i]; j < dg[i]; ++j) sigma += d[j] * xx[ci[j]];
+        for (int j = dg[i] + 1; j < rp[i + 1]; ++j) sigma += d[j] * x[ci[j]];
+        sigma = (b[i] - sigma) / d[dg[i]];
+        xx[i] = x[i] + pc->omega_f * (sigma - x[i]);
+    }
+    if (!pc->reverse) {
+        memcpy(x, xx, sizeof(double) * (size_t)n);
+        return;
+    }
+    for (int i = n - 1; i >= 0; --i) {
+        double sigma = 0;
+        for (int j = rp[i]; j < dg[i]; ++j) sigma += d[j] * xx[ci[j]];
+        for (int j = dg[i] + 1; j < rp[i + 1]; ++j) sigma += d[j] * x[ci[j]];
+        sigma = (b[i] - sigma) / d[dg[i]];
+        x[i] = xx[i] + pc->omega_r * (sigma - xx[i]);
+    }
+}
+
+int or_pc_set_params(or_pc *pc, double a, double b, int c)
+{
+    if (pc->kind == OR_PC_SSOR) {
+        /* SSOR.setOmega, S/SSOR.java:87-96 */
+        if (a < 0 || a > 2 || b < 0 || b > 2) return OR_ERR_ILLEGAL_ARGUMENT;
+        pc->omega_f = a;
+        pc->omega_r = b;
+        pc->reverse = c;
+    } else if (pc->kind == OR_PC_ILUT) {
+        pc->tau = a;
+        pc->p = c;
+    }
+    return OR_OK;
+}
+
+int or_pc_pattern(const or_pc *pc, int *rowptr, int *colind, int cap)
+{
+    if (pc->kind == OR_PC_ILUT) {
+        int tot = 0;
+        if (rowptr) rowptr[0] = 0;
+        for (int i = 0; i < pc->n; ++i) {
+            int len = ilut_row_len(pc, i);
+            for (int j = 0; j < len; ++j)
+                if (colind && tot + j < cap) colind[tot + j] = pc->rows[i].index[j];
+            tot += len;
+            if (rowptr) rowptr[i + 1] = tot;
+        }
+        return tot;
+    }
+    if (!pc->rowptr) return 0;
+    if (rowptr) memcpy(rowptr, pc->rowptr, sizeof(int) * (size_t)(pc->n + 1));
+    int m = pc->nnz < cap ? pc->nnz : cap;
+    if (colind) memcpy(colind, pc->colind, sizeof(int) * (size_t)m);
+    return pc->nnz;
+}
+
+/* position of each row's diagonal in or_pc_pattern's rows */
+int or_pc_diag(const or_pc *pc, int *diag)
+{
+    if (!pc->diagind) return 0;
+    memcpy(diag, pc->diagind, sizeof(int) * (size_t)pc->n);
+    return pc->n;
+}
+
 int or_pc_set_matrix(or_pc *pc, int n, const int *rowptr, const int *colind,
                      const double *val, int *detail)
 {
@@ -445,8 +779,10 @@ int or_pc_set_matrix(or_pc *pc, int n, const int *rowptr, const int *colind,
         memcpy(pc->colind, colind, sizeof(int) * (size_t)nnz);
         memcpy(pc->data, val, sizeof(double) * (size_t)nnz);
     }
+    if (pc->kind == OR_PC_ILUT) return ilut_factor(pc, rowptr, colind, val, detail);
     int st = find_diag(pc, detail);
     if (st != OR_OK) return st;
+    if (pc->kind == OR_PC_SSOR) return OR_OK;  /* SSOR.setMatrix, S/SSOR.java:98-113 */
     if (pc->kind == OR_PC_ILU) return ilu_factor(pc, detail);
     if (pc->kind == OR_PC_ICC_LITERAL) return icc_factor_literal(pc, detail);
     return icc_factor_reach(pc, detail);
@@ -454,6 +790,16 @@ int or_pc_set_matrix(or_pc *pc, int n, const int *rowptr, const int *colind,
 
 int or_pc_values(const or_pc *pc, double *out, int cap)
 {
+    if (pc->kind == OR_PC_ILUT) {
+        int tot = 0;
+        for (int i = 0; pc->rows && i < pc->n; ++i) {
+            int len = ilut_row_len(pc, i);
+            for (int j = 0; j < len; ++j)
+                if (out && tot + j < cap) out[tot + j] = pc->rows[i].data[j];
+            tot += len;
+        }
+        return tot;
+    }
     if (pc->kind == OR_PC_JACOBI) {
         int m = pc->n < cap ? pc->n : cap;
         memcpy(out, pc->invdiag, sizeof(double) * (size_t)m);
@@ -521,6 +867,12 @@ void or_pc_apply(or_pc *pc, const double *b, double *x)
         lower_solve(pc, b, pc->y);
         upper_solve(pc, pc->y, x);
         break;
+    case OR_PC_SSOR:
+        ssor_apply(pc, b, x);
+        break;
+    case OR_PC_ILUT:
+        ilut_apply(pc, b, x);
+        break;
     default: /* ICC.apply S/ICC.java:67-73 */
         upper_trans_solve(pc, b, pc->y);
         upper_solve(pc, pc->y, x);
@@ -533,7 +885,9 @@ void or_pc_trans_apply(or_pc *pc, const double *b, double *x)
     if (pc->kind == OR_PC_ILU) { /* S/ILU.java:72-78 */
         upper_trans_solve(pc, b, pc->y);
         lower_trans_solve(pc, pc->y, x);
-    } else {
+    } else if (pc->kind == OR_PC_ILUT) {
+        ilut_trans_apply(pc, b, x);
+    } else { /* SSOR.transApply assumes a symmetric matrix (S/SSOR.java:194-197) */
         or_pc_apply(pc, b, x);
     }
 }

@@ -41,7 +41,8 @@ enum {
 };
 
 enum { OR_NORM_ONE = 0, OR_NORM_TWO = 1, OR_NORM_TWO_ROBUST = 2, OR_NORM_INFINITY = 3 };
-enum { OR_PC_IDENTITY = 0, OR_PC_JACOBI = 1, OR_PC_ILU = 2, OR_PC_ICC = 3, OR_PC_ICC_LITERAL = 4 };
+enum { OR_PC_IDENTITY = 0, OR_PC_JACOBI = 1, OR_PC_ILU = 2, OR_PC_ICC = 3, OR_PC_ICC_LITERAL = 4, OR_PC_SSOR = 5,
+       OR_PC_ILUT = 6 };
 enum { OR_CG = 0, OR_BICGSTAB = 1, OR_GMRES = 2, OR_BICG = 3, OR_CGS = 4, OR_QMR = 5, OR_CHEBYSHEV = 6, OR_IR = 7 };
 /* or_result.detail of a breakdown: which quantity became zero */
 enum { OR_BD_RHO = 1, OR_BD_OMEGA = 2, OR_BD_XI = 3, OR_BD_DELTA = 4, OR_BD_EP = 5, OR_BD_BETA = 6, OR_BD_GAMMA = 7 };
@@ -87,8 +88,15 @@ int or_pc_set_matrix(or_pc *pc, int n, const int *rowptr, const int *colind,
                      const double *val, int *detail);
 void or_pc_apply(or_pc *pc, const double *b, double *x);
 void or_pc_trans_apply(or_pc *pc, const double *b, double *x);
-/* factor values (ILU/ICC: the in-place data array; Jacobi: invdiag) */
+/* factor values (ILU/ICC: the in-place data array; Jacobi: invdiag; ILUT:
+ * its rows' stored values, positions [0, max(used, diagind + 1)) per row) */
 int or_pc_values(const or_pc *pc, double *out, int cap);
+/* the factor's pattern in the layout of or_pc_values (returns the entry count) */
+int or_pc_pattern(const or_pc *pc, int *rowptr, int *colind, int cap);
+int or_pc_diag(const or_pc *pc, int *diag);
+/* SSOR: (omegaF, omegaR, reverse) (S/SSOR.java:62-96); ILUT: (tau, -, p)
+ * (S/ILUT.java:68-85).  Call before or_pc_set_matrix. */
+int or_pc_set_params(or_pc *pc, double a, double b, int c);
 
 /* IterativeSolver.solve (S/CG.java, S/BiCGstab.java, S/GMRES.java, S/BiCG.java,
  * S/CGS.java, S/QMR.java, S/Chebyshev.java, S/IR.java); pc NULL = identity */

@@ -28,7 +28,7 @@ SRC = os.path.join(HERE, "mtj_oracle.c")
 OK, NC_ITERATIONS, NC_DIVERGENCE, NC_BREAKDOWN = 0, 1, 2, 3
 ERR_ILLEGAL_ARGUMENT, ERR_ZERO_PIVOT, ERR_ZERO_DIAGONAL, ERR_MISSING_DIAGONAL, ERR_SINGULAR = 10, 20, 21, 22, 23
 NORM_ONE, NORM_TWO, NORM_TWO_ROBUST, NORM_INFINITY = 0, 1, 2, 3
-PC_IDENTITY, PC_JACOBI, PC_ILU, PC_ICC, PC_ICC_LITERAL = 0, 1, 2, 3, 4
+PC_IDENTITY, PC_JACOBI, PC_ILU, PC_ICC, PC_ICC_LITERAL, PC_SSOR, PC_ILUT = 0, 1, 2, 3, 4, 5, 6
 CG, BICGSTAB, GMRES, BICG, CGS, QMR, CHEBYSHEV, IR = 0, 1, 2, 3, 4, 5, 6, 7
 # breakdown detail: which quantity became zero
 BD_RHO, BD_OMEGA, BD_XI, BD_DELTA, BD_EP, BD_BETA, BD_GAMMA = 1, 2, 3, 4, 5, 6, 7
@@ -79,6 +79,9 @@ def lib():
         l.or_pc_apply.argtypes = [C.c_void_p, _dp, _dp]
         l.or_pc_trans_apply.argtypes = [C.c_void_p, _dp, _dp]
         l.or_pc_values.argtypes = [C.c_void_p, _dp, C.c_int]
+        l.or_pc_pattern.argtypes = [C.c_void_p, _ip, _ip, C.c_int]
+        l.or_pc_diag.argtypes = [C.c_void_p, _ip]
+        l.or_pc_set_params.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_int]
         l.or_solve.restype = C.c_int
         l.or_solve.argtypes = [C.c_int, C.c_int, C.c_int, _ip, _ip, _dp, C.c_void_p, _dp, _dp,
                                C.POINTER(Monitor), C.POINTER(Result), _dp, _ip, C.c_int]
@@ -177,15 +180,35 @@ class Precond:
         self.detail = d.value
         return self.status
 
-    def apply(self, b):
+    def set_params(self, a, b=0.0, c=0):
+        """SSOR: (omegaF, omegaR, reverse); ILUT: (tau, unused, p)."""
+        return lib().or_pc_set_params(self.h, float(a), float(b), int(c))
+
+    def apply(self, b, x0=None):
+        """M.apply(b, x); x0 is x's content before the call (SSOR starts its
+        sweep from it; the others ignore it).  Default: zeros."""
         b = np.ascontiguousarray(b, dtype=np.float64)
-        x = np.empty(max(self.n, 1))
+        x = np.zeros(max(self.n, 1))
+        if x0 is not None:
+            x[: self.n] = x0
         lib().or_pc_apply(self.h, _d(b), _d(x))
         return x[: self.n]
 
-    def trans_apply(self, b):
+    def pattern(self):
+        """(rowptr, colind, diag) of the factor (ILUT: its rows after the factor)."""
+        nnz = lib().or_pc_pattern(self.h, None, None, 0)
+        rp = np.empty(self.n + 1, dtype=np.int32)
+        ci = np.empty(max(nnz, 1), dtype=np.int32)
+        lib().or_pc_pattern(self.h, _i(rp), _i(ci), nnz)
+        dg = np.empty(max(self.n, 1), dtype=np.int32)
+        lib().or_pc_diag(self.h, _i(dg))
+        return rp, ci[:nnz], dg[: self.n]
+
+    def trans_apply(self, b, x0=None):
         b = np.ascontiguousarray(b, dtype=np.float64)
-        x = np.empty(max(self.n, 1))
+        x = np.zeros(max(self.n, 1))
+        if x0 is not None:
+            x[: self.n] = x0
         lib().or_pc_trans_apply(self.h, _d(b), _d(x))
         return x[: self.n]
 

@@ -562,3 +562,150 @@ def ir(rp, ci, v, b, x, M, mon):
         r = mult_add(rp, ci, v, -1.0, x, b)
         mon.iter += 1
     return x
+
+
+# ---------------------------------------------------------- SSOR and ILUT
+def ssor_apply(rp, ci, v, dg, b, x, omega_f=1.0, omega_r=1.0, reverse=True):
+    """SSOR.apply, S/SSOR.java:148-192: one symmetric SOR sweep starting
+    from x's content; returns the new x."""
+    n = len(rp) - 1
+    xd = list(x)
+    xx = list(x)
+    for i in range(n):
+        sigma = 0.0
+        for j in range(rp[i], dg[i]):
+            sigma = sigma + v[j] * xx[ci[j]]
+        for j in range(dg[i] + 1, rp[i + 1]):
+            sigma = sigma + v[j] * xd[ci[j]]
+        sigma = (b[i] - sigma) / v[dg[i]]
+        xx[i] = xd[i] + omega_f * (sigma - xd[i])
+    if not reverse:
+        return xx
+    for i in range(n - 1, -1, -1):
+        sigma = 0.0
+        for j in range(rp[i], dg[i]):
+            sigma = sigma + v[j] * xx[ci[j]]
+        for j in range(dg[i] + 1, rp[i + 1]):
+            sigma = sigma + v[j] * xd[ci[j]]
+        sigma = (b[i] - sigma) / v[dg[i]]
+        xd[i] = xx[i] + omega_r * (sigma - xx[i])
+    return xd
+
+
+class SparseRow:
+    """SparseVector's storage (S/SparseVector.java): sorted index[:used];
+    the slots past used keep their old contents; full storage doubles (at
+    most to `size`) into fresh zeroed arrays (getIndex, :188-231)."""
+
+    def __init__(self, size, index, data):
+        self.size = size
+        self.index = list(index)
+        self.data = list(data)
+        self.used = len(index)
+
+    def _find_greater(self, key):  # Arrays.binarySearchGreater over [0, used)
+        lo, hi = 0, self.used
+        while lo < hi:
+            mid = (lo + hi) // 2
+            if self.index[mid] < key:
+                lo = mid + 1
+            else:
+                hi = mid
+        return lo
+
+    def set(self, ind, value):
+        i = self._find_greater(ind)
+        if not (i < self.used and self.index[i] == ind):
+            self.used += 1
+            if self.used > len(self.data):
+                cap = len(self.data) * 2 if self.data else 1
+                cap = min(cap, self.size)
+                ni, nd = self.index[:i] + [0] * (cap - i), self.data[:i] + [0.0] * (cap - i)
+            else:
+                ni, nd = self.index, self.data
+            tail_i = self.index[i:self.used - 1]
+            tail_d = self.data[i:self.used - 1]
+            ni[i + 1:self.used] = tail_i
+            nd[i + 1:self.used] = tail_d
+            ni[i], nd[i] = ind, 0.0
+            self.index, self.data = ni, nd
+        self.data[i] = value
+
+    def zero(self):
+        self.data = [0.0] * len(self.data)
+        self.used = 0
+
+
+def ilut_factor(rp, ci, v, tau=1e-6, p=25):
+    """ILUT.setMatrix + factor, S/ILUT.java:119-272, literally; returns
+    (rows, diagind) or raises RuntimeError."""
+    n = len(rp) - 1
+    rows = []
+    for k in range(n):
+        pairs = [(ci[j], v[j]) for j in range(rp[k], rp[k + 1]) if v[j] != 0.0]
+        rows.append(SparseRow(n, [c for c, _ in pairs], [x for _, x in pairs]))
+    diag = []
+    for k in range(n):
+        r = rows[k]
+        j = bisect.bisect_left(r.index[:r.used], k)
+        if j >= r.used or r.index[j] != k:
+            raise RuntimeError(f"Missing diagonal entry on row {k + 1}")
+        diag.append(j)
+    for i in range(1, n):
+        rowi = rows[i]
+        s = 0.0
+        for t in range(rowi.used):
+            s = s + rowi.data[t] * rowi.data[t]
+        taui = math.sqrt(s) * tau
+        z = [0.0] * n
+        for t in range(rowi.used):
+            z[rowi.index[t]] = rowi.data[t]
+        for k in range(i):
+            rk = rows[k]
+            dk = rk.data[diag[k]]
+            if dk == 0:
+                raise RuntimeError(f"Zero diagonal entry on row {k + 1} during ILU process")
+            lik = z[k] / dk
+            if abs(lik) <= taui:
+                continue
+            for j in range(diag[k] + 1, rk.used):
+                z[rk.index[j]] = z[rk.index[j]] - lik * rk.data[j]
+            z[k] = lik
+        nl = sum(1 for t in range(rowi.used) if rowi.index[t] < i)
+        nu = sum(1 for t in range(rowi.used) if rowi.index[t] > i)
+        rowi.zero()
+        lower = [(c, z[c]) for c in range(i) if abs(z[c]) > taui]
+        upper = [(c, z[c]) for c in range(i + 1, n) if abs(z[c]) > taui]
+        lower.sort(key=lambda e: -abs(e[1]))  # stable, as Collections.sort
+        upper.sort(key=lambda e: -abs(e[1]))
+        rowi.set(i, z[i])
+        for c, x in lower[:min(nl + p, len(lower))]:
+            rowi.set(c, x)
+        for c, x in upper[:min(nu + p, len(upper))]:
+            rowi.set(c, x)
+        d = diag[i]
+        if d >= len(rowi.index) or rowi.index[d] != i:
+            j = bisect.bisect_left(rowi.index[:rowi.used], i)
+            diag[i] = j
+    return rows, diag
+
+
+def ilut_apply(rows, diag, b, y):
+    """ILUT.apply (S/ILUT.java:111-113): the unit lower solve into y (whose
+    previous content it may read, as MTJ does), then the upper solve."""
+    n = len(rows)
+    y = list(y)
+    for i in range(n):
+        r = rows[i]
+        s = 0.0
+        for j in range(diag[i]):
+            s = s + r.data[j] * y[r.index[j]]
+        y[i] = b[i] - s
+    x = [0.0] * n
+    for i in range(n - 1, -1, -1):
+        r = rows[i]
+        s = 0.0
+        for j in range(diag[i] + 1, r.used):
+            s = s + r.data[j] * x[r.index[j]]
+        x[i] = (y[i] - s) / r.data[diag[i]] if r.data[diag[i]] != 0 else math.copysign(math.inf, y[i] - s)
+    return x, y

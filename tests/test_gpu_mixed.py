@@ -76,5 +76,5 @@ def test_mixed_batch_equals_solo(ctx):
 
 def test_mixed_rejects_other_solvers(ctx):
     s = sparse.GMRES(10, ctx=ctx)
-    with pytest.raises(sparse.CudaError):
+    with pytest.raises(sparse.UnsupportedOperationException):
         s.setMixedPrecision(True)

@@ -3,7 +3,12 @@
 Same bars as the CG / BiCGstab / GMRES parity tests: the oracle's status
 and breakdown reason, its iteration count within 2, the relative residual
 history r_k / r_0 within 1e-10 over the common prefix (the same iteration
-numbers passed to the reporter), x within 1e-8; and the reference's own
+numbers passed to the reporter), x within 1e-8.  Like BiCGstab, the
+Lanczos-type solvers (BiCG, CGS, QMR) move their own history by more than
+that under a mere change of the order of the oracle's dot products (CGS
+without a preconditioner by 1e-2 of r_0); there the history bar is four
+times that measured envelope and the iteration bar two more than its
+iteration spread.  And the reference's own
 solver tests (TS/BiCGTest, CGSTest, QMRTest, ChebyshevTest and their
 Diagonal / ILU variants): x recovered within 1e-4 on seeded random systems
 of the reference's shapes."""
@@ -102,9 +107,29 @@ def test_matches_oracle(ctx, numerics, case):
         eig = (float(ev[0]), float(ev[-1]))
     x, exc, solver, mon, xo, res, hr, hi = _both(ctx, name, pname, n, rp, ci, v, b, np.zeros(n), eig=eig)
     assert res.status == 0 and exc is None, (res.status, exc)
-    assert abs(mon.iterations() - res.iterations) <= 2, (mon.iterations(), res.iterations)
-    assert _gap(solver, hr, hi) <= 1e-10
+    env, it_env = _order_envelope(name, pname, n, rp, ci, v, b, hr, res.iterations, eig)
+    assert abs(mon.iterations() - res.iterations) <= 2 + it_env, (mon.iterations(), res.iterations, it_env)
+    assert _gap(solver, hr, hi) <= max(1e-10, 4 * env), env
     assert np.max(np.abs(x - xo)) <= 1e-8 * max(1.0, np.max(np.abs(xo)))
+
+
+def _order_envelope(name, pname, n, rp, ci, v, b, h_seq, it_seq, eig):
+    """How far the oracle's own history (relative to r_0) and iteration count
+    move when only its dot products and norms are summed in another order."""
+    Ao = O.Csr(n, n, rp, ci, v)
+    pco = None
+    if PCS[pname][1] is not None:
+        pco = O.Precond(PCS[pname][1], n)
+        pco.set_matrix(Ao)
+    env, it_env = 0.0, 0
+    for block in (16, 64, 256, 1024):
+        with O.sum_order(block):
+            _, res, h, _ = O.solve(KIND[name], Ao, b, np.zeros(n), pco, max_iter=3000, rtol=1e-10, eigmin=eig[0],
+                                   eigmax=eig[1])
+        k = min(len(h), len(h_seq))
+        env = max(env, float(np.max(np.abs(h[:k] - h_seq[:k])) / h_seq[0]))
+        it_env = max(it_env, abs(res.iterations - it_seq))
+    return env, it_env
 
 
 BREAKDOWNS = [

@@ -332,3 +332,135 @@ def test_rank2_solvers_recover_x(seed, name, pk):
                            eigmin=float(ev[0]), eigmax=float(ev[-1]))
     assert res.status == 0
     assert np.max(np.abs(x - xt)) <= 1e-4
+
+
+# ------------------------------------------------------------ SSOR and ILUT
+@pytest.mark.parametrize("seed", range(12))
+@pytest.mark.parametrize("omega,reverse", [((1.0, 1.0), 1), ((1.3, 0.7), 1), ((0.5, 1.9), 0)])
+def test_ssor_apply_bitwise(seed, omega, reverse):
+    n, rp, ci, v, A, rng = _py_system(seed + 500, False)
+    pc = O.Precond(O.PC_SSOR, n)
+    assert pc.set_params(omega[0], omega[1], reverse) == O.OK
+    assert pc.set_matrix(A) == O.OK
+    dg = pyref.diag_positions(rp, ci)
+    b = list(rng.standard_normal(n))
+    x0 = list(rng.standard_normal(n))  # SSOR starts from x's content
+    want = pyref.ssor_apply(rp, ci, v, dg, b, x0, omega[0], omega[1], bool(reverse))
+    assert np.array_equal(pc.apply(b, x0), np.array(want))
+
+
+def test_ssor_rejects_bad_omega():
+    pc = O.Precond(O.PC_SSOR, 3)
+    assert pc.set_params(2.5, 1.0, 1) == O.ERR_ILLEGAL_ARGUMENT
+    assert pc.set_params(1.0, -0.1, 1) == O.ERR_ILLEGAL_ARGUMENT
+
+
+def _ilut_layout(rows, diag):
+    rp, ci, vals = [0], [], []
+    for r, d in zip(rows, diag):
+        ln = max(r.used, d + 1)
+        ci += r.index[:ln]
+        vals += r.data[:ln]
+        rp.append(len(ci))
+    return np.array(rp), np.array(ci), np.array(vals)
+
+
+@pytest.mark.parametrize("seed", range(16))
+@pytest.mark.parametrize("tau,p", [(1e-6, 25), (0.05, 1), (0.3, 0), (0.0, 3)])
+def test_ilut_factor_and_apply_bitwise(seed, tau, p):
+    n, rp, ci, v, A, rng = _py_system(seed + 700, False)
+    pc = O.Precond(O.PC_ILUT, n)
+    pc.set_params(tau, 0.0, p)
+    st = pc.set_matrix(A)
+    try:
+        rows, diag = pyref.ilut_factor(rp, ci, v, tau, p)
+    except RuntimeError:
+        assert st != O.OK
+        return
+    assert st == O.OK
+    orp, oci, odg = pc.pattern()
+    prp, pci, pvals = _ilut_layout(rows, diag)
+    assert np.array_equal(orp, prp) and np.array_equal(oci, pci) and np.array_equal(odg, np.array(diag))
+    assert np.array_equal(pc.values(), pvals)
+    b = list(rng.standard_normal(n))
+    x, _ = pyref.ilut_apply(rows, diag, b, [0.0] * n)
+    assert np.array_equal(pc.apply(b), np.array(x))
+
+
+@pytest.mark.parametrize("n", range(1, 11))
+@pytest.mark.parametrize("shape", ["tri", "penta"])
+@pytest.mark.parametrize("kind", [O.PC_ILUT, O.PC_SSOR])
+def test_ilut_ssor_on_banded(n, shape, kind):
+    # TS/ILUTTest with TS/IncompleteFactorizationTestAbstract.java:31-69: an
+    # exact solve on tri- and penta-diagonal systems (ILUT keeps every entry
+    # there); SSOR, not a factorization, must at least reduce the residual
+    Ad = tridiagonal(n) if shape == "tri" else pentadiagonal(n)
+    A = _csr(Ad)[-1]
+    pc = O.Precond(kind, n)
+    assert pc.set_matrix(A) == O.OK
+    x = np.ones(n)
+    b = Ad @ x
+    y = pc.apply(b)
+    if kind == O.PC_ILUT:
+        assert np.linalg.norm(b - Ad @ y) <= 1e-5
+    else:
+        assert np.linalg.norm(b - Ad @ y) < np.linalg.norm(b)
+
+
+@pytest.mark.parametrize("seed", range(8))
+@pytest.mark.parametrize("name", ["cg", "chebyshev", "ir"])
+@pytest.mark.parametrize("max_iter", [3, 400])
+def test_ssor_in_solvers_bitwise(seed, name, max_iter):
+    # TS/CGSSORTest, TS/ChebyshevSSORTest: M.apply(r, z) starts from the
+    # previous z (zeros at first), which the pyref closure carries along
+    n, rp, ci, v, A, rng = _py_system(seed + 900, True)
+    pc = O.Precond(O.PC_SSOR, n)
+    assert pc.set_matrix(A) == O.OK
+    dg = pyref.diag_positions(rp, ci)
+    state = [[0.0] * n]
+
+    def M(r):
+        state[0] = pyref.ssor_apply(rp, ci, v, dg, r, state[0])
+        return list(state[0])
+
+    b = list(rng.standard_normal(n))
+    x0 = list(rng.standard_normal(n))
+    mon = pyref.Monitor(max_iter, 1e-10)
+    eig = (0.0, 0.0)
+    if name == "cg":
+        xp, code, detail = _run_py(pyref.cg, rp, ci, v, b, x0, M, mon)
+    elif name == "ir":
+        xp, code, detail = _run_py(pyref.ir, rp, ci, v, b, x0, M, mon)
+    else:
+        Ad = np.zeros((n, n))
+        for i in range(n):
+            Ad[i, ci[rp[i]:rp[i + 1]]] = v[rp[i]:rp[i + 1]]
+        ev = np.linalg.eigvalsh(Ad)
+        eig = (float(ev[0]), float(ev[-1]))
+        xp, code, detail = _run_py(pyref.chebyshev, rp, ci, v, b, x0, M, mon, *eig)
+    kind = {"cg": O.CG, "chebyshev": O.CHEBYSHEV, "ir": O.IR}[name]
+    xo, res, hr, hi = O.solve(kind, A, np.array(b), np.array(x0), pc, max_iter=max_iter, rtol=1e-10,
+                              eigmin=eig[0], eigmax=eig[1])
+    assert res.status == code and res.iterations == mon.iter
+    assert np.array_equal(hr, np.array([h[0] for h in mon.hist]))
+    if code == 0:
+        assert np.array_equal(xo, np.array(xp))
+
+
+@pytest.mark.parametrize("seed", range(8))
+@pytest.mark.parametrize("name", ["bicgstab", "gmres", "bicg", "qmr"])
+def test_ilut_in_solvers_recover_x(seed, name):
+    # TS/BiCGstabILUTTest, GMRESILUTTest, QMRILUTTest, CGSILUTTest shapes
+    rng = np.random.default_rng(6000 + seed)
+    n = int(rng.integers(2, 51))
+    bw = int(rng.integers(1, min(10, n) + 1))
+    Ad = nonsingular_system(n, bw, rng)
+    n, _, rp, ci, v = dense_to_csr(Ad)
+    A = O.Csr(n, n, rp, ci, v)
+    pc = O.Precond(O.PC_ILUT, n)
+    assert pc.set_matrix(A) == O.OK
+    xt = rng.random(n)
+    kind = {"bicgstab": O.BICGSTAB, "gmres": O.GMRES, "bicg": O.BICG, "qmr": O.QMR}[name]
+    x, res, _, _ = O.solve(kind, A, Ad @ xt, rng.random(n), pc, max_iter=100000, rtol=1e-10)
+    assert res.status == 0
+    assert np.max(np.abs(x - xt)) <= 1e-4
