@@ -188,6 +188,21 @@ MTJG_API int mtjg_vector_parse_matrix_market(const char *text, int64_t len, doub
  * (S/CompRowMatrix.java:255-271): the device CSR copied to host arrays of
  * num_rows + 1 and nnz entries (any of them may be NULL). */
 MTJG_API int mtjg_csr_to_host(const mtjg_csr *A, int *rowptr, int *colind, double *val);
+/* new CompRowMatrix(A) for a CompColMatrix A (S/CompRowMatrix.java:210-243,
+ * S/CompColMatrix.java:190-215): 0-based column pointers and row indices
+ * (strictly ascending within a column), converted to the device CSR on the
+ * device.  The result is a CompRowMatrix: its products round as
+ * CompRowMatrix's do. */
+MTJG_API int mtjg_csr_upload_csc(mtjg_ctx *ctx, int num_rows, int num_cols, const int *colptr, const int *rowind,
+                                 const double *val, mtjg_csr **out);
+/* new CompRowMatrix(A) for a FlexCompRowMatrix A (S/CompRowMatrix.java:210-243,
+ * S/FlexCompRowMatrix.java): its rows' SparseVector storage in one slab of
+ * `slab` entries -- row i's indices (strictly ascending, in [0, num_cols))
+ * and values at [row_start[i], row_start[i] + row_used[i]) -- compacted into
+ * the device CSR on the device. */
+MTJG_API int mtjg_csr_upload_rows(mtjg_ctx *ctx, int num_rows, int num_cols, const int64_t *row_start,
+                                  const int *row_used, const int *index, const double *data, int64_t slab,
+                                  mtjg_csr **out);
 /* New values, same pattern (CompRowMatrix.set on the data array). */
 MTJG_API int mtjg_csr_update_values(mtjg_csr *A, const double *val);
 MTJG_API int mtjg_csr_destroy(mtjg_csr *A);

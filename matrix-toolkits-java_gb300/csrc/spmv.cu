@@ -379,6 +379,8 @@ static int csr_validate(int n, int m, const int *rowptr, const int *colind)
     return MTJG_OK;
 }
 
+static int csr_finish(mtjg_csr *A, int num_sys, const int *sys_rows);
+
 // Uploads a CSR; with sys_rows (num_sys + 1 row offsets) it is a batch of
 // independent systems whose tiles are planned system by system.
 static int csr_upload_impl(mtjg_ctx *ctx, int n, int m, const int *rowptr, const int *colind, const double *val,
@@ -431,9 +433,26 @@ static int csr_upload_impl(mtjg_ctx *ctx, int n, int m, const int *rowptr, const
         if (cudaMemcpy(A->rowptr + n + 1, pad, sizeof(pad), cudaMemcpyHostToDevice) != cudaSuccess)
             return bail(fail(MTJG_ERR_CUDA, "copying the CSR matrix to the device failed"));
     }
-    // tiles, system by system (tiles never straddle two systems); each
-    // system's lanes per row follow its own entries per row, so its tiles and
-    // its results do not depend on the rest of a batch
+    st = csr_finish(A, num_sys, sys_rows);
+    if (st != MTJG_OK) return bail(st);
+    *out = A;
+    return MTJG_OK;
+}
+
+// The tiles, reduction scratch and staging vectors of a CSR whose arrays are
+// on the device and whose row pointers are in A->h_rowptr.  Tiles are
+// planned system by system (they never straddle two systems); each system's
+// lanes per row follow its own entries per row, so its tiles and its results
+// do not depend on the rest of a batch.
+static int csr_finish(mtjg_csr *A, int num_sys, const int *sys_rows)
+{
+    const int n = A->n, m = A->m;
+    const int64_t nnz = A->nnz;
+    const int *rowptr = A->h_rowptr.data();
+    int st = MTJG_OK;
+    if (!A->d_x && (cudaMalloc(&A->d_x, sizeof(double) * (size_t)std::max(1, std::max(n, m))) != cudaSuccess ||
+                    cudaMalloc(&A->d_y, sizeof(double) * (size_t)std::max(1, std::max(n, m))) != cudaSuccess))
+        return fail(MTJG_ERR_OUT_OF_MEMORY, "cudaMalloc failed for the CSR matrix");
     const int vec = choose_vec(nnz, n);
     std::vector<int> tile_row, rtile_row, tile_sys, rtile_sys, sys_tile = {0}, rsys_tile = {0};
     std::vector<unsigned char> tile_flags, rtile_flags;
@@ -456,20 +475,48 @@ static int csr_upload_impl(mtjg_ctx *ctx, int n, int m, const int *rowptr, const
     // GPU by itself
     st = upload_tiles(A->tiles, tile_row, tile_flags, sys_rows ? &tile_sys : nullptr, sys_tile, vec, rowptr,
                       kGroupTiles, sys_rows ? kBatchGroupDiv : kGroupDiv);
-    if (st != MTJG_OK) return bail(st);
+    if (st != MTJG_OK) return st;
     st = upload_tiles(A->rtiles, rtile_row, rtile_flags, sys_rows ? &rtile_sys : nullptr, rsys_tile, 1, nullptr, 1);
-    if (st != MTJG_OK) return bail(st);
+    if (st != MTJG_OK) return st;
     const size_t nt = std::max<size_t>(1, std::max(tile_flags.size(), rtile_flags.size()));
     if (cudaMalloc(&A->part, sizeof(double) * nt * kParts) != cudaSuccess ||
         cudaMalloc(&A->cnt, sizeof(unsigned) * (size_t)std::max(4, ns)) != cudaSuccess ||
         cudaMalloc(&A->num_running, sizeof(int) * 4) != cudaSuccess)
-        return bail(fail(MTJG_ERR_OUT_OF_MEMORY, "cudaMalloc failed for reduction scratch"));
+        return fail(MTJG_ERR_OUT_OF_MEMORY, "cudaMalloc failed for reduction scratch");
     cudaMemset(A->cnt, 0, sizeof(unsigned) * (size_t)std::max(4, ns));
     cudaMemset(A->num_running, 0, sizeof(int) * 4);
     if (sys_rows) A->sys_rows.assign(sys_rows, sys_rows + num_sys + 1);
+    return MTJG_OK;
+}
+
+namespace mtjg {
+// A CSR handle over device arrays the caller hands over (rowptr with
+// kRowptrPad padding entries, colind padded with 4 entries of -1, val with 2
+// zeros), with its host row pointers.  The arrays belong to the handle from
+// the call on: a failure frees them with it.
+int csr_adopt(mtjg_ctx *ctx, int n, int m, std::vector<int> &&h_rowptr, int *d_rowptr, int *d_colind, double *d_val,
+              mtjg_csr **out)
+{
+    *out = nullptr;
+    mtjg_csr *A = new mtjg_csr();
+    A->ctx = ctx;
+    ctx_retain(ctx);
+    A->n = n;
+    A->m = m;
+    A->nnz = h_rowptr[(size_t)n];
+    A->h_rowptr = std::move(h_rowptr);
+    A->rowptr = d_rowptr;
+    A->colind = d_colind;
+    A->val = d_val;
+    const int st = csr_finish(A, 1, nullptr);
+    if (st != MTJG_OK) {
+        mtjg_csr_destroy(A);
+        return st;
+    }
     *out = A;
     return MTJG_OK;
 }
+}  // namespace mtjg
 
 extern "C" int mtjg_csr_upload(mtjg_ctx *ctx, int n, int m, const int *rowptr, const int *colind,
                                const double *val, mtjg_csr **out)

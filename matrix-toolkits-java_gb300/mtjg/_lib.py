@@ -92,6 +92,9 @@ PROTOTYPES = {
     "mtjg_vector_read_matrix_market": (C.c_int, [C.c_char_p, _dp, _i64, C.POINTER(_i64)]),
     "mtjg_vector_parse_matrix_market": (C.c_int, [C.c_char_p, _i64, _dp, _i64, C.POINTER(_i64)]),
     "mtjg_csr_to_host": (C.c_int, [_vp, _ip, _ip, _dp]),
+    "mtjg_csr_upload_csc": (C.c_int, [_vp, C.c_int, C.c_int, _ip, _ip, _dp, C.POINTER(_vp)]),
+    "mtjg_csr_upload_rows": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(_i64), _ip, _ip, _dp, _i64,
+                                       C.POINTER(_vp)]),
     "mtjg_csr_destroy": (C.c_int, [_vp]),
     "mtjg_csr_dims": (C.c_int, [_vp, _ip, _ip, C.POINTER(_i64)]),
     "mtjg_csr_mult": (C.c_int, [_vp, _dp, _dp]),

@@ -214,6 +214,58 @@ class CompRowMatrix:
         self.colind, self.data = self.colind[:nnz.value], self.data[:nnz.value]
         return self
 
+    @classmethod
+    def _adopt(cls, ctx, h):
+        self = cls.__new__(cls)
+        self.ctx = ctx
+        self._lib = ctx._lib
+        self.h = h
+        n, m, nnz = C.c_int(), C.c_int(), C.c_int64()
+        _raise(self._lib.mtjg_csr_dims(h, C.byref(n), C.byref(m), C.byref(nnz)), "dims")
+        self.n, self.m = n.value, m.value
+        self.rowptr = np.empty(self.n + 1, dtype=np.int32)
+        self.colind = np.empty(max(nnz.value, 1), dtype=np.int32)
+        self.data = np.empty(max(nnz.value, 1))
+        _raise(self._lib.mtjg_csr_to_host(h, L.iptr(self.rowptr), L.iptr(self.colind), L.dptr(self.data)), "to_host")
+        self.colind, self.data = self.colind[:nnz.value], self.data[:nnz.value]
+        return self
+
+    @classmethod
+    def fromCompColMatrix(cls, numRows, numColumns, colptr, rowind, data, ctx=None):
+        """new CompRowMatrix(CompColMatrix A) (S/CompRowMatrix.java:210-243):
+        A's CSC arrays, converted on the device (mtjg_csr_upload_csc)."""
+        ctx = ctx or default_context()
+        cp, ri, v = L.i32(colptr), L.i32(rowind), L.f64(data)
+        h = C.c_void_p()
+        _raise(ctx._lib.mtjg_csr_upload_csc(ctx.h, int(numRows), int(numColumns), L.iptr(cp), L.iptr(ri), L.dptr(v),
+                                            C.byref(h)), "upload_csc")
+        return cls._adopt(ctx, h)
+
+    @classmethod
+    def fromFlexCompRowMatrix(cls, numColumns, rows, ctx=None, slack=0):
+        """new CompRowMatrix(FlexCompRowMatrix A) (S/CompRowMatrix.java:210-243):
+        ``rows`` holds each row's SparseVector as (index, data) (sorted
+        indices); they are laid out in one slab, each row's storage `slack`
+        entries longer than its used part as a SparseVector's may be, and
+        compacted on the device (mtjg_csr_upload_rows)."""
+        ctx = ctx or default_context()
+        n = len(rows)
+        used = np.array([len(r[0]) for r in rows], dtype=np.int32)
+        start = np.zeros(n, dtype=np.int64)
+        if n:
+            start[1:] = np.cumsum(used.astype(np.int64) + slack)[:-1]
+        total = int(start[-1] + used[-1] + slack) if n else 0
+        index = np.full(max(total, 1), -7, dtype=np.int32)
+        data = np.full(max(total, 1), np.nan)
+        for i, (ix, dv) in enumerate(rows):
+            index[start[i]:start[i] + used[i]] = ix
+            data[start[i]:start[i] + used[i]] = dv
+        h = C.c_void_p()
+        _raise(ctx._lib.mtjg_csr_upload_rows(ctx.h, n, int(numColumns), start.ctypes.data_as(C.POINTER(C.c_int64)),
+                                             L.iptr(used), L.iptr(index), L.dptr(data), total, C.byref(h)),
+               "upload_rows")
+        return cls._adopt(ctx, h)
+
     def numRows(self):
         return self.n
 
