@@ -892,12 +892,22 @@ def run_batch(args):
         out[mode] = {"ms": statistics.mean(times), "solves_s": count * 1e3 / statistics.mean(times),
                      "converged": sum(1 for k in range(count) if per[k].status == 0),
                      "max_iterations": max(its), "mean_iterations": float(np.mean(its))}
+    # the lanes per row the batch autotuner chose, per system class present
+    tuned = {}
+    for k, (n_k, rp_k, _, _) in enumerate(systems):
+        lanes = C.c_int(0)
+        lib.mtjg_batch_tuning(n_k, int(rp_k[-1]), C.byref(lanes))
+        rows_band = int(np.searchsorted([2048, 8192, 32768, 131072], n_k, side="right"))
+        per_band = int(np.searchsorted([6, 12, 24, 48], rp_k[-1] / max(1, n_k), side="right"))
+        tuned[f"rows band {rows_band}, entries/row band {per_band}"] = lanes.value
     line = {"metric": "batched solves/s", "value": out["mixed"]["solves_s"], "unit": "solves/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": out["mixed"]["ms"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
             "config": {"workload": f"batched: {count} random SPD Laplacians, n log-uniform [500, 50000], CG + Jacobi, "
                                    "rtol 1e-10", "rows": nt, "nnz": int(A.rowptr[-1]), "seed": 4},
-            "fp64": out["fp64"], "mixed": out["mixed"], "mixed_vs_fp64": out["fp64"]["ms"] / out["mixed"]["ms"]}
+            "fp64": out["fp64"], "mixed": out["mixed"], "mixed_vs_fp64": out["fp64"]["ms"] / out["mixed"]["ms"],
+            "launch": "one persistent launch per solve (each CTA runs whole systems, largest first)",
+            "tuned_lanes_per_row": dict(sorted(tuned.items()))}
     print(json.dumps(line))
 
 

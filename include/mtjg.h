@@ -203,6 +203,16 @@ MTJG_API int mtjg_csr_upload_csc(mtjg_ctx *ctx, int num_rows, int num_cols, cons
 MTJG_API int mtjg_csr_upload_rows(mtjg_ctx *ctx, int num_rows, int num_cols, const int64_t *row_start,
                                   const int *row_used, const int *index, const double *data, int64_t slab,
                                   mtjg_csr **out);
+/* The lanes per row the batch autotuner chose for systems of `rows` rows and
+ * `nnz` entries (its class: bands of rows and of entries per row); 0 while
+ * no batch of that class has been solved.  A batch from mtjg_batch_upload
+ * solved by CG with the identity or Jacobi preconditioner (FP64 or mixed)
+ * runs as one persistent launch: each CTA takes whole systems, largest
+ * first, and runs their CG to the end.  On the first batch holding a class,
+ * short probe solves time each lanes-per-row candidate; the fastest is kept
+ * for the process (MTJG_TUNE=0 in the environment: the entries-per-row rule
+ * instead).  No counterpart in the reference. */
+MTJG_API int mtjg_batch_tuning(int64_t rows, int64_t nnz, int *lanes_per_row);
 /* New values, same pattern (CompRowMatrix.set on the data array). */
 MTJG_API int mtjg_csr_update_values(mtjg_csr *A, const double *val);
 MTJG_API int mtjg_csr_destroy(mtjg_csr *A);

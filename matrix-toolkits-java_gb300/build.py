@@ -23,7 +23,7 @@ OBJ = os.path.join(LIB, "_obj")
 INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["spmv.cu", "precond.cu", "solver.cu", "server.cu", "noalloc.cu", "convert.cu"]
+CU_SOURCES = ["spmv.cu", "precond.cu", "solver.cu", "server.cu", "noalloc.cu", "convert.cu", "batch.cu"]
 CPP_SOURCES = ["abi.cpp", "icc_host.cpp", "ilut_host.cpp", "mmio.cpp"]
 
 

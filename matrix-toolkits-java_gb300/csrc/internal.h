@@ -204,6 +204,7 @@ struct mtjg_csr {
     double *val = nullptr;     // device [nnz + 2]
     std::vector<int> h_rowptr; // host copy (tiling, validation)
     std::vector<int> sys_rows; // batch: first row of each system (+ end); empty for one system
+    int *d_sys_rows = nullptr; // the same on the device (persistent batched CG), made on first use
     mtjg::TileSet tiles;       // product tiles
     mtjg::TileSet rtiles;      // row-kernel tiles (kBlock rows)
     // transpose (built on first transMult): CSR of A'

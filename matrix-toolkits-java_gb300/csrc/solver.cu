@@ -11,7 +11,9 @@
 // status word between chunks.
 #include <algorithm>
 #include <cstring>
+#include <numeric>
 
+#include "batch.cuh"
 #include "krylov_ext.cuh"
 
 // resident blocks per SM the CG update is compiled for (it keeps four rows of
@@ -679,6 +681,14 @@ struct mtjg_solver {
     cudaEvent_t ev[2] = {nullptr, nullptr};
     SysState last{};
     int last_valid = 0;
+    // persistent batched CG (batch.cu): work order, lanes per row, ticket,
+    // and a copy of x kept while the autotuner probes
+    int *b_order = nullptr;
+    unsigned char *b_vec = nullptr;
+    unsigned *b_ticket = nullptr;
+    double *b_xsave = nullptr;
+    int b_cap = 0;
+    int64_t b_xcap = 0;
     int last_sys = 0;          // the system of the last solve that S->last describes
     bool last_empty = false;   // the last solve had n == 0: its history is empty_it (residuals 0)
     std::vector<int> empty_it;
@@ -1300,6 +1310,173 @@ int run(mtjg_solver *S, mtjg_csr *A, mtjg_result *res)
     return report(S, res);
 }
 
+// A batch from mtjg_batch_upload solved by CG with the identity or Jacobi
+// preconditioner runs as one persistent launch (batch.cu); other batches
+// run the tiled phases.
+bool batch_persistent(const mtjg_solver *S, const mtjg_csr *A)
+{
+    return !A->sys_rows.empty() && S->kind == MTJG_CG &&
+           (!S->M || S->M->kind == MTJG_PC_IDENTITY || S->M->kind == MTJG_PC_JACOBI);
+}
+
+int run_batch(mtjg_solver *S, mtjg_csr *A, mtjg_result *res)
+{
+    mtjg_ctx *ctx = S->ctx;
+    const int ns = (int)A->sys_rows.size() - 1;
+    int st = ensure_state(S, ns);
+    if (st != MTJG_OK) return st;
+    S->num_sys = ns;
+    SysState init;
+    std::memset(&init, 0, sizeof(init));
+    init.status = ST_RUNNING;
+    init.gate = ST_RUNNING;
+    init.rho_1 = init.rho_2 = init.alpha = init.beta = init.omega = 1.0;
+    S->last_all.assign(ns, init);
+    if (S->mixed) {
+        st = mixed_prepare(S, A);
+        if (st != MTJG_OK) return st;
+    }
+    if (ns > S->b_cap) {
+        cudaFree(S->b_order);
+        cudaFree(S->b_vec);
+        S->b_order = nullptr;
+        S->b_vec = nullptr;
+        S->b_cap = 0;
+        MTJG_CUDA(cudaMalloc(&S->b_order, sizeof(int) * (size_t)ns));
+        MTJG_CUDA(cudaMalloc(&S->b_vec, (size_t)ns));
+        S->b_cap = ns;
+    }
+    if (!S->b_ticket) MTJG_CUDA(cudaMalloc(&S->b_ticket, sizeof(unsigned)));
+    const int *srow = A->sys_rows.data();
+    const int *hrp = A->h_rowptr.data();
+    // the systems' row offsets on the device, uploaded once per matrix
+    if (!A->d_sys_rows) {
+        MTJG_CUDA(cudaMalloc(&A->d_sys_rows, sizeof(int) * (size_t)(ns + 1)));
+        MTJG_CUDA(cudaMemcpy(A->d_sys_rows, srow, sizeof(int) * (size_t)(ns + 1), cudaMemcpyHostToDevice));
+    }
+    BatchCg a{};
+    a.rowptr = A->rowptr;
+    a.colind = A->colind;
+    a.val = A->val;
+    a.val32 = A->val32;
+    a.sys_rows = A->d_sys_rows;
+    a.order = S->b_order;
+    a.vec = S->b_vec;
+    a.ticket = S->b_ticket;
+    a.pc = pc_mode(S);
+    a.invdiag = S->M && S->M->kind == MTJG_PC_JACOBI ? S->M->invdiag : nullptr;
+    a.invdiag32 = S->invdiag32;
+    a.b = S->vecs[V_B];
+    a.x = S->vecs[V_X];
+    a.r = S->vecs[V_R];
+    a.z = S->vecs[V_Z];
+    a.p = S->vecs[V_P];
+    a.q = S->vecs[V_Q];
+    if (S->mixed) {
+        a.d32 = S->v32[0];
+        a.r32 = S->v32[1];
+        a.z32 = S->v32[2];
+        a.p32 = S->v32[3];
+        a.q32 = S->v32[4];
+    }
+    a.st = S->st;
+    a.mon = mon_dev(S);
+    a.hist_r = S->hist_r;
+    a.hist_it = S->hist_it;
+    a.mix = S->mix;
+    a.mix.rtol = S->mon.rtol;
+    a.mix.atol = S->mon.atol;
+    auto upload_states = [&]() {
+        return cudaMemcpyAsync(S->st, S->last_all.data(), sizeof(SysState) * (size_t)ns, cudaMemcpyHostToDevice,
+                               ctx->stream);
+    };
+    auto go = [&](const BatchCg &args, const std::vector<int> &order) -> cudaError_t {
+        cudaError_t e = cudaMemcpyAsync(S->b_order, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice,
+                                        ctx->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(S->b_ticket, 0, sizeof(unsigned), ctx->stream);
+        if (e == cudaSuccess) e = batch_launch(ctx, args, S->mixed);
+        return e;
+    };
+    // lanes per row: STRICT sums every row in entry order (one lane)
+    std::vector<unsigned char> vec;
+    if (ctx->numerics == MTJG_NUMERICS_STRICT) {
+        vec.assign((size_t)ns, 1);
+    } else {
+        const int64_t n = A->n;
+        bool saved = false;
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        auto probe = [&](const std::vector<int> &pick, int lanes, int iters) -> double {
+            if (!saved) {
+                if (n > S->b_xcap) {
+                    cudaFree(S->b_xsave);
+                    S->b_xsave = nullptr;
+                    S->b_xcap = 0;
+                    if (cudaMalloc(&S->b_xsave, sizeof(double) * (size_t)std::max<int64_t>(1, n)) != cudaSuccess)
+                        return -1;
+                    S->b_xcap = n;
+                }
+                if (cudaMemcpyAsync(S->b_xsave, S->vecs[V_X], sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice,
+                                    ctx->stream) != cudaSuccess ||
+                    cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+                    return -1;
+                saved = true;
+            }
+            std::vector<unsigned char> all((size_t)ns, (unsigned char)lanes);
+            BatchCg pa = a;
+            pa.count = (int)pick.size();
+            pa.mon.hist_cap = 0;
+            if (S->mixed) {
+                pa.mon.max_iter = 1;
+                pa.mix.in_max = iters;
+            } else {
+                pa.mon.max_iter = iters;
+            }
+            if (upload_states() != cudaSuccess ||
+                cudaMemcpyAsync(S->b_vec, all.data(), all.size(), cudaMemcpyHostToDevice, ctx->stream) !=
+                    cudaSuccess ||
+                cudaEventRecord(e0, ctx->stream) != cudaSuccess || go(pa, pick) != cudaSuccess ||
+                cudaEventRecord(e1, ctx->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess)
+                return -1;
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            return ms;
+        };
+        st = batch_vec(ns, srow, hrp, vec, probe);
+        if (saved) {
+            cudaMemcpyAsync(S->vecs[V_X], S->b_xsave, sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice,
+                            ctx->stream);
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+        }
+        if (st != MTJG_OK) return fail(st, "batch autotuner probe failed");
+    }
+    // work order: largest systems first (longest-processing-time first)
+    std::vector<int> order((size_t)ns);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        return (int64_t)hrp[srow[x + 1]] - hrp[srow[x]] > (int64_t)hrp[srow[y + 1]] - hrp[srow[y]];
+    });
+    a.count = ns;
+    MTJG_CUDA(cudaMemcpyAsync(S->b_vec, vec.data(), vec.size(), cudaMemcpyHostToDevice, ctx->stream));
+    MTJG_CUDA(upload_states());
+    MTJG_CUDA(cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream));
+    MTJG_CUDA(go(a, order));
+    MTJG_CUDA(cudaMemcpyAsync(S->last_all.data(), S->st, sizeof(SysState) * (size_t)ns, cudaMemcpyDeviceToHost,
+                              ctx->stream));
+    MTJG_CUDA(cudaStreamSynchronize(ctx->stream));
+    S->last = S->last_all[0];
+    S->last_valid = 1;
+    S->last_empty = false;
+    S->last_sys = 0;
+    for (size_t i = 0; i < S->last_all.size(); ++i)
+        if (S->last_all[i].status != ST_DONE) {
+            S->last = S->last_all[i];
+            S->last_sys = (int)i;
+            break;
+        }
+    return report(S, res);
+}
+
 // n == 0: every vector is empty and every norm 0, so the monitor sees r = 0
 // at every test (DefaultIterationMonitor.convergedI,
 // S/DefaultIterationMonitor.java:133-155): it converges at the first test iff
@@ -1442,6 +1619,10 @@ extern "C" int mtjg_solver_destroy(mtjg_solver *S)
     cudaFree(S->st);
     cudaFree(S->hist_r);
     cudaFree(S->hist_it);
+    cudaFree(S->b_order);
+    cudaFree(S->b_vec);
+    cudaFree(S->b_ticket);
+    cudaFree(S->b_xsave);
     if (S->ev[0]) cudaEventDestroy(S->ev[0]);
     if (S->ev[1]) cudaEventDestroy(S->ev[1]);
     mtjg_ctx *ctx = S->ctx;
@@ -1547,7 +1728,7 @@ extern "C" int mtjg_solver_solve(mtjg_solver *S, mtjg_csr *A, const double *b, d
     const size_t nb = sizeof(double) * (size_t)S->n;
     MTJG_CUDA(cudaMemcpyAsync(S->vecs[V_B], b, nb, cudaMemcpyHostToDevice, ctx->stream));
     MTJG_CUDA(cudaMemcpyAsync(S->vecs[V_X], x, nb, cudaMemcpyHostToDevice, ctx->stream));
-    st = run(S, A, res);
+    st = batch_persistent(S, A) ? run_batch(S, A, res) : run(S, A, res);
     if (st == MTJG_ERR_CUDA || st == MTJG_ERR_OUT_OF_MEMORY || st == MTJG_ERR_DEVICE_TIMEOUT) return st;
     MTJG_CUDA(cudaMemcpyAsync(x, S->vecs[V_X], nb, cudaMemcpyDeviceToHost, ctx->stream));
     MTJG_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -1566,7 +1747,7 @@ extern "C" int mtjg_solver_solve_dev(mtjg_solver *S, mtjg_csr *A, const double *
     const size_t nb = sizeof(double) * (size_t)S->n;
     MTJG_CUDA(cudaMemcpyAsync(S->vecs[V_B], db, nb, cudaMemcpyDeviceToDevice, ctx->stream));
     MTJG_CUDA(cudaMemcpyAsync(S->vecs[V_X], dx, nb, cudaMemcpyDeviceToDevice, ctx->stream));
-    st = run(S, A, res);
+    st = batch_persistent(S, A) ? run_batch(S, A, res) : run(S, A, res);
     if (st == MTJG_ERR_CUDA || st == MTJG_ERR_OUT_OF_MEMORY || st == MTJG_ERR_DEVICE_TIMEOUT) return st;
     MTJG_CUDA(cudaMemcpyAsync(dx, S->vecs[V_X], nb, cudaMemcpyDeviceToDevice, ctx->stream));
     MTJG_CUDA(cudaStreamSynchronize(ctx->stream));

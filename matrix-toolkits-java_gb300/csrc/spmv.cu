@@ -565,6 +565,7 @@ extern "C" int mtjg_csr_destroy(mtjg_csr *A)
     cudaFree(A->t_colind);
     cudaFree(A->t_val);
     cudaFree(A->t_part);
+    cudaFree(A->d_sys_rows);
     cudaFree(A->val32);
     cudaFree(A->part);
     cudaFree(A->cnt);

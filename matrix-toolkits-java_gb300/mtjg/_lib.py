@@ -138,6 +138,7 @@ PROTOTYPES = {
     "mtjg_server_context": (C.c_int, [_vp, C.POINTER(_vp)]),
     "mtjg_server_destroy": (C.c_int, [_vp]),
     "mtjg_solver_batch_results": (C.c_int, [_vp, C.POINTER(Result), C.c_int]),
+    "mtjg_batch_tuning": (C.c_int, [_i64, _i64, _ip]),
     "mtjg_solver_batch_history": (C.c_int, [_vp, C.c_int, _dp, _ip, C.c_int, _ip]),
 }
 

@@ -158,3 +158,28 @@ def test_batch_rejects_coupled_systems(ctx):
     sys_rows = np.array([0, 1, 2], dtype=np.int32)
     code = lib.mtjg_batch_upload(ctx.h, 2, L.iptr(sys_rows), L.iptr(rp), L.iptr(ci), L.dptr(v), C.byref(h))
     assert code == L.ERR_ILLEGAL_ARGUMENT
+
+
+def test_autotuner_records_a_choice_per_class(ctx):
+    # the persistent batched CG tunes lanes per row per system class on the
+    # first batch holding the class; the choice is one of the candidates and
+    # stays fixed for the process, so a second solve is bit-identical
+    import ctypes as C
+    systems = [workloads.laplacian(3000 + 500 * k, 70 + k) for k in range(5)]
+    A = sparse.BatchCompRowMatrix(systems, ctx)
+    s = sparse.CG(A.numRows(), ctx=ctx)
+    M = sparse.DiagonalPreconditioner(A.numRows(), ctx)
+    M.setMatrix(A)
+    s.setPreconditioner(M)
+    s.setIterationMonitor(sparse.DefaultIterationMonitor(500, 1e-10, 1e-50, 1e5))
+    b = np.concatenate(_rhs(systems))
+    x1 = np.zeros(A.numRows())
+    out1 = s.solveBatch(A, b, x1)
+    lanes = C.c_int(-1)
+    n, rp, ci, v = systems[0]
+    assert ctx._lib.mtjg_batch_tuning(n, int(rp[-1]), C.byref(lanes)) == 0
+    assert lanes.value in (1, 2, 4, 8, 32)
+    x2 = np.zeros(A.numRows())
+    out2 = s.solveBatch(A, b, x2)
+    assert out1 == out2 and np.array_equal(x1, x2)
+    assert all(st == 0 for st, _, _ in out1)

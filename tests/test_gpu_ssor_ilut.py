@@ -173,7 +173,18 @@ def test_solvers_with_ssor_ilut_match_oracle(ctx, numerics, case):
     assert np.array_equal(gi[:k], hi[:k])
     # a history that diverges is compared up to the oracle's divergence test
     fin = np.isfinite(gr[:k]) & np.isfinite(hr[:k]) & (hr[:k] < 1e3 * hr[0])
-    assert float(np.max(np.abs(gr[:k][fin] - hr[:k][fin])) / hr[0]) <= 1e-10
+    bar = 1e-10
+    if name == "qmr":
+        # QMR's history moves by more than that under a mere change of the
+        # order of the oracle's own dot products: four times that envelope
+        for block in (16, 64, 256, 1024):
+            Mb = O.Precond(pk, n)
+            Mb.set_matrix(Ao)
+            with O.sum_order(block):
+                _, _, hb, _ = O.solve(KIND[name], Ao, b, np.zeros(n), Mb, max_iter=max_iter, rtol=1e-10)
+            kb = min(len(hb), len(hr))
+            bar = max(bar, 4 * float(np.max(np.abs(hb[:kb] - hr[:kb])) / hr[0]))
+    assert float(np.max(np.abs(gr[:k][fin] - hr[:k][fin])) / hr[0]) <= bar
     if res.status == 0:
         assert np.max(np.abs(x - xo)) <= 1e-8 * max(1.0, np.max(np.abs(xo)))
 
