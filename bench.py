@@ -14,15 +14,18 @@ One step = serving the whole stream (1500 requests, 437 matrices).
   e2e       the same stream through the host API as it arrives: matrices
             registered on first use, each request submitted at its arrival
             time; solves/s and p50/p99 latency (arrival -> x on the host)
+  latency   p50/p99 at the stream's rate (above capacity), at a rate below
+            capacity (300 requests/s), and at that rate with the resident
+            matrices held to a 1.5 GiB budget (the stream's take about 6):
+            idle matrices evicted least recently used, uploaded again on use
   plain_fp64  the plain FP64 drop-in (CG + DiagonalPreconditioner, one
             request at a time through the host API) on the same stream
   roofline  the CSR product kernel (CompRowMatrix.mult) on 3D 7-point Poisson
             128^3: algorithmic bytes 12*nnz + 4*(n+1) + 16*n per launch over
             its CUDA-event duration, against the measured HBM peak
   poisson3d_128  plain FP64 CG + Jacobi solves/s on that 3D Poisson system
-  cpu_baseline  the oracle's FP64 CG + Jacobi on one host core on a bounded
-            sample of the stream (8 iterations per request, scaled by the
-            request's iteration count)
+  cpu_baseline  the oracle's FP64 CG + Jacobi on one host core: full solves
+            of the stream's first requests for about 20 s
 
 ``--workload poisson3d`` makes the 3D Poisson CG solve the headline instead.
 ``--impl reference`` times the reference's CPU path (the oracle restatement
@@ -416,14 +419,18 @@ def serve_backlog(ctx, mats, reqs, steps, warmup, max_systems, pool_rows, inner_
     return times, results, rhs, stats, launches
 
 
-def serve_open_loop(ctx, mats, reqs, max_systems, pool_rows, inner_rtol):
+def serve_open_loop(ctx, mats, reqs, max_systems, pool_rows, inner_rtol, rate=SERVE_RATE, budget=0):
     """The arrival stream end to end through the public API: a new matrix
     is registered when its first request arrives, each request is submitted
     at its arrival time (or as soon as the client is free), and latency runs
-    from the scheduled arrival to the result being on the host."""
+    from the scheduled arrival to the result being on the host.  `rate`
+    rescales the stream's arrival times to that mean rate; `budget` is the
+    server's matrix budget in bytes (0: every matrix stays resident)."""
     from mtjg import serve
     srv = serve.Server(ctx, max_systems=max_systems, pool_rows=pool_rows, max_iter=100, rtol=RTOL,
-                       inner_rtol=inner_rtol)
+                       inner_rtol=inner_rtol, matrix_budget=budget)
+    scale = SERVE_RATE / rate
+    reqs = [(ta * scale, m, s, new) for ta, m, s, new in reqs]
     rhs = [_rhs(mats[m][0], s) for _, m, s, _ in reqs]
     ids = {}
     arrival_of, lat = {}, []
@@ -450,10 +457,13 @@ def serve_open_loop(ctx, mats, reqs, max_systems, pool_rows, inner_rtol):
         collect()
         time.sleep(0.0002)
     wall = time.perf_counter() - t0
+    res = srv.residency()
     srv.close()
     lat = np.array(lat)
     return {"wall_s": wall, "solves_s": len(reqs) / wall, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
-            "p99_ms": 1e3 * float(np.percentile(lat, 99)), "h2d_bytes": h2d, "d2h_bytes": d2h}
+            "p99_ms": 1e3 * float(np.percentile(lat, 99)), "h2d_bytes": h2d, "d2h_bytes": d2h,
+            "offered_rate": rate, "uploads": res["uploads"], "evictions": res["evictions"],
+            "matrix_budget": budget}
 
 
 def plain_fp64(ctx, mats, reqs, budget_s):
@@ -486,24 +496,6 @@ def plain_fp64(ctx, mats, reqs, budget_s):
     return out
 
 
-def _oracle_iter_time(args):
-    """Seconds per oracle CG + Jacobi iteration on one request (a capped run)."""
-    spec, seed, iters = args
-    sys.path.insert(0, ORACLE_DIR)
-    sys.path.insert(0, PKG)
-    import oracle as O
-    from mtjg import workloads
-    kind, n, s = spec
-    n, rp, ci, v = workloads.poisson2d(n) if kind == "poisson2d" else workloads.laplacian(n, s)
-    A = O.Csr(n, n, rp, ci, v)
-    pc = O.Precond(O.PC_JACOBI, n)
-    pc.set_matrix(A)
-    b = workloads.uniform(n, seed)
-    t0 = time.perf_counter()
-    _, res, _, _ = O.solve(O.CG, A, b, np.zeros(n), pc, max_iter=iters, rtol=RTOL, hist_cap=0)
-    return (time.perf_counter() - t0) / max(1, res.iterations)
-
-
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -526,8 +518,15 @@ def main():
     ap.add_argument("--serve-max-systems", type=int, default=512)
     ap.add_argument("--serve-pool-rows", type=int, default=1 << 26)
     ap.add_argument("--inner-rtol", type=float, default=1e-6)
+    ap.add_argument("--serve-low-rate", type=float, default=300.0,
+                    help="offered load (requests/s) of the below-capacity latency run")
+    ap.add_argument("--serve-matrix-budget", type=float, default=1.5,
+                    help="GiB of resident matrices in the budgeted run (the stream's matrices take about 6)")
     ap.add_argument("--plain-budget", type=float, default=8.0, help="seconds of plain FP64 one-at-a-time solves")
     ap.add_argument("--ref-seconds", type=float, default=6.0, help="reference arm: seconds of work per step")
+    ap.add_argument("--ref-prepare", type=int, default=40,
+                    help="reference arm: requests each process prepares (matrices built before the clock)")
+    ap.add_argument("--cpu-seconds", type=float, default=20.0, help="cpu_baseline: seconds of oracle solves")
     args = ap.parse_args()
     if args.only_spmv:
         print(json.dumps(spmv_only(args)))
@@ -610,23 +609,20 @@ def main_poisson3d(args):
     print(json.dumps(line))
 
 
-def _ref_worker(args):
-    """Reference arm worker: the oracle's FP64 CG + Jacobi (MTJ's CPU path,
-    restated) on requests w, w + P, ... of the stream until `seconds` have
-    passed; the request in progress at the deadline is finished and counted."""
-    w, procs, count, seconds = args
+def _oracle_requests(specs, reqs, ks, seconds, limit=None):
+    """The oracle's FP64 CG + Jacobi (MTJ's CPU path, restated) on requests
+    ks of the stream, in order, until `seconds` of solving have passed (the
+    request in progress at the deadline is finished and counted).  Matrices
+    and their Jacobi diagonals are built before the clock starts, as the
+    served `value` registers its matrices first.  Returns (solved, seconds)."""
     sys.path.insert(0, ORACLE_DIR)
     sys.path.insert(0, PKG)
     import oracle as O
     from mtjg import workloads
-    specs, reqs = serve_stream(count)
+    ks = list(ks)[:limit] if limit else list(ks)
     cache = {}
-    done = 0
-    t0 = time.perf_counter()
-    for k in range(w, len(reqs), procs):
-        if time.perf_counter() - t0 > seconds:
-            break
-        _, m, s, _ = reqs[k]
+    for k in ks:
+        m = reqs[k][1]
         if m not in cache:
             kind, n, ms = specs[m]
             n, rp, ci, v = workloads.poisson2d(n) if kind == "poisson2d" else workloads.laplacian(n, ms)
@@ -634,11 +630,24 @@ def _ref_worker(args):
             pc = O.Precond(O.PC_JACOBI, n)
             pc.set_matrix(A)
             cache[m] = (n, A, pc)
-        n, A, pc = cache[m]
-        _, res, _, _ = O.solve(O.CG, A, workloads.uniform(n, s), np.zeros(n), pc, max_iter=100000, rtol=RTOL,
-                               hist_cap=0)
+    rhs = {k: workloads.uniform(cache[reqs[k][1]][0], reqs[k][2]) for k in ks}
+    done = 0
+    t0 = time.perf_counter()
+    for k in ks:
+        if time.perf_counter() - t0 > seconds:
+            break
+        n, A, pc = cache[reqs[k][1]]
+        O.solve(O.CG, A, rhs[k], np.zeros(n), pc, max_iter=100000, rtol=RTOL, hist_cap=0)
         done += 1
     return done, time.perf_counter() - t0
+
+
+def _ref_worker(args):
+    """Reference arm worker: requests w, w + P, ... of the stream (at most
+    `cap` of them prepared) for `seconds` of solving."""
+    w, procs, count, seconds, cap = args
+    specs, reqs = serve_stream(count)
+    return _oracle_requests(specs, reqs, range(w, len(reqs), procs), seconds, cap)
 
 
 def _serve_config(args, nmat):
@@ -662,7 +671,8 @@ def reference_serve(args):
     vals = []
     with ctx.Pool(procs) as pool:
         for _ in range(args.warmup + args.steps):
-            out = pool.map(_ref_worker, [(w, procs, args.serve_requests, args.ref_seconds) for w in range(procs)])
+            out = pool.map(_ref_worker, [(w, procs, args.serve_requests, args.ref_seconds, args.ref_prepare)
+                                         for w in range(procs)])
             vals.append(sum(d for d, _ in out) / max(t for _, t in out))
     val = statistics.median(vals[args.warmup:])
     specs, _ = serve_stream(args.serve_requests)
@@ -671,8 +681,9 @@ def reference_serve(args):
             "ms_per_step": 1e3 * args.ref_seconds, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": _serve_config(args, len(specs)),
             "cpu_baseline": {"value": val, "unit": "solves/s", "cores": procs, "kind": "port",
-                             "sample": f"{procs} processes, each solving the stream's requests in order (FP64 "
-                                       f"CG + Jacobi to rtol 1e-10) for {args.ref_seconds:.0f} s per step"},
+                             "sample": f"{procs} processes, each solving every {procs}th request of the stream in "
+                                       f"order (FP64 CG + Jacobi to rtol 1e-10, matrices built before the clock "
+                                       f"starts) for {args.ref_seconds:.0f} s per step"},
             "e2e": {"value": val, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -715,6 +726,10 @@ def main_serve(args):
     row_it = sum(float(mats[m][0]) * inner[k] for k, (_, m, _, _) in enumerate(reqs))
     nnz_it = sum(float(len(mats[m][2])) * inner[k] for k, (_, m, _, _) in enumerate(reqs))
     open_loop = serve_open_loop(ctx, mats, reqs, *knobs)
+    low = serve_open_loop(ctx, mats, reqs, *knobs, rate=args.serve_low_rate)
+    budget = int(args.serve_matrix_budget * (1 << 30))
+    tight = serve_open_loop(ctx, mats, reqs, *knobs, rate=args.serve_low_rate, budget=budget)
+    stream_bytes = sum(16 * len(mats[m][2]) + 8 * mats[m][0] for m in {m for _, m, _, _ in reqs})
     plain = plain_fp64(ctx, mats, reqs, args.plain_budget)
     sec = statistics.mean(times)
     value_rank = len(reqs) / sec
@@ -729,16 +744,11 @@ def main_serve(args):
     e2e = sum(o["e2e"] for o in objs)
     cpu = None
     if not args.no_cpu:
-        # the oracle on 1 core: per-iteration time of each of the first sampled
-        # requests (a capped run) times that request's FP64 iteration count
-        sample = plain[:40]
-        t_cpu = 0.0
-        for k, _, it in sample:
-            _, m, s, _ = reqs[k]
-            t_cpu += _oracle_iter_time((specs[m], s, 8)) * it
-        cpu = {"value": len(sample) / t_cpu, "unit": "solves/s", "cores": 1, "kind": "port",
-               "sample": f"oracle FP64 CG + Jacobi on the stream's first {len(sample)} requests: 8 iterations "
-                         f"each, timed, times the request's FP64 iteration count on the GPU"}
+        # the oracle on 1 core: full solves of the stream's first requests
+        done, t_cpu = _oracle_requests(specs, reqs, range(len(reqs)), args.cpu_seconds, 80)
+        cpu = {"value": done / t_cpu, "unit": "solves/s", "cores": 1, "kind": "port",
+               "sample": f"oracle FP64 CG + Jacobi, full solves to rtol 1e-10 of the stream's first {done} "
+                         f"requests in order ({t_cpu:.1f} s; matrices built before the clock starts)"}
     o0 = c2
     line = {
         "metric": "served solves/s", "value": value, "unit": "solves/s", "n_gpus": args.gpus,
@@ -753,8 +763,15 @@ def main_serve(args):
                    "inner_bytes": "8 per entry (FP32 value + column) + 56 per row (FP32 vectors) per inner iteration",
                    "scheduler_s": {k: stats[k] for k in ("gpu_s", "host_s", "wait_s")},
                    "mean_admitted_rows": stats["mean_rows"], "chunks": stats["chunks"]},
-        "latency": {"p50_ms": open_loop["p50_ms"], "p99_ms": open_loop["p99_ms"], "arrival_rate": SERVE_RATE,
-                    "solves_s": open_loop["solves_s"]},
+        "latency": {
+            "p50_ms": open_loop["p50_ms"], "p99_ms": open_loop["p99_ms"], "arrival_rate": SERVE_RATE,
+            "solves_s": open_loop["solves_s"],
+            "below_capacity": {k: low[k] for k in ("offered_rate", "p50_ms", "p99_ms", "solves_s")},
+            "matrix_budget": {**{k: tight[k] for k in ("offered_rate", "p50_ms", "p99_ms", "solves_s", "uploads",
+                                                      "evictions")},
+                              "budget_bytes": budget, "stream_matrix_bytes": stream_bytes,
+                              "what": "below-capacity load with resident matrices held to the budget: idle "
+                                      "matrices evicted LRU and uploaded again on their next request"}},
         "plain_fp64": {"solves_s": plain_rate, "requests": len(plain),
                        "mean_iterations": float(np.mean([it for _, _, it in plain])),
                        "what": "CG + DiagonalPreconditioner FP64, one request at a time through the host API"},

@@ -347,16 +347,22 @@ MTJG_API int mtjg_solver_destroy(mtjg_solver *S);
 /* ---- Serving ------------------------------------------------------------
  * A continuous-batching solve server.  No counterpart in the reference,
  * which solves one system per IterativeSolver.solve call.  Matrices are
- * registered once and stay resident (CSR, FP32 values, Jacobi diagonal).
- * Requests (matrix, b, x0) queue on the host; a scheduler thread admits each
- * into a free slot as soon as a slot and a segment of the pooled vector
- * workspace are free (admission by device-memory footprint: 40 bytes per row),
- * runs a chunk of mixed-precision CG + Jacobi iterations over every admitted
- * system at once, and retires finished systems between chunks, so requests
- * that arrive while others are on the GPU join the running batch.  A
- * system's result does not depend on the other systems in flight.  The
- * server runs on a context and stream of its own, on ctx's device; ctx stays
- * free for other work.  mtjg_server_destroy abandons unfinished requests.   */
+ * registered once; a resident matrix holds its CSR with FP64 and FP32 values
+ * and its Jacobi diagonal (about 16 bytes per entry + 8 per row).  Requests
+ * (matrix, b, x0) queue on the host; a scheduler thread admits each into a
+ * free slot as soon as a slot, a segment of the pooled vector workspace (40
+ * bytes per row) and room for its matrix are free (admission by device-memory
+ * footprint), runs a chunk of mixed-precision CG + Jacobi iterations over
+ * every admitted system at once, and retires finished systems between chunks,
+ * so requests that arrive while others are on the GPU join the running batch.
+ * With matrix_budget > 0 the resident matrices stay within that many bytes:
+ * each keeps a host copy, is uploaded when first needed, and idle ones (no
+ * system in flight) are evicted least recently used and uploaded again on
+ * their next request; a request whose matrix cannot get room waits at the
+ * head of the queue.  A system's result does not depend on the other systems
+ * in flight nor on evictions.  The server runs on a context and stream of its
+ * own, on ctx's device; ctx stays free for other work.  mtjg_server_destroy
+ * abandons unfinished requests.                                              */
 typedef struct mtjg_server mtjg_server;
 
 typedef struct mtjg_server_config {
@@ -366,6 +372,7 @@ typedef struct mtjg_server_config {
     double rtol, atol, dtol;
     double inner_rtol;     /* FP32 inner CG: residual decrease per refinement step */
     int inner_max_iter;
+    int64_t matrix_budget; /* device bytes for resident matrices; 0: no limit, no eviction */
 } mtjg_server_config;
 
 typedef struct mtjg_server_result {
@@ -378,8 +385,10 @@ typedef struct mtjg_server_result {
 
 MTJG_API void mtjg_server_config_defaults(mtjg_server_config *cfg);
 MTJG_API int mtjg_server_create(mtjg_ctx *ctx, const mtjg_server_config *cfg, mtjg_server **out);
-/* Registers a resident SPD matrix (0-based CSR, sorted columns, with a
- * nonzero diagonal); *matrix_id identifies it in submissions. */
+/* Registers an SPD matrix (0-based CSR, sorted columns, with a nonzero
+ * diagonal); *matrix_id identifies it in submissions.  It is uploaded now if
+ * it fits the matrix budget without evicting, else on its first request; a
+ * matrix larger than the whole budget is refused (MTJG_ERR_ILLEGAL_ARGUMENT). */
 MTJG_API int mtjg_server_add_matrix(mtjg_server *S, int n, const int *rowptr, const int *colind,
                                     const double *val, int *matrix_id);
 /* Releases a registered matrix: new submissions naming it fail at once;
@@ -400,6 +409,10 @@ MTJG_API int mtjg_server_drain(mtjg_server *S, double timeout_s);
  * the server's clock (seconds since creation). */
 MTJG_API int mtjg_server_stats(mtjg_server *S, int64_t *chunks, int64_t *admitted, int64_t *max_active,
                                double *clock_s);
+/* Bytes and number of the matrices resident (or being uploaded), uploads so
+ * far (registrations included) and evictions. */
+MTJG_API int mtjg_server_residency(mtjg_server *S, int64_t *resident_bytes, int64_t *resident_matrices,
+                                   int64_t *uploads, int64_t *evictions);
 /* Where the scheduler's time went: GPU time of the chunks (CUDA events),
  * host time spent retiring, admitting and queueing, host time waiting for a
  * chunk, and the mean number of admitted rows per chunk. */

@@ -17,6 +17,10 @@ void set_error(const std::string &msg);
 int fail(int code, const std::string &msg);
 int cuda_fail(cudaError_t e, const char *what);
 
+// Checks a host CSR (0-based, sorted columns in range), as CompRowMatrix's
+// constructor does; MTJG_ERR_ILLEGAL_ARGUMENT names the offending entry.
+int csr_validate(int n, int m, const int *rowptr, const int *colind);
+
 }  // namespace mtjg
 struct mtjg_ctx;
 namespace mtjg {

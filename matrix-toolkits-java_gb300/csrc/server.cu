@@ -1,12 +1,21 @@
 // server.cu -- continuous-batching solve server.
 //
-// Matrices are registered once and stay resident on the device (CSR, FP32
-// values, Jacobi inverse diagonals).  Requests (matrix, b, x0) queue on the
-// host; a scheduler thread admits them into free slots whenever a slot and
-// a contiguous segment of the pooled vector workspace are free (admission
-// by HBM footprint), runs chunks of the mixed-precision CG phases over all
-// admitted systems at once, and retires finished systems between chunks, so
-// requests that arrive while others are on the GPU join the running batch.
+// Matrices are registered once; a resident matrix holds its CSR (FP64 and
+// FP32 values) and its Jacobi inverse diagonal in one device allocation.
+// Requests (matrix, b, x0) queue on the host; a scheduler thread admits them
+// into free slots whenever a slot and a contiguous segment of the pooled
+// vector workspace are free and the request's matrix is resident (admission
+// by device-memory footprint), runs chunks of the mixed-precision CG phases
+// over all admitted systems at once, and retires finished systems between
+// chunks, so requests that arrive while others are on the GPU join the
+// running batch.
+//
+// With a matrix budget, the resident matrices' bytes stay within it: each
+// matrix keeps a host copy, is uploaded when a request first needs it, and
+// idle matrices (no system admitted) are evicted least recently used to make
+// room, to be uploaded again on their next request.  A request whose matrix
+// cannot be made resident (the budget is held by matrices in use) waits at
+// the head of the queue.
 //
 // The scheduler keeps two chunks queued on its stream: while the GPU runs
 // chunk k+1, the host reads chunk k's statuses, retires finished systems,
@@ -51,29 +60,117 @@ struct ProdTiles {
     }
 };
 
+// Byte offsets of a served matrix's arrays in its one device allocation
+// (each array starts on a 256-byte boundary).  The padding matches
+// mtjg_csr_upload's: rowptr[n] repeated kRowptrPad times, colind padded with
+// -1, the values with zeros, so the product kernels' bulk copies stay inside.
+struct MatLayout {
+    size_t rowptr = 0, colind = 0, val = 0, val32 = 0, invdiag32 = 0, bytes = 0;
+    MatLayout(int n, int64_t nnz)
+    {
+        auto take = [&](size_t b) {
+            const size_t o = bytes;
+            bytes = (bytes + b + 255) & ~(size_t)255;
+            return o;
+        };
+        rowptr = take(sizeof(int) * ((size_t)n + 1 + kRowptrPad));
+        colind = take(sizeof(int) * (size_t)(nnz + 4));
+        val = take(sizeof(double) * (size_t)(nnz + 2));
+        val32 = take(sizeof(float) * (size_t)(nnz + 4));
+        invdiag32 = take(sizeof(float) * (size_t)std::max(1, n));
+    }
+};
+
+// The device copy of a served matrix: what the chunk kernels read.
+struct DevMat {
+    void *base = nullptr;
+    int *rowptr = nullptr, *colind = nullptr;
+    double *val = nullptr;
+    float *val32 = nullptr, *invdiag32 = nullptr;
+    void release()
+    {
+        cudaFree(base);  // waits for the device
+        *this = DevMat();
+    }
+};
+
 struct ResMat {
     int n = 0;
     int64_t nnz = 0;
-    mtjg_csr *A = nullptr;          // resident CSR (rows 0..n-1), FP32 values in A->val32
-    mtjg_precond *J = nullptr;      // Jacobi (its invdiag)
-    float *invdiag32 = nullptr;
+    int64_t bytes = 0;                 // device bytes while resident
+    DevMat dev;                        // set while resident
+    std::vector<float> inv32;          // Jacobi inverse diagonal, FP32 (host)
+    std::vector<int> h_rowptr, h_colind;  // host copy for uploads after an eviction
+    std::vector<double> h_val;            // (kept only by servers with a matrix budget)
     ProdTiles t64, t32;  // product tiles for FP64 and FP32 values (local rows and entries)
-    int uses = 0;          // requests submitted and not yet delivered (under the server lock)
-    bool removed = false;  // mtjg_server_remove_matrix: freed once uses reaches 0
+    bool resident = false;  // dev holds the matrix
+    bool loading = false;   // picked for upload by the scheduler, not yet attached
+    int busy = 0;           // systems admitted and not yet delivered: the device copy stays
+    int64_t last_use = 0;   // LRU clock at the last admission or delivery
+    int uses = 0;           // requests submitted and not yet delivered
+    bool removed = false;   // mtjg_server_remove_matrix: freed once uses reaches 0
+    // (every field but dev and the host arrays is read and written under the server lock)
 };
 
 void free_matrix(ResMat *m)
 {
-    mtjg_precond_destroy(m->J);
-    mtjg_csr_destroy(m->A);
-    cudaFree(m->invdiag32);
+    m->dev.release();
     delete m;
+}
+
+// Copies a matrix into a fresh device allocation on u's stream and makes its
+// FP32 values there; returns once the copy is complete.
+int upload_matrix(mtjg_ctx *u, const ResMat *m, const int *rowptr, const int *colind, const double *val,
+                  DevMat &d)
+{
+    const int n = m->n;
+    const int64_t nnz = m->nnz;
+    const MatLayout L(n, nnz);
+    DevMat t;
+    if (cudaMalloc(&t.base, L.bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(MTJG_ERR_OUT_OF_MEMORY, "no device memory for a served matrix");
+    }
+    char *b = static_cast<char *>(t.base);
+    t.rowptr = reinterpret_cast<int *>(b + L.rowptr);
+    t.colind = reinterpret_cast<int *>(b + L.colind);
+    t.val = reinterpret_cast<double *>(b + L.val);
+    t.val32 = reinterpret_cast<float *>(b + L.val32);
+    t.invdiag32 = reinterpret_cast<float *>(b + L.invdiag32);
+    int pad[kRowptrPad];
+    for (int k = 0; k < kRowptrPad; ++k) pad[k] = rowptr[n];
+    cudaStream_t s = u->stream;
+    cudaError_t e = cudaMemcpyAsync(t.rowptr, rowptr, sizeof(int) * ((size_t)n + 1), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(t.rowptr + n + 1, pad, sizeof(pad), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(t.colind + nnz, 0xff, sizeof(int) * 4, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(t.val + nnz, 0, sizeof(double) * 2, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(t.val32 + nnz, 0, sizeof(float) * 4, s);
+    if (e == cudaSuccess && nnz)
+        e = cudaMemcpyAsync(t.colind, colind, sizeof(int) * (size_t)nnz, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && nnz)
+        e = cudaMemcpyAsync(t.val, val, sizeof(double) * (size_t)nnz, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(t.invdiag32, m->inv32.data(), sizeof(float) * (size_t)n, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && nnz) {
+        k_to_f32<<<u->num_sms * 8, kBlock, 0, s>>>(nnz, t.val, t.val32);
+        u->launches++;
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        cudaStreamSynchronize(s);
+        t.release();
+        return cuda_fail(e, "uploading a served matrix");
+    }
+    d = t;
+    return MTJG_OK;
 }
 
 struct Req {
     int64_t ticket = 0;
     int mid = 0;
-    const ResMat *mat = nullptr;  // fixed at submission (the matrix table may grow meanwhile)
+    ResMat *mat = nullptr;  // fixed at submission (the matrix table may grow meanwhile)
     std::vector<double> b, x0;
     double *x_out = nullptr;
     double t_submit = 0, t_admit = 0;
@@ -138,6 +235,8 @@ using namespace mtjg;
 struct mtjg_server {
     mtjg_ctx *ctx = nullptr;   // the scheduler's own context (own stream), on the caller's device
     mtjg_ctx *uctx = nullptr;  // matrix registration (own stream, so uploads never wait for chunks)
+    mtjg_ctx *lctx = nullptr;  // the scheduler's uploads of evicted matrices
+    std::mutex up_mu;          // registering threads share uctx
     mtjg_server_config cfg{};
     std::vector<ResMat *> mats;
     std::mutex mats_mu;
@@ -180,6 +279,8 @@ struct mtjg_server {
     std::string error_msg;
     std::thread th;
     std::chrono::steady_clock::time_point t0;
+    // residency (under mu)
+    int64_t resident_bytes = 0, use_clock = 0, uploads = 0, evictions = 0;
     // statistics
     int64_t chunks = 0, admitted = 0, retired = 0, max_active = 0;
     double gpu_s = 0, host_s = 0, wait_s = 0, row_chunks = 0;
@@ -417,11 +518,15 @@ int deliver(mtjg_server *S, std::vector<Retired> &staged, int par)
             std::memcpy(f.r->x_out, S->h_x + f.r->voff, sizeof(double) * (size_t)f.r->mat->n);
             f.out.latency_s = tn - f.r->t_submit;
             S->done.push_back(f.out);
-            ResMat *m = S->mats[f.r->mid];
+            ResMat *m = f.r->mat;
+            // no queued chunk reads a delivered system's matrix: it may be
+            // evicted from here on
+            m->busy--;
+            m->last_use = ++S->use_clock;
             if (--m->uses == 0 && m->removed) {
-                // its last request is out; no queued chunk reads a retired system's matrix
                 release.push_back(m);
                 S->mats[f.r->mid] = nullptr;
+                if (m->resident) S->resident_bytes -= m->bytes;
             }
             delete f.r;
         }
@@ -431,6 +536,33 @@ int deliver(mtjg_server *S, std::vector<Retired> &staged, int par)
     staged.clear();
     for (ResMat *m : release) free_matrix(m);
     return MTJG_OK;
+}
+
+// Makes room in the matrix budget for `need` more bytes by evicting idle
+// resident matrices, least recently used first; their device copies are
+// moved to `evict` (freed by the caller outside the lock).  Evicts nothing
+// and returns false when the idle matrices cannot free enough.  Under mu.
+bool make_room(mtjg_server *S, int64_t need, std::vector<DevMat> &evict)
+{
+    const int64_t B = S->cfg.matrix_budget;
+    if (B <= 0 || S->resident_bytes + need <= B) return true;
+    std::vector<ResMat *> idle;
+    for (ResMat *q : S->mats)
+        if (q && q->resident && q->busy == 0) idle.push_back(q);
+    std::sort(idle.begin(), idle.end(), [](const ResMat *a, const ResMat *b) { return a->last_use < b->last_use; });
+    int64_t freed = 0;
+    size_t k = 0;
+    while (k < idle.size() && S->resident_bytes - freed + need > B) freed += idle[k++]->bytes;
+    if (S->resident_bytes - freed + need > B) return false;
+    for (size_t i = 0; i < k; ++i) {
+        ResMat *q = idle[i];
+        evict.push_back(q->dev);
+        q->dev = DevMat();
+        q->resident = false;
+        S->resident_bytes -= q->bytes;
+        S->evictions++;
+    }
+    return true;
 }
 
 void scheduler(mtjg_server *S)
@@ -505,8 +637,11 @@ void scheduler(mtjg_server *S)
             }
             continue;  // the next pass delivers, admits and queues
         }
-        // 2. admission (FIFO while a slot and a workspace segment are free)
+        // 2. admission (FIFO while a slot, a workspace segment and room for
+        //    the request's matrix are free)
         std::vector<Req *> admit;
+        std::vector<ResMat *> load;  // matrices to upload before their systems run
+        std::vector<DevMat> evict;   // device copies of evicted matrices
         {
             std::unique_lock<std::mutex> lk(S->mu);
             if (launched == processed && staged.empty())
@@ -521,7 +656,8 @@ void scheduler(mtjg_server *S)
             }
             while (!S->pending.empty()) {
                 Req *r = S->pending.front();
-                const int n = r->mat->n;
+                ResMat *m = r->mat;
+                const int n = m->n;
                 int slot = -1;
                 for (int s = 0; s < ns; ++s)
                     if (!S->slot_req[s]) {
@@ -529,6 +665,12 @@ void scheduler(mtjg_server *S)
                         break;
                     }
                 if (slot < 0) break;
+                if (!m->resident && !m->loading) {
+                    if (!make_room(S, m->bytes, evict)) break;
+                    m->loading = true;
+                    S->resident_bytes += m->bytes;
+                    load.push_back(m);
+                }
                 const int voff = seg_alloc(S, n);
                 if (voff < 0) break;
                 S->pending.pop_front();
@@ -540,6 +682,8 @@ void scheduler(mtjg_server *S)
                 S->active++;
                 S->active_rows += n;
                 S->admitted++;
+                m->busy++;
+                m->last_use = ++S->use_clock;
                 admit.push_back(r);
             }
             S->max_active = std::max<int64_t>(S->max_active, S->active);
@@ -547,6 +691,18 @@ void scheduler(mtjg_server *S)
         auto th = std::chrono::steady_clock::now();
         if (!staged.empty() && launched == processed) {
             if (deliver(S, staged, staged_par) != MTJG_OK) return fatal(MTJG_ERR_CUDA);
+        }
+        // evictions before uploads: the budget counted the freed bytes already
+        for (DevMat &d : evict) d.release();
+        for (ResMat *m : load) {
+            DevMat d;
+            int ust = upload_matrix(S->lctx, m, m->h_rowptr.data(), m->h_colind.data(), m->h_val.data(), d);
+            if (ust != MTJG_OK) return fatal(ust);
+            std::lock_guard<std::mutex> lk(S->mu);
+            m->dev = d;
+            m->resident = true;
+            m->loading = false;
+            S->uploads++;
         }
         const int par = (int)(launched % 2);  // this parity's staging was last read before chunk launched-2
         for (Req *r : admit) {
@@ -560,9 +716,9 @@ void scheduler(mtjg_server *S)
                 std::memcpy(S->h_x0 + r->voff, r->x0.data(), nb);
                 cudaMemcpyAsync(S->x64 + r->voff, S->h_x0 + r->voff, nb, cudaMemcpyHostToDevice, ctx->stream);
             }
-            cudaMemcpyAsync(S->inv32 + r->voff, m->invdiag32, sizeof(float) * (size_t)m->n, cudaMemcpyDeviceToDevice,
-                            ctx->stream);
-            S->h_sd[r->slot] = SysDesc{m->A->rowptr, m->A->colind, m->A->val, m->A->val32, r->voff, 0};
+            cudaMemcpyAsync(S->inv32 + r->voff, m->dev.invdiag32, sizeof(float) * (size_t)m->n,
+                            cudaMemcpyDeviceToDevice, ctx->stream);
+            S->h_sd[r->slot] = SysDesc{m->dev.rowptr, m->dev.colind, m->dev.val, m->dev.val32, r->voff, 0};
             SysState &init = S->h_init[par][r->slot];
             std::memset(&init, 0, sizeof(init));
             init.status = ST_RUNNING;
@@ -617,6 +773,7 @@ extern "C" void mtjg_server_config_defaults(mtjg_server_config *cfg)
     cfg->dtol = 1e+5;
     cfg->inner_rtol = 1e-6;
     cfg->inner_max_iter = 2000;
+    cfg->matrix_budget = 0;
 }
 
 extern "C" int mtjg_server_create(mtjg_ctx *ctx, const mtjg_server_config *cfg, mtjg_server **out)
@@ -624,22 +781,25 @@ extern "C" int mtjg_server_create(mtjg_ctx *ctx, const mtjg_server_config *cfg, 
     if (!ctx || !cfg || !out) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL argument");
     *out = nullptr;
     if (cfg->max_systems <= 0 || cfg->pool_rows <= 0 || cfg->pool_rows >= (1LL << 31) || cfg->max_iter < 0 ||
-        !(cfg->inner_rtol > 0 && cfg->inner_rtol < 1) || cfg->inner_max_iter <= 0)
+        !(cfg->inner_rtol > 0 && cfg->inner_rtol < 1) || cfg->inner_max_iter <= 0 || cfg->matrix_budget < 0)
         return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "bad server configuration");
     MTJG_CUDA(cudaSetDevice(ctx->device));
     // the scheduler thread and matrix registration work on streams of their
     // own, so the caller's context stays free for other work
-    mtjg_ctx *own = nullptr, *up = nullptr;
+    mtjg_ctx *own = nullptr, *up = nullptr, *ld = nullptr;
     int cst = mtjg_ctx_create(ctx->device, &own);
     if (cst != MTJG_OK) return cst;
     cst = mtjg_ctx_create(ctx->device, &up);
+    if (cst == MTJG_OK) cst = mtjg_ctx_create(ctx->device, &ld);
     if (cst != MTJG_OK) {
         mtjg_ctx_destroy(own);
+        if (up) mtjg_ctx_destroy(up);
         return cst;
     }
     mtjg_server *S = new mtjg_server();
     S->ctx = own;
     S->uctx = up;
+    S->lctx = ld;
     S->cfg = *cfg;
     S->t0 = std::chrono::steady_clock::now();
     const size_t P = (size_t)cfg->pool_rows, ns = (size_t)cfg->max_systems;
@@ -682,36 +842,58 @@ extern "C" int mtjg_server_create(mtjg_ctx *ctx, const mtjg_server_config *cfg, 
 extern "C" int mtjg_server_add_matrix(mtjg_server *S, int n, const int *rowptr, const int *colind, const double *val,
                                       int *matrix_id)
 {
-    if (!S || !matrix_id) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL argument");
+    if (!S || !matrix_id || !rowptr || (!val && n > 0 && rowptr[n] > 0))
+        return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL argument");
     if (n <= 0 || n > S->cfg.pool_rows)
         return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "matrix larger than the server's vector pool");
-    mtjg_ctx *u = S->uctx;
+    int st = csr_validate(n, n, rowptr, colind);
+    if (st != MTJG_OK) return st;
+    MTJG_CUDA(cudaSetDevice(S->ctx->device));
     ResMat *m = new ResMat();
     m->n = n;
-    int st = mtjg_csr_upload(u, n, n, rowptr, colind, val, &m->A);
-    if (st == MTJG_OK) st = mtjg_precond_create(u, MTJG_PC_JACOBI, n, &m->J);
-    if (st == MTJG_OK) st = mtjg_precond_set_matrix(m->J, m->A, nullptr);
-    if (st != MTJG_OK) {
-        free_matrix(m);
-        return st;
+    m->nnz = rowptr[n];
+    m->bytes = (int64_t)MatLayout(n, m->nnz).bytes;
+    const int64_t B = S->cfg.matrix_budget;
+    if (B > 0 && m->bytes > B) {
+        delete m;
+        return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "matrix larger than the server's matrix budget (" +
+                                                   std::to_string(m->bytes) + " > " + std::to_string(B) + " bytes)");
     }
-    m->nnz = m->A->nnz;
-    const int grid = u->num_sms * 8;
-    // every failure from here on releases what the matrix holds so far
-    cudaError_t e = cudaMalloc(&m->A->val32, sizeof(float) * (size_t)(m->nnz + 4));
-    if (e == cudaSuccess)
-        e = cudaMemsetAsync(m->A->val32, 0, sizeof(float) * (size_t)(m->nnz + 4), u->stream);
-    if (e == cudaSuccess) e = cudaMalloc(&m->invdiag32, sizeof(float) * (size_t)n);
-    if (e == cudaSuccess) {
-        k_to_f32<<<grid, kBlock, 0, u->stream>>>(m->nnz, m->A->val, m->A->val32);
-        k_to_f32<<<grid, kBlock, 0, u->stream>>>(n, m->J->invdiag, m->invdiag32);
-        u->launches += 2;
-        e = cudaGetLastError();
+    // DiagonalPreconditioner.setMatrix (S/DiagonalPreconditioner.java:64-76):
+    // 1 / A.get(i,i), the first zero diagonal an error; kept in FP32
+    m->inv32.resize((size_t)n);
+    for (int i = 0; i < n; ++i) {
+        const int *c0 = colind + rowptr[i], *c1 = colind + rowptr[i + 1];
+        const int *p = std::lower_bound(c0, c1, i);
+        const double d = (p != c1 && *p == i) ? val[p - colind] : 0.0;
+        if (d == 0) {
+            delete m;
+            return fail(MTJG_ERR_ZERO_DIAGONAL, "Zero diagonal on row " + std::to_string(i + 1));
+        }
+        m->inv32[(size_t)i] = (float)(1 / d);
     }
-    if (e == cudaSuccess) e = cudaStreamSynchronize(u->stream);
-    if (e != cudaSuccess) {
-        free_matrix(m);
-        return cuda_fail(e, "registering a server matrix");
+    if (B > 0) {
+        m->h_rowptr.assign(rowptr, rowptr + n + 1);
+        m->h_colind.assign(colind, colind + m->nnz);
+        m->h_val.assign(val, val + m->nnz);
+    }
+    // uploaded now if it fits the budget without evicting, else on its first request
+    bool now;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        now = B == 0 || S->resident_bytes + m->bytes <= B;
+        if (now) S->resident_bytes += m->bytes;
+    }
+    if (now) {
+        std::lock_guard<std::mutex> ul(S->up_mu);
+        st = upload_matrix(S->uctx, m, rowptr, colind, val, m->dev);
+        if (st != MTJG_OK) {
+            std::lock_guard<std::mutex> lk(S->mu);
+            S->resident_bytes -= m->bytes;
+            delete m;
+            return st;
+        }
+        m->resident = true;
     }
     // the matrix's own product tiles: FP64 as mtjg_csr_upload plans them,
     // and larger FP32 tiles for the inner products
@@ -721,6 +903,7 @@ extern "C" int mtjg_server_add_matrix(mtjg_server *S, int n, const int *rowptr, 
     std::lock_guard<std::mutex> lk(S->mats_mu);
     std::lock_guard<std::mutex> lk2(S->mu);
     *matrix_id = (int)S->mats.size();
+    if (now) S->uploads++;
     S->mats.push_back(m);
     return MTJG_OK;
 }
@@ -772,6 +955,7 @@ extern "C" int mtjg_server_remove_matrix(mtjg_server *S, int matrix_id)
         if (m->uses == 0) {
             release = m;
             S->mats[matrix_id] = nullptr;
+            if (m->resident) S->resident_bytes -= m->bytes;
         }
     }
     // freed outside the lock: cudaFree waits for the device
@@ -813,6 +997,21 @@ extern "C" int mtjg_server_stats(mtjg_server *S, int64_t *chunks, int64_t *admit
     if (admitted) *admitted = S->admitted;
     if (max_active) *max_active = S->max_active;
     if (clock_s) *clock_s = S->now();
+    return MTJG_OK;
+}
+
+extern "C" int mtjg_server_residency(mtjg_server *S, int64_t *resident_bytes, int64_t *resident_matrices,
+                                     int64_t *uploads, int64_t *evictions)
+{
+    if (!S) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL server");
+    std::lock_guard<std::mutex> lk(S->mu);
+    int64_t k = 0;
+    for (const ResMat *m : S->mats)
+        if (m && (m->resident || m->loading)) ++k;
+    if (resident_bytes) *resident_bytes = S->resident_bytes;
+    if (resident_matrices) *resident_matrices = k;
+    if (uploads) *uploads = S->uploads;
+    if (evictions) *evictions = S->evictions;
     return MTJG_OK;
 }
 
@@ -874,9 +1073,10 @@ extern "C" int mtjg_server_destroy(mtjg_server *S)
         if (S->ev_done[p]) cudaEventDestroy(S->ev_done[p]);
         if (S->ev_ret[p]) cudaEventDestroy(S->ev_ret[p]);
     }
-    mtjg_ctx *ctx = S->ctx, *u = S->uctx;
+    mtjg_ctx *ctx = S->ctx, *u = S->uctx, *ld = S->lctx;
     delete S;
     mtjg_ctx_destroy(ctx);
     mtjg_ctx_destroy(u);
+    mtjg_ctx_destroy(ld);
     return MTJG_OK;
 }

@@ -358,7 +358,7 @@ struct EpiTransMultAdd {
 using namespace mtjg;
 
 // ------------------------------------------------------------- handle ops
-static int csr_validate(int n, int m, const int *rowptr, const int *colind)
+int mtjg::csr_validate(int n, int m, const int *rowptr, const int *colind)
 {
     if (n < 0 || m < 0) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "negative matrix dimension");
     if (!rowptr) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "rowptr is NULL");

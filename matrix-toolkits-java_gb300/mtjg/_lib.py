@@ -54,7 +54,7 @@ class Result(C.Structure):
 class ServerConfig(C.Structure):
     _fields_ = [("max_systems", C.c_int), ("pool_rows", C.c_int64), ("max_iter", C.c_int),
                 ("rtol", C.c_double), ("atol", C.c_double), ("dtol", C.c_double),
-                ("inner_rtol", C.c_double), ("inner_max_iter", C.c_int)]
+                ("inner_rtol", C.c_double), ("inner_max_iter", C.c_int), ("matrix_budget", C.c_int64)]
 
 
 class ServerResult(C.Structure):
@@ -135,6 +135,8 @@ PROTOTYPES = {
     "mtjg_server_stats": (C.c_int, [_vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                     C.POINTER(C.c_double)]),
     "mtjg_server_timing": (C.c_int, [_vp, _dp, _dp, _dp, _dp]),
+    "mtjg_server_residency": (C.c_int, [_vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                        C.POINTER(C.c_int64)]),
     "mtjg_server_context": (C.c_int, [_vp, C.POINTER(_vp)]),
     "mtjg_server_destroy": (C.c_int, [_vp]),
     "mtjg_solver_batch_results": (C.c_int, [_vp, C.POINTER(Result), C.c_int]),

@@ -1,14 +1,16 @@
 """Continuous-batching solve server (include/mtjg.h, mtjg_server_*).
 
-    srv = Server(max_systems=256, pool_rows=1 << 24)
-    mid = srv.addMatrix(n, rowptr, colind, data)      # resident on the device
+    srv = Server(max_systems=256, pool_rows=1 << 24, matrix_budget=8 << 30)
+    mid = srv.addMatrix(n, rowptr, colind, data)      # uploaded now or on first use
     t = srv.submit(mid, b)                            # returns a ticket
     for r in srv.poll(): ...                          # finished requests
     srv.drain(); srv.close()
 
 Each request is solved by mixed-precision CG + Jacobi (FP64 refinement,
-FP32 inner iterations) to `rtol` on the FP64 true residual.  No counterpart
-in the reference.
+FP32 inner iterations) to `rtol` on the FP64 true residual.  With a
+`matrix_budget` (bytes) the resident matrices are evicted least recently used
+when idle and uploaded again on their next request.  No counterpart in the
+reference.
 """
 from __future__ import annotations
 
@@ -37,7 +39,7 @@ class Finished:
 
 class Server:
     def __init__(self, ctx: Context | None = None, max_systems=256, pool_rows=1 << 24, max_iter=100, rtol=1e-10,
-                 atol=1e-50, dtol=1e5, inner_rtol=1e-6, inner_max_iter=2000):
+                 atol=1e-50, dtol=1e5, inner_rtol=1e-6, inner_max_iter=2000, matrix_budget=0):
         self.ctx = ctx or default_context()
         self._lib = self.ctx._lib
         cfg = L.ServerConfig()
@@ -45,6 +47,7 @@ class Server:
         cfg.max_systems, cfg.pool_rows, cfg.max_iter = int(max_systems), int(pool_rows), int(max_iter)
         cfg.rtol, cfg.atol, cfg.dtol = float(rtol), float(atol), float(dtol)
         cfg.inner_rtol, cfg.inner_max_iter = float(inner_rtol), int(inner_max_iter)
+        cfg.matrix_budget = int(matrix_budget)
         h = C.c_void_p()
         _raise(self._lib.mtjg_server_create(self.ctx.h, C.byref(cfg), C.byref(h)), "server_create")
         self.h = h
@@ -95,6 +98,12 @@ class Server:
         c, a, m, t = C.c_int64(), C.c_int64(), C.c_int64(), C.c_double()
         _raise(self._lib.mtjg_server_stats(self.h, C.byref(c), C.byref(a), C.byref(m), C.byref(t)), "stats")
         return {"chunks": c.value, "admitted": a.value, "max_active": m.value, "clock_s": t.value}
+
+    def residency(self):
+        """Resident matrix bytes and count, uploads (registrations included), evictions."""
+        v = [C.c_int64() for _ in range(4)]
+        _raise(self._lib.mtjg_server_residency(self.h, *[C.byref(x) for x in v]), "residency")
+        return dict(zip(("resident_bytes", "resident_matrices", "uploads", "evictions"), (x.value for x in v)))
 
     def timing(self):
         g, h, w, r = C.c_double(), C.c_double(), C.c_double(), C.c_double()

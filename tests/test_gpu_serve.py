@@ -150,3 +150,102 @@ def test_zero_rhs_and_iteration_limit(servers):
     res = {r.ticket: r for r in tight.poll()}
     assert res[lim].status == 1  # IterativeSolverNotConvergedException, Reason.Iterations
     assert res[lim].iterations <= 2
+
+
+def _sizes(servers, mats):
+    """Device bytes of each matrix, read from an unlimited server's residency."""
+    srv = servers(max_systems=4, pool_rows=1 << 20)
+    out, prev = [], 0
+    for m in mats:
+        srv.addMatrix(*m)
+        now = srv.residency()["resident_bytes"]
+        out.append(now - prev)
+        prev = now
+    srv.close()
+    return out
+
+
+def test_matrix_budget_evicts_and_results_do_not_change(servers):
+    """A budget that holds about two of the six matrices: idle matrices are
+    evicted and uploaded again on demand, the resident bytes never exceed
+    the budget, and every result equals the one from a server that keeps
+    all six resident."""
+    mats = _library()
+    sizes = _sizes(servers, mats)
+    budget = sorted(sizes)[-1] + sorted(sizes)[-2]
+    reqs = _rhs(mats, 40, 11)
+    ref = servers(max_systems=64, pool_rows=1 << 20)
+    rids = [ref.addMatrix(*m) for m in mats]
+    want = _solve_all(ref, rids, reqs, False)
+    srv = servers(max_systems=64, pool_rows=1 << 20, matrix_budget=budget)
+    mids = [srv.addMatrix(*m) for m in mats]
+    reg = srv.residency()
+    assert reg["resident_bytes"] <= budget and reg["evictions"] == 0  # registration never evicts
+    assert reg["resident_matrices"] < len(mats)
+    got = _solve_all(srv, mids, reqs, False)
+    res = srv.residency()
+    assert res["evictions"] > 0 and res["uploads"] > len(mats)
+    assert res["resident_bytes"] <= budget
+    for k in range(len(reqs)):
+        assert got[k].status == 0
+        assert got[k].iterations == want[k].iterations
+        assert np.array_equal(got[k].x, want[k].x), k
+
+
+def test_lru_order_of_evictions(servers):
+    """With room for two of three equal matrices, using A, B, A, C evicts B
+    (least recently used), not A; a request for B then uploads it again."""
+    mats = [workloads.laplacian(5000, 20 + k) for k in range(3)]
+    sizes = _sizes(servers, mats)
+    srv = servers(max_systems=8, pool_rows=1 << 18, matrix_budget=max(sizes) * 2 + 1024)
+    A, B, C = [srv.addMatrix(*m) for m in mats]
+    assert srv.residency()["resident_matrices"] == 2  # C waits for its first request
+    for mid in (A, B, A):
+        srv.submit(mid, workloads.uniform(5000, mid))
+        srv.drain(60.0)
+    assert srv.residency()["evictions"] == 0
+    srv.submit(C, workloads.uniform(5000, 9))
+    srv.drain(60.0)
+    r = srv.residency()
+    assert r["evictions"] == 1 and r["uploads"] == 3
+    srv.submit(A, workloads.uniform(5000, 10))  # A stayed: no upload
+    srv.drain(60.0)
+    assert srv.residency()["uploads"] == 3
+    srv.submit(B, workloads.uniform(5000, 11))  # B was the one evicted
+    srv.drain(60.0)
+    r = srv.residency()
+    assert r["uploads"] == 4 and r["evictions"] == 2
+    assert all(f.status == 0 for f in srv.poll())
+
+
+def test_budget_held_by_busy_matrices_makes_requests_wait(servers):
+    """Room for one matrix: requests for two matrices alternate, so the
+    second matrix's request waits until the first one's systems are
+    delivered; everything still finishes."""
+    mats = [workloads.poisson2d(120), workloads.poisson2d(121)]
+    sizes = _sizes(servers, mats)
+    srv = servers(max_systems=8, pool_rows=1 << 18, matrix_budget=max(sizes) + 1024)
+    mids = [srv.addMatrix(*m) for m in mats]
+    reqs = [(k % 2, workloads.uniform(mats[k % 2][0], 300 + k)) for k in range(6)]
+    out = _solve_all(srv, mids, reqs, False)
+    assert all(out[k].status == 0 for k in range(6))
+    r = srv.residency()
+    assert r["resident_matrices"] == 1 and r["evictions"] >= 5
+
+
+def test_registration_checks(servers):
+    from mtjg import sparse
+    n, rp, ci, v = workloads.poisson2d(30)
+    sizes = _sizes(servers, [(n, rp, ci, v)])
+    srv = servers(max_systems=4, pool_rows=1 << 16, matrix_budget=sizes[0] - 1)
+    with pytest.raises(sparse.IllegalArgumentException):  # larger than the whole budget
+        srv.addMatrix(n, rp, ci, v)
+    v0 = v.copy()
+    v0[rp[7] + list(ci[rp[7]:rp[8]]).index(7)] = 0.0
+    srv2 = servers(max_systems=4, pool_rows=1 << 16)
+    with pytest.raises(RuntimeError, match="Zero diagonal on row 8"):
+        srv2.addMatrix(n, rp, ci, v0)
+    with pytest.raises(sparse.IllegalArgumentException):  # unsorted columns
+        bad = ci.copy()
+        bad[rp[3]], bad[rp[3] + 1] = bad[rp[3] + 1], bad[rp[3]]
+        srv2.addMatrix(n, rp, bad, v)
