@@ -510,14 +510,16 @@ def main():
     ap.add_argument("--only-spmv", action="store_true",
                     help="run only the CSR product loop (for profiling the product kernel)")
     ap.add_argument("--workload", default="serve",
-                    choices=["serve", "poisson3d", "c4"] + sorted(CONFIGS),
+                    choices=["serve", "poisson3d", "c4", "c3mixed"] + sorted(CONFIGS),
                     help="serve: the served request stream (headline); poisson3d: one CG + Jacobi system; "
-                         "c1/c2icc/c3gmres/c3bicg: the other single-system configurations; c4: the batch")
+                         "c1/c2icc/c3gmres/c3bicg: the other single-system configurations; c4: the batch; c3mixed: FP64 vs mixed-precision GMRES / BiCGstab + ILU on 96^3")
     ap.add_argument("--batch-systems", type=int, default=4096)
     ap.add_argument("--serve-requests", type=int, default=1500)
     ap.add_argument("--serve-max-systems", type=int, default=512)
     ap.add_argument("--serve-pool-rows", type=int, default=1 << 26)
     ap.add_argument("--inner-rtol", type=float, default=1e-6)
+    ap.add_argument("--inner-rtol-c3", type=float, default=1e-4,
+                    help="inner residual decrease of the mixed GMRES / BiCGstab solves (c3mixed)")
     ap.add_argument("--serve-low-rate", type=float, default=300.0,
                     help="offered load (requests/s) of the below-capacity latency run")
     ap.add_argument("--serve-matrix-budget", type=float, default=1.5,
@@ -537,6 +539,8 @@ def main():
         main_poisson3d(args)
     elif args.workload == "c4":
         run_batch(args)
+    elif args.workload == "c3mixed":
+        run_c3mixed(args)
     else:
         run_config(args)
 
@@ -854,6 +858,97 @@ def run_config(args):
                        "seed": seed},
             "iterations": res.iterations, "final_rel_residual": float(np.linalg.norm(b - A.mult(xh)) / np.linalg.norm(b)),
             "precond_setup_s": setup_s}
+    print(json.dumps(line))
+
+
+def _timed_solves(lib, ctx, solver, A, db, dx, n, steps, warmup):
+    """Mean CUDA-event milliseconds of `steps` device-resident solves from
+    x0 = 0 (after `warmup` untimed ones) and the last result."""
+    from mtjg import _lib as L
+    zeros = np.zeros(n)
+    res = L.Result()
+    times = []
+    for i in range(warmup + steps):
+        lib.mtjg_memcpy_h2d(ctx.h, dx, zeros.ctypes.data_as(C.c_void_p), 8 * n)
+        lib.mtjg_ctx_event_record(ctx.h, 0)
+        code = lib.mtjg_solver_solve_dev(solver.h, A.h, db, dx, C.byref(res))
+        lib.mtjg_ctx_event_record(ctx.h, 1)
+        ms = C.c_float()
+        lib.mtjg_ctx_event_elapsed(ctx.h, 0, 1, C.byref(ms))
+        if code != 0:
+            raise RuntimeError(f"solve failed: {code} {L.last_error()}")
+        if i >= warmup:
+            times.append(ms.value)
+    return statistics.mean(times), res
+
+
+def run_c3mixed(args):
+    """The precision form on 3D convection-diffusion 96^3: GMRES(30) + ILU(0)
+    and BiCGstab + ILU(0), plain FP64 against mixed precision (FP32 inner
+    solves with an FP32 ILU copy inside FP64 refinement), both to rtol 1e-10
+    on the FP64 true residual; device-resident, CUDA events.  The oracle's
+    FP64 GMRES(30) + ILU solve is the CPU baseline and the reference solution
+    for the final error."""
+    from mtjg import _lib as L
+    from mtjg import sparse, workloads
+
+    (kind, N), seed = ("convdiff3d", 96), 3
+    lib = L.load()
+    ctx = sparse.Context(int(os.environ.get("LOCAL_RANK", "0")))
+    n, rp, ci, v = workloads.convdiff3d(N)
+    A = sparse.CompRowMatrix(n, n, rp, ci, v, ctx)
+    b = A.mult(workloads.uniform(n, seed))
+    M = sparse.ILU(A)
+    M.setMatrix(A)
+    db, dx = C.c_void_p(), C.c_void_p()
+    lib.mtjg_dev_alloc(ctx.h, 8 * n, C.byref(db))
+    lib.mtjg_dev_alloc(ctx.h, 8 * n, C.byref(dx))
+    lib.mtjg_memcpy_h2d(ctx.h, db, b.ctypes.data_as(C.c_void_p), 8 * n)
+    out, xs = {}, {}
+    for sname in ("gmres", "bicgstab"):
+        for mode in ("fp64", "mixed"):
+            solver = sparse.GMRES(n, restart=30, ctx=ctx) if sname == "gmres" else sparse.BiCGstab(n, ctx=ctx)
+            solver.setPreconditioner(M)
+            solver.setIterationMonitor(sparse.DefaultIterationMonitor(MAX_ITER if mode == "fp64" else 100, RTOL,
+                                                                      1e-50, 1e5))
+            if mode == "mixed":
+                solver.setMixedPrecision(True, args.inner_rtol_c3, 3000)
+            solver._sync_monitor()
+            ms, res = _timed_solves(lib, ctx, solver, A, db, dx, n, args.steps, args.warmup)
+            xh = np.empty(n)
+            lib.mtjg_memcpy_d2h(ctx.h, xh.ctypes.data_as(C.c_void_p), dx, 8 * n)
+            xs[(sname, mode)] = xh
+            out.setdefault(sname, {})[mode] = {
+                "ms": ms, "solves_s": 1e3 / ms, "iterations": res.iterations,
+                "inner_iterations": res.inner_iterations if mode == "mixed" else None,
+                "final_rel_residual": float(np.linalg.norm(b - A.mult(xh)) / np.linalg.norm(b))}
+        out[sname]["mixed_vs_fp64"] = out[sname]["fp64"]["ms"] / out[sname]["mixed"]["ms"]
+        out[sname]["max_abs_diff_mixed_vs_fp64"] = float(np.max(np.abs(xs[(sname, "mixed")] - xs[(sname, "fp64")])))
+    cpu = None
+    if not args.no_cpu:
+        sys.path.insert(0, ORACLE_DIR)
+        import oracle as O
+        Ao = O.Csr(n, n, rp, ci, v)
+        pc = O.Precond(O.PC_ILU, n)
+        t0 = time.perf_counter()
+        pc.set_matrix(Ao)
+        xo, ores, _, _ = O.solve(O.GMRES, Ao, b, np.zeros(n), pc, max_iter=MAX_ITER, rtol=RTOL, hist_cap=0)
+        t_cpu = time.perf_counter() - t0
+        cpu = {"value": 1.0 / t_cpu, "unit": "solves/s", "cores": 1, "kind": "port",
+               "sample": f"one oracle FP64 GMRES(30) + ILU(0) solve of this system (factorisation included), "
+                         f"{ores.iterations} iterations, {t_cpu:.1f} s"}
+        scale = float(np.max(np.abs(xo)))
+        for sname in ("gmres", "bicgstab"):
+            for mode in ("fp64", "mixed"):
+                out[sname][mode]["max_rel_error_vs_oracle"] = float(np.max(np.abs(xs[(sname, mode)] - xo)) / scale)
+    g = out["gmres"]["mixed"]
+    line = {"metric": "solves/s", "value": g["solves_s"], "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": g["ms"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": f"mixed-precision GMRES(30) + ILU(0), {kind} {N}^3, rtol 1e-10 on the FP64 "
+                                   f"true residual, x0 = 0 (BiCGstab + ILU(0) and the FP64 solves beside it)",
+                       "n": n, "nnz": len(ci), "seed": seed, "inner_rtol": args.inner_rtol_c3},
+            "solvers": out, "cpu_baseline": cpu}
     print(json.dumps(line))
 
 

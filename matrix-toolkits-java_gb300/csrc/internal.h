@@ -253,6 +253,9 @@ struct mtjg_precond {
     double omega_f = 1, omega_r = 1;
     double tau = 1e-6;
     int p = 25;
+    // FP32 copies for the mixed-precision inner solves (built on first use)
+    float *data32 = nullptr, *invdiag32 = nullptr, *y32 = nullptr;
+    int64_t v32 = -1;                   // version the copies were made from
 };
 
 struct mtjg_solver;

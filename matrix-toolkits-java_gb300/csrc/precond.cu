@@ -179,9 +179,12 @@ __global__ void k_ilu_level(const int *perm, int beg, int cnt, const int *rp, co
 }
 
 // ---------------------------------------------------- triangular sweeps
-// x entries not yet solved hold this signalling NaN.
+// x entries not yet solved hold this signalling NaN (FP64; kPending32 in the
+// FP32 sweeps of the mixed-precision inner solves).
 constexpr unsigned long long kPending = 0x7FF40000DEADBEEFull;
 constexpr unsigned long long kQuietNaN = 0x7FF8000000000000ull;
+constexpr unsigned kPending32 = 0x7FA0BEEFu;
+constexpr unsigned kQuietNaN32 = 0x7FC00000u;
 constexpr long long kSweepSpinLimit = 1LL << 21;
 constexpr int kSweepBlock = 128;
 // warps per SM a sweep launches, and polls of a pending entry before the
@@ -215,18 +218,41 @@ __device__ __forceinline__ void st_relaxed(double *p, double v)
                  : "memory");
 }
 
-__device__ __forceinline__ bool pending(double v) { return (unsigned long long)__double_as_longlong(v) == kPending; }
+__device__ __forceinline__ float ld_relaxed(const float *p)
+{
+    unsigned v;
+    asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return __uint_as_float(v);
+}
 
-// Fills the outputs of the coming sweeps with kPending and resets their
-// ticket counters.  x2 may be null.
-__global__ void k_sweep_prep(int n, double *x1, double *x2, unsigned *t1, unsigned *t2, const int *status)
+__device__ __forceinline__ void st_relaxed(float *p, float v)
+{
+    asm volatile("st.relaxed.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(__float_as_uint(v)) : "memory");
+}
+
+__device__ __forceinline__ bool pending(double v) { return (unsigned long long)__double_as_longlong(v) == kPending; }
+__device__ __forceinline__ bool pending(float v) { return __float_as_uint(v) == kPending32; }
+template <class T>
+__device__ __forceinline__ T pending_value();
+template <>
+__device__ __forceinline__ double pending_value<double>() { return __longlong_as_double((long long)kPending); }
+template <>
+__device__ __forceinline__ float pending_value<float>() { return __uint_as_float(kPending32); }
+// a result that happens to carry the pending pattern is stored as a quiet NaN
+__device__ __forceinline__ double unpend(double v) { return pending(v) ? __longlong_as_double((long long)kQuietNaN) : v; }
+__device__ __forceinline__ float unpend(float v) { return pending(v) ? __uint_as_float(kQuietNaN32) : v; }
+
+// Fills the outputs of the coming sweeps with the pending pattern and resets
+// their ticket counters.  x2 may be null.
+template <class T>
+__global__ void k_sweep_prep(int n, T *x1, T *x2, unsigned *t1, unsigned *t2, const int *status)
 {
     if (status && *status != ST_RUNNING) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         if (t1) *t1 = 0u;
         if (t2) *t2 = 0u;
     }
-    const double p = __longlong_as_double((long long)kPending);
+    const T p = pending_value<T>();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         x1[i] = p;
         if (x2) x2[i] = p;
@@ -236,9 +262,10 @@ __global__ void k_sweep_prep(int n, double *x1, double *x2, unsigned *t1, unsign
 // x_c for a row of the sweep: a relaxed load, polled while it is pending.
 // Gives up (bad) after kSweepSpinLimit polls or when another wait has given
 // up (the context's error flag is set).
-__device__ __forceinline__ double wait_x(const double *x, int c, const int *err, int spin, bool &bad)
+template <class T>
+__device__ __forceinline__ T wait_x(const T *x, int c, const int *err, int spin, bool &bad)
 {
-    double v = ld_relaxed(x + c);
+    T v = ld_relaxed(x + c);
     if (!pending(v)) return v;
     unsigned ns = 32;
     for (long long polls = 1;; ++polls) {
@@ -250,7 +277,7 @@ __device__ __forceinline__ double wait_x(const double *x, int c, const int *err,
         if (!pending(v)) return v;
         if (polls > kSweepSpinLimit || ((polls & 31) == 0 && *(volatile const int *)err)) {
             bad = true;
-            return 0.0;
+            return T(0);
         }
     }
 }
@@ -272,16 +299,17 @@ __device__ __forceinline__ double wait_x(const double *x, int c, const int *err,
 //          aux (the forward iterate), upper entries from the new x (waited
 //          for); x_i = aux_i + omega (sigma' - aux_i)
 // A row's entries are read in groups of kGrp, whose x loads are all in
-// flight before the first wait.
-template <bool S, int MODE>
+// flight before the first wait.  T = float: the FP32 sweeps (MODE 0 and 1)
+// of the mixed-precision inner solves, on an FP32 copy of the factor.
+template <bool S, int MODE, class T = double>
 __global__ void __launch_bounds__(kSweepBlock) k_trsv_sweep(const int *__restrict__ perm,
                                                           const int *__restrict__ chunk, int num_chunks,
                                                           const int *__restrict__ rp, const int *__restrict__ ci,
-                                                          const double *__restrict__ v,
+                                                          const T *__restrict__ v,
                                                           const int *__restrict__ diag,
-                                                          const double *__restrict__ diagv, const double *b,
-                                                          double *x, unsigned *ticket, const int *status, int *err,
-                                                          int spin, const double *__restrict__ aux, double omega)
+                                                          const T *__restrict__ diagv, const T *b,
+                                                          T *x, unsigned *ticket, const int *status, int *err,
+                                                          int spin, const T *__restrict__ aux, T omega)
 {
     constexpr int kGrp = 4;
     if (status && *status != ST_RUNNING) return;
@@ -295,7 +323,7 @@ __global__ void __launch_bounds__(kSweepBlock) k_trsv_sweep(const int *__restric
         bool bad = false;
         if (lane < cnt) {
             const int i = perm[beg + lane];
-            const double bi = b[i];
+            const T bi = b[i];
             // entry range, walked upwards from kb (MODE 3: downwards from ke - 1)
             int kb, ke, dk = -1;
             if constexpr (MODE == 0) {
@@ -309,22 +337,22 @@ __global__ void __launch_bounds__(kSweepBlock) k_trsv_sweep(const int *__restric
                 ke = rp[i + 1];
             }
             if constexpr (MODE >= 4) dk = diag[i];
-            double acc = (MODE == 2 || MODE == 3) ? bi : 0.0;
+            T acc = (MODE == 2 || MODE == 3) ? bi : T(0);
             for (int k0 = 0; k0 < ke - kb && !bad; k0 += kGrp) {
                 int cc[kGrp];
-                double vv[kGrp], xv[kGrp];
+                T vv[kGrp], xv[kGrp];
                 bool wt[kGrp];  // the entry is read from the sweep's own output
 #pragma unroll
                 for (int u = 0; u < kGrp; ++u) {
                     const int k = MODE == 3 ? ke - 1 - (k0 + u) : kb + k0 + u;
                     const bool in = k0 + u < ke - kb && k != dk;
                     cc[u] = in ? ci[k] : -1;
-                    vv[u] = in ? v[k] : 0.0;
+                    vv[u] = in ? v[k] : T(0);
                     wt[u] = MODE == 4 ? k < dk : (MODE == 5 ? k > dk : true);
                 }
 #pragma unroll
                 for (int u = 0; u < kGrp; ++u)
-                    xv[u] = cc[u] < 0 ? 0.0 : (wt[u] ? ld_relaxed(x + cc[u]) : aux[cc[u]]);
+                    xv[u] = cc[u] < 0 ? T(0) : (wt[u] ? ld_relaxed(x + cc[u]) : aux[cc[u]]);
 #pragma unroll
                 for (int u = 0; u < kGrp; ++u) {
                     if (cc[u] < 0 || bad) continue;
@@ -333,20 +361,19 @@ __global__ void __launch_bounds__(kSweepBlock) k_trsv_sweep(const int *__restric
                     else acc = fmac<S>(-vv[u], xv[u], acc);
                 }
             }
-            double xi;
+            T xi;
             if constexpr (MODE == 0) xi = bi - acc;
             else if constexpr (MODE == 1) xi = (bi - acc) / v[diag[i]];
             else if constexpr (MODE == 2) xi = acc / diagv[i];
             else if constexpr (MODE == 3) xi = acc;
             else {
                 // sigma = (b_i - sigma) / a_ii; x_i = old_i + omega (sigma - old_i)
-                const double sig = (bi - acc) / v[dk], old = aux[i];
+                const T sig = (bi - acc) / v[dk], old = aux[i];
                 if constexpr (S) xi = __dadd_rn(old, __dmul_rn(omega, __dsub_rn(sig, old)));
                 else xi = fma(omega, sig - old, old);
             }
             // a stored pending pattern would read as "not solved": store a quiet NaN
-            if ((unsigned long long)__double_as_longlong(xi) == kPending) xi = __longlong_as_double((long long)kQuietNaN);
-            if (!bad) st_relaxed(x + i, xi);
+            if (!bad) st_relaxed(x + i, unpend(xi));
         }
         if (__any_sync(0xffffffffu, bad)) {
             if (lane == 0) atomicExch(err, 1);
@@ -557,6 +584,119 @@ int precond_apply_dev(mtjg_precond *M, const double *b, double *x, const int *st
     return MTJG_OK;
 }
 
+// ------------------------------------------------ FP32 copies and applies
+// The mixed-precision inner solves apply M in FP32: an FP32 copy of the
+// ILU / ILUT factor values (sweeps with the FP64 factor's levels) or of the
+// Jacobi inverse diagonal.  precond_prepare32 builds the copy (it allocates,
+// so it runs before a solve's loop) and rebuilds it after setMatrix.
+int precond_prepare32(mtjg_precond *M);
+int precond_apply32(mtjg_precond *M, const float *b, float *x, const int *status);
+
+__global__ void k_copy32(int n, const float *b, float *x, const int *status)
+{
+    if (status && *status != ST_RUNNING) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] = b[i];
+}
+
+__global__ void k_jacobi_apply32(int n, const float *invdiag, const float *b, float *x, const int *status)
+{
+    if (status && *status != ST_RUNNING) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] = b[i] * invdiag[i];
+}
+
+__global__ void k_narrow(int64_t n, const double *a, float *b)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+
+template <int MODE>
+static cudaError_t sweep32(mtjg_ctx *ctx, const LevelSchedule &s, const int *rp, const int *ci, const float *v,
+                           const int *diag, const float *b, float *x, const int *status)
+{
+    if (s.num_chunks == 0) return cudaSuccess;
+    const int warps = ctx->num_sms * env_int("MTJG_SWEEP_WARPS", kSweepWarpsPerSm, 1, 40);
+    const int spin = env_int("MTJG_SWEEP_SPIN", kSweepSpin, 0, 1 << 20);
+    const int grid = (std::min(warps, s.num_chunks) + kSweepBlock / 32 - 1) / (kSweepBlock / 32);
+    k_trsv_sweep<false, MODE, float><<<grid, kSweepBlock, 0, ctx->stream>>>(
+        s.perm, s.chunk, s.num_chunks, rp, ci, v, diag, nullptr, b, x, s.ticket, status, ctx->d_flag, spin, nullptr,
+        0.0f);
+    ctx->launches++;
+    return cudaGetLastError();
+}
+
+int precond_prepare32(mtjg_precond *M)
+{
+    if (!M->ready) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "preconditioner has no matrix (call setMatrix first)");
+    if (M->kind != MTJG_PC_IDENTITY && M->kind != MTJG_PC_JACOBI && M->kind != MTJG_PC_ILU &&
+        M->kind != MTJG_PC_ILUT)
+        return fail(MTJG_ERR_UNSUPPORTED, "mixed precision applies the identity, Jacobi, ILU or ILUT preconditioner");
+    if (M->v32 == M->version) return MTJG_OK;
+    mtjg_ctx *ctx = M->ctx;
+    cudaFree(M->data32);
+    cudaFree(M->invdiag32);
+    cudaFree(M->y32);
+    M->data32 = M->invdiag32 = M->y32 = nullptr;
+    const int n = M->n;
+    if (M->kind == MTJG_PC_JACOBI) {
+        MTJG_CUDA(cudaMalloc(&M->invdiag32, sizeof(float) * (size_t)std::max(1, n)));
+        if (n) k_narrow<<<grid_for(ctx, n), kBlock, 0, ctx->stream>>>(n, M->invdiag, M->invdiag32);
+        ctx->launches++;
+    } else if (M->kind != MTJG_PC_IDENTITY) {
+        MTJG_CUDA(cudaMalloc(&M->data32, sizeof(float) * (size_t)std::max<int64_t>(1, M->nnz)));
+        MTJG_CUDA(cudaMalloc(&M->y32, sizeof(float) * (size_t)std::max(1, n)));
+        if (M->nnz) k_narrow<<<ctx->num_sms * 8, kBlock, 0, ctx->stream>>>(M->nnz, M->data, M->data32);
+        ctx->launches++;
+    }
+    MTJG_CUDA(cudaGetLastError());
+    M->v32 = M->version;
+    return MTJG_OK;
+}
+
+// x = M \ b in FP32, gated like precond_apply_dev; needs precond_prepare32.
+int precond_apply32(mtjg_precond *M, const float *b, float *x, const int *status)
+{
+    mtjg_ctx *ctx = M->ctx;
+    const int n = M->n;
+    if (n == 0) return MTJG_OK;
+    if (M->v32 != M->version) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "FP32 preconditioner copy is stale");
+    cudaError_t e = cudaSuccess;
+    switch (M->kind) {
+    case MTJG_PC_IDENTITY:
+        if (x != b) {
+            k_copy32<<<grid_for(ctx, n), kBlock, 0, ctx->stream>>>(n, b, x, status);
+            ctx->launches++;
+        }
+        e = cudaGetLastError();
+        break;
+    case MTJG_PC_JACOBI:
+        k_jacobi_apply32<<<grid_for(ctx, n), kBlock, 0, ctx->stream>>>(n, M->invdiag32, b, x, status);
+        ctx->launches++;
+        e = cudaGetLastError();
+        break;
+    default: {  // ILU / ILUT: L y = b, then U x = y, on the FP32 factor
+        const bool alias = x == b;
+        k_sweep_prep<float><<<grid_for(ctx, n), kBlock, 0, ctx->stream>>>(n, M->y32, alias ? nullptr : x,
+                                                                          M->lo.ticket, M->up.ticket, status);
+        ctx->launches++;
+        e = cudaGetLastError();
+        if (e == cudaSuccess)
+            e = sweep32<0>(ctx, M->lo, M->rowptr, M->colind, M->data32, M->diag, b, M->y32, status);
+        if (e == cudaSuccess && alias) {
+            k_sweep_prep<float><<<grid_for(ctx, n), kBlock, 0, ctx->stream>>>(n, x, nullptr, nullptr, nullptr,
+                                                                              status);
+            ctx->launches++;
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess)
+            e = sweep32<1>(ctx, M->up, M->rowptr, M->colind, M->data32, M->diag, M->y32, x, status);
+        break;
+    }
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "FP32 preconditioner apply");
+    return MTJG_OK;
+}
+
 // Preconditioner.transApply on device vectors, gated like
 // precond_apply_dev; and the set-up it needs (ILU's transposed factors),
 // which allocates and so must run before any stream capture.
@@ -587,6 +727,11 @@ static void precond_release(mtjg_precond *M)
     cudaFree(M->rt_colind);
     cudaFree(M->rt_val);
     cudaFree(M->diagv);
+    cudaFree(M->data32);
+    cudaFree(M->invdiag32);
+    cudaFree(M->y32);
+    M->data32 = M->invdiag32 = M->y32 = nullptr;
+    M->v32 = -1;
     free_sched(M->lo);
     free_sched(M->up);
     M->invdiag = M->data = M->rt_val = M->diagv = nullptr;

@@ -15,6 +15,7 @@
 
 #include "batch.cuh"
 #include "krylov_ext.cuh"
+#include "mixed_ir_phases.cuh"
 
 // resident blocks per SM the CG update is compiled for (it keeps four rows of
 // five FP64 vectors in flight per thread)
@@ -32,6 +33,8 @@ namespace mtjg {
 int precond_apply_dev(mtjg_precond *M, const double *b, double *x, const int *status);
 int precond_trans_apply_dev(mtjg_precond *M, const double *b, double *x, const int *status);
 int precond_prepare_trans(mtjg_precond *M);
+int precond_prepare32(mtjg_precond *M);
+int precond_apply32(mtjg_precond *M, const float *b, float *x, const int *status);
 int csr_ensure_transpose(mtjg_csr *A);
 
 
@@ -690,6 +693,11 @@ struct mtjg_solver {
     int b_cap = 0;
     int64_t b_xcap = 0;
     int last_sys = 0;          // the system of the last solve that S->last describes
+    // mixed GMRES / BiCGstab (mixed_ir.cuh): FP32 vectors, FP64 partials and
+    // scalars, pinned copies of the scalars
+    float *ir_f = nullptr;
+    double *ir_d = nullptr, *ir_h = nullptr;
+    int64_t ir_fcap = 0, ir_dcap = 0, ir_hcap = 0;
     bool last_empty = false;   // the last solve had n == 0: its history is empty_it (residuals 0)
     std::vector<int> empty_it;
 };
@@ -1310,6 +1318,8 @@ int run(mtjg_solver *S, mtjg_csr *A, mtjg_result *res)
     return report(S, res);
 }
 
+#include "mixed_ir.cuh"
+
 // A batch from mtjg_batch_upload solved by CG with the identity or Jacobi
 // preconditioner runs as one persistent launch (batch.cu); other batches
 // run the tiled phases.
@@ -1535,9 +1545,18 @@ int check_sizes(mtjg_solver *S, mtjg_csr *A)
     if (S->M && !S->M->ready) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "preconditioner setMatrix has not been called");
     if (S->kind == MTJG_CHEBYSHEV && !S->eig_set)
         return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "Chebyshev needs its eigenvalue bounds (mtjg_solver_set_eigenvalues)");
-    if (S->mixed && (S->kind != MTJG_CG ||
-                     (S->M && S->M->kind != MTJG_PC_IDENTITY && S->M->kind != MTJG_PC_JACOBI)))
-        return fail(MTJG_ERR_UNSUPPORTED, "mixed precision supports CG with the identity or Jacobi preconditioner");
+    if (S->mixed && S->kind == MTJG_CG && S->M && S->M->kind != MTJG_PC_IDENTITY && S->M->kind != MTJG_PC_JACOBI)
+        return fail(MTJG_ERR_UNSUPPORTED, "mixed-precision CG supports the identity or Jacobi preconditioner");
+    if (S->mixed && S->kind != MTJG_CG) {
+        if (S->M && S->M->kind != MTJG_PC_IDENTITY && S->M->kind != MTJG_PC_JACOBI && S->M->kind != MTJG_PC_ILU &&
+            S->M->kind != MTJG_PC_ILUT)
+            return fail(MTJG_ERR_UNSUPPORTED,
+                        "mixed-precision GMRES and BiCGstab support the identity, Jacobi, ILU and ILUT preconditioners");
+        if (A->tiles.num_sys > 1)
+            return fail(MTJG_ERR_UNSUPPORTED, "mixed-precision GMRES and BiCGstab solve one system at a time");
+        if (S->kind == MTJG_GMRES && S->restart > 63)
+            return fail(MTJG_ERR_UNSUPPORTED, "mixed-precision GMRES supports restart <= 63");
+    }
     if (A->tiles.num_sys > 1) {
         if (S->kind == MTJG_GMRES)
             return fail(MTJG_ERR_UNSUPPORTED, "batched solves support CG and BiCGstab");
@@ -1623,6 +1642,9 @@ extern "C" int mtjg_solver_destroy(mtjg_solver *S)
     cudaFree(S->b_vec);
     cudaFree(S->b_ticket);
     cudaFree(S->b_xsave);
+    cudaFree(S->ir_f);
+    cudaFree(S->ir_d);
+    if (S->ir_h) cudaFreeHost(S->ir_h);
     if (S->ev[0]) cudaEventDestroy(S->ev[0]);
     if (S->ev[1]) cudaEventDestroy(S->ev[1]);
     mtjg_ctx *ctx = S->ctx;
@@ -1673,7 +1695,8 @@ extern "C" int mtjg_solver_set_eigenvalues(mtjg_solver *S, double eigmin, double
 extern "C" int mtjg_solver_set_mixed(mtjg_solver *S, int enable, double inner_rtol, int inner_max_iter)
 {
     if (!S) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL solver");
-    if (enable && S->kind != MTJG_CG) return fail(MTJG_ERR_UNSUPPORTED, "mixed precision supports CG");
+    if (enable && S->kind != MTJG_CG && S->kind != MTJG_GMRES && S->kind != MTJG_BICGSTAB)
+        return fail(MTJG_ERR_UNSUPPORTED, "mixed precision supports CG, GMRES and BiCGstab");
     if (enable && (!(inner_rtol > 0.0 && inner_rtol < 1.0) || inner_max_iter <= 0))
         return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "inner_rtol must lie in (0, 1) and inner_max_iter be positive");
     MTJG_CUDA(cudaSetDevice(S->ctx->device));
@@ -1728,7 +1751,9 @@ extern "C" int mtjg_solver_solve(mtjg_solver *S, mtjg_csr *A, const double *b, d
     const size_t nb = sizeof(double) * (size_t)S->n;
     MTJG_CUDA(cudaMemcpyAsync(S->vecs[V_B], b, nb, cudaMemcpyHostToDevice, ctx->stream));
     MTJG_CUDA(cudaMemcpyAsync(S->vecs[V_X], x, nb, cudaMemcpyHostToDevice, ctx->stream));
-    st = batch_persistent(S, A) ? run_batch(S, A, res) : run(S, A, res);
+    st = batch_persistent(S, A)            ? run_batch(S, A, res)
+         : S->mixed && S->kind != MTJG_CG ? run_mixed_ir(S, A, res)
+                                           : run(S, A, res);
     if (st == MTJG_ERR_CUDA || st == MTJG_ERR_OUT_OF_MEMORY || st == MTJG_ERR_DEVICE_TIMEOUT) return st;
     MTJG_CUDA(cudaMemcpyAsync(x, S->vecs[V_X], nb, cudaMemcpyDeviceToHost, ctx->stream));
     MTJG_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -1747,7 +1772,9 @@ extern "C" int mtjg_solver_solve_dev(mtjg_solver *S, mtjg_csr *A, const double *
     const size_t nb = sizeof(double) * (size_t)S->n;
     MTJG_CUDA(cudaMemcpyAsync(S->vecs[V_B], db, nb, cudaMemcpyDeviceToDevice, ctx->stream));
     MTJG_CUDA(cudaMemcpyAsync(S->vecs[V_X], dx, nb, cudaMemcpyDeviceToDevice, ctx->stream));
-    st = batch_persistent(S, A) ? run_batch(S, A, res) : run(S, A, res);
+    st = batch_persistent(S, A)            ? run_batch(S, A, res)
+         : S->mixed && S->kind != MTJG_CG ? run_mixed_ir(S, A, res)
+                                           : run(S, A, res);
     if (st == MTJG_ERR_CUDA || st == MTJG_ERR_OUT_OF_MEMORY || st == MTJG_ERR_DEVICE_TIMEOUT) return st;
     MTJG_CUDA(cudaMemcpyAsync(dx, S->vecs[V_X], nb, cudaMemcpyDeviceToDevice, ctx->stream));
     MTJG_CUDA(cudaStreamSynchronize(ctx->stream));

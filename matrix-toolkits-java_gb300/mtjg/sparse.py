@@ -671,8 +671,10 @@ class AbstractIterativeSolver:
         return self.iter
 
     def setMixedPrecision(self, enable=True, inner_rtol=1e-4, inner_max_iter=1000):
-        """CG only: FP32 inner solves inside FP64 iterative refinement
-        (mtjg_solver_set_mixed).  iterations() then counts refinement steps."""
+        """FP32 inner solves inside FP64 iterative refinement
+        (mtjg_solver_set_mixed): CG (identity or Jacobi), GMRES and BiCGstab
+        (identity, Jacobi, ILU or ILUT).  iterations() then counts refinement
+        steps and innerIterations() the FP32 iterations."""
         _raise(self._lib.mtjg_solver_set_mixed(self.h, 1 if enable else 0, float(inner_rtol), int(inner_max_iter)),
                "set_mixed")
 

@@ -75,6 +75,98 @@ def test_mixed_batch_equals_solo(ctx):
 
 
 def test_mixed_rejects_other_solvers(ctx):
-    s = sparse.GMRES(10, ctx=ctx)
+    s = sparse.QMR(10, ctx=ctx)
     with pytest.raises(sparse.UnsupportedOperationException):
         s.setMixedPrecision(True)
+
+
+def test_mixed_rejects_other_preconditioners(ctx):
+    n, rp, ci, v = workloads.poisson2d(12)
+    A = sparse.CompRowMatrix(n, n, rp, ci, v, ctx)
+    for make, M in ((sparse.CG, sparse.ILU(A)), (sparse.GMRES, sparse.ICC(A)), (sparse.BiCGstab, sparse.SSOR(A))):
+        M.setMatrix(A)
+        s = make(n, ctx=ctx)
+        s.setPreconditioner(M)
+        s.setMixedPrecision(True)
+        with pytest.raises(sparse.UnsupportedOperationException):
+            s.solve(A, np.ones(n), np.zeros(n))
+
+
+def _krylov(ctx, kind, n, M, rtol=1e-10, inner_rtol=1e-4, max_iter=60):
+    s = sparse.GMRES(n, ctx=ctx) if kind == "gmres" else sparse.BiCGstab(n, ctx=ctx)
+    if M is not None:
+        s.setPreconditioner(M)
+    mon = sparse.DefaultIterationMonitor(max_iter, rtol, 1e-50, 1e5)
+    mon.setIterationReporter(None, history_cap=256)
+    s.setIterationMonitor(mon)
+    s.setMixedPrecision(True, inner_rtol, 3000)
+    return s
+
+
+_ORACLE_PC = {"identity": None, "jacobi": "PC_JACOBI", "ilu": "PC_ILU", "ilut": "PC_ILUT"}
+
+
+@pytest.mark.parametrize("kind", ["gmres", "bicgstab"])
+@pytest.mark.parametrize("pc,mat,N", [("ilu", "convdiff3d", 20), ("ilu", "convdiff3d", 32), ("ilut", "convdiff3d", 16),
+                                      ("jacobi", "poisson2d", 48), ("identity", "convdiff3d", 12)])
+def test_mixed_krylov_reaches_fp64_tolerance(ctx, kind, pc, mat, N):
+    """Mixed GMRES(30) / BiCGstab: FP32 inner solves with an FP32 copy of the
+    preconditioner inside FP64 refinement meet rtol 1e-10 on the FP64 true
+    residual, with one monitor test per refinement step, and agree with an
+    FP64 oracle solve of the same system."""
+    n, rp, ci, v = getattr(workloads, mat)(N)
+    A = sparse.CompRowMatrix(n, n, rp, ci, v, ctx)
+    Ao = O.Csr(n, n, rp, ci, v)
+    b = O.mult(Ao, workloads.uniform(n, 4))
+    M = None
+    if pc != "identity":
+        M = {"ilu": sparse.ILU, "ilut": sparse.ILUT, "jacobi": sparse.DiagonalPreconditioner}[pc](
+            A if pc != "jacobi" else n, *(() if pc != "jacobi" else (ctx,)))
+        M.setMatrix(A)
+    s = _krylov(ctx, kind, n, M)
+    x = np.zeros(n)
+    s.solve(A, b, x)
+    r = O.mult_add(Ao, -1.0, x, b)
+    assert np.linalg.norm(r) < 1e-10 * np.linalg.norm(b)
+    hist, its = s.history
+    assert np.array_equal(its, np.arange(len(its)))
+    assert abs(hist[0] - np.linalg.norm(b)) <= 1e-12 * np.linalg.norm(b)
+    assert hist[-1] < 1e-10 * hist[0]
+    assert s.getIterationMonitor().iterations() <= 8 and s.innerIterations() > 0
+    pco = None
+    if pc != "identity":
+        pco = O.Precond(getattr(O, _ORACLE_PC[pc]), n)
+        pco.set_matrix(Ao)
+    xo, res, _, _ = O.solve(O.GMRES if kind == "gmres" else O.BICGSTAB, Ao, b, np.zeros(n), pco, max_iter=20000,
+                            rtol=1e-10)
+    assert res.status == 0
+    assert np.max(np.abs(x - xo)) <= 1e-6 * np.max(np.abs(xo))
+
+
+@pytest.mark.parametrize("kind", ["gmres", "bicgstab"])
+def test_mixed_krylov_repeatable(ctx, kind):
+    """Two solves from the same x0 give the same x bit for bit: every
+    reduction runs in a fixed order."""
+    n, rp, ci, v = workloads.convdiff3d(14)
+    A = sparse.CompRowMatrix(n, n, rp, ci, v, ctx)
+    b = A.mult(workloads.uniform(n, 8))
+    M = sparse.ILU(A)
+    M.setMatrix(A)
+    s = _krylov(ctx, kind, n, M)
+    x1, x2 = np.zeros(n), np.zeros(n)
+    s.solve(A, b, x1)
+    it1, in1 = s.getIterationMonitor().iterations(), s.innerIterations()
+    s.solve(A, b, x2)
+    assert np.array_equal(x1, x2)
+    assert s.getIterationMonitor().iterations() == it1 and s.innerIterations() == in1
+
+
+def test_mixed_krylov_iteration_limit(ctx):
+    """A refinement budget too small to reach rtol ends with Reason.Iterations."""
+    n, rp, ci, v = workloads.convdiff3d(16)
+    A = sparse.CompRowMatrix(n, n, rp, ci, v, ctx)
+    b = A.mult(workloads.uniform(n, 9))
+    s = _krylov(ctx, "gmres", n, None, inner_rtol=0.5, max_iter=2)
+    with pytest.raises(sparse.IterativeSolverNotConvergedException):
+        s.solve(A, b, np.zeros(n))
+    assert s.getIterationMonitor().iterations() == 2
