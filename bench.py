@@ -510,9 +510,9 @@ def main():
     ap.add_argument("--only-spmv", action="store_true",
                     help="run only the CSR product loop (for profiling the product kernel)")
     ap.add_argument("--workload", default="serve",
-                    choices=["serve", "poisson3d", "c4", "c3mixed"] + sorted(CONFIGS),
+                    choices=["serve", "poisson3d", "c4", "c4poisson", "c3mixed"] + sorted(CONFIGS),
                     help="serve: the served request stream (headline); poisson3d: one CG + Jacobi system; "
-                         "c1/c2icc/c3gmres/c3bicg: the other single-system configurations; c4: the batch; c3mixed: FP64 vs mixed-precision GMRES / BiCGstab + ILU on 96^3")
+                         "c1/c2icc/c3gmres/c3bicg: the other single-system configurations; c4: the batch; c4poisson: a batch of 2D Poisson systems; c3mixed: FP64 vs mixed-precision GMRES / BiCGstab + ILU on 96^3")
     ap.add_argument("--batch-systems", type=int, default=4096)
     ap.add_argument("--serve-requests", type=int, default=1500)
     ap.add_argument("--serve-max-systems", type=int, default=512)
@@ -537,7 +537,7 @@ def main():
         main_serve(args)
     elif args.workload == "poisson3d":
         main_poisson3d(args)
-    elif args.workload == "c4":
+    elif args.workload in ("c4", "c4poisson"):
         run_batch(args)
     elif args.workload == "c3mixed":
         run_c3mixed(args)
@@ -960,10 +960,23 @@ def run_batch(args):
     from mtjg import _lib as L
     from mtjg import sparse, workloads
 
-    count = args.batch_systems
-    sizes = workloads.batch_sizes(count, 4)
-    with ThreadPoolExecutor(16) as ex:
-        systems = list(ex.map(lambda k: workloads.laplacian(int(sizes[k]), 4 + k), range(count)))
+    poisson = args.workload == "c4poisson"
+    if poisson:
+        # 2D Poisson grids N log-uniform in [32, 256]: hundreds of CG
+        # iterations per system, where FP32 inner iterations pay
+        count = args.batch_systems if args.batch_systems != 4096 else 1024
+        grids = workloads.batch_sizes(count, 14, 32, 256)
+        with ThreadPoolExecutor(16) as ex:
+            systems = list(ex.map(lambda k: workloads.poisson2d(int(grids[k])), range(count)))
+        what = f"batched: {count} 2D 5-point Poisson systems, grid N log-uniform [32, 256], CG + Jacobi, rtol 1e-10"
+        seed = 14
+    else:
+        count = args.batch_systems
+        sizes = workloads.batch_sizes(count, 4)
+        with ThreadPoolExecutor(16) as ex:
+            systems = list(ex.map(lambda k: workloads.laplacian(int(sizes[k]), 4 + k), range(count)))
+        what = f"batched: {count} random SPD Laplacians, n log-uniform [500, 50000], CG + Jacobi, rtol 1e-10"
+        seed = 4
     lib = L.load()
     ctx = sparse.Context(int(os.environ.get("LOCAL_RANK", "0")))
     A = sparse.BatchCompRowMatrix(systems, ctx)
@@ -1015,8 +1028,7 @@ def run_batch(args):
     line = {"metric": "batched solves/s", "value": out["mixed"]["solves_s"], "unit": "solves/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": out["mixed"]["ms"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-            "config": {"workload": f"batched: {count} random SPD Laplacians, n log-uniform [500, 50000], CG + Jacobi, "
-                                   "rtol 1e-10", "rows": nt, "nnz": int(A.rowptr[-1]), "seed": 4},
+            "config": {"workload": what, "rows": nt, "nnz": int(A.rowptr[-1]), "seed": seed},
             "fp64": out["fp64"], "mixed": out["mixed"], "mixed_vs_fp64": out["fp64"]["ms"] / out["mixed"]["ms"],
             "launch": "one persistent launch per solve (each CTA runs whole systems, largest first)",
             "tuned_lanes_per_row": dict(sorted(tuned.items()))}
