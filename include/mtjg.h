@@ -324,14 +324,19 @@ MTJG_API int mtjg_solver_solve(mtjg_solver *S, mtjg_csr *A, const double *b, dou
 MTJG_API int mtjg_solver_solve_dev(mtjg_solver *S, mtjg_csr *A, const double *db,
                                    double *dx, mtjg_result *res);
 /* Mixed precision for CG with the identity or Jacobi preconditioner (also
- * batched).  The solve becomes iterative refinement in the shape of MTJ's IR
- * (S/IR.java:57-70): the outer loop keeps x, the true residual r = b - A x
- * and the monitor's test in FP64, exactly as DefaultIterationMonitor sees
- * them, and each correction comes from an inner CG whose matrix values,
- * vectors, products and preconditioner are FP32, run until its residual
- * falls by inner_rtol or for inner_max_iter iterations.  iterations() then
- * counts refinement steps; mtjg_result.inner_iterations the inner ones.
- * enable = 0 restores the FP64 solver.  No counterpart in the reference. */
+ * batched), and for GMRES(m <= 63) and BiCGstab with the identity, Jacobi,
+ * ILU or ILUT preconditioner (one system).  The solve becomes iterative
+ * refinement in the shape of MTJ's IR (S/IR.java:57-70): the outer loop keeps
+ * x, the true residual r = b - A x and the monitor's test in FP64, exactly as
+ * DefaultIterationMonitor sees them, and each correction comes from an inner
+ * solve of the same kind (CG; right-preconditioned GMRES(m) or BiCGstab)
+ * whose matrix values, vectors, products and preconditioner (an FP32 copy of
+ * the factor or diagonal) are FP32, run until its residual falls by
+ * inner_rtol or for inner_max_iter iterations (GMRES: in all, per solve).
+ * iterations() then counts refinement steps; mtjg_result.inner_iterations
+ * the inner ones.  Other solvers are MTJG_ERR_UNSUPPORTED here, other
+ * preconditioners at solve time.  enable = 0 restores the FP64 solver.  No
+ * counterpart in the reference. */
 MTJG_API int mtjg_solver_set_mixed(mtjg_solver *S, int enable, double inner_rtol, int inner_max_iter);
 /* Residual history of the last solve: the (residual, iteration) pairs passed
  * to IterationReporter.monitor, oldest first (up to history_cap); for a

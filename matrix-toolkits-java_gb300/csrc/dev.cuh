@@ -226,24 +226,23 @@ __device__ __forceinline__ void group_partial(Acc &a, int group, const RedCtx &r
     }
 }
 
-// The reduction of a phase finishes with one sum per system of its group
-// partials in group order (thread t takes groups t, t+B, t+2B, ... with four
-// loads in flight, then the fixed block tree), and thread 0 runs
-// op.scalar(s, sums).  With a counter array (RedCtx::cnt) the phase's own
-// kernel does it: the block that stores a system's last group partial (a
-// fence, then a count) sums them and rearms the counter, so the reduction
-// costs no launch.  Without one, k_finalize does it in a launch of its own,
-// whose boundary orders the partial stores before it.  Both sum in the same
-// order with the same block shape, so their results are identical.
+// The reduction of a phase finishes in k_finalize (a launch of its own after
+// the phase's kernel): block s sums system s's group partials in group order
+// (thread t takes groups t, t+B, t+2B, ... with four loads in flight, then
+// the fixed block tree) and thread 0 runs op.scalar(s, sums).  No atomics
+// and no fences: the launch boundary orders the partial stores before it.
 //
 // Kernel templates and their launchers live in an unnamed namespace: without
 // relocatable device code every translation unit carries its own device
 // image, so each one instantiates (and sets attributes on) its own kernels.
-// System sys's group partials summed in group order (valid in thread 0).
-// L2 loads: in the fused form other blocks stored them during this launch.
-template <int SLOTS>
-__device__ __forceinline__ Acc system_sum(const RedCtx &rc, int sys, int type, double *sm)
+namespace {
+template <class Op>
+__global__ void __launch_bounds__(kBlock) k_finalize(Op op, RedCtx rc, int type)
 {
+    constexpr int SLOTS = OpSlots<Op>::value;
+    __shared__ double sm[kParts * kBlock];
+    const int sys = blockIdx.x;
+    if (!op.active(sys)) return;
     const int g0 = rc.sys_group[sys], g1 = rc.sys_group[sys + 1];
     const int stride = blockDim.x;
     Acc s;
@@ -255,58 +254,14 @@ __device__ __forceinline__ Acc system_sum(const RedCtx &rc, int sys, int type, d
             const int g = base + u * stride;
 #pragma unroll
             for (int i = 0; i < kParts; ++i)
-                o[u].v[i] = (g < g1 && (SLOTS & (i < 2 ? kSlotNorm : (1 << i))))
-                                ? __ldcg(rc.part + (size_t)g * kParts + i)
-                                : 0.0;
+                o[u].v[i] = (g < g1 && (SLOTS & (i < 2 ? kSlotNorm : (1 << i)))) ? rc.part[(size_t)g * kParts + i]
+                                                                                  : 0.0;
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u)
             if (base + u * stride < g1) acc_merge_m<SLOTS>(s, o[u], type);
     }
     block_reduce<SLOTS>(s, type, sm);
-    return s;
-}
-
-// The last block's part of the fused finish: out of line, so that the
-// scalar step's registers do not weigh on the product loop around the call.
-template <int SLOTS, class Op>
-__device__ __noinline__ void system_finish(Op &op, int sys, const RedCtx &rc, int type, double *sm)
-{
-    __threadfence();  // every counted partial before the loads
-    const Acc s = system_sum<SLOTS>(rc, sys, type, sm);
-    if (threadIdx.x == 0) {
-        op.scalar(sys, s);
-        rc.cnt[sys] = 0u;
-    }
-}
-
-// The fused finish of a group (every thread of the block calls it after
-// group_partial): count the group; the block that completes system sys
-// sums its partials, runs op.scalar and rearms the count for the next launch.
-template <int SLOTS, class Op>
-__device__ __forceinline__ void group_done(Op &op, int sys, const RedCtx &rc, int type, double *sm)
-{
-    __shared__ int s_last;
-    if (threadIdx.x == 0) {
-        __threadfence();  // this group's partial before its count
-        const unsigned groups = (unsigned)(rc.sys_group[sys + 1] - rc.sys_group[sys]);
-        s_last = atomicAdd(rc.cnt + sys, 1u) + 1u == groups;
-    }
-    __syncthreads();
-    if (s_last) system_finish<SLOTS>(op, sys, rc, type, sm);
-}
-
-// EMPTY: only the systems without a group (the fused form never reaches them).
-namespace {
-template <class Op, bool EMPTY = false>
-__global__ void __launch_bounds__(kBlock) k_finalize(Op op, RedCtx rc, int type)
-{
-    constexpr int SLOTS = OpSlots<Op>::value;
-    __shared__ double sm[kParts * kBlock];
-    const int sys = blockIdx.x;
-    if (EMPTY && rc.sys_group[sys] != rc.sys_group[sys + 1]) return;
-    if (!op.active(sys)) return;
-    const Acc s = system_sum<SLOTS>(rc, sys, type, sm);
     if (threadIdx.x == 0) op.scalar(sys, s);
 }
 }  // namespace

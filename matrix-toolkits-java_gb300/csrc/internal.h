@@ -145,8 +145,7 @@ struct MonCfgDev {
 // systems (groups of system s are [sys_group[s], sys_group[s+1])).
 struct RedCtx {
     double *part;          // [num_groups * kParts]
-    unsigned *cnt;         // [num_sys] group partials stored so far in the running launch
-                           // (zero between launches); nullptr: a k_finalize launch sums
+    unsigned *cnt;         // [num_sys] (unused on the hot path)
     const int *sys_group;  // [num_sys + 1]
     int *num_running;      // number of systems with status RUNNING
 };
@@ -168,7 +167,6 @@ struct TileSet {
     // device [num_tiles]: (lanes per row << 1) | 1 if the tile is a single long row
     unsigned char *tile_flags = nullptr;
     int vec_mask = 0;          // OR of the lanes-per-row classes of the tiles
-    int empty_sys = 0;         // systems without a group (their sums are zero)
     std::vector<int> h_tile_row;
 };
 

@@ -833,7 +833,6 @@ extern "C" int mtjg_server_create(mtjg_ctx *ctx, const mtjg_server_config *cfg, 
     S->slot_req.assign(ns, nullptr);
     cudaMemcpy(S->st, empty.data(), sizeof(SysState) * ns, cudaMemcpyHostToDevice);
     cudaMemset(S->num_running, 0, sizeof(int) * 4);
-    cudaMemset(S->cnt, 0, sizeof(unsigned) * ns);  // the fused reductions' group counts
     S->free_seg[0] = (int)cfg->pool_rows;
     S->th = std::thread(scheduler, S);
     *out = S;

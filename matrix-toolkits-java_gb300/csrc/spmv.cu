@@ -71,8 +71,6 @@ int upload_tiles(TileSet &ts, const std::vector<int> &tile_row, const std::vecto
         sys_group.push_back((int)group_tile.size());
     }
     ts.num_groups = (int)group_tile.size();
-    ts.empty_sys = 0;
-    for (int q = 0; q < ts.num_sys; ++q) ts.empty_sys += sys_group[q + 1] == sys_group[q];
     std::vector<int> group_info(std::max<size_t>(1, group_tile.size()));
     for (int s = 0, g = 0; s < ts.num_sys; ++s)
         for (; g < sys_group[s + 1]; ++g) group_info[g] = (s << 8) | (tile_flags[group_tile[g]] >> 1);

@@ -476,7 +476,6 @@ __global__ void __launch_bounds__(kBlock, EpiCtas<Epi>::value)
             if constexpr (Epi::kReduce) {
                 group_partial<OpSlots<Epi>::value>(acc, g, rc, normtype, red_sm);
                 acc_zero(acc);
-                if (rc.cnt) group_done<OpSlots<Epi>::value>(epi, ta.group_info[g] >> 8, rc, normtype, red_sm);
             }
         }
         s = s + 1 == NST ? 0 : s + 1;
@@ -537,10 +536,7 @@ __global__ void __launch_bounds__(kBlock, OpMinBlocks<Op>::value) k_rows(TileArg
 #pragma unroll 2
         for (int r = r0 + (int)threadIdx.x; r < r1; r += kBlock) op.row(r, sys, acc);
     }
-    if constexpr (Op::kReduce) {
-        group_partial<OpSlots<Op>::value>(acc, t, rc, normtype, red_sm);
-        if (rc.cnt) group_done<OpSlots<Op>::value>(op, sys, rc, normtype, red_sm);
-    }
+    if constexpr (Op::kReduce) group_partial<OpSlots<Op>::value>(acc, t, rc, normtype, red_sm);
 }
 
 inline TileArgs tile_args(const TileSet &ts)
@@ -559,17 +555,10 @@ inline TileArgs tile_args(const TileSet &ts)
                     ts.sd};
 }
 
-// The reduction's finish after a phase's kernel: all of it without a
-// counter array, else only the systems without a group (if any).
 template <class Op>
 cudaError_t launch_finalize(mtjg_ctx *ctx, const TileSet &ts, const Op &op, const RedCtx &rc, int normtype)
 {
-    if (!rc.cnt)
-        k_finalize<Op><<<ts.num_sys, kBlock, 0, ctx->stream>>>(op, rc, normtype);
-    else if (ts.empty_sys > 0)
-        k_finalize<Op, true><<<ts.num_sys, kBlock, 0, ctx->stream>>>(op, rc, normtype);
-    else
-        return cudaSuccess;
+    k_finalize<Op><<<ts.num_sys, kBlock, 0, ctx->stream>>>(op, rc, normtype);
     ctx->launches++;
     return cudaGetLastError();
 }
