@@ -419,13 +419,16 @@ def serve_backlog(ctx, mats, reqs, steps, warmup, max_systems, pool_rows, inner_
     return times, results, rhs, stats, launches
 
 
-def serve_open_loop(ctx, mats, reqs, max_systems, pool_rows, inner_rtol, rate=SERVE_RATE, budget=0):
+def serve_open_loop(ctx, mats, reqs, max_systems, pool_rows, inner_rtol, rate=SERVE_RATE, budget=0, gmres_every=0,
+                    gmres_mats=frozenset()):
     """The arrival stream end to end through the public API: a new matrix
     is registered when its first request arrives, each request is submitted
     at its arrival time (or as soon as the client is free), and latency runs
     from the scheduled arrival to the result being on the host.  `rate`
     rescales the stream's arrival times to that mean rate; `budget` is the
-    server's matrix budget in bytes (0: every matrix stays resident)."""
+    server's matrix budget in bytes (0: every matrix stays resident);
+    `gmres_every` = k sends every k-th request on a matrix in `gmres_mats` to
+    the Krylov lane as GMRES."""
     from mtjg import serve
     srv = serve.Server(ctx, max_systems=max_systems, pool_rows=pool_rows, max_iter=100, rtol=RTOL,
                        inner_rtol=inner_rtol, matrix_budget=budget)
@@ -433,14 +436,14 @@ def serve_open_loop(ctx, mats, reqs, max_systems, pool_rows, inner_rtol, rate=SE
     reqs = [(ta * scale, m, s, new) for ta, m, s, new in reqs]
     rhs = [_rhs(mats[m][0], s) for _, m, s, _ in reqs]
     ids = {}
-    arrival_of, lat = {}, []
+    arrival_of, lat, lat_g, gm = {}, [], [], set()
     h2d = d2h = 0
     t0 = time.perf_counter()
 
     def collect():
         now = time.perf_counter() - t0
         for r in srv.poll(cap=4096):
-            lat.append(now - arrival_of.pop(r.ticket))
+            (lat_g if r.ticket in gm else lat).append(now - arrival_of.pop(r.ticket))
 
     for k, (ta, m, _, _) in enumerate(reqs):
         while time.perf_counter() - t0 < ta:
@@ -449,7 +452,10 @@ def serve_open_loop(ctx, mats, reqs, max_systems, pool_rows, inner_rtol, rate=SE
             n, rp, ci, v = mats[m]
             ids[m] = srv.addMatrix(n, rp, ci, v)
             h2d += 4 * (n + 1) + 12 * len(ci)
-        t = srv.submit(ids[m], rhs[k])
+        g = gmres_every > 0 and m in gmres_mats and k % gmres_every == gmres_every - 1
+        t = srv.submit(ids[m], rhs[k], solver="gmres" if g else "cg")
+        if g:
+            gm.add(t)
         arrival_of[t] = ta
         h2d += 8 * mats[m][0]
         d2h += 8 * mats[m][0]
@@ -460,10 +466,14 @@ def serve_open_loop(ctx, mats, reqs, max_systems, pool_rows, inner_rtol, rate=SE
     res = srv.residency()
     srv.close()
     lat = np.array(lat)
-    return {"wall_s": wall, "solves_s": len(reqs) / wall, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
-            "p99_ms": 1e3 * float(np.percentile(lat, 99)), "h2d_bytes": h2d, "d2h_bytes": d2h,
-            "offered_rate": rate, "uploads": res["uploads"], "evictions": res["evictions"],
-            "matrix_budget": budget}
+    out = {"wall_s": wall, "solves_s": len(reqs) / wall, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+           "p99_ms": 1e3 * float(np.percentile(lat, 99)), "h2d_bytes": h2d, "d2h_bytes": d2h,
+           "offered_rate": rate, "uploads": res["uploads"], "evictions": res["evictions"],
+           "matrix_budget": budget}
+    if lat_g:
+        out["gmres"] = {"requests": len(lat_g), "p50_ms": 1e3 * float(np.percentile(lat_g, 50)),
+                        "p99_ms": 1e3 * float(np.percentile(lat_g, 99))}
+    return out
 
 
 def plain_fp64(ctx, mats, reqs, budget_s):
@@ -733,6 +743,10 @@ def main_serve(args):
     low = serve_open_loop(ctx, mats, reqs, *knobs, rate=args.serve_low_rate)
     budget = int(args.serve_matrix_budget * (1 << 30))
     tight = serve_open_loop(ctx, mats, reqs, *knobs, rate=args.serve_low_rate, budget=budget)
+    # GMRES(30) + Jacobi on the stream's Laplacians (the Poisson grids need
+    # thousands of restarted iterations without a stronger preconditioner)
+    lap = frozenset(i for i, sp in enumerate(specs) if sp[0] == "laplacian")
+    with_gmres = serve_open_loop(ctx, mats, reqs, *knobs, rate=args.serve_low_rate, gmres_every=5, gmres_mats=lap)
     stream_bytes = sum(16 * len(mats[m][2]) + 8 * mats[m][0] for m in {m for _, m, _, _ in reqs})
     plain = plain_fp64(ctx, mats, reqs, args.plain_budget)
     sec = statistics.mean(times)
@@ -775,7 +789,12 @@ def main_serve(args):
                                                       "evictions")},
                               "budget_bytes": budget, "stream_matrix_bytes": stream_bytes,
                               "what": "below-capacity load with resident matrices held to the budget: idle "
-                                      "matrices evicted LRU and uploaded again on their next request"}},
+                                      "matrices evicted LRU and uploaded again on their next request"},
+            "with_gmres": {**{k: with_gmres[k] for k in ("offered_rate", "p50_ms", "p99_ms", "solves_s")},
+                           "gmres": with_gmres.get("gmres"),
+                           "what": "below-capacity load with every 5th request on a Laplacian a mixed-precision "
+                                   "GMRES(30) + Jacobi solve on the Krylov lane; p50/p99 of the CG requests, and of "
+                                   "the GMRES ones apart"}},
         "plain_fp64": {"solves_s": plain_rate, "requests": len(plain),
                        "mean_iterations": float(np.mean([it for _, _, it in plain])),
                        "what": "CG + DiagonalPreconditioner FP64, one request at a time through the host API"},

@@ -406,6 +406,15 @@ MTJG_API int mtjg_server_remove_matrix(mtjg_server *S, int matrix_id);
  * reported by mtjg_server_poll. */
 MTJG_API int mtjg_server_submit(mtjg_server *S, int matrix_id, const double *b, const double *x0,
                                 double *x_out, int64_t *ticket);
+/* mtjg_server_submit with a choice of solver: MTJG_CG (the batched lane
+ * above), or MTJG_GMRES / MTJG_BICGSTAB, which a second lane solves one at a
+ * time on its own stream -- mixed-precision GMRES(30) or BiCGstab with the
+ * Jacobi preconditioner and the server's monitor and inner settings, as
+ * mtjg_solver_solve would -- on the resident matrix, pinned for the solve
+ * under the same matrix budget, concurrently with the CG batch.  Other
+ * solvers are MTJG_ERR_UNSUPPORTED. */
+MTJG_API int mtjg_server_submit_solver(mtjg_server *S, int matrix_id, int solver, const double *b,
+                                       const double *x0, double *x_out, int64_t *ticket);
 /* Finished requests since the last poll (non-blocking). */
 MTJG_API int mtjg_server_poll(mtjg_server *S, mtjg_server_result *out, int cap, int *count);
 /* Waits until every submitted request has finished (or the timeout). */

@@ -5,6 +5,11 @@
 
 Translation units compile in parallel; the whole build takes well under a
 minute.  Run as ``python build.py`` or through ``build()``.
+
+MTJG_BUILD_DEFINES (environment) adds -D flags to every translation unit,
+for the build-time tuning knobs of csrc/internal.h and csrc/spmv.cuh, e.g.
+``MTJG_BUILD_DEFINES="-DMTJG_TILE_ROWS=512 -DMTJG_TILE_NNZ=2304"``; objects
+built with other defines are rebuilt.
 """
 from __future__ import annotations
 
@@ -56,7 +61,10 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
     os.makedirs(OBJ, exist_ok=True)
     # objects built on another host architecture are never reused
     stamp = os.path.join(OBJ, "ARCH")
-    arch = platform.machine()
+    defines = os.environ.get("MTJG_BUILD_DEFINES", "").split()
+    if any(not d.startswith("-D") for d in defines):
+        raise RuntimeError("MTJG_BUILD_DEFINES takes -D flags only")
+    arch = " ".join([platform.machine()] + defines)
     if not os.path.exists(stamp) or open(stamp).read().strip() != arch:
         for f in os.listdir(OBJ):
             os.remove(os.path.join(OBJ, f))
@@ -77,7 +85,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
             continue
         cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr",
-               "-I", CSRC, "-I", INCLUDE, "-c", path, "-o", obj]
+               *defines, "-I", CSRC, "-I", INCLUDE, "-c", path, "-o", obj]
         if ptxas_info:
             cmd.insert(1, "-Xptxas=-v")
         jobs.append(cmd)
@@ -87,7 +95,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
         objs.append(obj)
         if _newer(obj, [path] + headers):
             continue
-        jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fvisibility=hidden",
+        jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fvisibility=hidden", *defines,
                      "-I", os.path.join(cuda, "include"), "-I", CSRC, "-I", INCLUDE,
                      "-c", path, "-o", obj])
     with ThreadPoolExecutor(max_workers=max(1, min(8, len(jobs)))) as ex:

@@ -225,6 +225,7 @@ struct mtjg_csr {
     int *num_running = nullptr;
     // staging vectors for host-pointer calls
     double *d_x = nullptr, *d_y = nullptr;
+    bool borrowed = false;     // rowptr, colind, val, val32 belong to someone else (csr_borrow)
 };
 
 struct mtjg_precond {

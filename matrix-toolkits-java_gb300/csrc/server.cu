@@ -17,6 +17,12 @@
 // cannot be made resident (the budget is held by matrices in use) waits at
 // the head of the queue.
 //
+// GMRES and BiCGstab requests take a second lane: a worker thread with its
+// own stream solves them one at a time (mixed-precision GMRES(30) or
+// BiCGstab with the Jacobi preconditioner, through the solver's own code)
+// on the resident matrix, pinned for the solve under the same budget, while
+// the CG batch runs on the scheduler's stream.
+//
 // The scheduler keeps two chunks queued on its stream: while the GPU runs
 // chunk k+1, the host reads chunk k's statuses, retires finished systems,
 // admits new ones and rebuilds the tile tables.  Everything the host hands
@@ -40,6 +46,10 @@
 #include "phases.cuh"
 
 namespace mtjg {
+// A CSR handle over a served matrix's device arrays (spmv.cu).
+int csr_borrow(mtjg_ctx *ctx, int n, const int *h_rowptr, const int *d_rowptr, const int *d_colind,
+               const double *d_val, const float *d_val32, mtjg_csr **out);
+
 namespace {
 
 // Product tiles of one matrix (host copies).
@@ -104,7 +114,8 @@ struct ResMat {
     std::vector<double> h_val;            // (kept only by servers with a matrix budget)
     ProdTiles t64, t32;  // product tiles for FP64 and FP32 values (local rows and entries)
     bool resident = false;  // dev holds the matrix
-    bool loading = false;   // picked for upload by the scheduler, not yet attached
+    bool loading = false;   // picked for upload, not yet attached
+    int loader = 0;         // who is uploading it: 1 the scheduler, 2 the Krylov lane
     int busy = 0;           // systems admitted and not yet delivered: the device copy stays
     int64_t last_use = 0;   // LRU clock at the last admission or delivery
     int uses = 0;           // requests submitted and not yet delivered
@@ -170,6 +181,7 @@ int upload_matrix(mtjg_ctx *u, const ResMat *m, const int *rowptr, const int *co
 struct Req {
     int64_t ticket = 0;
     int mid = 0;
+    int kind = MTJG_CG;     // MTJG_CG: the batched lane; MTJG_GMRES / MTJG_BICGSTAB: the Krylov lane
     ResMat *mat = nullptr;  // fixed at submission (the matrix table may grow meanwhile)
     std::vector<double> b, x0;
     double *x_out = nullptr;
@@ -236,6 +248,7 @@ struct mtjg_server {
     mtjg_ctx *ctx = nullptr;   // the scheduler's own context (own stream), on the caller's device
     mtjg_ctx *uctx = nullptr;  // matrix registration (own stream, so uploads never wait for chunks)
     mtjg_ctx *lctx = nullptr;  // the scheduler's uploads of evicted matrices
+    mtjg_ctx *kctx = nullptr;  // the Krylov lane (GMRES / BiCGstab requests): own stream
     std::mutex up_mu;          // registering threads share uctx
     mtjg_server_config cfg{};
     std::vector<ResMat *> mats;
@@ -271,6 +284,9 @@ struct mtjg_server {
     std::mutex mu;
     std::condition_variable cv, cv_done;
     std::deque<Req *> pending;
+    std::deque<Req *> lane_pending;  // GMRES / BiCGstab requests, FIFO
+    std::condition_variable lane_cv;
+    std::thread lane;
     std::deque<mtjg_server_result> done;
     int64_t next_ticket = 1;
     int64_t inflight = 0;
@@ -665,11 +681,15 @@ void scheduler(mtjg_server *S)
                         break;
                     }
                 if (slot < 0) break;
-                if (!m->resident && !m->loading) {
-                    if (!make_room(S, m->bytes, evict)) break;
-                    m->loading = true;
-                    S->resident_bytes += m->bytes;
-                    load.push_back(m);
+                if (!m->resident) {
+                    if (m->loading && m->loader != 1) break;  // the Krylov lane is uploading it
+                    if (!m->loading) {
+                        if (!make_room(S, m->bytes, evict)) break;
+                        m->loading = true;
+                        m->loader = 1;
+                        S->resident_bytes += m->bytes;
+                        load.push_back(m);
+                    }
                 }
                 const int voff = seg_alloc(S, n);
                 if (voff < 0) break;
@@ -760,6 +780,140 @@ void scheduler(mtjg_server *S)
     }
 }
 
+constexpr int kLaneRestart = 30;
+
+// One GMRES / BiCGstab request on the resident matrix: mixed precision with
+// the Jacobi preconditioner and the server's monitor and inner settings,
+// through the solver used by mtjg_solver_solve (so the result is what a lone
+// solve with these settings gives).
+int lane_solve(mtjg_server *S, const Req *r, std::vector<double> &x, mtjg_result &res)
+{
+    mtjg_ctx *c = S->kctx;
+    const ResMat *m = r->mat;
+    const int n = m->n;
+    mtjg_csr *A = nullptr;
+    mtjg_precond *M = nullptr;
+    mtjg_solver *sol = nullptr;
+    int st = csr_borrow(c, n, m->h_rowptr.data(), m->dev.rowptr, m->dev.colind, m->dev.val, m->dev.val32, &A);
+    int err_row = 0;
+    if (st == MTJG_OK) st = mtjg_precond_create(c, MTJG_PC_JACOBI, n, &M);
+    if (st == MTJG_OK) st = mtjg_precond_set_matrix(M, A, &err_row);
+    if (st == MTJG_OK) st = mtjg_solver_create(c, r->kind, n, kLaneRestart, &sol);
+    if (st == MTJG_OK) st = mtjg_solver_set_precond(sol, M);
+    mtjg_monitor mon;
+    mtjg_monitor_defaults(&mon);
+    mon.max_iter = S->cfg.max_iter;
+    mon.rtol = S->cfg.rtol;
+    mon.atol = S->cfg.atol;
+    mon.dtol = S->cfg.dtol;
+    if (st == MTJG_OK) st = mtjg_solver_set_monitor(sol, &mon);
+    if (st == MTJG_OK) st = mtjg_solver_set_mixed(sol, 1, S->cfg.inner_rtol, S->cfg.inner_max_iter);
+    if (r->x0.empty())
+        x.assign((size_t)n, 0.0);
+    else
+        x = r->x0;
+    std::memset(&res, 0, sizeof(res));
+    if (st == MTJG_OK) st = mtjg_solver_solve(sol, A, r->b.data(), x.data(), &res);
+    mtjg_solver_destroy(sol);
+    mtjg_precond_destroy(M);
+    mtjg_csr_destroy(A);
+    return st;
+}
+
+// The Krylov lane: makes each request's matrix resident (evicting idle ones
+// under the budget, as the scheduler does), pins it, solves, delivers.
+void lane_worker(mtjg_server *S)
+{
+    cudaSetDevice(S->kctx->device);
+    std::vector<double> x;
+    for (;;) {
+        Req *r = nullptr;
+        {
+            std::unique_lock<std::mutex> lk(S->mu);
+            S->lane_cv.wait(lk, [&] { return S->stop || S->error != MTJG_OK || !S->lane_pending.empty(); });
+            if (S->stop || S->error != MTJG_OK) return;
+            r = S->lane_pending.front();
+            S->lane_pending.pop_front();
+        }
+        ResMat *m = r->mat;
+        std::vector<DevMat> evict;
+        bool load = false;
+        for (;;) {
+            std::unique_lock<std::mutex> lk(S->mu);
+            if (S->stop || S->error != MTJG_OK) {
+                delete r;
+                return;
+            }
+            if (m->resident) {
+                m->busy++;
+                break;
+            }
+            if (!m->loading && make_room(S, m->bytes, evict)) {
+                m->loading = true;
+                m->loader = 2;
+                m->busy++;
+                S->resident_bytes += m->bytes;
+                load = true;
+                break;
+            }
+            // being uploaded by the scheduler, or the budget is held by busy matrices
+            S->lane_cv.wait_for(lk, std::chrono::milliseconds(1));
+        }
+        r->t_admit = S->now();
+        for (DevMat &d : evict) d.release();
+        if (load) {
+            DevMat d;
+            const int ust = upload_matrix(S->kctx, m, m->h_rowptr.data(), m->h_colind.data(), m->h_val.data(), d);
+            if (ust != MTJG_OK) {
+                fail_all(S, ust, mtjg_last_error());
+                delete r;
+                return;
+            }
+            std::lock_guard<std::mutex> lk(S->mu);
+            m->dev = d;
+            m->resident = true;
+            m->loading = false;
+            m->loader = 0;
+            S->uploads++;
+        }
+        mtjg_result res;
+        const int st = lane_solve(S, r, x, res);
+        if (st >= MTJG_ERR_CUDA) {
+            fail_all(S, st, mtjg_last_error());
+            std::lock_guard<std::mutex> lk(S->mu);
+            m->busy--;
+            delete r;
+            return;
+        }
+        ResMat *release = nullptr;
+        {
+            std::lock_guard<std::mutex> lk(S->mu);
+            std::memcpy(r->x_out, x.data(), sizeof(double) * (size_t)m->n);
+            mtjg_server_result out;
+            std::memset(&out, 0, sizeof(out));
+            out.ticket = r->ticket;
+            out.matrix = r->mid;
+            out.result = res;
+            out.result.status = st;
+            out.latency_s = S->now() - r->t_submit;
+            out.queue_s = r->t_admit - r->t_submit;
+            S->done.push_back(out);
+            m->busy--;
+            m->last_use = ++S->use_clock;
+            if (--m->uses == 0 && m->removed) {
+                release = m;
+                S->mats[r->mid] = nullptr;
+                if (m->resident) S->resident_bytes -= m->bytes;
+            }
+            S->admitted++;
+            S->inflight--;
+            S->cv_done.notify_all();
+        }
+        if (release) free_matrix(release);
+        delete r;
+    }
+}
+
 }  // namespace
 
 extern "C" void mtjg_server_config_defaults(mtjg_server_config *cfg)
@@ -786,20 +940,23 @@ extern "C" int mtjg_server_create(mtjg_ctx *ctx, const mtjg_server_config *cfg, 
     MTJG_CUDA(cudaSetDevice(ctx->device));
     // the scheduler thread and matrix registration work on streams of their
     // own, so the caller's context stays free for other work
-    mtjg_ctx *own = nullptr, *up = nullptr, *ld = nullptr;
+    mtjg_ctx *own = nullptr, *up = nullptr, *ld = nullptr, *kr = nullptr;
     int cst = mtjg_ctx_create(ctx->device, &own);
     if (cst != MTJG_OK) return cst;
     cst = mtjg_ctx_create(ctx->device, &up);
     if (cst == MTJG_OK) cst = mtjg_ctx_create(ctx->device, &ld);
+    if (cst == MTJG_OK) cst = mtjg_ctx_create(ctx->device, &kr);
     if (cst != MTJG_OK) {
         mtjg_ctx_destroy(own);
         if (up) mtjg_ctx_destroy(up);
+        if (ld) mtjg_ctx_destroy(ld);
         return cst;
     }
     mtjg_server *S = new mtjg_server();
     S->ctx = own;
     S->uctx = up;
     S->lctx = ld;
+    S->kctx = kr;
     S->cfg = *cfg;
     S->t0 = std::chrono::steady_clock::now();
     const size_t P = (size_t)cfg->pool_rows, ns = (size_t)cfg->max_systems;
@@ -835,6 +992,7 @@ extern "C" int mtjg_server_create(mtjg_ctx *ctx, const mtjg_server_config *cfg, 
     cudaMemset(S->num_running, 0, sizeof(int) * 4);
     S->free_seg[0] = (int)cfg->pool_rows;
     S->th = std::thread(scheduler, S);
+    S->lane = std::thread(lane_worker, S);
     *out = S;
     return MTJG_OK;
 }
@@ -872,8 +1030,8 @@ extern "C" int mtjg_server_add_matrix(mtjg_server *S, int n, const int *rowptr, 
         }
         m->inv32[(size_t)i] = (float)(1 / d);
     }
+    m->h_rowptr.assign(rowptr, rowptr + n + 1);  // the Krylov lane's tiles
     if (B > 0) {
-        m->h_rowptr.assign(rowptr, rowptr + n + 1);
         m->h_colind.assign(colind, colind + m->nnz);
         m->h_val.assign(val, val + m->nnz);
     }
@@ -911,8 +1069,17 @@ extern "C" int mtjg_server_add_matrix(mtjg_server *S, int n, const int *rowptr, 
 extern "C" int mtjg_server_submit(mtjg_server *S, int matrix_id, const double *b, const double *x0, double *x_out,
                                   int64_t *ticket)
 {
+    return mtjg_server_submit_solver(S, matrix_id, MTJG_CG, b, x0, x_out, ticket);
+}
+
+extern "C" int mtjg_server_submit_solver(mtjg_server *S, int matrix_id, int solver, const double *b,
+                                         const double *x0, double *x_out, int64_t *ticket)
+{
     if (!S || !b || !x_out || !ticket) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL argument");
+    if (solver != MTJG_CG && solver != MTJG_GMRES && solver != MTJG_BICGSTAB)
+        return fail(MTJG_ERR_UNSUPPORTED, "the server solves with CG, GMRES or BiCGstab");
     Req *r = new Req();
+    r->kind = solver;
     {
         std::lock_guard<std::mutex> lk(S->mu);
         if (S->error != MTJG_OK) {
@@ -934,10 +1101,13 @@ extern "C" int mtjg_server_submit(mtjg_server *S, int matrix_id, const double *b
         r->t_submit = S->now();
         r->ticket = S->next_ticket++;
         *ticket = r->ticket;
-        S->pending.push_back(r);
+        (solver == MTJG_CG ? S->pending : S->lane_pending).push_back(r);
         S->inflight++;
     }
-    S->cv.notify_one();
+    if (solver == MTJG_CG)
+        S->cv.notify_one();
+    else
+        S->lane_cv.notify_one();
     return MTJG_OK;
 }
 
@@ -1042,10 +1212,13 @@ extern "C" int mtjg_server_destroy(mtjg_server *S)
         S->stop = true;
     }
     S->cv.notify_all();
+    S->lane_cv.notify_all();
     if (S->th.joinable()) S->th.join();
+    if (S->lane.joinable()) S->lane.join();
     cudaSetDevice(S->ctx->device);
     cudaStreamSynchronize(S->ctx->stream);
     for (Req *r : S->pending) delete r;
+    for (Req *r : S->lane_pending) delete r;
     for (Req *r : S->slot_req) delete r;
     for (ResMat *m : S->mats)
         if (m) free_matrix(m);
@@ -1073,10 +1246,11 @@ extern "C" int mtjg_server_destroy(mtjg_server *S)
         if (S->ev_done[p]) cudaEventDestroy(S->ev_done[p]);
         if (S->ev_ret[p]) cudaEventDestroy(S->ev_ret[p]);
     }
-    mtjg_ctx *ctx = S->ctx, *u = S->uctx, *ld = S->lctx;
+    mtjg_ctx *ctx = S->ctx, *u = S->uctx, *ld = S->lctx, *kr = S->kctx;
     delete S;
     mtjg_ctx_destroy(ctx);
     mtjg_ctx_destroy(u);
     mtjg_ctx_destroy(ld);
+    mtjg_ctx_destroy(kr);
     return MTJG_OK;
 }

@@ -516,6 +516,33 @@ int csr_adopt(mtjg_ctx *ctx, int n, int m, std::vector<int> &&h_rowptr, int *d_r
     *out = A;
     return MTJG_OK;
 }
+
+// A CSR handle over device arrays owned by someone else (a served matrix):
+// its tiles and scratch are its own, the arrays are not freed with it.
+int csr_borrow(mtjg_ctx *ctx, int n, const int *h_rowptr, const int *d_rowptr, const int *d_colind,
+               const double *d_val, const float *d_val32, mtjg_csr **out)
+{
+    *out = nullptr;
+    mtjg_csr *A = new mtjg_csr();
+    A->ctx = ctx;
+    ctx_retain(ctx);
+    A->borrowed = true;
+    A->n = n;
+    A->m = n;
+    A->nnz = h_rowptr[n];
+    A->h_rowptr.assign(h_rowptr, h_rowptr + n + 1);
+    A->rowptr = const_cast<int *>(d_rowptr);
+    A->colind = const_cast<int *>(d_colind);
+    A->val = const_cast<double *>(d_val);
+    A->val32 = const_cast<float *>(d_val32);
+    const int st = csr_finish(A, 1, nullptr);
+    if (st != MTJG_OK) {
+        mtjg_csr_destroy(A);
+        return st;
+    }
+    *out = A;
+    return MTJG_OK;
+}
 }  // namespace mtjg
 
 extern "C" int mtjg_csr_upload(mtjg_ctx *ctx, int n, int m, const int *rowptr, const int *colind,
@@ -535,6 +562,7 @@ extern "C" int mtjg_batch_upload(mtjg_ctx *ctx, int num_systems, const int *sys_
 extern "C" int mtjg_csr_update_values(mtjg_csr *A, const double *val)
 {
     if (!A || (!val && A->nnz)) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL argument");
+    if (A->borrowed) return fail(MTJG_ERR_UNSUPPORTED, "the matrix's values belong to a server");
     MTJG_CUDA(cudaSetDevice(A->ctx->device));
     MTJG_CUDA(cudaStreamSynchronize(A->ctx->stream));
     if (A->nnz) MTJG_CUDA(cudaMemcpy(A->val, val, sizeof(double) * (size_t)A->nnz, cudaMemcpyHostToDevice));
@@ -558,15 +586,17 @@ extern "C" int mtjg_csr_destroy(mtjg_csr *A)
     if (!A) return MTJG_OK;
     if (A->ctx) cudaSetDevice(A->ctx->device);
     if (A->ctx) cudaStreamSynchronize(A->ctx->stream);
-    cudaFree(A->rowptr);
-    cudaFree(A->colind);
-    cudaFree(A->val);
+    if (!A->borrowed) {
+        cudaFree(A->rowptr);
+        cudaFree(A->colind);
+        cudaFree(A->val);
+        cudaFree(A->val32);
+    }
     cudaFree(A->t_rowptr);
     cudaFree(A->t_colind);
     cudaFree(A->t_val);
     cudaFree(A->t_part);
     cudaFree(A->d_sys_rows);
-    cudaFree(A->val32);
     cudaFree(A->part);
     cudaFree(A->cnt);
     cudaFree(A->num_running);

@@ -130,6 +130,7 @@ PROTOTYPES = {
     "mtjg_server_add_matrix": (C.c_int, [_vp, C.c_int, _ip, _ip, _dp, _ip]),
     "mtjg_server_remove_matrix": (C.c_int, [_vp, C.c_int]),
     "mtjg_server_submit": (C.c_int, [_vp, C.c_int, _dp, _dp, _dp, C.POINTER(C.c_int64)]),
+    "mtjg_server_submit_solver": (C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp, _dp, C.POINTER(C.c_int64)]),
     "mtjg_server_poll": (C.c_int, [_vp, C.POINTER(ServerResult), C.c_int, _ip]),
     "mtjg_server_drain": (C.c_int, [_vp, C.c_double]),
     "mtjg_server_stats": (C.c_int, [_vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64),

@@ -7,7 +7,10 @@
     srv.drain(); srv.close()
 
 Each request is solved by mixed-precision CG + Jacobi (FP64 refinement,
-FP32 inner iterations) to `rtol` on the FP64 true residual.  With a
+FP32 inner iterations) to `rtol` on the FP64 true residual; requests
+submitted with solver="gmres" or "bicgstab" take a second lane
+(mixed-precision GMRES(30) / BiCGstab + Jacobi, one at a time on its own
+stream, concurrently with the CG batch).  With a
 `matrix_budget` (bytes) the resident matrices are evicted least recently used
 when idle and uploaded again on their next request.  No counterpart in the
 reference.
@@ -67,7 +70,11 @@ class Server:
         _raise(self._lib.mtjg_server_remove_matrix(self.h, int(mid)), "remove_matrix")
         self.sizes.pop(mid, None)
 
-    def submit(self, mid: int, b, x0=None) -> int:
+    SOLVERS = {"cg": L.CG, "gmres": L.GMRES, "bicgstab": L.BICGSTAB}
+
+    def submit(self, mid: int, b, x0=None, solver: str = "cg") -> int:
+        """Queues a solve; solver "cg" joins the batched lane, "gmres" and
+        "bicgstab" the Krylov lane (mtjg_server_submit_solver)."""
         n = self.sizes[mid]
         b = L.f64(b)
         if b.shape != (n,):
@@ -75,7 +82,8 @@ class Server:
         x = np.zeros(n)
         x0p = L.dptr(L.f64(x0)) if x0 is not None else None
         t = C.c_int64()
-        _raise(self._lib.mtjg_server_submit(self.h, mid, L.dptr(b), x0p, L.dptr(x), C.byref(t)), "submit")
+        _raise(self._lib.mtjg_server_submit_solver(self.h, mid, self.SOLVERS[solver], L.dptr(b), x0p, L.dptr(x),
+                                                   C.byref(t)), "submit")
         self._out[t.value] = (x, b)
         return t.value
 

@@ -249,3 +249,86 @@ def test_registration_checks(servers):
         bad = ci.copy()
         bad[rp[3]], bad[rp[3] + 1] = bad[rp[3] + 1], bad[rp[3]]
         srv2.addMatrix(n, rp, bad, v)
+
+
+def _direct_krylov(ctx, kind, mat, b):
+    """What a lone mtjg_solver_solve gives with the server's default settings:
+    mixed-precision GMRES(30) / BiCGstab + Jacobi, 100 refinements, rtol 1e-10,
+    inner_rtol 1e-6, 2000 inner iterations."""
+    from mtjg import sparse
+    n, rp, ci, v = mat
+    A = sparse.CompRowMatrix(n, n, rp, ci, v, ctx)
+    s = sparse.GMRES(n, restart=30, ctx=ctx) if kind == "gmres" else sparse.BiCGstab(n, ctx=ctx)
+    M = sparse.DiagonalPreconditioner(n, ctx)
+    M.setMatrix(A)
+    s.setPreconditioner(M)
+    s.setIterationMonitor(sparse.DefaultIterationMonitor(100, 1e-10, 1e-50, 1e5))
+    s.setMixedPrecision(True, 1e-6, 2000)
+    x = np.zeros(n)
+    s.solve(A, b, x)
+    return x, s.getIterationMonitor().iterations()
+
+
+def test_krylov_lane_in_the_mix(servers, ctx):
+    """GMRES and BiCGstab requests beside CG requests: each Krylov-lane result
+    equals a lone solver call with the same settings and the same request
+    served alone, bit for bit, and meets rtol on its FP64 residual; the CG
+    results equal their alone results too."""
+    mats = _library()
+    rng = np.random.default_rng(21)
+    reqs = []
+    for k in range(24):
+        m = int(rng.integers(0, len(mats)))
+        reqs.append((m, workloads.uniform(mats[m][0], 500 + k), ("cg", "gmres", "bicgstab")[k % 3]))
+    srv = servers(max_systems=64, pool_rows=1 << 20)
+    mids = [srv.addMatrix(*m) for m in mats]
+
+    def run(batch):
+        tickets = {srv.submit(mids[m], b, solver=kind): k for k, (m, b, kind) in batch}
+        srv.drain(300.0)
+        return {tickets[r.ticket]: r for r in srv.poll()}
+
+    mix = run(list(enumerate(reqs)))
+    assert len(mix) == len(reqs)
+    for k, (m, b, kind) in enumerate(reqs):
+        alone = run([(k, (m, b, kind))])[k]
+        got = mix[k]
+        assert got.status == 0 and alone.status == 0
+        assert np.array_equal(got.x, alone.x), (k, kind)
+        n, rp, ci, v = mats[m]
+        r = O.mult_add(O.Csr(n, n, rp, ci, v), -1.0, got.x, b)
+        assert np.linalg.norm(r) < 1e-10 * np.linalg.norm(b)
+        if kind != "cg" and k < 9:
+            xd, it = _direct_krylov(ctx, kind, mats[m], b)
+            assert np.array_equal(got.x, xd) and got.iterations == it
+
+
+def test_krylov_lane_under_a_matrix_budget(servers):
+    """GMRES requests on six matrices with room for two: matrices are evicted
+    and uploaded again, and the results equal those of an unlimited server."""
+    mats = _library()
+    sizes = _sizes(servers, mats)
+    reqs = [(k % len(mats), workloads.uniform(mats[k % len(mats)][0], 900 + k)) for k in range(12)]
+    out = []
+    for budget in (0, sorted(sizes)[-1] + sorted(sizes)[-2]):
+        srv = servers(max_systems=16, pool_rows=1 << 20, matrix_budget=budget)
+        mids = [srv.addMatrix(*m) for m in mats]
+        tickets = {srv.submit(mids[m], b, solver="gmres"): k for k, (m, b) in enumerate(reqs)}
+        srv.drain(300.0)
+        out.append(({tickets[r.ticket]: r for r in srv.poll()}, srv.residency()))
+    (free, _), (tight, res) = out
+    assert res["evictions"] > 0 and res["resident_bytes"] <= sorted(sizes)[-1] + sorted(sizes)[-2]
+    for k in range(len(reqs)):
+        assert free[k].status == 0 and np.array_equal(free[k].x, tight[k].x)
+
+
+def test_server_rejects_other_solvers(servers):
+    import ctypes as C
+    from mtjg import _lib as L
+    srv = servers(max_systems=4, pool_rows=1 << 14)
+    n, rp, ci, v = workloads.poisson2d(10)
+    mid = srv.addMatrix(n, rp, ci, v)
+    b, x = np.ones(n), np.zeros(n)
+    t = C.c_int64()
+    code = srv._lib.mtjg_server_submit_solver(srv.h, mid, L.QMR, L.dptr(b), None, L.dptr(x), C.byref(t))
+    assert code == L.ERR_UNSUPPORTED
