@@ -80,6 +80,54 @@ __device__ __forceinline__ T row_dot(const int *__restrict__ rp, const int *__re
     return sum;
 }
 
+// Build-time knobs: MTJG_BATCH_PAIR = 0 sums the two rows of a product step
+// one after the other; MTJG_BATCH_U is the rows per thread and step of the
+// element-wise loops (1: one row at a time).  Neither changes a result.
+#ifndef MTJG_BATCH_PAIR
+#define MTJG_BATCH_PAIR 1
+#endif
+#ifndef MTJG_BATCH_U
+#define MTJG_BATCH_U 4
+#endif
+
+// Rows ia and ib together (the same sums as two row_dot calls): their
+// gathers are in flight at once, so a thread waits one latency round for
+// both.  Each row keeps its entry order and its butterfly.
+template <int VEC, bool S, class T>
+__device__ __forceinline__ void row_dot2(const int *__restrict__ rp, const int *__restrict__ ci,
+                                         const T *__restrict__ v, const T *x, int ia, bool ina, int ib, bool inb,
+                                         int l, T &sa, T &sb)
+{
+    if constexpr (!MTJG_BATCH_PAIR) {
+        sa = row_dot<VEC, S>(rp, ci, v, x, ia, ina, l);
+        sb = row_dot<VEC, S>(rp, ci, v, x, ib, inb, l);
+        return;
+    }
+    T a = T(0), b = T(0);
+    const int ba = ina ? __ldg(rp + ia) : 0, la = ina ? __ldg(rp + ia + 1) - ba : 0;
+    const int bb = inb ? __ldg(rp + ib) : 0, lb = inb ? __ldg(rp + ib + 1) - bb : 0;
+    const int lm = la > lb ? la : lb;
+#pragma unroll 4
+    for (int k = l; k < lm; k += VEC) {
+        if (k < la) a = fmac<S>(__ldg(v + ba + k), x[__ldg(ci + ba + k)], a);
+        if (k < lb) b = fmac<S>(__ldg(v + bb + k), x[__ldg(ci + bb + k)], b);
+    }
+#pragma unroll
+    for (int off = VEC / 2; off > 0; off >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, off, VEC);
+        b += __shfl_xor_sync(0xffffffffu, b, off, VEC);
+    }
+    sa = a;
+    sb = b;
+}
+
+// Element-wise loops over a system's rows take kU rows per thread and step:
+// every load of the step is issued before its first store (the vectors may
+// alias, so the compiler cannot hoist them itself); rows are still visited,
+// and accumulated, in the order i = r0 + tid, r0 + tid + kBatchBlock, ...
+constexpr int kU = MTJG_BATCH_U;
+constexpr int kU2 = kU > 2 ? 2 : kU;  // the FP64 update loop, whose rows carry five doubles
+
 __device__ __forceinline__ int batch_check(const BatchCg &a, SysState &t, int sys, double r)
 {
     const size_t h = (size_t)sys * a.mon.hist_cap;
@@ -108,20 +156,24 @@ __device__ void cg_system(const BatchCg &a, int sys, Shared &sh)
     const double *inv = a.invdiag;
     Acc acc;
     acc_zero(acc);
-    for (int base = r0; base < r1; base += RPS) {  // r = b - A x; z = M r; |r|; r.z
-        const int i = base + g;
-        const bool in = i < r1;
-        const double d = row_dot<VEC, S>(a.rowptr, a.colind, a.val, (const double *)x, i, in, l);
-        if (in && l == 0) {
-            const double rr = a.b[i] - d;
-            r[i] = rr;
-            norm_add<S>(acc, rr, nt);
-            if (jac) {
-                const double zz = rr * inv[i];
-                z[i] = zz;
-                acc.v[2] = fmac<S>(rr, zz, acc.v[2]);
-            } else {
-                acc.v[2] = fmac<S>(rr, rr, acc.v[2]);
+    for (int base = r0; base < r1; base += 2 * RPS) {  // r = b - A x; z = M r; |r|; r.z
+        double dv[2];
+        row_dot2<VEC, S>(a.rowptr, a.colind, a.val, (const double *)x, base + g, base + g < r1, base + RPS + g,
+                         base + RPS + g < r1, l, dv[0], dv[1]);
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int i = base + u * RPS + g;
+            if (i < r1 && l == 0) {
+                const double rr = a.b[i] - dv[u];
+                r[i] = rr;
+                norm_add<S>(acc, rr, nt);
+                if (jac) {
+                    const double zz = rr * inv[i];
+                    z[i] = zz;
+                    acc.v[2] = fmac<S>(rr, zz, acc.v[2]);
+                } else {
+                    acc.v[2] = fmac<S>(rr, rr, acc.v[2]);
+                }
             }
         }
     }
@@ -140,18 +192,34 @@ __device__ void cg_system(const BatchCg &a, int sys, Shared &sh)
     while (sh.status == ST_RUNNING) {
         const bool first = sh.iter == 0;
         const double beta = sh.sc[1];
-        for (int i = r0 + tid; i < r1; i += kBatchBlock)  // p = z or p = beta p + z
-            p[i] = first ? z[i] : fmac<S>(p[i], beta, z[i]);
+        for (int base = r0 + tid; base < r1; base += kU * kBatchBlock) {  // p = z or p = beta p + z
+            double zv[kU], pv[kU];
+#pragma unroll
+            for (int u = 0; u < kU; ++u) {
+                const int i = base + u * kBatchBlock;
+                zv[u] = i < r1 ? z[i] : 0.0;
+                pv[u] = i < r1 && !first ? p[i] : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < kU; ++u) {
+                const int i = base + u * kBatchBlock;
+                if (i < r1) p[i] = first ? zv[u] : fmac<S>(pv[u], beta, zv[u]);
+            }
+        }
         __syncthreads();
         acc_zero(acc);
-        for (int base = r0; base < r1; base += RPS) {  // q = A p; p.q
-            const int i = base + g;
-            const bool in = i < r1;
-            const double d = row_dot<VEC, S>(a.rowptr, a.colind, a.val, (const double *)p, i, in, l);
-            if (in && l == 0) {
-                const double qq = mtj_assign(d);
-                q[i] = qq;
-                acc.v[2] = fmac<S>(p[i], qq, acc.v[2]);
+        for (int base = r0; base < r1; base += 2 * RPS) {  // q = A p; p.q
+            double dv[2];
+            row_dot2<VEC, S>(a.rowptr, a.colind, a.val, (const double *)p, base + g, base + g < r1, base + RPS + g,
+                             base + RPS + g < r1, l, dv[0], dv[1]);
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int i = base + u * RPS + g;
+                if (i < r1 && l == 0) {
+                    const double qq = mtj_assign(dv[u]);
+                    q[i] = qq;
+                    acc.v[2] = fmac<S>(p[i], qq, acc.v[2]);
+                }
             }
         }
         cta_reduce<kSlotD2>(acc, nt, sh.warp_acc, sh.out);
@@ -163,20 +231,36 @@ __device__ void cg_system(const BatchCg &a, int sys, Shared &sh)
         __syncthreads();
         const double al = sh.sc[0];
         acc_zero(acc);
-        for (int i = r0 + tid; i < r1; i += kBatchBlock) {  // x += alpha p; r -= alpha q; z = M r
-            double rr = r[i];
-            if (al != 0) {
-                x[i] = fmac<S>(al, p[i], x[i]);
-                rr = fmac<S>(-al, q[i], rr);
-                r[i] = rr;
+        for (int base = r0 + tid; base < r1; base += kU2 * kBatchBlock) {  // x += alpha p; r -= alpha q; z = M r
+            double rv[kU2], xv[kU2], pv[kU2], qv[kU2], iv[kU2];
+#pragma unroll
+            for (int u = 0; u < kU2; ++u) {
+                const int i = base + u * kBatchBlock;
+                const bool in = i < r1;
+                rv[u] = in ? r[i] : 0.0;
+                xv[u] = in && al != 0 ? x[i] : 0.0;
+                pv[u] = in && al != 0 ? p[i] : 0.0;
+                qv[u] = in && al != 0 ? q[i] : 0.0;
+                iv[u] = in && jac ? inv[i] : 0.0;
             }
-            norm_add<S>(acc, rr, nt);
-            if (jac) {
-                const double zz = rr * inv[i];
-                z[i] = zz;
-                acc.v[2] = fmac<S>(rr, zz, acc.v[2]);
-            } else {
-                acc.v[2] = fmac<S>(rr, rr, acc.v[2]);
+#pragma unroll
+            for (int u = 0; u < kU2; ++u) {
+                const int i = base + u * kBatchBlock;
+                if (i >= r1) break;
+                double rr = rv[u];
+                if (al != 0) {
+                    x[i] = fmac<S>(al, pv[u], xv[u]);
+                    rr = fmac<S>(-al, qv[u], rr);
+                    r[i] = rr;
+                }
+                norm_add<S>(acc, rr, nt);
+                if (jac) {
+                    const double zz = rr * iv[u];
+                    z[i] = zz;
+                    acc.v[2] = fmac<S>(rr, zz, acc.v[2]);
+                } else {
+                    acc.v[2] = fmac<S>(rr, rr, acc.v[2]);
+                }
             }
         }
         cta_reduce<kSlotNorm | kSlotD2>(acc, nt, sh.warp_acc, sh.out);
@@ -219,7 +303,21 @@ __device__ void mixed_system(const BatchCg &a, int sys, Shared &sh)
         const bool pend = sh.flag != 0;
         __syncthreads();  // every thread has read the flag before it is rewritten
         if (pend) {
-            for (int i = r0 + tid; i < r1; i += kBatchBlock) x[i] = x[i] + (double)d[i];
+            for (int base = r0 + tid; base < r1; base += kU * kBatchBlock) {
+                double xv[kU];
+                float dv[kU];
+#pragma unroll
+                for (int u = 0; u < kU; ++u) {
+                    const int i = base + u * kBatchBlock;
+                    xv[u] = i < r1 ? x[i] : 0.0;
+                    dv[u] = i < r1 ? d[i] : 0.0f;
+                }
+#pragma unroll
+                for (int u = 0; u < kU; ++u) {
+                    const int i = base + u * kBatchBlock;
+                    if (i < r1) x[i] = xv[u] + (double)dv[u];
+                }
+            }
             __syncthreads();
             if (tid == 0) {
                 SysState &t = a.st[sys];
@@ -230,23 +328,27 @@ __device__ void mixed_system(const BatchCg &a, int sys, Shared &sh)
         // ... then r = b - A x in FP64, the monitor's test, the inner start (MxOuter)
         Acc acc;
         acc_zero(acc);
-        for (int base = r0; base < r1; base += RPS) {
-            const int i = base + g;
-            const bool in = i < r1;
-            const double dd = row_dot<VEC, S>(a.rowptr, a.colind, a.val, (const double *)x, i, in, l);
-            if (in && l == 0) {
-                const double rr = a.b[i] - dd;
-                norm_add<false>(acc, rr, nt);
-                const float rf = (float)rr;
-                rin[i] = rf;
-                d[i] = 0.0f;
-                float zf = rf;
-                if (jac) {
-                    zf = rf * inv[i];
-                    z[i] = zf;
+        for (int base = r0; base < r1; base += 2 * RPS) {
+            double dv[2];
+            row_dot2<VEC, S>(a.rowptr, a.colind, a.val, (const double *)x, base + g, base + g < r1, base + RPS + g,
+                             base + RPS + g < r1, l, dv[0], dv[1]);
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int i = base + u * RPS + g;
+                if (i < r1 && l == 0) {
+                    const double rr = a.b[i] - dv[u];
+                    norm_add<false>(acc, rr, nt);
+                    const float rf = (float)rr;
+                    rin[i] = rf;
+                    d[i] = 0.0f;
+                    float zf = rf;
+                    if (jac) {
+                        zf = rf * inv[i];
+                        z[i] = zf;
+                    }
+                    acc.f[0] = fmaf(rf, zf, acc.f[0]);
+                    acc.f[1] = fmaf(rf, rf, acc.f[1]);
                 }
-                acc.f[0] = fmaf(rf, zf, acc.f[0]);
-                acc.f[1] = fmaf(rf, rf, acc.f[1]);
             }
         }
         cta_reduce<kSlotNorm | kSlotD2 | kSlotD3>(acc, nt, sh.warp_acc, sh.out);
@@ -277,16 +379,33 @@ __device__ void mixed_system(const BatchCg &a, int sys, Shared &sh)
             const bool fresh = sh.flag != 0;
             const float beta = (float)sh.sc[1];
             __syncthreads();  // read before thread 0 rewrites them
-            for (int i = r0 + tid; i < r1; i += kBatchBlock) p[i] = fresh ? z[i] : fmaf(p[i], beta, z[i]);
+            for (int base = r0 + tid; base < r1; base += kU * kBatchBlock) {
+                float zv[kU], pv[kU];
+#pragma unroll
+                for (int u = 0; u < kU; ++u) {
+                    const int i = base + u * kBatchBlock;
+                    zv[u] = i < r1 ? z[i] : 0.0f;
+                    pv[u] = i < r1 && !fresh ? p[i] : 0.0f;
+                }
+#pragma unroll
+                for (int u = 0; u < kU; ++u) {
+                    const int i = base + u * kBatchBlock;
+                    if (i < r1) p[i] = fresh ? zv[u] : fmaf(pv[u], beta, zv[u]);
+                }
+            }
             __syncthreads();
             acc_zero(acc);
-            for (int base = r0; base < r1; base += RPS) {  // q = A32 p; p.q
-                const int i = base + g;
-                const bool in = i < r1;
-                const float dd = row_dot<VEC, false>(a.rowptr, a.colind, a.val32, (const float *)p, i, in, l);
-                if (in && l == 0) {
-                    q[i] = dd;
-                    acc.f[0] = fmaf(p[i], dd, acc.f[0]);
+            for (int base = r0; base < r1; base += 2 * RPS) {  // q = A32 p; p.q
+                float dv[2];
+                row_dot2<VEC, false>(a.rowptr, a.colind, a.val32, (const float *)p, base + g, base + g < r1,
+                                     base + RPS + g, base + RPS + g < r1, l, dv[0], dv[1]);
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const int i = base + u * RPS + g;
+                    if (i < r1 && l == 0) {
+                        q[i] = dv[u];
+                        acc.f[0] = fmaf(p[i], dv[u], acc.f[0]);
+                    }
                 }
             }
             cta_reduce<kSlotD2>(acc, nt, sh.warp_acc, sh.out);
@@ -298,17 +417,33 @@ __device__ void mixed_system(const BatchCg &a, int sys, Shared &sh)
             __syncthreads();
             const float al = (float)sh.sc[0];
             acc_zero(acc);
-            for (int i = r0 + tid; i < r1; i += kBatchBlock) {  // d += alpha p; rin -= alpha q; z = M rin
-                d[i] = fmaf(al, p[i], d[i]);
-                const float rf = fmaf(-al, q[i], rin[i]);
-                rin[i] = rf;
-                float zf = rf;
-                if (jac) {
-                    zf = rf * inv[i];
-                    z[i] = zf;
+            for (int base = r0 + tid; base < r1; base += kU * kBatchBlock) {  // d += alpha p; rin -= alpha q; z = M rin
+                float dv[kU], pv[kU], qv[kU], rv[kU], iv[kU];
+#pragma unroll
+                for (int u = 0; u < kU; ++u) {
+                    const int i = base + u * kBatchBlock;
+                    const bool in = i < r1;
+                    dv[u] = in ? d[i] : 0.0f;
+                    pv[u] = in ? p[i] : 0.0f;
+                    qv[u] = in ? q[i] : 0.0f;
+                    rv[u] = in ? rin[i] : 0.0f;
+                    iv[u] = in && jac ? inv[i] : 0.0f;
                 }
-                acc.f[0] = fmaf(rf, zf, acc.f[0]);
-                acc.f[1] = fmaf(rf, rf, acc.f[1]);
+#pragma unroll
+                for (int u = 0; u < kU; ++u) {
+                    const int i = base + u * kBatchBlock;
+                    if (i >= r1) break;
+                    d[i] = fmaf(al, pv[u], dv[u]);
+                    const float rf = fmaf(-al, qv[u], rv[u]);
+                    rin[i] = rf;
+                    float zf = rf;
+                    if (jac) {
+                        zf = rf * iv[u];
+                        z[i] = zf;
+                    }
+                    acc.f[0] = fmaf(rf, zf, acc.f[0]);
+                    acc.f[1] = fmaf(rf, rf, acc.f[1]);
+                }
             }
             cta_reduce<kSlotD2 | kSlotD3>(acc, nt, sh.warp_acc, sh.out);
             if (tid == 0) {
