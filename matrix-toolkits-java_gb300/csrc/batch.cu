@@ -38,6 +38,7 @@ constexpr int kBatchMinBlocks = 3;
 constexpr int kProbeIters = 12;
 constexpr int kProbeSystems = 24;
 constexpr int kVecCandidates[] = {1, 2, 4, 8, 32};
+constexpr unsigned char kPairFlag = 0x80;  // in a system's lanes byte: pair its FP32 product rows
 
 namespace {
 
@@ -80,25 +81,26 @@ __device__ __forceinline__ T row_dot(const int *__restrict__ rp, const int *__re
     return sum;
 }
 
-// Build-time knobs: MTJG_BATCH_PAIR = 0 sums the two rows of a product step
-// one after the other; MTJG_BATCH_U is the rows per thread and step of the
-// element-wise loops (1: one row at a time).  Neither changes a result.
-#ifndef MTJG_BATCH_PAIR
-#define MTJG_BATCH_PAIR 1
-#endif
+// Build-time knob: MTJG_BATCH_U is the rows per thread and step of the
+// element-wise loops (1: one row at a time); it changes no result.
 #ifndef MTJG_BATCH_U
 #define MTJG_BATCH_U 4
 #endif
 
-// Rows ia and ib together (the same sums as two row_dot calls): their
-// gathers are in flight at once, so a thread waits one latency round for
-// both.  Each row keeps its entry order and its butterfly.
+// Rows ia and ib of a product step.  Paired (`pair`), their gathers are in
+// flight at once, so a thread waits one latency round for both; else one
+// after the other.  Each row keeps its entry order and its butterfly, so
+// the sums are the same either way.  Measured on GB300 (C4 and a batch of
+// 2D Poisson grids): pairing made the FP32 inner products of 5-entry rows
+// 10 % faster and those of ~19-entry rows, and every FP64 product, slower;
+// a system pairs its FP32 products when its rows average under 12 entries
+// (kPairFlag in its lanes byte).
 template <int VEC, bool S, class T>
 __device__ __forceinline__ void row_dot2(const int *__restrict__ rp, const int *__restrict__ ci,
                                          const T *__restrict__ v, const T *x, int ia, bool ina, int ib, bool inb,
-                                         int l, T &sa, T &sb)
+                                         int l, T &sa, T &sb, bool pair)
 {
-    if constexpr (!MTJG_BATCH_PAIR) {
+    if (!pair) {
         sa = row_dot<VEC, S>(rp, ci, v, x, ia, ina, l);
         sb = row_dot<VEC, S>(rp, ci, v, x, ib, inb, l);
         return;
@@ -159,7 +161,7 @@ __device__ void cg_system(const BatchCg &a, int sys, Shared &sh)
     for (int base = r0; base < r1; base += 2 * RPS) {  // r = b - A x; z = M r; |r|; r.z
         double dv[2];
         row_dot2<VEC, S>(a.rowptr, a.colind, a.val, (const double *)x, base + g, base + g < r1, base + RPS + g,
-                         base + RPS + g < r1, l, dv[0], dv[1]);
+                         base + RPS + g < r1, l, dv[0], dv[1], false);
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
             const int i = base + u * RPS + g;
@@ -211,7 +213,7 @@ __device__ void cg_system(const BatchCg &a, int sys, Shared &sh)
         for (int base = r0; base < r1; base += 2 * RPS) {  // q = A p; p.q
             double dv[2];
             row_dot2<VEC, S>(a.rowptr, a.colind, a.val, (const double *)p, base + g, base + g < r1, base + RPS + g,
-                             base + RPS + g < r1, l, dv[0], dv[1]);
+                             base + RPS + g < r1, l, dv[0], dv[1], false);
 #pragma unroll
             for (int u = 0; u < 2; ++u) {
                 const int i = base + u * RPS + g;
@@ -287,6 +289,7 @@ __device__ void cg_system(const BatchCg &a, int sys, Shared &sh)
 template <int VEC, bool S>
 __device__ void mixed_system(const BatchCg &a, int sys, Shared &sh)
 {
+    const bool pair = (a.vec[sys] & kPairFlag) != 0;
     const int r0 = a.sys_rows[sys], r1 = a.sys_rows[sys + 1];
     const int tid = threadIdx.x, g = tid / VEC, l = tid % VEC;
     constexpr int RPS = kBatchBlock / VEC;
@@ -331,7 +334,7 @@ __device__ void mixed_system(const BatchCg &a, int sys, Shared &sh)
         for (int base = r0; base < r1; base += 2 * RPS) {
             double dv[2];
             row_dot2<VEC, S>(a.rowptr, a.colind, a.val, (const double *)x, base + g, base + g < r1, base + RPS + g,
-                             base + RPS + g < r1, l, dv[0], dv[1]);
+                             base + RPS + g < r1, l, dv[0], dv[1], false);
 #pragma unroll
             for (int u = 0; u < 2; ++u) {
                 const int i = base + u * RPS + g;
@@ -398,7 +401,7 @@ __device__ void mixed_system(const BatchCg &a, int sys, Shared &sh)
             for (int base = r0; base < r1; base += 2 * RPS) {  // q = A32 p; p.q
                 float dv[2];
                 row_dot2<VEC, false>(a.rowptr, a.colind, a.val32, (const float *)p, base + g, base + g < r1,
-                                     base + RPS + g, base + RPS + g < r1, l, dv[0], dv[1]);
+                                     base + RPS + g, base + RPS + g < r1, l, dv[0], dv[1], pair);
 #pragma unroll
                 for (int u = 0; u < 2; ++u) {
                     const int i = base + u * RPS + g;
@@ -481,7 +484,7 @@ __global__ void __launch_bounds__(kBatchBlock, kBatchMinBlocks) k_batch_cg(Batch
         __syncthreads();
         if (k >= a.count) return;
         const int sys = a.order[k];
-        const int vec = S ? 1 : a.vec[sys];
+        const int vec = S ? 1 : (a.vec[sys] & ~kPairFlag);
         if constexpr (MIXED) {
             switch (vec) {
             case 2: mixed_system<2, S>(a, sys, sh); break;
@@ -600,7 +603,11 @@ int batch_vec(int num_sys, const int *sys_rows, const int *h_rowptr, std::vector
             std::lock_guard<std::mutex> lk(g_tune_mu);
             if (tune) g_tuned.emplace(kv.first, v);
         }
-        for (int s : kv.second) vec[(size_t)s] = (unsigned char)v;
+        for (int s : kv.second) {
+            const int64_t rows = sys_rows[s + 1] - sys_rows[s];
+            const int64_t nnz = (int64_t)h_rowptr[sys_rows[s + 1]] - h_rowptr[sys_rows[s]];
+            vec[(size_t)s] = (unsigned char)(v | (nnz < 12 * rows ? kPairFlag : 0));
+        }
     }
     return MTJG_OK;
 }
