@@ -59,6 +59,7 @@ void ctx_release(mtjg_ctx *ctx);
 constexpr int kBlock = 256;
 constexpr int kTileRows = MTJG_TILE_ROWS;
 constexpr int kTileNnz = MTJG_TILE_NNZ;
+constexpr int kLongSeg = 4096;        // entries per segment of a long row (FAST pre-pass)
 constexpr int kParts = 4;             // partial-sum slots per group
 // A reduction group is what one block sums before a block-wide reduction:
 // up to kGroupTiles consecutive product tiles of one system, or one row
@@ -167,6 +168,15 @@ struct TileSet {
     // device [num_tiles]: (lanes per row << 1) | 1 if the tile is a single long row
     unsigned char *tile_flags = nullptr;
     int vec_mask = 0;          // OR of the lanes-per-row classes of the tiles
+    // rows longer than a stage (tiles of their own), summed ahead of a FAST
+    // product by many CTAs: fixed segments of kLongSeg entries, then the
+    // segments of each row in order (k_long_seg, k_long_sum)
+    int num_long = 0, num_segs = 0;
+    int *seg_begin = nullptr, *seg_end = nullptr;  // device [num_segs]: entries of each segment
+    int *long_first = nullptr;                     // device [num_long + 1]: first segment of each long row
+    int *long_tile = nullptr;                      // device [num_long]: its tile
+    double *seg_part = nullptr;                    // device [num_segs]: segment sums
+    double *long_sum = nullptr;                    // device [num_tiles]: row sums, by tile
     std::vector<int> h_tile_row;
 };
 

@@ -96,6 +96,34 @@ int upload_tiles(TileSet &ts, const std::vector<int> &tile_row, const std::vecto
     MTJG_CUDA(cudaMalloc(&ts.tile_flags, std::max<size_t>(1, tile_flags.size())));
     if (!tile_flags.empty())
         MTJG_CUDA(cudaMemcpy(ts.tile_flags, tile_flags.data(), tile_flags.size(), cudaMemcpyHostToDevice));
+    if (rowptr) {
+        // long rows (tiles of a single row longer than a stage): segments for the FAST pre-pass
+        std::vector<int> sb, se, lf{0}, lt;
+        for (int t = 0; t < ts.num_tiles; ++t) {
+            if (!(tile_flags[(size_t)t] & 1)) continue;
+            const int r = tile_row[(size_t)t], b = rowptr[r], e = rowptr[r + 1];
+            for (int k = b; k < e; k += kLongSeg) {
+                sb.push_back(k);
+                se.push_back(std::min(e, k + kLongSeg));
+            }
+            lf.push_back((int)sb.size());
+            lt.push_back(t);
+        }
+        if (!lt.empty()) {
+            ts.num_long = (int)lt.size();
+            ts.num_segs = (int)sb.size();
+            MTJG_CUDA(cudaMalloc(&ts.seg_begin, sizeof(int) * sb.size()));
+            MTJG_CUDA(cudaMalloc(&ts.seg_end, sizeof(int) * se.size()));
+            MTJG_CUDA(cudaMalloc(&ts.long_first, sizeof(int) * lf.size()));
+            MTJG_CUDA(cudaMalloc(&ts.long_tile, sizeof(int) * lt.size()));
+            MTJG_CUDA(cudaMalloc(&ts.seg_part, sizeof(double) * sb.size()));
+            MTJG_CUDA(cudaMalloc(&ts.long_sum, sizeof(double) * (size_t)ts.num_tiles));
+            MTJG_CUDA(cudaMemcpy(ts.seg_begin, sb.data(), sizeof(int) * sb.size(), cudaMemcpyHostToDevice));
+            MTJG_CUDA(cudaMemcpy(ts.seg_end, se.data(), sizeof(int) * se.size(), cudaMemcpyHostToDevice));
+            MTJG_CUDA(cudaMemcpy(ts.long_first, lf.data(), sizeof(int) * lf.size(), cudaMemcpyHostToDevice));
+            MTJG_CUDA(cudaMemcpy(ts.long_tile, lt.data(), sizeof(int) * lt.size(), cudaMemcpyHostToDevice));
+        }
+    }
     if (tile_sys) {
         MTJG_CUDA(cudaMalloc(&ts.tile_sys, sizeof(int) * std::max<size_t>(1, tile_sys->size())));
         if (!tile_sys->empty())
@@ -116,6 +144,15 @@ void free_tiles(TileSet &ts)
     cudaFree(ts.tile_flags);
     ts.tile_row = ts.tile_nz = ts.tile_sys = ts.group_tile = ts.group_info = ts.sys_group = nullptr;
     ts.tile_flags = nullptr;
+    cudaFree(ts.seg_begin);
+    cudaFree(ts.seg_end);
+    cudaFree(ts.long_first);
+    cudaFree(ts.long_tile);
+    cudaFree(ts.seg_part);
+    cudaFree(ts.long_sum);
+    ts.seg_begin = ts.seg_end = ts.long_first = ts.long_tile = nullptr;
+    ts.seg_part = ts.long_sum = nullptr;
+    ts.num_long = ts.num_segs = 0;
     ts.num_tiles = 0;
     ts.num_groups = 0;
 }

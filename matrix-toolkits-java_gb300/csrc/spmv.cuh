@@ -92,6 +92,7 @@ struct TileArgs {
     const int *group_tile;
     const int *group_info;  // per group: (system << 8) | lanes per row of its tiles
     const SysDesc *sd;  // nullptr: one CSR (the kernel's argument), rows = vector indices
+    const double *long_sum;  // FAST: the sums of the long rows, by tile (k_long_sum), else nullptr
 };
 
 template <class T>
@@ -425,6 +426,14 @@ __global__ void __launch_bounds__(kBlock, EpiCtas<Epi>::value)
                     if (r < r1 && l == 0) epi.row(vgo + r, sys, sum, Epi::kNeedsXr ? __ldg(xs + r) : T(0), acc);
                 }
             }
+        } else if (!st && ta.long_sum) {
+            // a single row longer than a stage, summed ahead by k_long_seg / k_long_sum
+            const int sys = tile_system(ta, t);
+            const int r = ta.tile_row[t];
+            const MatView mv = view(t);
+            if (tid == 0)
+                epi.row(mv.voff + r, sys, epi.init(mv.voff + r, sys) + (T)ta.long_sum[t],
+                        Epi::kNeedsXr ? __ldg(x + mv.voff + r) : T(0), acc);
         } else if (!st) {
             // a single row longer than a stage: straight from global memory
             const int sys = tile_system(ta, t);
@@ -539,7 +548,7 @@ __global__ void __launch_bounds__(kBlock, OpMinBlocks<Op>::value) k_rows(TileArg
     if constexpr (Op::kReduce) group_partial<OpSlots<Op>::value>(acc, t, rc, normtype, red_sm);
 }
 
-inline TileArgs tile_args(const TileSet &ts)
+inline TileArgs tile_args(const TileSet &ts, bool long_sums = false)
 {
     // contiguous tilings end each tile where the next one starts
     return TileArgs{ts.num_tiles,
@@ -552,7 +561,52 @@ inline TileArgs tile_args(const TileSet &ts)
                     ts.tile_flags,
                     ts.group_tile,
                     ts.group_info,
-                    ts.sd};
+                    ts.sd,
+                    long_sums ? ts.long_sum : nullptr};
+}
+
+// Long rows, FAST: block s sums segment s (thread-strided, then a fixed
+// shuffle tree and the warps in order); then each long row's segments are
+// added in segment order.  Fixed segments and orders: the sums depend on
+// the matrix alone, not on the grid.
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_long_seg(CsrArgsT<T> A, const int *seg_begin, const int *seg_end,
+                                                     const T *__restrict__ x, double *part)
+{
+    __shared__ T s_w[kBlock / 32];
+    const int sg = blockIdx.x, b = seg_begin[sg], e = seg_end[sg];
+    T sum = T(0);
+    for (int k = b + (int)threadIdx.x; k < e; k += kBlock) sum = fmac<false>(A.val[k], __ldg(x + A.colind[k]), sum);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, off);
+    if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = sum;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        T s = s_w[0];
+        for (int w = 1; w < kBlock / 32; ++w) s += s_w[w];
+        part[sg] = (double)s;
+    }
+}
+
+__global__ void k_long_sum(int num_long, const int *long_first, const int *long_tile, const double *part,
+                           double *long_sum)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= num_long) return;
+    double s = 0.0;
+    for (int q = long_first[j]; q < long_first[j + 1]; ++q) s += part[q];
+    long_sum[long_tile[j]] = s;
+}
+
+template <class T>
+cudaError_t launch_long_rows(mtjg_ctx *ctx, CsrArgsT<T> A, const TileSet &ts, const T *x)
+{
+    k_long_seg<T><<<ts.num_segs, kBlock, 0, ctx->stream>>>(A, ts.seg_begin, ts.seg_end, x, ts.seg_part);
+    k_long_sum<<<(ts.num_long + kBlock - 1) / kBlock, kBlock, 0, ctx->stream>>>(ts.num_long, ts.long_first,
+                                                                               ts.long_tile, ts.seg_part,
+                                                                               ts.long_sum);
+    ctx->launches += 2;
+    return cudaGetLastError();
 }
 
 template <class Op>
@@ -578,7 +632,8 @@ cudaError_t launch_spmv_t(mtjg_ctx *ctx, CsrArgsT<T> A, const TileSet &ts, const
     }
     const int cap = ctx->num_sms * EpiCtas<Epi>::value;
     const int grid = ts.num_groups < cap ? ts.num_groups : cap;
-    k<<<grid, kBlock, spmv_smem<T>(), ctx->stream>>>(A, tile_args(ts), x, epi, rc, normtype, ctx->d_flag);
+    k<<<grid, kBlock, spmv_smem<T>(), ctx->stream>>>(A, tile_args(ts, !S && ts.num_long > 0 && !ts.sd), x, epi, rc, normtype,
+                                                     ctx->d_flag);
     ctx->launches++;
     return cudaGetLastError();
 }
@@ -593,6 +648,10 @@ cudaError_t launch_spmv(mtjg_ctx *ctx, CsrArgsT<T> A, const TileSet &ts, const T
     RedCtx r = rc;
     r.sys_group = ts.sys_group;  // partial slots are this tiling's groups
     cudaError_t e = cudaSuccess;
+    // FAST: rows longer than a stage are summed ahead, over many CTAs (a
+    // single CSR; served batches keep one CTA per long row)
+    if (ctx->numerics != MTJG_NUMERICS_STRICT && ts.num_long > 0 && !ts.sd) e = launch_long_rows<T>(ctx, A, ts, x);
+    if (e != cudaSuccess) return e;
     if (ctx->numerics == MTJG_NUMERICS_STRICT) {
         e = launch_spmv_t<1, true, T>(ctx, A, ts, x, epi, r, normtype);
     } else {
