@@ -273,11 +273,18 @@ __global__ void k_tr_fill(int n, const int *rowptr, const int *colind, const dou
         }
 }
 
-// each transposed row sorted by source row (insertion sort; rows are short)
+// Each transposed row sorted by source row (the fill's atomics leave it in
+// any order).  Rows of up to kTrShort entries: an insertion sort by one
+// thread.  Longer rows (a dense column of A) would make that quadratic:
+// k_tr_sort_long gives each one a block, which sorts it with a bitonic
+// network in scratch, padded to a power of two with keys above every row.
+constexpr int kTrShort = 64;
+
 __global__ void k_tr_sort(int m, const int *t_rowptr, int *t_colind, double *t_val)
 {
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < m; c += gridDim.x * blockDim.x) {
         int b = t_rowptr[c], e = t_rowptr[c + 1];
+        if (e - b > kTrShort) continue;
         for (int p = b + 1; p < e; ++p) {
             int key = t_colind[p];
             double v = t_val[p];
@@ -290,6 +297,43 @@ __global__ void k_tr_sort(int m, const int *t_rowptr, int *t_colind, double *t_v
             t_colind[q + 1] = key;
             t_val[q + 1] = v;
         }
+    }
+}
+
+__global__ void k_tr_sort_long(const int *rows, const int64_t *soff, const int *t_rowptr, int *t_colind,
+                               double *t_val, int *skey, double *sval)
+{
+    const int c = rows[blockIdx.x];
+    const int b = t_rowptr[c], len = t_rowptr[c + 1] - b;
+    int P = 1;
+    while (P < len) P <<= 1;
+    int *K = skey + soff[blockIdx.x];
+    double *V = sval + soff[blockIdx.x];
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {
+        K[i] = i < len ? t_colind[b + i] : 0x7fffffff;
+        V[i] = i < len ? t_val[b + i] : 0.0;
+    }
+    __syncthreads();
+    for (int k = 2; k <= P; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < P; i += blockDim.x) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const int ki = K[i], kl = K[l];
+                    if ((ki > kl) == ((i & k) == 0)) {
+                        K[i] = kl;
+                        K[l] = ki;
+                        const double t = V[i];
+                        V[i] = V[l];
+                        V[l] = t;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    for (int i = threadIdx.x; i < len; i += blockDim.x) {
+        t_colind[b + i] = K[i];
+        t_val[b + i] = V[i];
     }
 }
 
@@ -328,6 +372,43 @@ int csr_transpose(mtjg_ctx *ctx, int n, int m, const int *rowptr, const int *col
         const int gm = std::max(1, std::min((m + kBlock - 1) / kBlock, ctx->num_sms * 8));
         k_tr_sort<<<gm, kBlock, 0, ctx->stream>>>(m, trp, tci, tv);
         ctx->launches++;
+    }
+    // the long transposed rows (found from the row pointers on the host)
+    std::vector<int> h_trp((size_t)m + 1);
+    if (m > 0) MTJG_CUDA(cudaMemcpy(h_trp.data(), trp, sizeof(int) * ((size_t)m + 1), cudaMemcpyDeviceToHost));
+    std::vector<int> lrows;
+    std::vector<int64_t> loff{0};
+    for (int c = 0; c < m; ++c) {
+        const int len = h_trp[(size_t)c + 1] - h_trp[(size_t)c];
+        if (len <= kTrShort) continue;
+        int64_t P = 1;
+        while (P < len) P <<= 1;
+        lrows.push_back(c);
+        loff.push_back(loff.back() + P);
+    }
+    if (!lrows.empty()) {
+        int *d_rows = nullptr, *skey = nullptr;
+        int64_t *d_off = nullptr;
+        double *sval = nullptr;
+        cudaError_t e = cudaMalloc(&d_rows, sizeof(int) * lrows.size());
+        if (e == cudaSuccess) e = cudaMalloc(&d_off, sizeof(int64_t) * loff.size());
+        if (e == cudaSuccess) e = cudaMalloc(&skey, sizeof(int) * (size_t)loff.back());
+        if (e == cudaSuccess) e = cudaMalloc(&sval, sizeof(double) * (size_t)loff.back());
+        if (e == cudaSuccess)
+            e = cudaMemcpy(d_rows, lrows.data(), sizeof(int) * lrows.size(), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(d_off, loff.data(), sizeof(int64_t) * loff.size(), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) {
+            k_tr_sort_long<<<(unsigned)lrows.size(), 1024, 0, ctx->stream>>>(d_rows, d_off, trp, tci, tv, skey, sval);
+            ctx->launches++;
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        cudaFree(d_rows);
+        cudaFree(d_off);
+        cudaFree(skey);
+        cudaFree(sval);
+        if (e != cudaSuccess) return cuda_fail(e, "sorting the long rows of a transpose");
     }
     MTJG_CUDA(cudaStreamSynchronize(ctx->stream));
     cudaFree(cnt);
