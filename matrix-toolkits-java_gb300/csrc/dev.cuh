@@ -29,6 +29,12 @@ __device__ __forceinline__ float fmac(float a, float b, float c)
         return fmaf(a, b, c);
 }
 
+// the rounded product and the rounded sum of STRICT, apart
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+
 // MTJ assigns a row sum only when it is nonzero (CompRowMatrix.mult,
 // S/CompRowMatrix.java:309-311), so a -0.0 sum leaves +0.0 behind.  Done on
 // the bits: an FP64 compare would take an issue slot of the narrow FP64 pipe

@@ -60,6 +60,7 @@ constexpr int kBlock = 256;
 constexpr int kTileRows = MTJG_TILE_ROWS;
 constexpr int kTileNnz = MTJG_TILE_NNZ;
 constexpr int kLongSeg = 4096;        // entries per segment of a long row (FAST pre-pass)
+constexpr int kWideRow = 64;          // rows this long among shorter ones get a warp each (plan_tiles)
 constexpr int kParts = 4;             // partial-sum slots per group
 // A reduction group is what one block sums before a block-wide reduction:
 // up to kGroupTiles consecutive product tiles of one system, or one row

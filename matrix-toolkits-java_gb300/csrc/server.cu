@@ -350,10 +350,12 @@ struct ProdTables {
     {
         const int T = (int)mt.row.size(), t0 = (int)row.size();
         const int gs = std::max(1, std::min(kGroupTiles, T / group_div));
-        for (int k = 0; k < T; ++k) {
-            if (k % gs == 0) {
+        // groups of up to gs tiles of one lanes-per-row class
+        for (int k = 0, k0 = 0; k < T; ++k) {
+            if (k == 0 || k - k0 == gs || (mt.flags[k] >> 1) != (mt.flags[k0] >> 1)) {
                 ginfo.push_back((s << 8) | (mt.flags[k] >> 1));
                 grp.push_back(t0 + k);
+                k0 = k;
             }
             vec_mask |= mt.flags[k] >> 1;
         }

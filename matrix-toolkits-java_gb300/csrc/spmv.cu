@@ -16,10 +16,16 @@ int choose_vec(int64_t nnz, int64_t n)
     return 32;
 }
 
+// Tiles of consecutive rows, at most rows_cap_all / lanes rows and nnz_cap
+// entries.  A row of the system's lanes-per-row class `vec` that is much
+// longer than its neighbours (kWideRow entries or more, over 8 per lane)
+// would keep one thread busy while the rest of its tile waits: such rows
+// form tiles of their own summed by a whole warp per row (class 32).  A row
+// longer than a stage is a tile of its own (long-row bit).
 void plan_tiles(const int *rowptr, int row_begin, int row_end, int vec, std::vector<int> &tile_row,
                 std::vector<unsigned char> &tile_flags, int nnz_cap, int rows_cap_all)
 {
-    const int rows_cap = rows_cap_all / vec;
+    auto lanes_for = [&](int len) { return vec < 32 && len >= kWideRow && len > 8 * vec ? 32 : vec; };
     int r = row_begin;
     while (r < row_end) {
         tile_row.push_back(r);
@@ -29,16 +35,18 @@ void plan_tiles(const int *rowptr, int row_begin, int row_end, int vec, std::vec
             r += 1;
             continue;
         }
+        const int tv = lanes_for(len0);
+        const int rows_cap = rows_cap_all / tv;
         int nz = len0, rows = 1;
         r += 1;
         while (r < row_end && rows < rows_cap) {
             int len = rowptr[r + 1] - rowptr[r];
-            if (nz + len > nnz_cap) break;
+            if (nz + len > nnz_cap || lanes_for(len) != tv) break;
             nz += len;
             rows++;
             r++;
         }
-        tile_flags.push_back((unsigned char)(vec << 1));
+        tile_flags.push_back((unsigned char)(tv << 1));
     }
 }
 
@@ -62,12 +70,17 @@ int upload_tiles(TileSet &ts, const std::vector<int> &tile_row, const std::vecto
     // system of T tiles uses groups of min(group_size, T / kGroupDiv) tiles (at
     // least 1): large systems amortise the block reduction over several
     // tiles while keeping thousands of groups for the CTAs to share evenly;
-    // the size depends on the system alone, never on the rest of a batch.
+    // the size depends on the system alone, never on the rest of a batch.  A
+    // group holds tiles of one lanes-per-row class (a launch takes a class).
     std::vector<int> group_tile, sys_group = {0};
     for (int s = 0; s < ts.num_sys; ++s) {
         const int t0 = sys_tile[s], t1 = sys_tile[s + 1];
         const int gs = std::max(1, std::min(group_size, (t1 - t0) / group_div));
-        for (int t = t0; t < t1; t += gs) group_tile.push_back(t);
+        for (int t = t0, g0 = t0; t < t1; ++t)
+            if (t == t0 || t - g0 == gs || (tile_flags[(size_t)t] >> 1) != (tile_flags[(size_t)g0] >> 1)) {
+                group_tile.push_back(t);
+                g0 = t;
+            }
         sys_group.push_back((int)group_tile.size());
     }
     ts.num_groups = (int)group_tile.size();

@@ -444,8 +444,23 @@ __global__ void __launch_bounds__(kBlock, EpiCtas<Epi>::value)
             const int b = mv.rowptr[r], e = mv.rowptr[r + 1];
             T sum = tid == 0 ? epi.init(vgo + r, sys) : T(0);
             if constexpr (S) {
-                if (tid == 0)
-                    for (int k = b; k < e; ++k) sum = fmac<S>(mv.val[k], __ldg(xs + mv.colind[k]), sum);
+                // Java's order: products rounded, then added one by one in
+                // entry order.  Warp 0's lanes form 32 rounded products at a
+                // time (the next 32 loading while lane 0 adds these), so the
+                // row is bound by the add chain, not by a load per entry.
+                if (tid < 32) {
+                    T nxt = b + tid < e ? mul_rn(mv.val[b + tid], __ldg(xs + mv.colind[b + tid])) : T(0);
+                    for (int k0 = b; k0 < e; k0 += 32) {
+                        const T cur = nxt;
+                        const int kn = k0 + 32 + tid;
+                        nxt = kn < e ? mul_rn(mv.val[kn], __ldg(xs + mv.colind[kn])) : T(0);
+                        const int cnt = e - k0 < 32 ? e - k0 : 32;
+                        for (int u = 0; u < cnt; ++u) {
+                            const T pu = __shfl_sync(0xffffffffu, cur, u);
+                            if (tid == 0) sum = add_rn(sum, pu);
+                        }
+                    }
+                }
             } else {
                 for (int k = b + tid; k < e; k += kBlock) sum = fmac<S>(mv.val[k], __ldg(xs + mv.colind[k]), sum);
 #pragma unroll

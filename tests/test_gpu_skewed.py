@@ -89,3 +89,61 @@ def test_long_row_cg(ctx, arrow, mixed):
         gr, gi = s.history
         k = min(len(gr), len(hr))
         assert np.max(np.abs(gr[:k] - hr[:k])) / hr[0] <= 1e-10
+
+
+def _power_law(n=60_000, seed=3):
+    """Rows of 3 to 900 entries (a heavy tail: 2 % of rows hold 64 or more),
+    symmetrised and made diagonally dominant, so SPD."""
+    import scipy.sparse as sp
+    rng = np.random.default_rng(seed)
+    deg = np.minimum(900, np.maximum(3, (rng.pareto(1.2, n) * 3).astype(np.int64)))
+    rows = np.repeat(np.arange(n), deg)
+    cols = rng.integers(0, n, len(rows))
+    A = sp.csr_array((np.full(len(rows), -0.5), (rows, cols)), shape=(n, n))
+    A = A + A.T
+    A.setdiag(0)
+    A.eliminate_zeros()
+    d = np.asarray(abs(A).sum(axis=1)).ravel() + 1.0
+    A = (A + sp.diags_array(d)).tocsr()
+    A.sum_duplicates()
+    A.sort_indices()
+    return n, A.indptr.astype(np.int32), A.indices.astype(np.int32), A.data.astype(np.float64)
+
+
+@pytest.mark.parametrize("numerics", [0, 1], ids=["fast", "strict"])
+def test_heavy_tailed_rows(ctx, numerics):
+    """Rows of a few hundred entries among short ones get a warp each (their
+    own tiles); products match the oracle and CG + Jacobi its history."""
+    n, rp, ci, v = _power_law()
+    lens = np.diff(rp)
+    assert lens.max() >= 300 and (lens >= 64).sum() > 100 and np.median(lens) < 24
+    A = sparse.CompRowMatrix(n, n, rp, ci, v, ctx)
+    Ao = O.Csr(n, n, rp, ci, v)
+    x = workloads.uniform(n, 41)
+    ctx.setNumerics(numerics)
+    try:
+        y = A.mult(x)
+        b = O.mult(Ao, workloads.uniform(n, 42))
+        s = sparse.CG(n, ctx=ctx)
+        M = sparse.DiagonalPreconditioner(n, ctx)
+        M.setMatrix(A)
+        s.setPreconditioner(M)
+        mon = sparse.DefaultIterationMonitor(1000, 1e-10, 1e-50, 1e5)
+        mon.setIterationReporter(None, history_cap=1000)
+        s.setIterationMonitor(mon)
+        xs = np.zeros(n)
+        s.solve(A, b, xs)
+    finally:
+        ctx.setNumerics(0)
+    yo = O.mult(Ao, x)
+    if numerics == 1:
+        assert np.array_equal(y, yo)
+    else:
+        assert np.all(np.abs(y - yo) <= 1e-13 * _scale(n, rp, ci, v, x) + 1e-300)
+    pc = O.Precond(O.PC_JACOBI, n)
+    pc.set_matrix(Ao)
+    xo, res, hr, hi = O.solve(O.CG, Ao, b, np.zeros(n), pc, max_iter=1000, rtol=1e-10)
+    assert res.status == 0 and abs(mon.iterations() - res.iterations) <= 2
+    gr, gi = s.history
+    k = min(len(gr), len(hr))
+    assert np.max(np.abs(gr[:k] - hr[:k])) / hr[0] <= 1e-10
