@@ -251,6 +251,9 @@ MTJG_API int mtjg_csr_trans_mult_dev(mtjg_csr *A, const double *dx, double *dy);
  *     systems.  Larger A gives MTJG_ERR_ILLEGAL_ARGUMENT.
  *   - Nothing has to start at zero: partials are written before they are read
  *     within the call, and each norm is stored, not accumulated.
+ *   - In FAST numerics, rows longer than a product stage (1152 entries) are
+ *     summed ahead into scratch that belongs to A (allocated when A was
+ *     uploaded, not by this call); overlapping calls on one A race there too.
  *   - The scratch is one array per device, shared by all contexts and threads:
  *     calls that overlap on one device (two streams, contexts or threads)
  *     race and return wrong norms.  Calls in order on one stream are safe.

@@ -455,9 +455,17 @@ __global__ void __launch_bounds__(kBlock, EpiCtas<Epi>::value)
                         const int kn = k0 + 32 + tid;
                         nxt = kn < e ? mul_rn(mv.val[kn], __ldg(xs + mv.colind[kn])) : T(0);
                         const int cnt = e - k0 < 32 ? e - k0 : 32;
-                        for (int u = 0; u < cnt; ++u) {
-                            const T pu = __shfl_sync(0xffffffffu, cur, u);
-                            if (tid == 0) sum = add_rn(sum, pu);
+                        if (cnt == 32) {  // unrolled: the shuffles run ahead of the add chain
+#pragma unroll
+                            for (int u = 0; u < 32; ++u) {
+                                const T pu = __shfl_sync(0xffffffffu, cur, u);
+                                if (tid == 0) sum = add_rn(sum, pu);
+                            }
+                        } else {
+                            for (int u = 0; u < cnt; ++u) {
+                                const T pu = __shfl_sync(0xffffffffu, cur, u);
+                                if (tid == 0) sum = add_rn(sum, pu);
+                            }
                         }
                     }
                 }
