@@ -116,6 +116,7 @@ struct ResMat {
     bool resident = false;  // dev holds the matrix
     bool loading = false;   // picked for upload, not yet attached
     int loader = 0;         // who is uploading it: 1 the scheduler, 2 the Krylov lane
+    int64_t epoch = 0;      // server-unique number of the current upload (0: none)
     int busy = 0;           // systems admitted and not yet delivered: the device copy stays
     int64_t last_use = 0;   // LRU clock at the last admission or delivery
     int uses = 0;           // requests submitted and not yet delivered
@@ -296,7 +297,7 @@ struct mtjg_server {
     std::thread th;
     std::chrono::steady_clock::time_point t0;
     // residency (under mu)
-    int64_t resident_bytes = 0, use_clock = 0, uploads = 0, evictions = 0;
+    int64_t resident_bytes = 0, use_clock = 0, uploads = 0, evictions = 0, upload_seq = 0;
     // statistics
     int64_t chunks = 0, admitted = 0, retired = 0, max_active = 0;
     double gpu_s = 0, host_s = 0, wait_s = 0, row_chunks = 0;
@@ -724,6 +725,7 @@ void scheduler(mtjg_server *S)
             m->dev = d;
             m->resident = true;
             m->loading = false;
+            m->epoch = ++S->upload_seq;
             S->uploads++;
         }
         const int par = (int)(launched % 2);  // this parity's staging was last read before chunk launched-2
@@ -784,42 +786,81 @@ void scheduler(mtjg_server *S)
 
 constexpr int kLaneRestart = 30;
 
-// One GMRES / BiCGstab request on the resident matrix: mixed precision with
-// the Jacobi preconditioner and the server's monitor and inner settings,
-// through the solver used by mtjg_solver_solve (so the result is what a lone
-// solve with these settings gives).
-int lane_solve(mtjg_server *S, const Req *r, std::vector<double> &x, mtjg_result &res)
+// The Krylov lane's solver state for one upload of a matrix and one solver
+// kind: a borrowed view of the resident arrays, its Jacobi preconditioner and
+// the solver with its workspace.  Kept while that upload is current, so a
+// matrix's later requests allocate (and free, which waits for the device)
+// nothing; an entry of an evicted upload is never used again and goes when
+// the cache needs its place.
+struct LaneState {
+    int64_t epoch = 0;
+    int kind = -1;
+    int64_t last = 0;
+    mtjg_csr *A = nullptr;
+    mtjg_precond *M = nullptr;
+    mtjg_solver *sol = nullptr;
+    void release()
+    {
+        mtjg_solver_destroy(sol);
+        mtjg_precond_destroy(M);
+        mtjg_csr_destroy(A);
+        *this = LaneState();
+    }
+};
+constexpr size_t kLaneCache = 4;
+
+// One GMRES / BiCGstab request on the resident, pinned matrix: mixed
+// precision with the Jacobi preconditioner and the server's monitor and
+// inner settings, through the solver used by mtjg_solver_solve (so the
+// result is what a lone solve with these settings gives).
+int lane_solve(mtjg_server *S, const Req *r, int64_t epoch, std::vector<LaneState> &cache, int64_t &clock,
+               std::vector<double> &x, mtjg_result &res)
 {
     mtjg_ctx *c = S->kctx;
     const ResMat *m = r->mat;
     const int n = m->n;
-    mtjg_csr *A = nullptr;
-    mtjg_precond *M = nullptr;
-    mtjg_solver *sol = nullptr;
-    int st = csr_borrow(c, n, m->h_rowptr.data(), m->dev.rowptr, m->dev.colind, m->dev.val, m->dev.val32, &A);
-    int err_row = 0;
-    if (st == MTJG_OK) st = mtjg_precond_create(c, MTJG_PC_JACOBI, n, &M);
-    if (st == MTJG_OK) st = mtjg_precond_set_matrix(M, A, &err_row);
-    if (st == MTJG_OK) st = mtjg_solver_create(c, r->kind, n, kLaneRestart, &sol);
-    if (st == MTJG_OK) st = mtjg_solver_set_precond(sol, M);
-    mtjg_monitor mon;
-    mtjg_monitor_defaults(&mon);
-    mon.max_iter = S->cfg.max_iter;
-    mon.rtol = S->cfg.rtol;
-    mon.atol = S->cfg.atol;
-    mon.dtol = S->cfg.dtol;
-    if (st == MTJG_OK) st = mtjg_solver_set_monitor(sol, &mon);
-    if (st == MTJG_OK) st = mtjg_solver_set_mixed(sol, 1, S->cfg.inner_rtol, S->cfg.inner_max_iter);
+    LaneState *ls = nullptr;
+    for (LaneState &e : cache)
+        if (e.epoch == epoch && e.kind == r->kind) ls = &e;
+    int st = MTJG_OK;
+    if (!ls) {
+        if (cache.size() >= kLaneCache) {
+            auto lru = std::min_element(cache.begin(), cache.end(),
+                                        [](const LaneState &a, const LaneState &b) { return a.last < b.last; });
+            lru->release();
+            ls = &*lru;
+        } else {
+            cache.emplace_back();
+            ls = &cache.back();
+        }
+        st = csr_borrow(c, n, m->h_rowptr.data(), m->dev.rowptr, m->dev.colind, m->dev.val, m->dev.val32, &ls->A);
+        int err_row = 0;
+        if (st == MTJG_OK) st = mtjg_precond_create(c, MTJG_PC_JACOBI, n, &ls->M);
+        if (st == MTJG_OK) st = mtjg_precond_set_matrix(ls->M, ls->A, &err_row);
+        if (st == MTJG_OK) st = mtjg_solver_create(c, r->kind, n, kLaneRestart, &ls->sol);
+        if (st == MTJG_OK) st = mtjg_solver_set_precond(ls->sol, ls->M);
+        mtjg_monitor mon;
+        mtjg_monitor_defaults(&mon);
+        mon.max_iter = S->cfg.max_iter;
+        mon.rtol = S->cfg.rtol;
+        mon.atol = S->cfg.atol;
+        mon.dtol = S->cfg.dtol;
+        if (st == MTJG_OK) st = mtjg_solver_set_monitor(ls->sol, &mon);
+        if (st == MTJG_OK) st = mtjg_solver_set_mixed(ls->sol, 1, S->cfg.inner_rtol, S->cfg.inner_max_iter);
+        if (st != MTJG_OK) {
+            ls->release();
+            return st;
+        }
+        ls->epoch = epoch;
+        ls->kind = r->kind;
+    }
+    ls->last = ++clock;
     if (r->x0.empty())
         x.assign((size_t)n, 0.0);
     else
         x = r->x0;
     std::memset(&res, 0, sizeof(res));
-    if (st == MTJG_OK) st = mtjg_solver_solve(sol, A, r->b.data(), x.data(), &res);
-    mtjg_solver_destroy(sol);
-    mtjg_precond_destroy(M);
-    mtjg_csr_destroy(A);
-    return st;
+    return mtjg_solver_solve(ls->sol, ls->A, r->b.data(), x.data(), &res);
 }
 
 // The Krylov lane: makes each request's matrix resident (evicting idle ones
@@ -828,6 +869,15 @@ void lane_worker(mtjg_server *S)
 {
     cudaSetDevice(S->kctx->device);
     std::vector<double> x;
+    std::vector<LaneState> cache;
+    int64_t clock = 0;
+    struct Drop {  // the cache goes with the thread, on every way out
+        std::vector<LaneState> &c;
+        ~Drop()
+        {
+            for (LaneState &e : c) e.release();
+        }
+    } drop{cache};
     for (;;) {
         Req *r = nullptr;
         {
@@ -840,6 +890,7 @@ void lane_worker(mtjg_server *S)
         ResMat *m = r->mat;
         std::vector<DevMat> evict;
         bool load = false;
+        int64_t epoch = 0;
         for (;;) {
             std::unique_lock<std::mutex> lk(S->mu);
             if (S->stop || S->error != MTJG_OK) {
@@ -848,6 +899,7 @@ void lane_worker(mtjg_server *S)
             }
             if (m->resident) {
                 m->busy++;
+                epoch = m->epoch;
                 break;
             }
             if (!m->loading && make_room(S, m->bytes, evict)) {
@@ -876,10 +928,12 @@ void lane_worker(mtjg_server *S)
             m->resident = true;
             m->loading = false;
             m->loader = 0;
+            m->epoch = ++S->upload_seq;
+            epoch = m->epoch;
             S->uploads++;
         }
         mtjg_result res;
-        const int st = lane_solve(S, r, x, res);
+        const int st = lane_solve(S, r, epoch, cache, clock, x, res);
         if (st >= MTJG_ERR_CUDA) {
             fail_all(S, st, mtjg_last_error());
             std::lock_guard<std::mutex> lk(S->mu);
@@ -1063,7 +1117,10 @@ extern "C" int mtjg_server_add_matrix(mtjg_server *S, int n, const int *rowptr, 
     std::lock_guard<std::mutex> lk(S->mats_mu);
     std::lock_guard<std::mutex> lk2(S->mu);
     *matrix_id = (int)S->mats.size();
-    if (now) S->uploads++;
+    if (now) {
+        S->uploads++;
+        m->epoch = ++S->upload_seq;
+    }
     S->mats.push_back(m);
     return MTJG_OK;
 }
