@@ -191,9 +191,6 @@ struct LevelSchedule {
     int *perm = nullptr;               // device: rows ordered by level (stable in row index)
     int *chunk = nullptr;              // device [num_chunks + 1]: first perm position of each chunk
     unsigned *ticket = nullptr;        // device: next chunk of the running sweep
-    int *chunk_level = nullptr;        // device [num_chunks]: the level of each chunk
-    int *level_rows = nullptr;         // device [num_levels]: rows per level
-    unsigned *level_done = nullptr;    // device [num_levels]: rows finished in the running sweep
     std::vector<int> level_ptr;        // host: [num_levels + 1]
 };
 

@@ -205,13 +205,6 @@ static int env_int(const char *name, int dflt, int lo, int hi)
     return x < lo ? lo : (x > hi ? hi : x);
 }
 
-// How a sweep's rows wait for their inputs: per x entry (0, the default) or
-// per level (MTJG_SWEEP_LEVELWAIT=1, k_trsv_sweep's LW form).
-#ifndef MTJG_SWEEP_LEVELWAIT_DEFAULT
-#define MTJG_SWEEP_LEVELWAIT_DEFAULT 0
-#endif
-static bool sweep_level_wait() { return env_int("MTJG_SWEEP_LEVELWAIT", MTJG_SWEEP_LEVELWAIT_DEFAULT, 0, 1) != 0; }
-
 __device__ __forceinline__ double ld_relaxed(const double *p)
 {
     unsigned long long v;
@@ -250,11 +243,9 @@ __device__ __forceinline__ double unpend(double v) { return pending(v) ? __longl
 __device__ __forceinline__ float unpend(float v) { return pending(v) ? __uint_as_float(kQuietNaN32) : v; }
 
 // Fills the outputs of the coming sweeps with the pending pattern and resets
-// their ticket counters and level counters (d1 / d2, nl1 / nl2 levels).  x2
-// may be null.
+// their ticket counters.  x2 may be null.
 template <class T>
-__global__ void k_sweep_prep(int n, T *x1, T *x2, unsigned *t1, unsigned *t2, const int *status,
-                             unsigned *d1 = nullptr, int nl1 = 0, unsigned *d2 = nullptr, int nl2 = 0)
+__global__ void k_sweep_prep(int n, T *x1, T *x2, unsigned *t1, unsigned *t2, const int *status)
 {
     if (status && *status != ST_RUNNING) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -262,22 +253,10 @@ __global__ void k_sweep_prep(int n, T *x1, T *x2, unsigned *t1, unsigned *t2, co
         if (t2) *t2 = 0u;
     }
     const T p = pending_value<T>();
-    const int m = n > nl1 ? (n > nl2 ? n : nl2) : (nl1 > nl2 ? nl1 : nl2);
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
-        if (i < n) {
-            x1[i] = p;
-            if (x2) x2[i] = p;
-        }
-        if (d1 && i < nl1) d1[i] = 0u;
-        if (d2 && i < nl2) d2[i] = 0u;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        x1[i] = p;
+        if (x2) x2[i] = p;
     }
-}
-
-__device__ __forceinline__ unsigned ld_acquire(const unsigned *p)
-{
-    unsigned v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
 }
 
 // x_c for a row of the sweep: a relaxed load, polled while it is pending.
@@ -322,12 +301,7 @@ __device__ __forceinline__ T wait_x(const T *x, int c, const int *err, int spin,
 // A row's entries are read in groups of kGrp, whose x loads are all in
 // flight before the first wait.  T = float: the FP32 sweeps (MODE 0 and 1)
 // of the mixed-precision inner solves, on an FP32 copy of the factor.
-// LW (level wait): a warp first waits, on one counter, until every row of
-// the level before its chunk's is solved, then reads its x entries without
-// polling them; after storing its rows it fences and counts them into its
-// level's counter.  Fewer pollers than the per-row waits; the same rows and
-// the same arithmetic.
-template <bool S, int MODE, class T = double, bool LW = false>
+template <bool S, int MODE, class T = double>
 __global__ void __launch_bounds__(kSweepBlock) k_trsv_sweep(const int *__restrict__ perm,
                                                           const int *__restrict__ chunk, int num_chunks,
                                                           const int *__restrict__ rp, const int *__restrict__ ci,
@@ -335,10 +309,7 @@ __global__ void __launch_bounds__(kSweepBlock) k_trsv_sweep(const int *__restric
                                                           const int *__restrict__ diag,
                                                           const T *__restrict__ diagv, const T *b,
                                                           T *x, unsigned *ticket, const int *status, int *err,
-                                                          int spin, const T *__restrict__ aux, T omega,
-                                                          const int *__restrict__ chunk_level = nullptr,
-                                                          const int *__restrict__ level_rows = nullptr,
-                                                          unsigned *level_done = nullptr)
+                                                          int spin, const T *__restrict__ aux, T omega)
 {
     constexpr int kGrp = 4;
     if (status && *status != ST_RUNNING) return;
@@ -350,25 +321,7 @@ __global__ void __launch_bounds__(kSweepBlock) k_trsv_sweep(const int *__restric
         if (c >= (unsigned)num_chunks) return;
         const int beg = chunk[c], cnt = chunk[c + 1] - beg;
         bool bad = false;
-        int lev = 0;
-        if constexpr (LW) {
-            lev = chunk_level[c];
-            if (lev > 0) {
-                const unsigned want = (unsigned)level_rows[lev - 1];
-                unsigned ns = 32;
-                for (long long polls = 0; ld_acquire(level_done + lev - 1) < want; ++polls) {
-                    if (polls > spin) {
-                        __nanosleep(ns);
-                        ns = ns < 256 ? 2 * ns : ns;
-                    }
-                    if (polls > kSweepSpinLimit || ((polls & 31) == 31 && *(volatile const int *)err)) {
-                        bad = true;
-                        break;
-                    }
-                }
-            }
-        }
-        if (lane < cnt && !bad) {
+        if (lane < cnt) {
             const int i = perm[beg + lane];
             const T bi = b[i];
             // entry range, walked upwards from kb (MODE 3: downwards from ke - 1)
@@ -426,11 +379,6 @@ __global__ void __launch_bounds__(kSweepBlock) k_trsv_sweep(const int *__restric
             if (lane == 0) atomicExch(err, 1);
             return;
         }
-        if constexpr (LW) {
-            __threadfence();  // this lane's x before the count
-            __syncwarp();
-            if (lane == 0) atomicAdd(level_done + lev, (unsigned)cnt);
-        }
     }
 }
 
@@ -450,11 +398,8 @@ static void free_sched(LevelSchedule &s)
     cudaFree(s.perm);
     cudaFree(s.chunk);
     cudaFree(s.ticket);
-    cudaFree(s.chunk_level);
-    cudaFree(s.level_rows);
-    cudaFree(s.level_done);
-    s.perm = s.chunk = s.chunk_level = s.level_rows = nullptr;
-    s.ticket = s.level_done = nullptr;
+    s.perm = s.chunk = nullptr;
+    s.ticket = nullptr;
     s.level_ptr.clear();
     s.num_levels = 0;
     s.num_chunks = 0;
@@ -512,17 +457,6 @@ static int build_levels(mtjg_ctx *ctx, int n, int desc, int range, const int *rp
     MTJG_CUDA(cudaMemcpy(out.chunk, chunk.data(), sizeof(int) * chunk.size(), cudaMemcpyHostToDevice));
     MTJG_CUDA(cudaMalloc(&out.ticket, sizeof(unsigned)));
     MTJG_CUDA(cudaMemset(out.ticket, 0, sizeof(unsigned)));
-    std::vector<int> clev(out.num_chunks), lrows(nl);
-    for (int l = 0, q = 0; l < nl; ++l) {
-        lrows[l] = out.level_ptr[l + 1] - out.level_ptr[l];
-        for (int p = out.level_ptr[l]; p < out.level_ptr[l + 1]; p += 32) clev[q++] = l;
-    }
-    MTJG_CUDA(cudaMalloc(&out.chunk_level, sizeof(int) * (size_t)std::max(1, out.num_chunks)));
-    MTJG_CUDA(cudaMemcpy(out.chunk_level, clev.data(), sizeof(int) * clev.size(), cudaMemcpyHostToDevice));
-    MTJG_CUDA(cudaMalloc(&out.level_rows, sizeof(int) * (size_t)nl));
-    MTJG_CUDA(cudaMemcpy(out.level_rows, lrows.data(), sizeof(int) * (size_t)nl, cudaMemcpyHostToDevice));
-    MTJG_CUDA(cudaMalloc(&out.level_done, sizeof(unsigned) * (size_t)nl));
-    MTJG_CUDA(cudaMemset(out.level_done, 0, sizeof(unsigned) * (size_t)nl));
     return MTJG_OK;
 }
 
@@ -531,9 +465,8 @@ static int build_levels(mtjg_ctx *ctx, int n, int desc, int range, const int *rp
 static cudaError_t sweep_prep(mtjg_ctx *ctx, int n, double *x1, double *x2, LevelSchedule *s1, LevelSchedule *s2,
                               const int *status)
 {
-    k_sweep_prep<<<grid_for(ctx, n), kBlock, 0, ctx->stream>>>(
-        n, x1, x2, s1 ? s1->ticket : nullptr, s2 ? s2->ticket : nullptr, status, s1 ? s1->level_done : nullptr,
-        s1 ? s1->num_levels : 0, s2 ? s2->level_done : nullptr, s2 ? s2->num_levels : 0);
+    k_sweep_prep<<<grid_for(ctx, n), kBlock, 0, ctx->stream>>>(n, x1, x2, s1 ? s1->ticket : nullptr,
+                                                               s2 ? s2->ticket : nullptr, status);
     ctx->launches++;
     return cudaGetLastError();
 }
@@ -547,19 +480,10 @@ static cudaError_t sweep_t(mtjg_ctx *ctx, bool strict, const LevelSchedule &s, c
     const int warps = ctx->num_sms * env_int("MTJG_SWEEP_WARPS", kSweepWarpsPerSm, 1, 40);
     const int spin = env_int("MTJG_SWEEP_SPIN", kSweepSpin, 0, 1 << 20);
     const int grid = (std::min(warps, s.num_chunks) + kSweepBlock / 32 - 1) / (kSweepBlock / 32);
-    const bool lw = sweep_level_wait();
-    if (strict && lw)
-        k_trsv_sweep<true, MODE, double, true><<<grid, kSweepBlock, 0, ctx->stream>>>(
-            s.perm, s.chunk, s.num_chunks, rp, ci, v, diag, diagv, b, x, s.ticket, status, ctx->d_flag, spin, aux,
-            omega, s.chunk_level, s.level_rows, s.level_done);
-    else if (strict)
+    if (strict)
         k_trsv_sweep<true, MODE><<<grid, kSweepBlock, 0, ctx->stream>>>(s.perm, s.chunk, s.num_chunks, rp, ci, v, diag,
                                                                       diagv, b, x, s.ticket, status, ctx->d_flag,
                                                                       spin, aux, omega);
-    else if (lw)
-        k_trsv_sweep<false, MODE, double, true><<<grid, kSweepBlock, 0, ctx->stream>>>(
-            s.perm, s.chunk, s.num_chunks, rp, ci, v, diag, diagv, b, x, s.ticket, status, ctx->d_flag, spin, aux,
-            omega, s.chunk_level, s.level_rows, s.level_done);
     else
         k_trsv_sweep<false, MODE><<<grid, kSweepBlock, 0, ctx->stream>>>(s.perm, s.chunk, s.num_chunks, rp, ci, v,
                                                                        diag, diagv, b, x, s.ticket, status,
@@ -694,14 +618,9 @@ static cudaError_t sweep32(mtjg_ctx *ctx, const LevelSchedule &s, const int *rp,
     const int warps = ctx->num_sms * env_int("MTJG_SWEEP_WARPS", kSweepWarpsPerSm, 1, 40);
     const int spin = env_int("MTJG_SWEEP_SPIN", kSweepSpin, 0, 1 << 20);
     const int grid = (std::min(warps, s.num_chunks) + kSweepBlock / 32 - 1) / (kSweepBlock / 32);
-    if (sweep_level_wait())
-        k_trsv_sweep<false, MODE, float, true><<<grid, kSweepBlock, 0, ctx->stream>>>(
-            s.perm, s.chunk, s.num_chunks, rp, ci, v, diag, nullptr, b, x, s.ticket, status, ctx->d_flag, spin,
-            nullptr, 0.0f, s.chunk_level, s.level_rows, s.level_done);
-    else
-        k_trsv_sweep<false, MODE, float><<<grid, kSweepBlock, 0, ctx->stream>>>(
-            s.perm, s.chunk, s.num_chunks, rp, ci, v, diag, nullptr, b, x, s.ticket, status, ctx->d_flag, spin,
-            nullptr, 0.0f);
+    k_trsv_sweep<false, MODE, float><<<grid, kSweepBlock, 0, ctx->stream>>>(
+        s.perm, s.chunk, s.num_chunks, rp, ci, v, diag, nullptr, b, x, s.ticket, status, ctx->d_flag, spin, nullptr,
+        0.0f);
     ctx->launches++;
     return cudaGetLastError();
 }
@@ -757,9 +676,8 @@ int precond_apply32(mtjg_precond *M, const float *b, float *x, const int *status
         break;
     default: {  // ILU / ILUT: L y = b, then U x = y, on the FP32 factor
         const bool alias = x == b;
-        k_sweep_prep<float><<<grid_for(ctx, n), kBlock, 0, ctx->stream>>>(
-            n, M->y32, alias ? nullptr : x, M->lo.ticket, M->up.ticket, status, M->lo.level_done, M->lo.num_levels,
-            M->up.level_done, M->up.num_levels);
+        k_sweep_prep<float><<<grid_for(ctx, n), kBlock, 0, ctx->stream>>>(n, M->y32, alias ? nullptr : x,
+                                                                          M->lo.ticket, M->up.ticket, status);
         ctx->launches++;
         e = cudaGetLastError();
         if (e == cudaSuccess)
