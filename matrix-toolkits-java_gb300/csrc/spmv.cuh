@@ -59,6 +59,17 @@ struct Stage {
 #define MTJG_SPMV_CTAS_REDUCE 5
 #endif
 constexpr int kSpmvStages = MTJG_SPMV_STAGES;  // tiles in shared memory per CTA (NST - 1 in flight ahead)
+// How a one-thread-per-row tile gets x_r for an epilogue that needs it:
+// caught from the row's own diagonal gather, or one load per row, which
+// saves a compare and a select per entry (the value is the same).  Measured
+// on GB300: the load made the served FP32 mix 1.5 % faster and the FP64 CG
+// 1 % slower, so FP32 tiles load and FP64 tiles catch (MTJG_SPMV_XR_LOAD=1
+// makes every tile load).
+#ifndef MTJG_SPMV_XR_LOAD
+#define MTJG_SPMV_XR_LOAD 0
+#endif
+template <class T>
+constexpr bool xr_load() { return MTJG_SPMV_XR_LOAD != 0 || sizeof(T) == 4; }
 template <class T>
 constexpr int spmv_smem() { return kSpmvStages * Stage<T>::kBytes; }
 // resident CTAs per SM the register budget is set for: products without a
@@ -343,7 +354,7 @@ __global__ void __launch_bounds__(kBlock, EpiCtas<Epi>::value)
                         if (k < la) {
                             const int c = sc[ba + k - co];
                             const T xv = __ldg(xs + c);
-                            if (c == ra) {
+                            if (!xr_load<T>() && c == ra) {
                                 xra = xv;
                                 da = true;
                             }
@@ -352,7 +363,7 @@ __global__ void __launch_bounds__(kBlock, EpiCtas<Epi>::value)
                         if (k < lb) {
                             const int c = sc[bb + k - co];
                             const T xv = __ldg(xs + c);
-                            if (c == rb) {
+                            if (!xr_load<T>() && c == rb) {
                                 xrb = xv;
                                 db = true;
                             }
@@ -376,7 +387,7 @@ __global__ void __launch_bounds__(kBlock, EpiCtas<Epi>::value)
                     for (int k = b; k < e; ++k) {
                         const int c = sc[k - co];
                         const T xv = __ldg(xs + c);
-                        if (c == r) {
+                        if (!xr_load<T>() && c == r) {
                             xr = xv;
                             diag = true;
                         }
