@@ -341,6 +341,15 @@ MTJG_API int mtjg_solver_solve_dev(mtjg_solver *S, mtjg_csr *A, const double *db
  * preconditioners at solve time.  enable = 0 restores the FP64 solver.  No
  * counterpart in the reference. */
 MTJG_API int mtjg_solver_set_mixed(mtjg_solver *S, int enable, double inner_rtol, int inner_max_iter);
+/* How the iterations of a solve are launched.  MTJG_LAUNCH_AUTO (the
+ * default): CG with the identity or Jacobi preconditioner on one system of at
+ * most 512 product tiles (about 80k rows at 7 entries per row, no row longer
+ * than 1152 entries) runs its whole loop in one cooperative launch, the
+ * matrix held in shared memory, with the results of the graph path bit for
+ * bit; every other solve runs a captured graph of its phase launches.
+ * MTJG_LAUNCH_GRAPH: always the graph.  No counterpart in the reference. */
+enum { MTJG_LAUNCH_AUTO = 0, MTJG_LAUNCH_GRAPH = 1 };
+MTJG_API int mtjg_solver_set_launch(mtjg_solver *S, int mode);
 /* Residual history of the last solve: the (residual, iteration) pairs passed
  * to IterationReporter.monitor, oldest first (up to history_cap); for a
  * batch, that of the system the result describes (the first that did not

@@ -232,23 +232,13 @@ __device__ __forceinline__ void group_partial(Acc &a, int group, const RedCtx &r
     }
 }
 
-// The reduction of a phase finishes in k_finalize (a launch of its own after
-// the phase's kernel): block s sums system s's group partials in group order
-// (thread t takes groups t, t+B, t+2B, ... with four loads in flight, then
-// the fixed block tree) and thread 0 runs op.scalar(s, sums).  No atomics
-// and no fences: the launch boundary orders the partial stores before it.
-//
-// Kernel templates and their launchers live in an unnamed namespace: without
-// relocatable device code every translation unit carries its own device
-// image, so each one instantiates (and sets attributes on) its own kernels.
-namespace {
-template <class Op>
-__global__ void __launch_bounds__(kBlock) k_finalize(Op op, RedCtx rc, int type)
+// System sys's group partials summed in group order by a block of kBlock
+// threads (valid in thread 0): thread t takes groups t, t+B, t+2B, ... with
+// four loads in flight, then the fixed block tree.  Plain loads: a kernel
+// may sum partials that its own blocks wrote before a grid barrier.
+template <int SLOTS>
+__device__ __forceinline__ Acc system_sum(const RedCtx &rc, int sys, int type, double *sm)
 {
-    constexpr int SLOTS = OpSlots<Op>::value;
-    __shared__ double sm[kParts * kBlock];
-    const int sys = blockIdx.x;
-    if (!op.active(sys)) return;
     const int g0 = rc.sys_group[sys], g1 = rc.sys_group[sys + 1];
     const int stride = blockDim.x;
     Acc s;
@@ -268,6 +258,27 @@ __global__ void __launch_bounds__(kBlock) k_finalize(Op op, RedCtx rc, int type)
             if (base + u * stride < g1) acc_merge_m<SLOTS>(s, o[u], type);
     }
     block_reduce<SLOTS>(s, type, sm);
+    return s;
+}
+
+// The reduction of a phase finishes in k_finalize (a launch of its own after
+// the phase's kernel): block s forms system s's sums and thread 0 runs
+// op.scalar(s, sums).  No atomics and no fences: the launch boundary orders
+// the partial stores before it.  (The one-launch CG sums a phase's partials
+// itself, with the same function, after a grid barrier.)
+//
+// Kernel templates and their launchers live in an unnamed namespace: without
+// relocatable device code every translation unit carries its own device
+// image, so each one instantiates (and sets attributes on) its own kernels.
+namespace {
+template <class Op>
+__global__ void __launch_bounds__(kBlock) k_finalize(Op op, RedCtx rc, int type)
+{
+    constexpr int SLOTS = OpSlots<Op>::value;
+    __shared__ double sm[kParts * kBlock];
+    const int sys = blockIdx.x;
+    if (!op.active(sys)) return;
+    const Acc s = system_sum<SLOTS>(rc, sys, type, sm);
     if (threadIdx.x == 0) op.scalar(sys, s);
 }
 }  // namespace

@@ -642,6 +642,8 @@ struct GmX {
 
 }  // namespace mtjg
 
+#include "persist.cuh"
+
 using namespace mtjg;
 
 // ================================================================ handle
@@ -700,6 +702,14 @@ struct mtjg_solver {
     int64_t ir_fcap = 0, ir_dcap = 0, ir_hcap = 0;
     bool last_empty = false;   // the last solve had n == 0: its history is empty_it (residuals 0)
     std::vector<int> empty_it;
+    // one-launch CG (persist.cuh): MTJG_LAUNCH_*, the product's partials,
+    // the barrier's arrival count and abort word
+    int launch_mode = MTJG_LAUNCH_AUTO;
+    double *pc_part = nullptr;
+    int64_t pc_part_cap = 0;
+    double *pc_p2 = nullptr;  // the second p buffer
+    unsigned long long *pc_bar = nullptr;
+    bool last_persistent = false;
 };
 
 namespace {
@@ -1229,6 +1239,103 @@ int ensure_state(mtjg_solver *S, int ns)
     return MTJG_OK;
 }
 
+// CG with the identity or Jacobi preconditioner on one system of at most
+// kPersistMaxTiles product tiles (no row longer than a tile) runs its loop in
+// one cooperative launch (persist.cuh) unless the graph path was asked for.
+bool persistent_cg(const mtjg_solver *S, const mtjg_csr *A)
+{
+    return S->launch_mode == MTJG_LAUNCH_AUTO && S->kind == MTJG_CG && !S->mixed && pc_mode(S) != kPcExternal &&
+           A->sys_rows.empty() && A->tiles.num_sys == 1 && A->rtiles.num_sys == 1 && A->tiles.num_long == 0 &&
+           A->tiles.num_tiles > 0 && A->tiles.num_tiles <= kPersistMaxTiles &&
+           A->tiles.num_groups == A->tiles.num_tiles && A->rtiles.num_groups == A->rtiles.num_tiles;
+}
+
+struct PersistPlan {
+    int grid = 0;
+    int slots = 0;  // cached product tiles per CTA
+    size_t smem = 0;
+};
+
+// The grid of the one-launch CG: as many co-resident CTAs as there are
+// tiles, up to 4 per SM, each caching ceil(tiles / grid) product tiles in
+// shared memory; fewer CTAs per SM (more slots each) when that does not fit.
+// False when no grid fits: the solve takes the graph path.
+template <bool STRICT>
+bool persist_plan(mtjg_ctx *ctx, const mtjg_csr *A, PersistPlan &pl)
+{
+    auto k = k_cg_persist<STRICT>;
+    int optin = 0;
+    cudaFuncAttributes fa{};
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device) != cudaSuccess ||
+        cudaFuncGetAttributes(&fa, k) != cudaSuccess)
+        return false;
+    const int maxdyn = optin - (int)fa.sharedSizeBytes;
+    if (maxdyn < kSlotBytes || cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, maxdyn) != cudaSuccess)
+        return false;
+    const int NT = A->tiles.num_tiles, NR = A->rtiles.num_tiles;
+    for (int per_sm = 4; per_sm >= 1; --per_sm) {
+        const int G = std::min(std::max(NT, NR), per_sm * ctx->num_sms);
+        const int slots = (NT + G - 1) / G;
+        const size_t smem = (size_t)slots * kSlotBytes;
+        if (smem > (size_t)maxdyn) continue;
+        int blocks = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k, kBlock, smem) != cudaSuccess) return false;
+        if ((int64_t)blocks * ctx->num_sms >= G) {
+            pl.grid = G;
+            pl.slots = slots;
+            pl.smem = smem;
+            return true;
+        }
+    }
+    return false;
+}
+
+// The loop body of CG after cg_init, in one launch; the state and the
+// running count end as the graph path leaves them.
+template <bool STRICT>
+int run_persistent_cg(mtjg_solver *S, mtjg_csr *A, const PersistPlan &pl)
+{
+    mtjg_ctx *ctx = S->ctx;
+    const int64_t need = (int64_t)(A->tiles.num_groups + 1) * kParts;
+    if (need > S->pc_part_cap) {
+        cudaFree(S->pc_part);
+        S->pc_part = nullptr;
+        S->pc_part_cap = 0;
+        MTJG_CUDA(cudaMalloc(&S->pc_part, sizeof(double) * (size_t)need));
+        S->pc_part_cap = need;
+    }
+    if (!S->pc_p2) MTJG_CUDA(cudaMalloc(&S->pc_p2, sizeof(double) * (size_t)std::max(1, S->n)));
+    if (!S->pc_bar) MTJG_CUDA(cudaMalloc(&S->pc_bar, 2 * sizeof(unsigned long long)));
+    MTJG_CUDA(cudaMemsetAsync(S->pc_bar, 0, 2 * sizeof(unsigned long long), ctx->stream));
+    const int pcm = pc_mode(S);
+    PersistCg c;
+    c.A = CsrArgs{A->rowptr, A->colind, A->val};
+    c.pt = tile_args(A->tiles);
+    c.rt = tile_args(A->rtiles);
+    c.invdiag = S->M && S->M->kind == MTJG_PC_JACOBI ? S->M->invdiag : nullptr;
+    c.x = S->vecs[V_X];
+    c.r = S->vecs[V_R];
+    c.z = pcm == kPcIdentity ? S->vecs[V_R] : S->vecs[V_Z];
+    c.q = S->vecs[V_Q];
+    c.p[0] = S->vecs[V_P];
+    c.p[1] = S->pc_p2;
+    c.pc = pcm;
+    c.slots = pl.slots;
+    c.rcq = RedCtx{S->pc_part, A->cnt, A->tiles.sys_group, A->num_running};
+    c.rcu = red_ctx(A, A->rtiles);
+    c.m = MonPtrs{S->st, mon_dev(S), S->hist_r, S->hist_it, A->num_running};
+    c.gb = GridBar{S->pc_bar, reinterpret_cast<int *>(S->pc_bar + 1)};
+    c.err = ctx->d_flag;
+    int normtype = S->mon.norm;
+    void *args[] = {&c, &normtype};
+    MTJG_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<void *>(k_cg_persist<STRICT>), dim3(pl.grid), dim3(kBlock),
+                                          args, pl.smem, ctx->stream));
+    ctx->launches++;
+    return MTJG_OK;
+}
+
+int finish_run(mtjg_solver *S, mtjg_result *res);
+
 // vectors b and x are in the solver's buffers
 int run(mtjg_solver *S, mtjg_csr *A, mtjg_result *res)
 {
@@ -1260,6 +1367,17 @@ int run(mtjg_solver *S, mtjg_csr *A, mtjg_result *res)
     }
     st = phase(S, A, true);
     if (st != MTJG_OK) return st;
+    PersistPlan pl;
+    const bool strict = ctx->numerics == MTJG_NUMERICS_STRICT;
+    S->last_persistent =
+        persistent_cg(S, A) && (strict ? persist_plan<true>(ctx, A, pl) : persist_plan<false>(ctx, A, pl));
+    if (S->last_persistent) {
+        // one launch runs the loop to the monitor's verdict (a solve that
+        // cg_init finished already leaves it nothing to do)
+        st = strict ? run_persistent_cg<true>(S, A, pl) : run_persistent_cg<false>(S, A, pl);
+        if (st != MTJG_OK) return st;
+        return finish_run(S, res);
+    }
     const bool stale = !S->gexec || S->g_A != A || S->g_M != S->M || S->g_numerics != ctx->numerics ||
                        S->g_norm != S->mon.norm || S->g_version != (S->M ? S->M->version : 0) ||
                        S->g_aversion != A->version;
@@ -1295,6 +1413,15 @@ int run(mtjg_solver *S, mtjg_csr *A, mtjg_result *res)
             }
         }
     }
+    return finish_run(S, res);
+}
+
+// After the loop: the systems' states and the error flag back to the host,
+// and the caller's view of them.
+int finish_run(mtjg_solver *S, mtjg_result *res)
+{
+    mtjg_ctx *ctx = S->ctx;
+    const int ns = S->num_sys;
     MTJG_CUDA(cudaMemcpyAsync(S->last_all.data(), S->st, sizeof(SysState) * (size_t)ns, cudaMemcpyDeviceToHost,
                               ctx->stream));
     int flag = 0;
@@ -1629,6 +1756,9 @@ extern "C" int mtjg_solver_destroy(mtjg_solver *S)
     drop_graph(S);
     for (double *p : S->vecs) cudaFree(p);
     for (float *p : S->v32) cudaFree(p);
+    cudaFree(S->pc_part);
+    cudaFree(S->pc_p2);
+    cudaFree(S->pc_bar);
     cudaFree(S->invdiag32);
     cudaFree(S->V);
     cudaFree(S->gm.H);
@@ -1710,6 +1840,15 @@ extern "C" int mtjg_solver_set_mixed(mtjg_solver *S, int enable, double inner_rt
     S->mixed = enable != 0;
     if (enable) S->mix = MixCfg{inner_rtol, inner_max_iter, 0, 0.0, 0.0};
     drop_graph(S);
+    return MTJG_OK;
+}
+
+extern "C" int mtjg_solver_set_launch(mtjg_solver *S, int mode)
+{
+    if (!S) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL solver");
+    if (mode != MTJG_LAUNCH_AUTO && mode != MTJG_LAUNCH_GRAPH)
+        return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "launch mode must be MTJG_LAUNCH_AUTO or MTJG_LAUNCH_GRAPH");
+    S->launch_mode = mode;
     return MTJG_OK;
 }
 

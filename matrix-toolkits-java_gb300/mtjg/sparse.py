@@ -678,6 +678,13 @@ class AbstractIterativeSolver:
         _raise(self._lib.mtjg_solver_set_mixed(self.h, 1 if enable else 0, float(inner_rtol), int(inner_max_iter)),
                "set_mixed")
 
+    def setGraphLaunch(self, enable=True):
+        """Run every iteration as graph-captured phase launches
+        (mtjg_solver_set_launch MTJG_LAUNCH_GRAPH), also where a small CG
+        solve would otherwise run its loop in one launch; enable=False
+        restores the default.  The results are the same either way."""
+        _raise(self._lib.mtjg_solver_set_launch(self.h, 1 if enable else 0), "set_launch")
+
     def innerIterations(self):
         r = getattr(self, "last_result", None)
         return r.inner_iterations if r is not None else 0
