@@ -299,8 +299,11 @@ __device__ __forceinline__ T wait_x(const T *x, int c, const int *err, int spin,
 //          aux (the forward iterate), upper entries from the new x (waited
 //          for); x_i = aux_i + omega (sigma' - aux_i)
 // A row's entries are read in groups of kGrp, whose x loads are all in
-// flight before the first wait.  T = float: the FP32 sweeps (MODE 0 and 1)
-// of the mixed-precision inner solves, on an FP32 copy of the factor.
+// flight before the first wait, and the operands that finish the row (the
+// diagonal, SSOR's old iterate) are loaded before the waits too: once the
+// last dependency arrives a row is arithmetic and one store, not further
+// dependent loads.  T = float: the FP32 sweeps (MODE 0 and 1) of the
+// mixed-precision inner solves, on an FP32 copy of the factor.
 template <bool S, int MODE, class T = double>
 __global__ void __launch_bounds__(kSweepBlock) k_trsv_sweep(const int *__restrict__ perm,
                                                           const int *__restrict__ chunk, int num_chunks,
@@ -337,6 +340,14 @@ __global__ void __launch_bounds__(kSweepBlock) k_trsv_sweep(const int *__restric
                 ke = rp[i + 1];
             }
             if constexpr (MODE >= 4) dk = diag[i];
+            // the row's finishing operands, ahead of the waits
+            T dfin = T(1), old = T(0);
+            if constexpr (MODE == 1) dfin = v[diag[i]];
+            else if constexpr (MODE == 2) dfin = diagv[i];
+            else if constexpr (MODE >= 4) {
+                dfin = v[dk];
+                old = aux[i];
+            }
             T acc = (MODE == 2 || MODE == 3) ? bi : T(0);
             for (int k0 = 0; k0 < ke - kb && !bad; k0 += kGrp) {
                 int cc[kGrp];
@@ -363,12 +374,12 @@ __global__ void __launch_bounds__(kSweepBlock) k_trsv_sweep(const int *__restric
             }
             T xi;
             if constexpr (MODE == 0) xi = bi - acc;
-            else if constexpr (MODE == 1) xi = (bi - acc) / v[diag[i]];
-            else if constexpr (MODE == 2) xi = acc / diagv[i];
+            else if constexpr (MODE == 1) xi = (bi - acc) / dfin;
+            else if constexpr (MODE == 2) xi = acc / dfin;
             else if constexpr (MODE == 3) xi = acc;
             else {
                 // sigma = (b_i - sigma) / a_ii; x_i = old_i + omega (sigma - old_i)
-                const T sig = (bi - acc) / v[dk], old = aux[i];
+                const T sig = (bi - acc) / dfin;
                 if constexpr (S) xi = __dadd_rn(old, __dmul_rn(omega, __dsub_rn(sig, old)));
                 else xi = fma(omega, sig - old, old);
             }
