@@ -4,10 +4,11 @@ With lookahead a row whose dependency is still pending computes that
 dependency's value itself, with the operations of the dependency's own row
 in the same order; the stored results, and so every solve built on them,
 must not change.  Each test runs with every mode looking ahead
-(MTJG_SWEEP_LOOKAHEAD=7) and with none (0); the default set lies between.  Covered: ILU(0) L and U sweeps and
-the ICC transposed-gather and U sweeps (FP64, both numerics), the FP32 ILU
-sweeps of a mixed-precision GMRES, and a matrix whose rows exceed the
-lookahead's four entries (those rows wait instead).  Parity of the sweeps
+(MTJG_SWEEP_LOOKAHEAD=7) and with none (0); the default set lies between.
+Covered: ILU(0) L and U sweeps and the ICC transposed-gather and U sweeps
+(FP64, both numerics), the FP32 ILU sweeps of a mixed-precision GMRES, and a
+matrix whose rows exceed the lookahead's four entries (those rows wait
+instead).  Parity of the sweeps
 with the oracle is covered by the parity and config tests.
 """
 import os
