@@ -34,7 +34,14 @@
 namespace mtjg {
 
 constexpr int kBatchBlock = 256;
-constexpr int kBatchMinBlocks = 3;
+// resident CTAs per SM the batched CG is compiled for (its register cap).
+// Measured on GB300 (C4, FP64 / mixed): 3 (80 registers) 168.5 / 115.7 ms;
+// 4 (64 registers) 200.9 / 128.0 ms; 5: 238.6 / 152.8 ms -- the rows a
+// thread keeps in flight matter more than resident warps.
+#ifndef MTJG_BATCH_MINB
+#define MTJG_BATCH_MINB 3
+#endif
+constexpr int kBatchMinBlocks = MTJG_BATCH_MINB;
 constexpr int kProbeIters = 12;
 constexpr int kProbeSystems = 24;
 constexpr int kVecCandidates[] = {1, 2, 4, 8, 32};
