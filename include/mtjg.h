@@ -341,6 +341,18 @@ MTJG_API int mtjg_solver_solve_dev(mtjg_solver *S, mtjg_csr *A, const double *db
  * preconditioners at solve time.  enable = 0 restores the FP64 solver.  No
  * counterpart in the reference. */
 MTJG_API int mtjg_solver_set_mixed(mtjg_solver *S, int enable, double inner_rtol, int inner_max_iter);
+/* setIterationMonitor(new MatrixIterationMonitor(normA, normb, ...))
+ * (S/MatrixIterationMonitor.java): with enable != 0 every convergence test
+ * converges iff r < max(rtol (normA |x| + normb), atol), |x| the current
+ * iterate's norm in the monitor's norm type, formed on the device before the
+ * test; divergence, iteration and NaN tests as DefaultIterationMonitor.  The
+ * other settings (maxIter, tolerances, norm) come from mtjg_solver_set_monitor.
+ * GMRES's inner test calls converged(double), which MatrixIterationMonitor
+ * does not support: a GMRES solve that does not converge at its first test
+ * ends MTJG_ERR_UNSUPPORTED (UnsupportedOperationException), as in MTJ.
+ * Single-system FP64 solves only (batched or mixed: MTJG_ERR_UNSUPPORTED at
+ * solve time).  enable = 0 restores DefaultIterationMonitor. */
+MTJG_API int mtjg_solver_set_matrix_monitor(mtjg_solver *S, int enable, double normA, double normb);
 /* How the iterations of a solve are launched.  MTJG_LAUNCH_AUTO (the
  * default): CG with the identity or Jacobi preconditioner on one system of at
  * most 512 product tiles (about 80k rows at 7 entries per row, no row longer

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <utility>
+
 #include "internal.h"
 
 namespace mtjg {
@@ -270,6 +272,17 @@ __device__ __forceinline__ Acc system_sum(const RedCtx &rc, int sys, int type, d
 // Kernel templates and their launchers live in an unnamed namespace: without
 // relocatable device code every translation unit carries its own device
 // image, so each one instantiates (and sets attributes on) its own kernels.
+// An op with a monitor (member m with MatrixIterationMonitor fields) has its
+// finalize form |x| first when a MatrixIterationMonitor is set (m.x).
+template <class Op, class = void>
+struct OpMon {
+    static constexpr bool value = false;
+};
+template <class Op>
+struct OpMon<Op, decltype((void)std::declval<const Op &>().m.mon.xmon)> {
+    static constexpr bool value = true;
+};
+
 namespace {
 template <class Op>
 __global__ void __launch_bounds__(kBlock) k_finalize(Op op, RedCtx rc, int type)
@@ -278,6 +291,9 @@ __global__ void __launch_bounds__(kBlock) k_finalize(Op op, RedCtx rc, int type)
     __shared__ double sm[kParts * kBlock];
     const int sys = blockIdx.x;
     if (!op.active(sys)) return;
+    if constexpr (OpMon<Op>::value) {
+        if (op.m.x) op.m.xnorm_block(sys, sm);
+    }
     const Acc s = system_sum<SLOTS>(rc, sys, type, sm);
     if (threadIdx.x == 0) op.scalar(sys, s);
 }
@@ -286,7 +302,9 @@ __global__ void __launch_bounds__(kBlock) k_finalize(Op op, RedCtx rc, int type)
 // ------------------------------------------------------------ monitor
 // AbstractIterationMonitor.converged(double) + DefaultIterationMonitor.convergedI
 // (S/AbstractIterationMonitor.java:81-93, S/DefaultIterationMonitor.java:133-156):
-// record (r, iter) for the reporter, then test in MTJ's order.
+// record (r, iter) for the reporter, then test in MTJ's order (with a
+// MatrixIterationMonitor, its convergence test, S/MatrixIterationMonitor.java
+// :108-130).
 __device__ __forceinline__ int monitor_check(SysState &st, const MonCfgDev &c, double r,
                                              double *hist_r, int *hist_it)
 {
@@ -297,11 +315,29 @@ __device__ __forceinline__ int monitor_check(SysState &st, const MonCfgDev &c, d
     st.hist_len++;
     st.residual = r;
     if (st.iter == 0) st.initR = r;
-    if (r < jmax(c.rtol * st.initR, c.atol)) return ST_DONE;
+    const double tol = c.xmon ? jmax(c.rtol * (c.normA * st.xnorm + c.normb), c.atol) : jmax(c.rtol * st.initR, c.atol);
+    if (r < tol) return ST_DONE;
     if (r > c.dtol * st.initR) return MTJG_NOT_CONVERGED_DIVERGENCE;
     if (st.iter >= c.max_iter) return MTJG_NOT_CONVERGED_ITERATIONS;
     if (r != r) return MTJG_NOT_CONVERGED_DIVERGENCE;
     return ST_RUNNING;
+}
+
+// AbstractIterationMonitor.converged(double) (S/AbstractIterationMonitor.java
+// :88-93), GMRES's inner test: the reporter and the residual, then
+// convergedI(r), which a MatrixIterationMonitor does not support
+// (S/MatrixIterationMonitor.java:132-135).
+__device__ __forceinline__ int monitor_check_scalar(SysState &st, const MonCfgDev &c, double r, double *hist_r,
+                                                    int *hist_it)
+{
+    if (!c.xmon) return monitor_check(st, c, r, hist_r, hist_it);
+    if (st.hist_len < c.hist_cap) {
+        hist_r[st.hist_len] = r;
+        hist_it[st.hist_len] = st.iter;
+    }
+    st.hist_len++;
+    st.residual = r;
+    return MTJG_ERR_UNSUPPORTED;
 }
 
 // ---------------------------------------------------- bulk copies (TMA)

@@ -133,6 +133,7 @@ struct SysState {
     // (coef[0], coef[1]) or the d / s scale factor (coef[0])
     double xi, gamma, gamma_1, theta, theta_1, eta, delta, ep;
     double coef[2];
+    double xnorm;  // MatrixIterationMonitor: |x| at the coming test
 };
 
 struct MonCfgDev {
@@ -141,6 +142,12 @@ struct MonCfgDev {
     int hist_cap;
     int pad;
     double rtol, atol, dtol;
+    // MatrixIterationMonitor (S/MatrixIterationMonitor.java:108-130): a test
+    // converges iff r < max(rtol (normA |x| + normb), atol), |x| being
+    // SysState::xnorm, the iterate's norm formed just before the test
+    int xmon = 0;
+    int pad2 = 0;
+    double normA = 0, normb = 0;
 };
 
 // Reduction context: per-group partial sums and the group ranges of the

@@ -501,7 +501,7 @@ struct GmNorm {
             t.inner_done = 0;
             t.scratch[0] = 1 / t.normr;  // v[0].set(1 / normr, r)
             if (g.restart > 0) {
-                c = m.check(t, sys, fabs(g.s[0]));
+                c = m.check_scalar(t, sys, fabs(g.s[0]));
                 if (c == ST_DONE) {
                     t.inner_done = 1;
                     c = ST_RUNNING;
@@ -578,7 +578,7 @@ struct GmMgs {
         t.inner = i + 1;
         int c = ST_RUNNING;
         if (i + 1 < g.restart) {
-            c = m.check(t, sys, fabs(g.s[i + 1]));
+            c = m.check_scalar(t, sys, fabs(g.s[i + 1]));
             if (c == ST_DONE) {
                 t.inner_done = 1;
                 c = ST_RUNNING;
@@ -710,6 +710,9 @@ struct mtjg_solver {
     double *pc_p2 = nullptr;  // the second p buffer
     unsigned long long *pc_bar = nullptr;
     bool last_persistent = false;
+    // MatrixIterationMonitor (mtjg_solver_set_matrix_monitor)
+    int xmon = 0;
+    double normA = 0, normb = 0;
 };
 
 namespace {
@@ -734,6 +737,9 @@ MonCfgDev mon_dev(const mtjg_solver *S)
     c.rtol = S->mon.rtol;
     c.atol = S->mon.atol;
     c.dtol = S->mon.dtol;
+    c.xmon = S->xmon;
+    c.normA = S->normA;
+    c.normb = S->normb;
     return c;
 }
 
@@ -750,7 +756,8 @@ struct Phases {
     mtjg_csr *A;
     MonPtrs mp() const
     {
-        return MonPtrs{S->st, mon_dev(S), S->hist_r, S->hist_it, A->num_running};
+        return MonPtrs{S->st, mon_dev(S), S->hist_r, S->hist_it, A->num_running,
+                       S->xmon ? S->vecs[V_X] : nullptr, S->n, STRICT ? 1 : 0};
     }
     CsrArgs csr() const { return CsrArgs{A->rowptr, A->colind, A->val}; }
     RedCtx rc() const { return red_ctx(A, A->tiles); }
@@ -1208,6 +1215,8 @@ int report(mtjg_solver *S, mtjg_result *res)
         set_error("Iterations");
     else if (code == MTJG_NOT_CONVERGED_DIVERGENCE)
         set_error("Divergence");
+    else if (code == MTJG_ERR_UNSUPPORTED)
+        set_error("MatrixIterationMonitor.convergedI(double) is not supported (GMRES's inner test)");
     else if (code == MTJG_ERR_SINGULAR)
         set_error("MatrixSingularException in the GMRES triangular solve");
     return code;
@@ -1244,7 +1253,8 @@ int ensure_state(mtjg_solver *S, int ns)
 // one cooperative launch (persist.cuh) unless the graph path was asked for.
 bool persistent_cg(const mtjg_solver *S, const mtjg_csr *A)
 {
-    return S->launch_mode == MTJG_LAUNCH_AUTO && S->kind == MTJG_CG && !S->mixed && pc_mode(S) != kPcExternal &&
+    return S->launch_mode == MTJG_LAUNCH_AUTO && S->kind == MTJG_CG && !S->mixed && !S->xmon &&
+           pc_mode(S) != kPcExternal &&
            A->sys_rows.empty() && A->tiles.num_sys == 1 && A->rtiles.num_sys == 1 && A->tiles.num_long == 0 &&
            A->tiles.num_tiles > 0 && A->tiles.num_tiles <= kPersistMaxTiles &&
            A->tiles.num_groups == A->tiles.num_tiles && A->rtiles.num_groups == A->rtiles.num_tiles;
@@ -1630,7 +1640,9 @@ int run_empty(mtjg_solver *S, mtjg_result *res)
     std::vector<int> &it = S->empty_it;
     it.assign(1, 0);
     const int mi = std::max(0, S->mon.max_iter);
-    const bool conv = 0.0 < std::max(S->mon.rtol * 0.0, S->mon.atol);
+    // MatrixIterationMonitor: rtol (normA |x| + normb) with |x| = 0
+    const double base = S->xmon ? S->normA * 0.0 + S->normb : 0.0;
+    const bool conv = 0.0 < std::max(S->mon.rtol * base, S->mon.atol);
     if (conv) {
         S->last.status = ST_DONE;
     } else if (mi == 0) {
@@ -1644,6 +1656,10 @@ int run_empty(mtjg_solver *S, mtjg_result *res)
         S->last.status = MTJG_NOT_CONVERGED_ITERATIONS;
         S->last.iter = mi;
         for (int k = 1; k <= mi; ++k) it.push_back(k);
+    } else if (S->xmon) {
+        // GMRES: the cycle's first inner test is converged(double)
+        S->last.status = MTJG_ERR_UNSUPPORTED;
+        it.push_back(0);
     } else if (mi < S->restart) {
         S->last.status = MTJG_NOT_CONVERGED_ITERATIONS;
         S->last.iter = mi;
@@ -1684,6 +1700,8 @@ int check_sizes(mtjg_solver *S, mtjg_csr *A)
         if (S->kind == MTJG_GMRES && S->restart > 63)
             return fail(MTJG_ERR_UNSUPPORTED, "mixed-precision GMRES supports restart <= 63");
     }
+    if (S->xmon && (S->mixed || A->tiles.num_sys > 1))
+        return fail(MTJG_ERR_UNSUPPORTED, "MatrixIterationMonitor runs with single-system FP64 solves");
     if (A->tiles.num_sys > 1) {
         if (S->kind == MTJG_GMRES)
             return fail(MTJG_ERR_UNSUPPORTED, "batched solves support CG and BiCGstab");
@@ -1839,6 +1857,16 @@ extern "C" int mtjg_solver_set_mixed(mtjg_solver *S, int enable, double inner_rt
     }
     S->mixed = enable != 0;
     if (enable) S->mix = MixCfg{inner_rtol, inner_max_iter, 0, 0.0, 0.0};
+    drop_graph(S);
+    return MTJG_OK;
+}
+
+extern "C" int mtjg_solver_set_matrix_monitor(mtjg_solver *S, int enable, double normA, double normb)
+{
+    if (!S) return fail(MTJG_ERR_ILLEGAL_ARGUMENT, "NULL solver");
+    S->xmon = enable ? 1 : 0;
+    S->normA = enable ? normA : 0.0;
+    S->normb = enable ? normb : 0.0;
     drop_graph(S);
     return MTJG_OK;
 }

@@ -125,6 +125,7 @@ PROTOTYPES = {
     "mtjg_batch_upload": (C.c_int, [_vp, C.c_int, _ip, _ip, _ip, _dp, C.POINTER(_vp)]),
     "mtjg_solver_set_mixed": (C.c_int, [_vp, C.c_int, C.c_double, C.c_int]),
     "mtjg_solver_set_launch": (C.c_int, [_vp, C.c_int]),
+    "mtjg_solver_set_matrix_monitor": (C.c_int, [_vp, C.c_int, C.c_double, C.c_double]),
     "mtjg_solver_set_eigenvalues": (C.c_int, [_vp, C.c_double, C.c_double]),
     "mtjg_server_config_defaults": (None, [C.POINTER(ServerConfig)]),
     "mtjg_server_create": (C.c_int, [_vp, C.POINTER(ServerConfig), C.POINTER(_vp)]),

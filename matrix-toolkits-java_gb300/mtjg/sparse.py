@@ -637,6 +637,30 @@ class DefaultIterationMonitor:
     def _struct(self) -> L.Monitor:
         return L.Monitor(self.maxIter, self.rtol, self.atol, self.dtol, int(self.normType), self.history_cap)
 
+    def _matrix_norms(self):
+        return None
+
+
+class MatrixIterationMonitor(DefaultIterationMonitor):
+    """S/MatrixIterationMonitor.java: converged iff r < max(rtol (normA |x|
+    + normb), atol), |x| the current iterate's norm in the monitor's norm
+    type (formed on the device before each test).  GMRES's inner test is
+    converged(double), which this monitor does not support: such a solve
+    raises UnsupportedOperationException, as in MTJ."""
+
+    def __init__(self, normA, normb, maxIter=100000, rtol=1e-5, atol=1e-50, dtol=1e+5):
+        super().__init__(maxIter, rtol, atol, dtol)
+        self.normA, self.normb = float(normA), float(normb)
+
+    def setMatrixNorm(self, normA):
+        self.normA = float(normA)
+
+    def setVectorNorm(self, normb):
+        self.normb = float(normb)
+
+    def _matrix_norms(self):
+        return (self.normA, self.normb)
+
 
 # --------------------------------------------------------------- solvers
 class AbstractIterativeSolver:
@@ -691,9 +715,12 @@ class AbstractIterativeSolver:
 
     def _sync_monitor(self):
         s = self.iter._struct()
-        key = (s.max_iter, s.rtol, s.atol, s.dtol, s.norm, s.history_cap)
+        mn = self.iter._matrix_norms()
+        key = (s.max_iter, s.rtol, s.atol, s.dtol, s.norm, s.history_cap, mn)
         if key != self._mon_key:
             _raise(self._lib.mtjg_solver_set_monitor(self.h, C.byref(s)), "set_monitor")
+            _raise(self._lib.mtjg_solver_set_matrix_monitor(self.h, 1 if mn else 0, *(mn or (0.0, 0.0))),
+                   "set_matrix_monitor")
             self._mon_key = key
 
     def solve(self, A: CompRowMatrix, b, x):

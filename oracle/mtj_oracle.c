@@ -187,6 +187,8 @@ static void vscale(int n, double *d, double alpha)
 
 typedef struct mon_state {
     const or_monitor *cfg;
+    int n;
+    const double *x;  /* the solver's iterate (MatrixIterationMonitor reads its norm) */
     int iter;
     double initR;
     double residual;
@@ -216,9 +218,43 @@ static int mon_check(mon_state *m, double r)
     return -1;
 }
 
+/* AbstractIterationMonitor.converged(Vector r, Vector x) (:76-86).  With a
+ * MatrixIterationMonitor, its convergedI(r, x)
+ * (S/MatrixIterationMonitor.java:108-130): initR on the first test; converged
+ * iff r < max(rtol (normA |x| + normb), atol), |x| in the monitor's norm;
+ * then DefaultIterationMonitor's divergence, iteration and NaN tests. */
 static int mon_check_vec(mon_state *m, int n, const double *r)
 {
-    return mon_check(m, or_norm(n, r, m->cfg->norm));
+    const double rn = or_norm(n, r, m->cfg->norm);
+    if (!m->cfg->matrix) return mon_check(m, rn);
+    if (m->hist_len < m->hist_cap) {
+        m->hist_r[m->hist_len] = rn;
+        m->hist_it[m->hist_len] = m->iter;
+    }
+    m->hist_len++;
+    m->residual = rn;
+    if (m->iter == 0) m->initR = rn;
+    const double xn = or_norm(m->n, m->x, m->cfg->norm);
+    if (rn < jmax(m->cfg->rtol * (m->cfg->normA * xn + m->cfg->normb), m->cfg->atol)) return OR_OK;
+    if (rn > m->cfg->dtol * m->initR) return OR_NC_DIVERGENCE;
+    if (m->iter >= m->cfg->max_iter) return OR_NC_ITERATIONS;
+    if (rn != rn) return OR_NC_DIVERGENCE;
+    return -1;
+}
+
+/* AbstractIterationMonitor.converged(double r) (:88-93): the reporter and the
+ * residual, then convergedI(r), which a MatrixIterationMonitor does not
+ * support (S/MatrixIterationMonitor.java:132-135). */
+static int mon_check_scalar(mon_state *m, double r)
+{
+    if (!m->cfg->matrix) return mon_check(m, r);
+    if (m->hist_len < m->hist_cap) {
+        m->hist_r[m->hist_len] = r;
+        m->hist_it[m->hist_len] = m->iter;
+    }
+    m->hist_len++;
+    m->residual = r;
+    return OR_ERR_UNSUPPORTED;
 }
 
 /* ------------------------------------------------------- preconditioners */
@@ -1050,7 +1086,7 @@ static int gmres_solve(int restart, int n, const int *rp, const int *ci, const d
         s[0] = normr;
         int i = 0;
         for (; i < restart; i++, m->iter++) {
-            st = mon_check(m, fabs(s[i]));
+            st = mon_check_scalar(m, fabs(s[i]));
             if (st > 0) goto done;     /* exception out of the inner loop */
             if (st == OR_OK) break;
             or_mult(n, rp, ci, v, V[i], u);
@@ -1319,6 +1355,8 @@ int or_solve_ex(int kind, int restart, double eigmin, double eigmax, int n, cons
     mon_state m;
     memset(&m, 0, sizeof(m));
     m.cfg = mon;
+    m.n = n;
+    m.x = x;
     m.hist_r = hist_r;
     m.hist_it = hist_it;
     m.hist_cap = hist_r && hist_it ? hist_cap : 0;

@@ -37,7 +37,8 @@ enum {
     OR_ERR_ZERO_PIVOT = 20,
     OR_ERR_ZERO_DIAGONAL = 21,
     OR_ERR_MISSING_DIAGONAL = 22,
-    OR_ERR_SINGULAR = 23
+    OR_ERR_SINGULAR = 23,
+    OR_ERR_UNSUPPORTED = 30
 };
 
 enum { OR_NORM_ONE = 0, OR_NORM_TWO = 1, OR_NORM_TWO_ROBUST = 2, OR_NORM_INFINITY = 3 };
@@ -47,10 +48,15 @@ enum { OR_CG = 0, OR_BICGSTAB = 1, OR_GMRES = 2, OR_BICG = 3, OR_CGS = 4, OR_QMR
 /* or_result.detail of a breakdown: which quantity became zero */
 enum { OR_BD_RHO = 1, OR_BD_OMEGA = 2, OR_BD_XI = 3, OR_BD_DELTA = 4, OR_BD_EP = 5, OR_BD_BETA = 6, OR_BD_GAMMA = 7 };
 
+/* DefaultIterationMonitor, or MatrixIterationMonitor when matrix != 0
+ * (S/MatrixIterationMonitor.java: convergence against rtol (normA |x| +
+ * normb) instead of rtol initR) */
 typedef struct or_monitor {
     int max_iter;
     double rtol, atol, dtol;
     int norm;
+    int matrix;
+    double normA, normb;
 } or_monitor;
 
 typedef struct or_result {

@@ -27,6 +27,7 @@ SRC = os.path.join(HERE, "mtj_oracle.c")
 
 OK, NC_ITERATIONS, NC_DIVERGENCE, NC_BREAKDOWN = 0, 1, 2, 3
 ERR_ILLEGAL_ARGUMENT, ERR_ZERO_PIVOT, ERR_ZERO_DIAGONAL, ERR_MISSING_DIAGONAL, ERR_SINGULAR = 10, 20, 21, 22, 23
+ERR_UNSUPPORTED = 30
 NORM_ONE, NORM_TWO, NORM_TWO_ROBUST, NORM_INFINITY = 0, 1, 2, 3
 PC_IDENTITY, PC_JACOBI, PC_ILU, PC_ICC, PC_ICC_LITERAL, PC_SSOR, PC_ILUT = 0, 1, 2, 3, 4, 5, 6
 CG, BICGSTAB, GMRES, BICG, CGS, QMR, CHEBYSHEV, IR = 0, 1, 2, 3, 4, 5, 6, 7
@@ -47,7 +48,8 @@ def build() -> str:
 
 class Monitor(C.Structure):
     _fields_ = [("max_iter", C.c_int), ("rtol", C.c_double), ("atol", C.c_double),
-                ("dtol", C.c_double), ("norm", C.c_int)]
+                ("dtol", C.c_double), ("norm", C.c_int), ("matrix", C.c_int), ("normA", C.c_double),
+                ("normb", C.c_double)]
 
 
 class Result(C.Structure):
@@ -226,9 +228,10 @@ class Precond:
 
 
 def solve(kind, A: Csr, b, x0, pc: Precond | None = None, max_iter=100000, rtol=1e-5, atol=1e-50, dtol=1e5,
-          norm_type=NORM_TWO, restart=30, hist_cap=None, eigmin=0.0, eigmax=0.0):
+          norm_type=NORM_TWO, restart=30, hist_cap=None, eigmin=0.0, eigmax=0.0, matrix_norms=None):
     """Runs the restated solver; returns (x, Result, hist_r, hist_it).
-    eigmin / eigmax are Chebyshev's eigenvalue bounds."""
+    eigmin / eigmax are Chebyshev's eigenvalue bounds; matrix_norms =
+    (normA, normb) makes the monitor a MatrixIterationMonitor."""
     b = np.ascontiguousarray(b, dtype=np.float64)
     x = np.array(x0, dtype=np.float64, copy=True)
     if hist_cap is None:
@@ -236,6 +239,9 @@ def solve(kind, A: Csr, b, x0, pc: Precond | None = None, max_iter=100000, rtol=
     hr = np.empty(max(hist_cap, 1))
     hi = np.empty(max(hist_cap, 1), dtype=np.int32)
     mon = Monitor(max_iter, rtol, atol, dtol, norm_type)
+    if matrix_norms is not None:
+        mon.matrix = 1
+        mon.normA, mon.normb = float(matrix_norms[0]), float(matrix_norms[1])
     res = Result()
     res.status = lib().or_solve_ex(kind, restart, eigmin, eigmax, A.n, _i(A.rp), _i(A.ci), _d(A.v),
                                    pc.h if pc else None, _d(b), _d(x) if len(x) else _d(np.zeros(1)), C.byref(mon),
