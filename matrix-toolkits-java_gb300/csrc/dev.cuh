@@ -304,7 +304,7 @@ __global__ void __launch_bounds__(kBlock) k_finalize(Op op, RedCtx rc, int type)
 // (S/AbstractIterationMonitor.java:81-93, S/DefaultIterationMonitor.java:133-156):
 // record (r, iter) for the reporter, then test in MTJ's order (with a
 // MatrixIterationMonitor, its convergence test, S/MatrixIterationMonitor.java
-// :108-130).
+// :101-124).
 __device__ __forceinline__ int monitor_check(SysState &st, const MonCfgDev &c, double r,
                                              double *hist_r, int *hist_it)
 {
@@ -326,7 +326,7 @@ __device__ __forceinline__ int monitor_check(SysState &st, const MonCfgDev &c, d
 // AbstractIterationMonitor.converged(double) (S/AbstractIterationMonitor.java
 // :88-93), GMRES's inner test: the reporter and the residual, then
 // convergedI(r), which a MatrixIterationMonitor does not support
-// (S/MatrixIterationMonitor.java:132-135).
+// (S/MatrixIterationMonitor.java:127-129).
 __device__ __forceinline__ int monitor_check_scalar(SysState &st, const MonCfgDev &c, double r, double *hist_r,
                                                     int *hist_it)
 {

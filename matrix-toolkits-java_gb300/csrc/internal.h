@@ -142,7 +142,7 @@ struct MonCfgDev {
     int hist_cap;
     int pad;
     double rtol, atol, dtol;
-    // MatrixIterationMonitor (S/MatrixIterationMonitor.java:108-130): a test
+    // MatrixIterationMonitor (S/MatrixIterationMonitor.java:101-124): a test
     // converges iff r < max(rtol (normA |x| + normb), atol), |x| being
     // SysState::xnorm, the iterate's norm formed just before the test
     int xmon = 0;

@@ -220,7 +220,7 @@ static int mon_check(mon_state *m, double r)
 
 /* AbstractIterationMonitor.converged(Vector r, Vector x) (:76-86).  With a
  * MatrixIterationMonitor, its convergedI(r, x)
- * (S/MatrixIterationMonitor.java:108-130): initR on the first test; converged
+ * (S/MatrixIterationMonitor.java:101-124): initR on the first test; converged
  * iff r < max(rtol (normA |x| + normb), atol), |x| in the monitor's norm;
  * then DefaultIterationMonitor's divergence, iteration and NaN tests. */
 static int mon_check_vec(mon_state *m, int n, const double *r)
@@ -244,7 +244,7 @@ static int mon_check_vec(mon_state *m, int n, const double *r)
 
 /* AbstractIterationMonitor.converged(double r) (:88-93): the reporter and the
  * residual, then convergedI(r), which a MatrixIterationMonitor does not
- * support (S/MatrixIterationMonitor.java:132-135). */
+ * support (S/MatrixIterationMonitor.java:127-129). */
 static int mon_check_scalar(mon_state *m, double r)
 {
     if (!m->cfg->matrix) return mon_check(m, r);

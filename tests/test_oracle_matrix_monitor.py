@@ -1,4 +1,4 @@
-"""The oracle's MatrixIterationMonitor (S/MatrixIterationMonitor.java:108-135).
+"""The oracle's MatrixIterationMonitor (S/MatrixIterationMonitor.java:101-129).
 
 Its convergence test is r < max(rtol (normA |x| + normb), atol) on the
 iterate of the moment; divergence, iteration and NaN tests are those of
