@@ -689,6 +689,9 @@ class AbstractIterativeSolver:
         return self.M
 
     def setIterationMonitor(self, mon: DefaultIterationMonitor):
+        # the monitor runs on the device: MTJ's two monitors only
+        if not isinstance(mon, DefaultIterationMonitor):
+            raise UnsupportedOperationException("only DefaultIterationMonitor and MatrixIterationMonitor run on the GPU")
         self.iter = mon
 
     def getIterationMonitor(self):

@@ -194,3 +194,15 @@ def test_matrix_monitor_refused_by_mixed_and_batched(ctx):
     s.setMixedPrecision(True)
     with pytest.raises(sparse.UnsupportedOperationException):
         s.solve(A, b, np.zeros(n))
+
+
+def test_custom_monitor_is_refused(ctx):
+    """Only MTJ's two monitors run on the device; any other is refused
+    (no CPU fallback)."""
+
+    class Custom:
+        pass
+
+    s = sparse.CG(10, ctx=ctx)
+    with pytest.raises(sparse.UnsupportedOperationException):
+        s.setIterationMonitor(Custom())
