@@ -272,8 +272,27 @@ __device__ __forceinline__ Acc system_sum(const RedCtx &rc, int sys, int type, d
 // Kernel templates and their launchers live in an unnamed namespace: without
 // relocatable device code every translation unit carries its own device
 // image, so each one instantiates (and sets attributes on) its own kernels.
-// An op with a monitor (member m with MatrixIterationMonitor fields) has its
-// finalize form |x| first when a MatrixIterationMonitor is set (m.x).
+// |x| in the monitor's norm for a MatrixIterationMonitor, by the whole block
+// (thread-strided sums, the fixed block tree), into t.xnorm ahead of the
+// test; sm holds kParts * kBlock doubles.
+__device__ __forceinline__ void xnorm_block(SysState &t, int type, double *sm)
+{
+    Acc a;
+    acc_zero(a);
+    const double *x = t.xm_x;
+    const int n = t.xm_n;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        if (t.xm_strict) norm_add<true>(a, x[i], type);
+        else norm_add<false>(a, x[i], type);
+    }
+    block_reduce<kSlotNorm>(a, type, sm);
+    if (threadIdx.x == 0) t.xnorm = norm_finish(a.v, type);
+    __syncthreads();
+}
+
+// An op with a monitor (member m) has its finalize form |x| first when a
+// MatrixIterationMonitor is set (a variant of its own, k_finalize<Op, true>,
+// so the default monitor's finalize carries none of it).
 template <class Op, class = void>
 struct OpMon {
     static constexpr bool value = false;
@@ -284,16 +303,14 @@ struct OpMon<Op, decltype((void)std::declval<const Op &>().m.mon.xmon)> {
 };
 
 namespace {
-template <class Op>
+template <class Op, bool XN = false>
 __global__ void __launch_bounds__(kBlock) k_finalize(Op op, RedCtx rc, int type)
 {
     constexpr int SLOTS = OpSlots<Op>::value;
     __shared__ double sm[kParts * kBlock];
     const int sys = blockIdx.x;
     if (!op.active(sys)) return;
-    if constexpr (OpMon<Op>::value) {
-        if (op.m.x) op.m.xnorm_block(sys, sm);
-    }
+    if constexpr (XN) xnorm_block(op.m.st[sys], op.m.mon.norm, sm);
     const Acc s = system_sum<SLOTS>(rc, sys, type, sm);
     if (threadIdx.x == 0) op.scalar(sys, s);
 }
@@ -315,7 +332,8 @@ __device__ __forceinline__ int monitor_check(SysState &st, const MonCfgDev &c, d
     st.hist_len++;
     st.residual = r;
     if (st.iter == 0) st.initR = r;
-    const double tol = c.xmon ? jmax(c.rtol * (c.normA * st.xnorm + c.normb), c.atol) : jmax(c.rtol * st.initR, c.atol);
+    const double tol =
+        c.xmon ? jmax(c.rtol * (st.xm_normA * st.xnorm + st.xm_normb), c.atol) : jmax(c.rtol * st.initR, c.atol);
     if (r < tol) return ST_DONE;
     if (r > c.dtol * st.initR) return MTJG_NOT_CONVERGED_DIVERGENCE;
     if (st.iter >= c.max_iter) return MTJG_NOT_CONVERGED_ITERATIONS;

@@ -133,21 +133,23 @@ struct SysState {
     // (coef[0], coef[1]) or the d / s scale factor (coef[0])
     double xi, gamma, gamma_1, theta, theta_1, eta, delta, ep;
     double coef[2];
-    double xnorm;  // MatrixIterationMonitor: |x| at the coming test
+    // MatrixIterationMonitor (MonCfgDev::xmon): the iterate, its length, the
+    // numerics its norm is formed in, normA, normb and |x| at the coming test
+    const double *xm_x;
+    int xm_n, xm_strict;
+    double xm_normA, xm_normb;
+    double xnorm;
 };
 
 struct MonCfgDev {
     int max_iter;
     int norm;
     int hist_cap;
-    int pad;
-    double rtol, atol, dtol;
     // MatrixIterationMonitor (S/MatrixIterationMonitor.java:101-124): a test
-    // converges iff r < max(rtol (normA |x| + normb), atol), |x| being
-    // SysState::xnorm, the iterate's norm formed just before the test
-    int xmon = 0;
-    int pad2 = 0;
-    double normA = 0, normb = 0;
+    // converges iff r < max(rtol (normA |x| + normb), atol), with normA,
+    // normb, the iterate and |x| (formed just before the test) in SysState
+    int xmon;
+    double rtol, atol, dtol;
 };
 
 // Reduction context: per-group partial sums and the group ranges of the

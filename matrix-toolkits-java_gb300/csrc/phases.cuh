@@ -29,12 +29,6 @@ struct MonPtrs {
     double *hr;
     int *hi;
     int *num_running;
-    // MatrixIterationMonitor (one system): the iterate whose norm each test
-    // reads, its length and the numerics its norm is formed in; x == nullptr
-    // for the default monitor
-    const double *x = nullptr;
-    int n = 0;
-    int strict = 0;
     __device__ __forceinline__ void finish(SysState &t, int code) const
     {
         t.status = code;
@@ -49,22 +43,6 @@ struct MonPtrs {
     __device__ __forceinline__ int check_scalar(SysState &t, int sys, double r) const
     {
         return monitor_check_scalar(t, mon, r, hr + (size_t)sys * mon.hist_cap, hi + (size_t)sys * mon.hist_cap);
-    }
-    // |x| in the monitor's norm, by the whole block (thread-strided sums, the
-    // fixed block tree), into st[sys].xnorm ahead of the test; sm holds
-    // kParts * kBlock doubles
-    __device__ void xnorm_block(int sys, double *sm) const
-    {
-        Acc a;
-        acc_zero(a);
-        const int type = mon.norm;
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            if (strict) norm_add<true>(a, x[i], type);
-            else norm_add<false>(a, x[i], type);
-        }
-        block_reduce<kSlotNorm>(a, type, sm);
-        if (threadIdx.x == 0) st[sys].xnorm = norm_finish(a.v, type);
-        __syncthreads();
     }
 };
 

@@ -478,7 +478,7 @@ int run_chunk(mtjg_server *S)
     mon.max_iter = S->cfg.max_iter;
     mon.norm = MTJG_NORM_TWO;
     mon.hist_cap = 0;
-    mon.pad = 0;
+    mon.xmon = 0;
     mon.rtol = S->cfg.rtol;
     mon.atol = S->cfg.atol;
     mon.dtol = S->cfg.dtol;

@@ -733,13 +733,10 @@ MonCfgDev mon_dev(const mtjg_solver *S)
     c.max_iter = S->mon.max_iter;
     c.norm = S->mon.norm;
     c.hist_cap = S->mon.history_cap;
-    c.pad = 0;
+    c.xmon = S->xmon;
     c.rtol = S->mon.rtol;
     c.atol = S->mon.atol;
     c.dtol = S->mon.dtol;
-    c.xmon = S->xmon;
-    c.normA = S->normA;
-    c.normb = S->normb;
     return c;
 }
 
@@ -756,8 +753,7 @@ struct Phases {
     mtjg_csr *A;
     MonPtrs mp() const
     {
-        return MonPtrs{S->st, mon_dev(S), S->hist_r, S->hist_it, A->num_running,
-                       S->xmon ? S->vecs[V_X] : nullptr, S->n, STRICT ? 1 : 0};
+        return MonPtrs{S->st, mon_dev(S), S->hist_r, S->hist_it, A->num_running};
     }
     CsrArgs csr() const { return CsrArgs{A->rowptr, A->colind, A->val}; }
     RedCtx rc() const { return red_ctx(A, A->tiles); }
@@ -1359,6 +1355,13 @@ int run(mtjg_solver *S, mtjg_csr *A, mtjg_result *res)
     init.status = ST_RUNNING;
     init.gate = ST_RUNNING;
     init.rho_1 = init.rho_2 = init.alpha = init.beta = init.omega = 1.0;
+    if (S->xmon) {  // MatrixIterationMonitor (one system): its norms and the iterate
+        init.xm_x = S->vecs[V_X];
+        init.xm_n = S->n;
+        init.xm_strict = ctx->numerics == MTJG_NUMERICS_STRICT ? 1 : 0;
+        init.xm_normA = S->normA;
+        init.xm_normb = S->normb;
+    }
     S->last_all.assign(ns, init);
     if (S->mixed) {
         st = mixed_prepare(S, A);

@@ -646,8 +646,14 @@ cudaError_t launch_long_rows(mtjg_ctx *ctx, CsrArgsT<T> A, const TileSet &ts, co
 template <class Op>
 cudaError_t launch_finalize(mtjg_ctx *ctx, const TileSet &ts, const Op &op, const RedCtx &rc, int normtype)
 {
-    k_finalize<Op><<<ts.num_sys, kBlock, 0, ctx->stream>>>(op, rc, normtype);
     ctx->launches++;
+    if constexpr (OpMon<Op>::value) {
+        if (op.m.mon.xmon) {  // MatrixIterationMonitor: |x| first
+            k_finalize<Op, true><<<ts.num_sys, kBlock, 0, ctx->stream>>>(op, rc, normtype);
+            return cudaGetLastError();
+        }
+    }
+    k_finalize<Op><<<ts.num_sys, kBlock, 0, ctx->stream>>>(op, rc, normtype);
     return cudaGetLastError();
 }
 
