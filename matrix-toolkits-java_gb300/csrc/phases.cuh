@@ -9,11 +9,11 @@
 #ifndef MTJG_MXUPD_MINB
 #define MTJG_MXUPD_MINB 0
 #endif
-// resident CTAs per SM of the FP32 product of the inner solve: 6 fit (40
-// registers, a one-slot reduction), but 5 leave L1 room for the gathers of
-// the served mix and measured 8 % faster there
+// resident CTAs per SM of the FP32 product of the inner solve: 4, as many
+// as the 2560-entry FP32 stages fit (with 1728-entry stages 5 had measured
+// 8 % faster than 6 on the served mix, leaving L1 room for the gathers)
 #ifndef MTJG_MXQ_CTAS
-#define MTJG_MXQ_CTAS 5
+#define MTJG_MXQ_CTAS 4
 #endif
 
 namespace mtjg {
