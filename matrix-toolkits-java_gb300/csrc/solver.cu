@@ -1703,7 +1703,7 @@ int check_sizes(mtjg_solver *S, mtjg_csr *A)
         if (S->kind == MTJG_GMRES && S->restart > 63)
             return fail(MTJG_ERR_UNSUPPORTED, "mixed-precision GMRES supports restart <= 63");
     }
-    if (S->xmon && (S->mixed || A->tiles.num_sys > 1))
+    if (S->xmon && (S->mixed || A->tiles.num_sys > 1 || !A->sys_rows.empty()))
         return fail(MTJG_ERR_UNSUPPORTED, "MatrixIterationMonitor runs with single-system FP64 solves");
     if (A->tiles.num_sys > 1) {
         if (S->kind == MTJG_GMRES)

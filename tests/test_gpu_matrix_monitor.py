@@ -196,6 +196,18 @@ def test_matrix_monitor_refused_by_mixed_and_batched(ctx):
         s.solve(A, b, np.zeros(n))
 
 
+def test_matrix_monitor_refused_by_a_batch_of_one(ctx):
+    """A batch upload (even of one system) runs the batched kernels, which
+    keep only the default monitor."""
+    n, rp, ci, v = workloads.poisson2d(12)
+    B = sparse.BatchCompRowMatrix([(n, rp, ci, v)], ctx)
+    b = workloads.uniform(n, 3)
+    s = sparse.CG(n, ctx=ctx)
+    s.setIterationMonitor(sparse.MatrixIterationMonitor(8.0, float(np.linalg.norm(b)), 2000, 1e-9))
+    with pytest.raises(sparse.UnsupportedOperationException):
+        s.solveBatch(B, b, np.zeros(n))
+
+
 def test_custom_monitor_is_refused(ctx):
     """Only MTJ's two monitors run on the device; any other is refused
     (no CPU fallback)."""
