@@ -18,6 +18,10 @@ class NotConverged(Exception):
         self.code, self.iters, self.resid, self.detail = code, iters, resid, detail
 
 
+class Unsupported(Exception):
+    """UnsupportedOperationException (MatrixIterationMonitor.convergedI(double))."""
+
+
 class Singular(Exception):
     pass
 
@@ -78,12 +82,14 @@ class Monitor:
         self.residual = 0.0
         self.hist = []
 
-    def converged(self, r):
+    def converged(self, r, x=None):
+        """converged(r, x) with the iterate, converged(r) without (GMRES's
+        inner test)."""
         self.hist.append((r, self.iter))
         self.residual = r
         if self.iter == 0:
             self.initR = r
-        if r < jmax(self.rtol * self.initR, self.atol):
+        if r < jmax(self._tol_base(x), self.atol):
             return True
         if r > self.dtol * self.initR:
             raise NotConverged(2, self.iter, r)
@@ -92,6 +98,28 @@ class Monitor:
         if r != r:
             raise NotConverged(2, self.iter, r)
         return False
+
+    def _tol_base(self, x):
+        return self.rtol * self.initR
+
+
+class MatrixMonitor(Monitor):
+    """MatrixIterationMonitor, S/MatrixIterationMonitor.java:101-129: the
+    test against rtol (normA |x|_2 + normb); converged(double) unsupported."""
+
+    def __init__(self, normA, normb, max_iter, rtol, atol=1e-50, dtol=1e5):
+        super().__init__(max_iter, rtol, atol, dtol)
+        self.normA, self.normb = normA, normb
+
+    def converged(self, r, x=None):
+        if x is None:
+            self.hist.append((r, self.iter))
+            self.residual = r
+            raise Unsupported()
+        return super().converged(r, x)
+
+    def _tol_base(self, x):
+        return self.rtol * (self.normA * norm2(x) + self.normb)
 
 
 def jacobi(rp, ci, v):
@@ -211,7 +239,7 @@ def cg(rp, ci, v, b, x, M, mon):
     p = [0.0] * n
     rho_1 = 0.0
     mon.iter = 0
-    while not mon.converged(norm2(r)):
+    while not mon.converged(norm2(r), x):
         z = M(r)
         rho = dot(r, z)
         if mon.iter == 0:
@@ -240,7 +268,7 @@ def bicgstab(rp, ci, v, b, x, M, mon):
     p = [0.0] * n
     vv = [0.0] * n
     mon.iter = 0
-    while not mon.converged(norm2(r)):
+    while not mon.converged(norm2(r), x):
         rho_1 = dot(rt, r)
         if rho_1 == 0:
             raise NotConverged(3, mon.iter, mon.residual, 1)
@@ -259,7 +287,7 @@ def bicgstab(rp, ci, v, b, x, M, mon):
         s = list(r) if alpha == 0 else [r[i] + (-alpha) * vv[i] for i in range(n)]
         if alpha != 0:
             x = [x[i] + alpha * phat[i] for i in range(n)]
-        if mon.converged(norm2(s)):
+        if mon.converged(norm2(s), x):
             return x
         shat = M(s)
         t = mult(rp, ci, v, shat)
@@ -299,7 +327,7 @@ def gmres(rp, ci, v, b, x, M, mon, restart=30):
     r = M(u)
     normr = norm2(r)
     mon.iter = 0
-    while not mon.converged(norm2(r)):
+    while not mon.converged(norm2(r), x):
         a = 1 / normr
         V = [[0.0] * n if a == 0 else [a * r[j] for j in range(n)]]
         s = [0.0] * (restart + 1)
@@ -393,7 +421,7 @@ def bicg(rp, ci, v, b, x, M, Mt, mon):
     rt = list(r)
     p = pt = [0.0] * n
     mon.iter = 0
-    while not mon.converged(norm2(r)):
+    while not mon.converged(norm2(r), x):
         z = M(r)
         zt = Mt(rt)
         rho_1 = dot(z, rt)
@@ -425,7 +453,7 @@ def cgs(rp, ci, v, b, x, M, mon):
     rt = list(r)
     p = q = [0.0] * n
     mon.iter = 0
-    while not mon.converged(norm2(r)):
+    while not mon.converged(norm2(r), x):
         rho_1 = dot(rt, r)
         if rho_1 == 0:
             raise NotConverged(3, mon.iter, mon.residual, 1)
@@ -467,7 +495,7 @@ def qmr(rp, ci, v, b, x, M, Mt, mon):
     xi = norm2(z)
     p = q = d = s = [0.0] * n
     mon.iter = 0
-    while not mon.converged(norm2(r)):
+    while not mon.converged(norm2(r), x):
         if rho == 0:
             raise NotConverged(3, mon.iter, mon.residual, 1)
         if xi == 0:
@@ -533,7 +561,7 @@ def chebyshev(rp, ci, v, b, x, M, mon, eigmin, eigmax):
     d = (eigmax + eigmin) / 2.0
     p = [0.0] * n
     mon.iter = 0
-    while not mon.converged(norm2(r)):
+    while not mon.converged(norm2(r), x):
         z = M(r)
         if mon.iter == 0:
             p = list(z)
@@ -556,7 +584,7 @@ def ir(rp, ci, v, b, x, M, mon):
     x = list(x)
     r = mult_add(rp, ci, v, -1.0, x, b)
     mon.iter = 0
-    while not mon.converged(norm2(r)):
+    while not mon.converged(norm2(r), x):
         z = M(r)
         x = [x[i] + z[i] for i in range(n)]
         r = mult_add(rp, ci, v, -1.0, x, b)

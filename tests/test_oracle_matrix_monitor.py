@@ -81,3 +81,52 @@ def test_gmres_converged_at_the_first_test():
     x, res, hr, hi = O.solve(O.GMRES, A, b, np.zeros(n), pc, max_iter=400, rtol=1e-8,
                              matrix_norms=(0.0, 1e12))
     assert res.status == O.OK and res.history_len == 1
+
+
+# ------------------------------------- against the independent Python restatement
+def _random_system(seed, spd):
+    from helpers import dense_to_csr, nonsingular_system, spd_system
+    rng = np.random.default_rng(900 + seed)
+    n = int(rng.integers(5, 60))
+    bw = int(rng.integers(1, min(6, n) + 1))
+    Ad = spd_system(n, bw, rng) if spd else nonsingular_system(n, bw, rng)
+    n, _, rp, ci, v = dense_to_csr(Ad)
+    b = list(rng.standard_normal(n))
+    return n, rp, ci, v, b
+
+
+@pytest.mark.parametrize("seed", range(6))
+@pytest.mark.parametrize("name", ["cg", "bicgstab", "gmres"])
+def test_oracle_matches_pyref_with_matrix_monitor(seed, name):
+    """Oracle and tests/pyref.py, both restating MTJ in plain IEEE double
+    arithmetic, agree bit for bit under a MatrixIterationMonitor: status,
+    iteration count, every recorded residual and x."""
+    import pyref
+    n, rp, ci, v, b = _random_system(seed, name == "cg")
+    A = O.Csr(n, n, rp, ci, v)
+    pc = O.Precond(O.PC_JACOBI, n)
+    assert pc.set_matrix(A) == 0
+    M = pyref.jacobi(list(rp), list(ci), list(v))
+    normA = max(float(np.abs(v[rp[i]:rp[i + 1]]).sum()) for i in range(n))
+    normb = float(np.linalg.norm(b))
+    mon = pyref.MatrixMonitor(normA, normb, 300, 1e-10)
+    kind = {"cg": O.CG, "bicgstab": O.BICGSTAB, "gmres": O.GMRES}[name]
+    x0 = [0.0] * n
+    code, xp = 0, None
+    try:
+        if name == "gmres":
+            xp = pyref.gmres(list(rp), list(ci), list(v), b, x0, M, mon, 4)
+        else:
+            xp = {"cg": pyref.cg, "bicgstab": pyref.bicgstab}[name](list(rp), list(ci), list(v), b, x0, M, mon)
+    except pyref.NotConverged as e:
+        code = e.code
+    except pyref.Unsupported:
+        code = O.ERR_UNSUPPORTED
+    xo, res, hr, hi = O.solve(kind, A, np.array(b), np.zeros(n), pc, max_iter=300, rtol=1e-10, restart=4,
+                              matrix_norms=(normA, normb))
+    assert res.status == code
+    assert res.iterations == mon.iter
+    assert np.array_equal(hr, np.array([h[0] for h in mon.hist]))
+    assert np.array_equal(hi, np.array([h[1] for h in mon.hist]))
+    if code == 0:
+        assert np.array_equal(xo, np.array(xp))
