@@ -1297,7 +1297,12 @@ bool persist_plan(mtjg_ctx *ctx, const mtjg_csr *A, PersistPlan &pl)
 }
 
 // The loop body of CG after cg_init, in one launch; the state and the
-// running count end as the graph path leaves them.
+// running count end as the graph path leaves them.  Returns kCoopRefused,
+// with nothing launched, when the device refuses the cooperative launch
+// (fewer co-resident CTAs than planned, e.g. under a partitioned device):
+// the solve then continues on the graph path.
+constexpr int kCoopRefused = -1;
+
 template <bool STRICT>
 int run_persistent_cg(mtjg_solver *S, mtjg_csr *A, const PersistPlan &pl)
 {
@@ -1334,8 +1339,13 @@ int run_persistent_cg(mtjg_solver *S, mtjg_csr *A, const PersistPlan &pl)
     c.err = ctx->d_flag;
     int normtype = S->mon.norm;
     void *args[] = {&c, &normtype};
-    MTJG_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<void *>(k_cg_persist<STRICT>), dim3(pl.grid), dim3(kBlock),
-                                          args, pl.smem, ctx->stream));
+    const cudaError_t e = cudaLaunchCooperativeKernel(reinterpret_cast<void *>(k_cg_persist<STRICT>), dim3(pl.grid),
+                                                      dim3(kBlock), args, pl.smem, ctx->stream);
+    if (e == cudaErrorCooperativeLaunchTooLarge || e == cudaErrorNotSupported) {
+        (void)cudaGetLastError();  // a launch-configuration error: nothing ran, nothing is sticky
+        return kCoopRefused;
+    }
+    MTJG_CUDA(e);
     ctx->launches++;
     return MTJG_OK;
 }
@@ -1388,8 +1398,12 @@ int run(mtjg_solver *S, mtjg_csr *A, mtjg_result *res)
         // one launch runs the loop to the monitor's verdict (a solve that
         // cg_init finished already leaves it nothing to do)
         st = strict ? run_persistent_cg<true>(S, A, pl) : run_persistent_cg<false>(S, A, pl);
-        if (st != MTJG_OK) return st;
-        return finish_run(S, res);
+        if (st == kCoopRefused) {
+            S->last_persistent = false;  // the graph path below runs the loop instead
+        } else {
+            if (st != MTJG_OK) return st;
+            return finish_run(S, res);
+        }
     }
     const bool stale = !S->gexec || S->g_A != A || S->g_M != S->M || S->g_numerics != ctx->numerics ||
                        S->g_norm != S->mon.norm || S->g_version != (S->M ? S->M->version : 0) ||
