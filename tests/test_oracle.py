@@ -268,13 +268,21 @@ def _run_py(fn, *a):
 @pytest.mark.parametrize("name", ["bicg", "cgs", "qmr", "ir", "chebyshev"])
 @pytest.mark.parametrize("pk", [O.PC_IDENTITY, O.PC_JACOBI, O.PC_ILU, O.PC_ICC])
 @pytest.mark.parametrize("max_iter", [3, 400])
-def test_rank2_solver_histories_bitwise(seed, name, pk, max_iter):
+@pytest.mark.parametrize("monitor", ["default", "matrix"])
+def test_rank2_solver_histories_bitwise(seed, name, pk, max_iter, monitor):
     spd = name == "chebyshev" or pk == O.PC_ICC
     n, rp, ci, v, A, rng = _py_system(seed + 300, spd)
     b = list(rng.standard_normal(n))
     x0 = list(rng.standard_normal(n))
     pc, M, Mt = _pc_pair(pk, rp, ci, v, A, n)
-    mon = pyref.Monitor(max_iter, 1e-10)
+    # MatrixIterationMonitor: |A|_inf and |b|_2 as its norms
+    norms = None
+    if monitor == "matrix":
+        norm_a = max(float(np.abs(np.asarray(v[rp[i]:rp[i + 1]])).sum()) for i in range(n))
+        norms = (norm_a, float(np.linalg.norm(b)))
+        mon = pyref.MatrixMonitor(norms[0], norms[1], max_iter, 1e-10)
+    else:
+        mon = pyref.Monitor(max_iter, 1e-10)
     kind = {"bicg": O.BICG, "cgs": O.CGS, "qmr": O.QMR, "ir": O.IR, "chebyshev": O.CHEBYSHEV}[name]
     eig = (0.0, 0.0)
     if name == "bicg":
@@ -294,7 +302,7 @@ def test_rank2_solver_histories_bitwise(seed, name, pk, max_iter):
         eig = (float(ev[0]), float(ev[-1]))
         xp, code, detail = _run_py(pyref.chebyshev, rp, ci, v, b, x0, M, mon, *eig)
     xo, res, hr, hi = O.solve(kind, A, np.array(b), np.array(x0), pc, max_iter=max_iter, rtol=1e-10,
-                              eigmin=eig[0], eigmax=eig[1])
+                              eigmin=eig[0], eigmax=eig[1], matrix_norms=norms)
     assert res.status == code and res.detail == detail, (res.status, code, res.detail, detail)
     assert res.iterations == mon.iter
     assert np.array_equal(hr, np.array([h[0] for h in mon.hist]))
