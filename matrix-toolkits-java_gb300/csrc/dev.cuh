@@ -263,15 +263,6 @@ __device__ __forceinline__ Acc system_sum(const RedCtx &rc, int sys, int type, d
     return s;
 }
 
-// The reduction of a phase finishes in k_finalize (a launch of its own after
-// the phase's kernel): block s forms system s's sums and thread 0 runs
-// op.scalar(s, sums).  No atomics and no fences: the launch boundary orders
-// the partial stores before it.  (The one-launch CG sums a phase's partials
-// itself, with the same function, after a grid barrier.)
-//
-// Kernel templates and their launchers live in an unnamed namespace: without
-// relocatable device code every translation unit carries its own device
-// image, so each one instantiates (and sets attributes on) its own kernels.
 // |x| in the monitor's norm for a MatrixIterationMonitor, by the whole block
 // (thread-strided sums, the fixed block tree), into t.xnorm ahead of the
 // test; sm holds kParts * kBlock doubles.
@@ -302,6 +293,15 @@ struct OpMon<Op, decltype((void)std::declval<const Op &>().m.mon.xmon)> {
     static constexpr bool value = true;
 };
 
+// The reduction of a phase finishes in k_finalize (a launch of its own after
+// the phase's kernel): block s forms system s's sums and thread 0 runs
+// op.scalar(s, sums).  No atomics and no fences: the launch boundary orders
+// the partial stores before it.  (The one-launch CG sums a phase's partials
+// itself, with the same function, after a grid barrier.)
+//
+// Kernel templates and their launchers live in an unnamed namespace: without
+// relocatable device code every translation unit carries its own device
+// image, so each one instantiates (and sets attributes on) its own kernels.
 namespace {
 template <class Op, bool XN = false>
 __global__ void __launch_bounds__(kBlock) k_finalize(Op op, RedCtx rc, int type)
